@@ -1,0 +1,160 @@
+/*
+ * phafd_gpu.h -- C ABI of libphafd_gpu.so, the GB300 (sm_103a) implementation
+ * of PHAFD's per-timestep particle-field hot path.
+ *
+ * The reference (samueljmcameron/PHAFD, src/) exposes this path as C++ style
+ * classes constructed by name from an input script (input.cpp:48-299) and
+ * driven through Fix / Pair / NPair hooks by Integrate::run
+ * (integrate.cpp:105-203).  Each entry point below replaces one of those
+ * hooks or commands; the citation on each line names the reference interface
+ * it stands in for.  All state lives on one GPU: the library owns device
+ * memory, the caller only passes host pointers and sizes.
+ *
+ * Conventions
+ *   - every call returns 0 on success or a negative PHAFD_ERR_* code;
+ *     phafd_last_error() gives the message (the reference throws
+ *     std::runtime_error with the same text at the same point);
+ *   - real grids are [z][y][x] row-major, x fastest, no padding;
+ *   - k-space arrays are exchanged in the reference's transposed FFTW-MPI
+ *     layout [ky][kz][kx] with kx in [0, Nx/2], interleaved (re, im) doubles
+ *     (grid.cpp:96-97);
+ *   - bead arrays are owned beads in creation order, xyz interleaved
+ *     (Eigen::Matrix3Xd column layout, atom.hpp:38);
+ *   - one context per host thread; calls are ordered on the context's stream.
+ */
+#ifndef PHAFD_GPU_H
+#define PHAFD_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define PHAFD_OK 0
+#define PHAFD_ERR_INVALID -1      /* bad argument / order of commands        */
+#define PHAFD_ERR_CUDA -2         /* CUDA runtime error                      */
+#define PHAFD_ERR_NAN -3          /* phi(0,0,0) is NaN (integrate.cpp:190)   */
+#define PHAFD_ERR_OVERFLOW -4     /* neighbor capacity exceeded              */
+#define PHAFD_ERR_CONSTRAINT -5   /* chain step failed (non-finite / stretch)*/
+#define PHAFD_ERR_UNSUPPORTED -6  /* size or option not built                */
+#define PHAFD_ERR_NOMEM -7
+
+/* ---- precision of the grid path ---- */
+#define PHAFD_FP64 64
+#define PHAFD_FP32 32
+
+/* ---- grid fields (grid.hpp:29-36) ---- */
+#define PHAFD_FIELD_PHI 0
+#define PHAFD_FIELD_CHEMPOT 1
+#define PHAFD_FIELD_GRADX 2
+#define PHAFD_FIELD_GRADY 3
+#define PHAFD_FIELD_GRADZ 4
+#define PHAFD_FIELD_FT_PHI 5
+#define PHAFD_FIELD_FT_CHEMPOT 6
+
+/* ---- gridatom pair styles (input.cpp:107-116) ---- */
+#define PHAFD_GRIDATOM_NONE 0
+#define PHAFD_GRIDATOM_GAUSSIAN 1      /* pair gridatom/gaussian     */
+#define PHAFD_GRIDATOM_LJISH 2         /* pair gridatom/LJish        */
+#define PHAFD_GRIDATOM_LJISH_LINEAR 3  /* pair gridatom/LJish/linear */
+
+/* ---- noise sources ---- */
+#define PHAFD_NOISE_OFF 0        /* zero noise, all other terms unchanged            */
+#define PHAFD_NOISE_REFERENCE 1  /* the reference's mt19937 + uniform_real stream    */
+#define PHAFD_NOISE_PHILOX 2     /* counter-based Philox4x32-10, generated on device */
+
+/* ---- periodic z images of beads ---- */
+#define PHAFD_ZGHOST_RANK1 0     /* reference with 1 MPI rank: no z images (comm_brick.cpp:300-318) */
+#define PHAFD_ZGHOST_PERIODIC 1  /* reference with >= 2 ranks: fully periodic                     */
+
+/* ---- step schedule of the field ---- */
+#define PHAFD_SCHEDULE_REFERENCE 0 /* r2c(phi) at every step start, as fixgrid_conjugate.cpp:62   */
+#define PHAFD_SCHEDULE_RESIDENT 1  /* phi-hat carried across steps (same maths, one FFT fewer)   */
+
+typedef struct phafd_semiflexible_params {
+  double bondlength; /* rest length of a bond                              */
+  double zeta_para;  /* friction along the local chain tangent             */
+  double zeta_perp;  /* friction across the local chain tangent            */
+  double bending;    /* bending energy: bending * sum (1 - cos theta)      */
+  double temp;       /* kT of the bead noise                               */
+  double kbond;      /* harmonic bond constant                             */
+  int seed;          /* Philox key of the bead noise                       */
+  int noise;         /* PHAFD_NOISE_OFF or PHAFD_NOISE_PHILOX              */
+} phafd_semiflexible_params;
+
+typedef struct phafd_counters {
+  long long num_less_zero;   /* FH reflections phi <= 0 (fixgrid_floryhuggins.cpp:74) */
+  long long num_great_zero;  /* FH reflections phi >= 1 (fixgrid_floryhuggins.cpp:77) */
+  long long neighbor_calls;  /* Neighbor::ncalls (neighbor.cpp:103)                    */
+  long long timestep;        /* Integrate::timestep                                    */
+  long long status;          /* sticky PHAFD_ERR_* raised on the device, 0 if none     */
+  long long nan_step;        /* first step whose phi(0,0,0) was NaN, -1 if none        */
+} phafd_counters;
+
+typedef struct phafd_ctx phafd_ctx;
+
+/* ---- context (replaces PHAFD::PHAFD / PHAFD::create, phafd.cpp:21-121) ---- */
+int phafd_ctx_create(phafd_ctx** out, int device, int precision);
+int phafd_ctx_destroy(phafd_ctx* ctx);
+const char* phafd_last_error(phafd_ctx* ctx);
+const char* phafd_build_info(void);
+
+/* ---- domain / grid (input.cpp:67-80) ---- */
+int phafd_domain(phafd_ctx* ctx, const double boxlo[3], const double period[3]); /* Domain::set_box, domain.cpp:30-76 */
+int phafd_grid_style(phafd_ctx* ctx, int nx, int ny, int nz);   /* Grid::create + create_concentration, grid.cpp:88-113,205-286 */
+int phafd_grid_populate_constant(phafd_ctx* ctx, double average, double variance, int seed); /* Grid::noisy_constant, grid.cpp:289-307 */
+int phafd_grid_set(phafd_ctx* ctx, int field, const double* host);   /* upload a real field, [z][y][x]              */
+int phafd_grid_get(phafd_ctx* ctx, int field, double* host);         /* download a real field or a k-space field    */
+int phafd_set_zghost(phafd_ctx* ctx, int mode);                      /* CommBrick::borders z swaps, comm_brick.cpp:283-352 */
+int phafd_set_schedule(phafd_ctx* ctx, int schedule);
+int phafd_set_keep_chempot(phafd_ctx* ctx, int keep);               /* also store mu = deposit + FH (grid->chempot) each step */
+
+/* ---- beads (atom_style / atom_populate, atom.cpp:26-110,219-252) ---- */
+int phafd_atoms_create(phafd_ctx* ctx, int n, const int* tags, const int* mol, const int* types, const double* x);
+int phafd_atoms_get(phafd_ctx* ctx, double* x, double* ux, double* f, int* images);
+
+/* ---- pairs (input.cpp:99-153) ---- */
+int phafd_pair_gridatom(phafd_ctx* ctx, int style, double cut);  /* PairGridAtom*::settings, pair_gridatom_gaussian.cpp:123-142 */
+int phafd_pair_gridatom_coeff(phafd_ctx* ctx, int type, int has_eps, double eps, int has_width, double nucwidth,
+                              int has_phi, double phi);           /* PairGridAtom*::coeff, pair_gridatom_gaussian.cpp:145-181 */
+int phafd_pair_lj_cut(phafd_ctx* ctx, double cut, double eps, double sigma); /* PairLJCut::settings, pair_lj_cut.cpp:103-119 */
+
+/* ---- neighbor (input.cpp:154-164) ---- */
+int phafd_neighbor(phafd_ctx* ctx, double skin);                  /* Neighbor::setup, neighbor.cpp:39-68 */
+
+/* ---- fixes (input.cpp:177-229) ---- */
+int phafd_fix_conjugate_volfrac(phafd_ctx* ctx, int seed, double mobility, double temp, double volFH, double gamma,
+                                int noise);                       /* FixGridConjugate<ConjugateVolFrac>::init, fixgrid_conjugate.cpp:21-45 */
+int phafd_fix_floryhuggins(phafd_ctx* ctx, double temp, double volFH, double chi); /* FixGridFloryHuggins::init, fixgrid_floryhuggins.cpp:22-56 */
+int phafd_fix_gradphi(phafd_ctx* ctx, int once);                  /* FixGridGradPhi, fixgrid_gradphi.cpp:42-99 */
+int phafd_fix_drag(phafd_ctx* ctx, int nranges, const int* starts, const int* ends, double drag); /* FixAtomDrag, fixatom_drag.cpp:24-66 */
+int phafd_fix_semiflexible(phafd_ctx* ctx, int nranges, const int* starts, const int* ends,
+                           const phafd_semiflexible_params* p);  /* FixAtomSemiFlexible<NoTether>, fixatom_semiflexible.cpp:27-191 */
+
+/* ---- integrate (input.cpp:256-273) ---- */
+int phafd_set_dt(phafd_ctx* ctx, double dt);                      /* "dt" command */
+int phafd_set_timestep(phafd_ctx* ctx, long long step);           /* "timestep" command */
+int phafd_setup(phafd_ctx* ctx);                                  /* Integrate::setup, integrate.cpp:33-88 */
+int phafd_run(phafd_ctx* ctx, int nsteps);                        /* Integrate::run, integrate.cpp:90-219 */
+int phafd_counters_get(phafd_ctx* ctx, phafd_counters* out);      /* Integrate::finalise counters, integrate.cpp:418-443 */
+int phafd_synchronize(phafd_ctx* ctx);
+
+/* ---- neighbor-list export (NeighList ilist/firstneigh, neigh_list.hpp) ----
+ * half list: (tag_i, tag_j, image code of j relative to i)
+ * grid list: (node index (z*Ny+y)*Nx+x, tag, image code of the bead)
+ * image code = (sx+1) + 3*(sy+1) + 9*(sz+1), s in {-1,0,1} periods added to the bead */
+int phafd_half_list_size(phafd_ctx* ctx, long long* n);
+int phafd_half_list(phafd_ctx* ctx, int* out3);
+int phafd_grid_list_size(phafd_ctx* ctx, long long* n);
+int phafd_grid_list(phafd_ctx* ctx, int* out3);
+
+/* ---- stage hooks for unit tests and partial pipelines ---- */
+int phafd_stage_gradient(phafd_ctx* ctx);          /* FixGridConjugate::start_of_step               */
+int phafd_stage_borders_and_build(phafd_ctx* ctx); /* Domain::pbc + CommBrick::borders + Neighbor::build */
+int phafd_stage_pairs(phafd_ctx* ctx);             /* Fs = 0, chempot = 0, pair->compute(), reverse_comm */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHAFD_GPU_H */

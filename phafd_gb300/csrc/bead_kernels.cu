@@ -1,0 +1,528 @@
+// Bead-side kernels of the particle-field step.
+//
+// One periodic domain on one GPU replaces the reference's gathered LOCAL and
+// GHOST copies (comm_brick.cpp:263-426): a periodic image of bead j is
+// x_j + s*L with s in {-1, 0, 1} per axis, computed exactly as the reference
+// computes a ghost coordinate (atom.cpp pack_comm: x + pbc), so distances and
+// cutoff tests see the same bits.  With the rank-1 z mode, images across z
+// are skipped, as borders() on one MPI rank never creates them.
+//
+// Neighbor rebuilds run on the device every step and exit at once unless the
+// skin trigger fired (neighbor.cpp:70-97): the step is a fixed launch
+// sequence that a CUDA graph can replay.
+//
+// Lists
+//   bead list : full list, nbr[i*maxnb + k] = (j << 5) | image code
+//   grid list : per bead, gl[i*maxg + k] = (node << 5) | image code,
+//               node = (z*Ny + y)*Nx + x, image code applied to the bead
+//   image code = (sx+1) + 3*(sy+1) + 9*(sz+1)
+// As sets of unordered pairs they equal the reference's half list
+// (npair_half_bin_newton.cpp:38-124) and grid list (npair_grid_bin.cpp:22-127).
+#include "bead_kernels.h"
+
+namespace phafd {
+
+namespace {
+
+constexpr int IMGMASK = 1023, IMGMAX = 512, IMGBITS = 10, IMG2BITS = 20;
+
+__device__ __forceinline__ double img_shift(int code, int d, const BeadArgs& a) {
+  int s = (code / (d == 0 ? 1 : d == 1 ? 3 : 9)) % 3 - 1;
+  return s == 0 ? 0.0 : (s > 0 ? a.period[d] : -a.period[d]);
+}
+
+__device__ __forceinline__ int bin_coord(double x, double lo, double inv, int nb) {
+  int b = (int)((x - lo) * inv);
+  return b < 0 ? 0 : (b >= nb ? nb - 1 : b);
+}
+
+}  // namespace
+
+// neighbor.cpp:79-97
+__global__ void k_check(BeadArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double d0 = a.x[3 * i] - a.xhold[3 * i];
+  const double d1 = a.x[3 * i + 1] - a.xhold[3 * i + 1];
+  const double d2 = a.x[3 * i + 2] - a.xhold[3 * i + 2];
+  const double rsq = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+  if (rsq > a.triggersq) *a.flag = 1;
+}
+
+// domain.cpp:102-163 then Domain::unmap
+__global__ void k_pbc(BeadArgs a) {
+  if (!*a.flag) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  int im = a.image[i];
+  double x[3] = {a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2]};
+  for (int d = 0; d < 3; ++d) {
+    const int sh = d == 0 ? 0 : (d == 1 ? IMGBITS : IMG2BITS);
+    const double lo = a.boxlo[d], hi = a.boxhi[d], L = a.period[d];
+    if (x[d] < lo) {
+      x[d] = __dadd_rn(x[d], L);
+      int idim = d == 2 ? (im >> IMG2BITS) : ((im >> sh) & IMGMASK);
+      const int other = im ^ (idim << sh);
+      idim = (idim - 1) & IMGMASK;
+      im = other | (idim << sh);
+    }
+    if (x[d] >= hi) {
+      x[d] = __dsub_rn(x[d], L);
+      x[d] = x[d] > lo ? x[d] : lo;
+      int idim = d == 2 ? (im >> IMG2BITS) : ((im >> sh) & IMGMASK);
+      const int other = im ^ (idim << sh);
+      idim = (idim + 1) & IMGMASK;
+      im = other | (idim << sh);
+    }
+  }
+  const int xbox = (im & IMGMASK) - IMGMAX;
+  const int ybox = (im >> IMGBITS & IMGMASK) - IMGMAX;
+  const int zbox = (im >> IMG2BITS) - IMGMAX;
+  a.image[i] = im;
+  for (int d = 0; d < 3; ++d) a.x[3 * i + d] = x[d];
+  a.ux[3 * i + 0] = __dadd_rn(x[0], __dmul_rn((double)xbox, a.period[0]));
+  a.ux[3 * i + 1] = __dadd_rn(x[1], __dmul_rn((double)ybox, a.period[1]));
+  a.ux[3 * i + 2] = __dadd_rn(x[2], __dmul_rn((double)zbox, a.period[2]));
+}
+
+__global__ void k_bin_clear(BeadArgs a) {
+  if (!*a.flag) return;
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < a.nbins; b += (long long)gridDim.x * blockDim.x) {
+    a.bin_count[b] = 0;
+    a.bin_cursor[b] = 0;
+  }
+}
+
+__global__ void k_bin_count(BeadArgs a) {
+  if (!*a.flag) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int bx = bin_coord(a.x[3 * i], a.boxlo[0], a.bininv[0], a.nb[0]);
+  const int by = bin_coord(a.x[3 * i + 1], a.boxlo[1], a.bininv[1], a.nb[1]);
+  const int bz = bin_coord(a.x[3 * i + 2], a.boxlo[2], a.bininv[2], a.nb[2]);
+  const int b = (bz * a.nb[1] + by) * a.nb[0] + bx;
+  a.bin_of[i] = b;
+  atomicAdd(&a.bin_count[b], 1);
+}
+
+// exclusive scan of bin_count into bin_start, in three launches
+__global__ void k_scan_block(BeadArgs a) {
+  if (!*a.flag) return;
+  __shared__ int warp_sums[32];
+  const long long base = (long long)blockIdx.x * 1024;
+  const long long i = base + threadIdx.x;
+  int v = i < a.nbins ? a.bin_count[i] : 0;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += t;
+  }
+  if (lane == 31) warp_sums[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int s = warp_sums[lane];
+    int si = s;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, si, off);
+      if (lane >= off) si += t;
+    }
+    warp_sums[lane] = si - s;
+    if (lane == 31) a.scan_tmp[blockIdx.x] = si;
+  }
+  __syncthreads();
+  if (i < a.nbins) a.bin_start[i] = incl - v + warp_sums[w];
+}
+
+__global__ void k_scan_sums(BeadArgs a, int nblocks) {
+  if (!*a.flag) return;
+  // single warp, sequential over chunks of 32
+  const int lane = threadIdx.x;
+  int carry = 0;
+  for (int c = 0; c < nblocks; c += 32) {
+    const int idx = c + lane;
+    int v = idx < nblocks ? a.scan_tmp[idx] : 0;
+    int incl = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += t;
+    }
+    if (idx < nblocks) a.scan_tmp[idx] = carry + incl - v;
+    carry += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (lane == 0) a.bin_start[a.nbins] = carry;
+}
+
+__global__ void k_scan_add(BeadArgs a) {
+  if (!*a.flag) return;
+  const long long i = (long long)blockIdx.x * 1024 + threadIdx.x;
+  if (i < a.nbins) a.bin_start[i] += a.scan_tmp[blockIdx.x];
+}
+
+__global__ void k_bin_fill(BeadArgs a) {
+  if (!*a.flag) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int b = a.bin_of[i];
+  const int pos = a.bin_start[b] + atomicAdd(&a.bin_cursor[b], 1);
+  a.sorted[pos] = i;
+}
+
+// order beads inside each bin by index so that the lists are deterministic
+__global__ void k_bin_sort(BeadArgs a) {
+  if (!*a.flag) return;
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < a.nbins; b += (long long)gridDim.x * blockDim.x) {
+    const int s = a.bin_start[b], e = a.bin_start[b + 1];
+    for (int p = s + 1; p < e; ++p) {
+      const int v = a.sorted[p];
+      int q = p - 1;
+      while (q >= s && a.sorted[q] > v) { a.sorted[q + 1] = a.sorted[q]; --q; }
+      a.sorted[q + 1] = v;
+    }
+  }
+}
+
+// stencil scans: full bead list and per-bead grid list
+__global__ void k_build(BeadArgs a) {
+  if (!*a.flag) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double xi[3] = {a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2]};
+  // ---- bead list
+  if (a.nbr) {
+    const int b = a.bin_of[i];
+    const int bx = b % a.nb[0], by = (b / a.nb[0]) % a.nb[1], bz = b / (a.nb[0] * a.nb[1]);
+    int cnt = 0;
+    for (int dz = -1; dz <= 1; ++dz) {
+      int cz = bz + dz, sz = 0;
+      if (cz < 0) { cz += a.nb[2]; sz = -1; } else if (cz >= a.nb[2]) { cz -= a.nb[2]; sz = 1; }
+      if (sz != 0 && !a.zperiodic) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        int cy = by + dy, sy = 0;
+        if (cy < 0) { cy += a.nb[1]; sy = -1; } else if (cy >= a.nb[1]) { cy -= a.nb[1]; sy = 1; }
+        for (int dx = -1; dx <= 1; ++dx) {
+          int cx = bx + dx, sx = 0;
+          if (cx < 0) { cx += a.nb[0]; sx = -1; } else if (cx >= a.nb[0]) { cx -= a.nb[0]; sx = 1; }
+          const int nbn = (cz * a.nb[1] + cy) * a.nb[0] + cx;
+          const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
+          const double s0 = sx == 0 ? 0.0 : (sx > 0 ? a.period[0] : -a.period[0]);
+          const double s1 = sy == 0 ? 0.0 : (sy > 0 ? a.period[1] : -a.period[1]);
+          const double s2 = sz == 0 ? 0.0 : (sz > 0 ? a.period[2] : -a.period[2]);
+          for (int p = a.bin_start[nbn]; p < a.bin_start[nbn + 1]; ++p) {
+            const int j = a.sorted[p];
+            if (j == i && code == 13) continue;
+            const double xj0 = sx ? __dadd_rn(a.x[3 * j], s0) : a.x[3 * j];
+            const double xj1 = sy ? __dadd_rn(a.x[3 * j + 1], s1) : a.x[3 * j + 1];
+            const double xj2 = sz ? __dadd_rn(a.x[3 * j + 2], s2) : a.x[3 * j + 2];
+            const double dx0 = __dsub_rn(xi[0], xj0), dx1 = __dsub_rn(xi[1], xj1), dx2 = __dsub_rn(xi[2], xj2);
+            const double rsq = __dadd_rn(__dadd_rn(__dmul_rn(dx0, dx0), __dmul_rn(dx1, dx1)), __dmul_rn(dx2, dx2));
+            if (rsq <= a.cutneighsq) {
+              if (cnt < a.maxnb) a.nbr[(size_t)i * a.maxnb + cnt] = (j << 5) | code;
+              ++cnt;
+            }
+          }
+        }
+      }
+    }
+    if (cnt > a.maxnb) { atomicOr(a.status, ST_OVERFLOW); cnt = a.maxnb; }
+    a.nnbr[i] = cnt;
+  }
+  // ---- grid list: nodes within cutneigh of each periodic image of bead i
+  if (a.gl) {
+    int lo3[3], hi3[3];
+    for (int d = 0; d < 3; ++d) {
+      const double u = (xi[d] - a.boxlo[d]) / a.dx[d];
+      const double r = a.cutneigh / a.dx[d];
+      lo3[d] = (int)floor(u - r) - 1;
+      hi3[d] = (int)ceil(u + r) + 1;
+    }
+    int cnt = 0;
+    for (int kz = lo3[2]; kz <= hi3[2]; ++kz) {
+      int wz = kz, sz = 0;
+      if (wz < 0) { wz += a.N[2]; sz = 1; } else if (wz >= a.N[2]) { wz -= a.N[2]; sz = -1; }
+      if (wz < 0 || wz >= a.N[2]) continue;
+      if (sz != 0 && !a.zperiodic) continue;
+      const double zt = __dadd_rn(__dmul_rn((double)wz, a.dx[2]), a.boxlo[2]);
+      const double bz = sz ? __dadd_rn(xi[2], sz > 0 ? a.period[2] : -a.period[2]) : xi[2];
+      const double dz = __dsub_rn(zt, bz);
+      for (int ky = lo3[1]; ky <= hi3[1]; ++ky) {
+        int wy = ky, sy = 0;
+        if (wy < 0) { wy += a.N[1]; sy = 1; } else if (wy >= a.N[1]) { wy -= a.N[1]; sy = -1; }
+        if (wy < 0 || wy >= a.N[1]) continue;
+        const double yt = __dadd_rn(__dmul_rn((double)wy, a.dx[1]), a.boxlo[1]);
+        const double by_ = sy ? __dadd_rn(xi[1], sy > 0 ? a.period[1] : -a.period[1]) : xi[1];
+        const double dy = __dsub_rn(yt, by_);
+        for (int kx = lo3[0]; kx <= hi3[0]; ++kx) {
+          int wx = kx, sx = 0;
+          if (wx < 0) { wx += a.N[0]; sx = 1; } else if (wx >= a.N[0]) { wx -= a.N[0]; sx = -1; }
+          if (wx < 0 || wx >= a.N[0]) continue;
+          const double xt = __dadd_rn(__dmul_rn((double)wx, a.dx[0]), a.boxlo[0]);
+          const double bx_ = sx ? __dadd_rn(xi[0], sx > 0 ? a.period[0] : -a.period[0]) : xi[0];
+          const double dxx = __dsub_rn(xt, bx_);
+          const double rsq = __dadd_rn(__dadd_rn(__dmul_rn(dxx, dxx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+          if (rsq <= a.cutneighsq) {
+            const uint32_t node = (uint32_t)(((long long)wz * a.N[1] + wy) * a.N[0] + wx);
+            const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
+            if (cnt < a.maxg) a.gl[(size_t)i * a.maxg + cnt] = (node << 5) | (uint32_t)code;
+            ++cnt;
+          }
+        }
+      }
+    }
+    if (cnt > a.maxg) { atomicOr(a.status, ST_OVERFLOW); cnt = a.maxg; }
+    a.ngl[i] = cnt;
+  }
+  // neighbor.cpp:106-109
+  a.xhold[3 * i] = xi[0];
+  a.xhold[3 * i + 1] = xi[1];
+  a.xhold[3 * i + 2] = xi[2];
+}
+
+__global__ void k_build_done(BeadArgs a) {
+  if (*a.flag) {
+    *a.ncalls += 1;
+    *a.flag = 0;
+  }
+}
+
+__global__ void k_step_begin(long long* d_step) { *d_step += 1; }
+
+// ---- pair forces: lj/cut over the bead list, gridatom over the grid list.
+// Each bead sums its own force (no atomics on F).  The mu deposit of the
+// gridatom styles goes to `dep` with atomics.
+template <typename T>
+__global__ void k_pair(BeadArgs a, PairArgs<T> p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double xi0 = a.x[3 * i], xi1 = a.x[3 * i + 1], xi2 = a.x[3 * i + 2];
+  // Kahan-compensated sums (exact no-ops in double beyond round-off)
+  T f[3] = {0, 0, 0}, c[3] = {0, 0, 0};
+  auto add = [&](int d, T v) {
+    T y = v - c[d];
+    T t = f[d] + y;
+    c[d] = (t - f[d]) - y;
+    f[d] = t;
+  };
+  if (p.lj && a.nbr) {
+    const int cnt = a.nnbr[i];
+    for (int k = 0; k < cnt; ++k) {
+      const int e = a.nbr[(size_t)i * a.maxnb + k];
+      const int j = e >> 5, code = e & 31;
+      const double d0 = xi0 - (a.x[3 * j] + img_shift(code, 0, a));
+      const double d1 = xi1 - (a.x[3 * j + 1] + img_shift(code, 1, a));
+      const double d2 = xi2 - (a.x[3 * j + 2] + img_shift(code, 2, a));
+      const T dx = (T)d0, dy = (T)d1, dz = (T)d2;
+      const T rsq = dx * dx + dy * dy + dz * dz;
+      if (rsq < (T)p.lj_cutsq) {
+        const T r2inv = (T)1 / rsq;
+        const T r6inv = r2inv * r2inv * r2inv;
+        const T forcelj = r6inv * ((T)p.lj1 * r6inv - (T)p.lj2);
+        const T fpair = forcelj * r2inv;
+        add(0, dx * fpair);
+        add(1, dy * fpair);
+        add(2, dz * fpair);
+      }
+    }
+  }
+  if (p.ga_style != PHAFD_GRIDATOM_NONE && a.gl) {
+    const int cnt = a.ngl[i];
+    const int t = a.type[i];
+    const T cutsq = (T)p.ga_cutsq[t], eps = (T)p.ga_eps[t], phit = (T)p.ga_phi[t];
+    for (int k = 0; k < cnt; ++k) {
+      const uint32_t e = a.gl[(size_t)i * a.maxg + k];
+      const uint32_t node = e >> 5;
+      const int code = (int)(e & 31u);
+      const int gx = (int)(node % (uint32_t)a.N[0]);
+      const int gy = (int)((node / (uint32_t)a.N[0]) % (uint32_t)a.N[1]);
+      const int gz = (int)(node / ((uint32_t)a.N[0] * (uint32_t)a.N[1]));
+      // node coordinate k*dx + boxlo without contraction (npair_grid_bin.cpp:76-88)
+      const double d0 = __dadd_rn(__dmul_rn((double)gx, a.dx[0]), a.boxlo[0]) - (xi0 + img_shift(code, 0, a));
+      const double d1 = __dadd_rn(__dmul_rn((double)gy, a.dx[1]), a.boxlo[1]) - (xi1 + img_shift(code, 1, a));
+      const double d2 = __dadd_rn(__dmul_rn((double)gz, a.dx[2]), a.boxlo[2]) - (xi2 + img_shift(code, 2, a));
+      const T dx = (T)d0, dy = (T)d1, dz = (T)d2;
+      T rsq = dx * dx + dy * dy + dz * dz;
+      const bool inside = (p.ga_style == PHAFD_GRIDATOM_GAUSSIAN) ? (rsq <= cutsq) : (rsq < cutsq);
+      if (!inside) continue;
+      rsq = rsq / cutsq;
+      T expfac, mu_add;
+      if (p.ga_style == PHAFD_GRIDATOM_GAUSSIAN) {
+        // pair_gridatom_gaussian.cpp:97-107
+        expfac = (exp(-rsq / (T)2.0) - exp((T)-0.5)) * exp((T)0.5) * eps;
+        const T delphi = p.phi[node] - phit;
+        mu_add = (T)2 * delphi * expfac;
+        expfac = expfac * ((T)2 * delphi * (T)p.dv);
+      } else if (p.ga_style == PHAFD_GRIDATOM_LJISH) {
+        // pair_gridatom_lj_ish.cpp:104-176
+        expfac = exp((T)-1. / ((T)1 - rsq) + (T)1) * eps;
+        const T delphi = p.phi[node] - phit;
+        mu_add = (T)2 * delphi * expfac;
+        expfac = expfac * ((T)2 * delphi * (T)p.dv);
+      } else {
+        // pair_gridatom_lj_ish_linear.cpp:104-168
+        expfac = (T)-1 * exp((T)-1. / ((T)1 - rsq) + (T)1) * eps;
+        mu_add = expfac;
+        expfac = expfac * (T)p.dv;
+      }
+      atomicAdd(p.dep + node, mu_add);
+      add(0, -p.gx[node] * expfac);
+      add(1, -p.gy[node] * expfac);
+      add(2, -p.gz[node] * expfac);
+    }
+  }
+  a.f[3 * i] = (double)f[0];
+  a.f[3 * i + 1] = (double)f[1];
+  a.f[3 * i + 2] = (double)f[2];
+}
+
+// zero the nodes a bead may have deposited on (sparse reset of dep)
+template <typename T>
+__global__ void k_dep_zero(BeadArgs a, T* dep) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n || !a.gl) return;
+  const int cnt = a.ngl[i];
+  for (int k = 0; k < cnt; ++k) dep[a.gl[(size_t)i * a.maxg + k] >> 5] = (T)0;
+}
+
+// fixatom_drag.cpp:47-52 / 58-62
+__global__ void k_drag(BeadArgs a, double dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double dr = a.dragc[i];
+  if (dr == 0.0) return;
+  for (int d = 0; d < 3; ++d)
+    a.x[3 * i + d] = __dadd_rn(a.x[3 * i + d], __dmul_rn(__dmul_rn(__dmul_rn(dr, a.f[3 * i + d]), dt), 0.5));
+}
+
+// chain model (no reference counterpart; the oracle's oracle_chain_force)
+__global__ void k_chain_force(BeadArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int fi = a.sf_fix[i];
+  if (fi < 0) return;
+  const SemiDev& P = a.sf[fi];
+  const int base = a.sf_start[i], n = a.sf_len[i], b = i - base;
+  const double* u = a.ux + 3 * (size_t)base;
+  double f[3] = {0, 0, 0};
+  for (int side = 0; side < 2; ++side) {
+    const int q = side == 0 ? b - 1 : b;
+    if (q < 0 || q + 1 >= n) continue;
+    const double r[3] = {u[3 * (q + 1)] - u[3 * q], u[3 * (q + 1) + 1] - u[3 * q + 1], u[3 * (q + 1) + 2] - u[3 * q + 2]};
+    const double len = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    const double g = P.kbond * (len - P.bondlength) / len;
+    const double sgn = (q == b) ? 1.0 : -1.0;
+    for (int d = 0; d < 3; ++d) f[d] += sgn * g * r[d];
+  }
+  if (P.bending != 0.0) {
+    for (int cc = b - 1; cc <= b + 1; ++cc) {
+      if (cc < 1 || cc + 1 >= n) continue;
+      double ra[3], rb[3];
+      for (int d = 0; d < 3; ++d) {
+        ra[d] = u[3 * cc + d] - u[3 * (cc - 1) + d];
+        rb[d] = u[3 * (cc + 1) + d] - u[3 * cc + d];
+      }
+      const double la = sqrt(ra[0] * ra[0] + ra[1] * ra[1] + ra[2] * ra[2]);
+      const double lb = sqrt(rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2]);
+      const double cs = (ra[0] * rb[0] + ra[1] * rb[1] + ra[2] * rb[2]) / (la * lb);
+      for (int d = 0; d < 3; ++d) {
+        const double dca = rb[d] / (la * lb) - cs * ra[d] / (la * la);
+        const double dcb = ra[d] / (la * lb) - cs * rb[d] / (lb * lb);
+        if (b == cc - 1) f[d] += P.bending * (-dca);
+        else if (b == cc) f[d] += P.bending * (dca - dcb);
+        else f[d] += P.bending * dcb;
+      }
+    }
+  }
+  const int lo = b > 0 ? b - 1 : b, hi = b + 1 < n ? b + 1 : b;
+  const double tv[3] = {u[3 * hi] - u[3 * lo], u[3 * hi + 1] - u[3 * lo + 1], u[3 * hi + 2] - u[3 * lo + 2]};
+  const double tl = sqrt(tv[0] * tv[0] + tv[1] * tv[1] + tv[2] * tv[2]);
+  for (int d = 0; d < 3; ++d) {
+    a.fchain[3 * i + d] = f[d];
+    a.tang[3 * i + d] = tl > 0 ? tv[d] / tl : 0.0;
+  }
+}
+
+__global__ void k_chain_move(BeadArgs a, int half, double dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int fi = a.sf_fix[i];
+  if (fi < 0) return;
+  const SemiDev& P = a.sf[fi];
+  double xi[3] = {0, 0, 0};
+  if (P.noise == PHAFD_NOISE_PHILOX && P.temp > 0) bead_gauss(P.seed, (uint64_t)(*a.d_step), half, i, xi);
+  const double* fc = a.fchain + 3 * (size_t)i;
+  const double* fp = a.f + 3 * (size_t)i;
+  const double* t = a.tang + 3 * (size_t)i;
+  const double h = 0.5 * dt;
+  const double ft[3] = {fc[0] + fp[0], fc[1] + fp[1], fc[2] + fp[2]};
+  const double tf = t[0] * ft[0] + t[1] * ft[1] + t[2] * ft[2];
+  const double tx = t[0] * xi[0] + t[1] * xi[1] + t[2] * xi[2];
+  const double aa = 1.0 / P.zeta_perp, bpar = 1.0 / P.zeta_para - 1.0 / P.zeta_perp;
+  const double sa = 1.0 / sqrt(P.zeta_perp), sb = 1.0 / sqrt(P.zeta_para) - 1.0 / sqrt(P.zeta_perp);
+  const double amp = sqrt(2.0 * P.temp * h);
+  const int im = a.image[i];
+  const int box[3] = {(im & IMGMASK) - IMGMAX, (im >> IMGBITS & IMGMASK) - IMGMAX, (im >> IMG2BITS) - IMGMAX};
+  bool bad = false;
+  for (int d = 0; d < 3; ++d) {
+    const double disp = h * (aa * ft[d] + bpar * tf * t[d]) + amp * (sa * xi[d] + sb * tx * t[d]);
+    const double nu = a.ux[3 * i + d] + disp;
+    a.ux[3 * i + d] = nu;
+    a.x[3 * i + d] = __dsub_rn(nu, __dmul_rn((double)box[d], a.period[d]));  // Domain::map, domain.cpp:180-193
+    bad |= !isfinite(nu);
+  }
+  if (bad) atomicOr(a.status, ST_CONSTRAINT);
+}
+
+// ---------------------------------------------------------------- launchers
+static inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+void launch_step_begin(long long* d_step, cudaStream_t st) { k_step_begin<<<1, 1, 0, st>>>(d_step); }
+
+void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st) {
+  if (a.n == 0) return;
+  const int T = 256;
+  if (force) cudaMemsetAsync(a.flag, 0xff, sizeof(int), st);
+  else k_check<<<nblk(a.n, T), T, 0, st>>>(a);
+  k_pbc<<<nblk(a.n, T), T, 0, st>>>(a);
+  k_bin_clear<<<nblk(a.nbins, T) > 4096 ? 4096 : nblk(a.nbins, T), T, 0, st>>>(a);
+  k_bin_count<<<nblk(a.n, T), T, 0, st>>>(a);
+  const int nblocks = (int)((a.nbins + 1023) / 1024);
+  k_scan_block<<<nblocks, 1024, 0, st>>>(a);
+  k_scan_sums<<<1, 32, 0, st>>>(a, nblocks);
+  k_scan_add<<<nblocks, 1024, 0, st>>>(a);
+  k_bin_fill<<<nblk(a.n, T), T, 0, st>>>(a);
+  k_bin_sort<<<nblk(a.nbins, T) > 4096 ? 4096 : nblk(a.nbins, T), T, 0, st>>>(a);
+  k_build<<<nblk(a.n, 128), 128, 0, st>>>(a);
+  k_build_done<<<1, 1, 0, st>>>(a);
+}
+
+template <typename T>
+void launch_pair(const BeadArgs& a, const PairArgs<T>& p, cudaStream_t st) {
+  if (a.n == 0) return;
+  k_pair<T><<<nblk(a.n, 128), 128, 0, st>>>(a, p);
+}
+template void launch_pair<float>(const BeadArgs&, const PairArgs<float>&, cudaStream_t);
+template void launch_pair<double>(const BeadArgs&, const PairArgs<double>&, cudaStream_t);
+
+template <typename T>
+void launch_dep_zero(const BeadArgs& a, T* dep, cudaStream_t st) {
+  if (a.n == 0) return;
+  k_dep_zero<T><<<nblk(a.n, 256), 256, 0, st>>>(a, dep);
+}
+template void launch_dep_zero<float>(const BeadArgs&, float*, cudaStream_t);
+template void launch_dep_zero<double>(const BeadArgs&, double*, cudaStream_t);
+
+void launch_drag(const BeadArgs& a, double dt, cudaStream_t st) {
+  if (a.n == 0 || !a.any_drag) return;
+  k_drag<<<nblk(a.n, 256), 256, 0, st>>>(a, dt);
+}
+
+void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st) {
+  if (a.n == 0 || !a.any_semi) return;
+  k_chain_force<<<nblk(a.n, 128), 128, 0, st>>>(a);
+  k_chain_move<<<nblk(a.n, 128), 128, 0, st>>>(a, half, dt);
+}
+
+}  // namespace phafd

@@ -1,0 +1,64 @@
+// Bead-side device arguments and launchers.
+#pragma once
+#include "internal.h"
+
+namespace phafd {
+
+struct SemiDev {
+  double bondlength, zeta_para, zeta_perp, bending, temp, kbond;
+  uint32_t seed;
+  int noise;
+};
+
+struct BeadArgs {
+  int n;
+  double *x, *ux, *f, *xhold, *fchain, *tang;
+  int *image, *type;
+  double boxlo[3], boxhi[3], period[3];
+  double triggersq, cutneigh, cutneighsq;
+  int* flag;            // rebuild requested (device)
+  int* status;          // sticky ST_* bits
+  long long* ncalls;    // Neighbor::ncalls
+  const long long* d_step;
+  // bins
+  int nb[3];
+  double bininv[3];
+  long long nbins;
+  int *bin_of, *bin_count, *bin_cursor, *bin_start, *sorted, *scan_tmp;
+  // lists
+  int* nbr;
+  int* nnbr;
+  int maxnb;
+  uint32_t* gl;
+  int* ngl;
+  int maxg;
+  int N[3];
+  double dx[3];
+  int zperiodic;
+  // fixes
+  double* dragc;
+  int any_drag;
+  int *sf_fix, *sf_start, *sf_len;
+  const SemiDev* sf;
+  int any_semi;
+};
+
+template <typename T>
+struct PairArgs {
+  int lj;
+  double lj_cutsq, lj1, lj2;
+  int ga_style;
+  const double *ga_cutsq, *ga_eps, *ga_phi;  // per type, device
+  const T *phi, *gx, *gy, *gz;
+  T* dep;
+  double dv;
+};
+
+void launch_step_begin(long long* d_step, cudaStream_t st);
+void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st);
+template <typename T> void launch_pair(const BeadArgs& a, const PairArgs<T>& p, cudaStream_t st);
+template <typename T> void launch_dep_zero(const BeadArgs& a, T* dep, cudaStream_t st);
+void launch_drag(const BeadArgs& a, double dt, cudaStream_t st);
+void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st);
+
+}  // namespace phafd

@@ -1,0 +1,1072 @@
+// libphafd_gpu C ABI: context, device memory, and the per-step launch
+// sequence (the GB300 restatement of Integrate::run, integrate.cpp:105-203).
+//
+// Step, "resident" schedule (default).  State at step start: phi_hat (the
+// unnormalised r2c of phi), phi and grad phi, all in HBM.
+//   neighbor check / rebuild          (device flag; no host round trip)
+//   pair forces + mu deposit          (lj/cut, gridatom/*)
+//   drag / chain first half           (initial_integrate)
+//   x-r2c fused with Flory-Huggins    (post_force + pre_final_integrate)
+//   y-fft, z-fft                      -> mu_hat
+//   z pass: Model-B update, z-ifft of phi_hat and of i qz phi_hat
+//   y pass: y-ifft (+ i qy)           x pass: c2r -> phi, dphi/dx, dphi/dy, dphi/dz
+//   drag / chain second half          (final_integrate)
+// The reference recomputes phi_hat = r2c(phi) at every step start
+// (fixgrid_conjugate.cpp:66); r2c(c2r(X)) equals X for the Hermitian
+// spectra the update produces, so the resident schedule carries phi_hat
+// across steps and saves one 3D FFT.  The "reference" schedule keeps the
+// reference's order exactly (one extra r2c per step).
+//
+// Every launch of a step reads its parameters from device memory, so the
+// whole step is captured once into a CUDA graph and replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "bead_kernels.h"
+
+using namespace phafd;
+
+namespace {
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+#define CK(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess) throw CudaError(std::string(#x) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  void alloc(size_t b) {
+    release();
+    if (b == 0) return;
+    CK(cudaMalloc(&p, b));
+    bytes = b;
+  }
+  void zero(cudaStream_t st) {
+    if (p) CK(cudaMemsetAsync(p, 0, bytes, st));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+  ~DevBuf() { release(); }
+};
+
+struct Range { int start, end; };
+
+int make_unique_seed(int baseseed) {  // utility.cpp:213-235, rank 0
+  std::mt19937 gen;
+  std::uniform_int_distribution<int> integer_dist;
+  gen.seed(baseseed);
+  return integer_dist(gen);
+}
+
+}  // namespace
+
+struct phafd_ctx {
+  std::string err;
+  int device = 0, precision = PHAFD_FP32;
+  cudaStream_t st = nullptr;
+  // domain / grid
+  bool boxset = false, gridset = false, populated = false;
+  double boxlo[3] = {0, 0, 0}, boxhi[3] = {0, 0, 0}, period[3] = {0, 0, 0};
+  int N[3] = {0, 0, 0};
+  size_t nreal = 0, ncplx = 0;
+  Geom geom{};
+  int zghost = PHAFD_ZGHOST_PERIODIC;
+  int schedule = PHAFD_SCHEDULE_RESIDENT;
+  bool keep_chempot = false;
+  bool chempot_from_mu = false;
+  int graph_cur = 0;
+  DevBuf phi, gx, gy, gz, dep, mu;
+  DevBuf phat[2], muhat, w1, wA, wB, wC, wD, wE;
+  int cur = 0;
+  DevBuf tw[3][2];  // [axis][0 fwd, 1 inv]
+  DevBuf uref;
+  double2* uref_h = nullptr;
+  // beads
+  int n = 0, ntypes = 0;
+  std::vector<int> tags, types, mol;
+  DevBuf bx, bux, bf, bxhold, bfchain, btang, bimage, btype;
+  DevBuf bin_of, bin_count, bin_cursor, bin_start, sorted, scan_tmp;
+  DevBuf nbr, nnbr, gl, ngl;
+  DevBuf dragc, sf_fix, sf_start, sf_len, sf_par;
+  BeadArgs ba{};
+  // pairs
+  bool have_lj = false;
+  double lj_cut = 0, lj1 = 0, lj2 = 0;
+  int ga_style = PHAFD_GRIDATOM_NONE;
+  double ga_maxcut = 0;
+  std::vector<double> ga_cutsq, ga_eps, ga_phi;
+  DevBuf ga_dev;  // 3 * ntypes doubles
+  // neighbor
+  bool neigh_set = false;
+  double skin = 0, cutneigh = 0;
+  // fixes
+  bool have_conj = false, have_fh = false, have_gradphi = false, gradphi_once = false;
+  double c_mobility = 1, c_temp = 1, c_volFH = 1, c_gamma = 1;
+  int c_seed = 0, c_noise = PHAFD_NOISE_PHILOX;
+  std::mt19937 c_gen;
+  double fh_temp = 1, fh_volFH = 1, fh_chi = 1;
+  std::vector<std::pair<std::vector<Range>, double>> drags;
+  std::vector<std::pair<std::vector<Range>, phafd_semiflexible_params>> semis;
+  // integrate
+  double dt = 0;
+  long long timestep = 0, firststep = 0;
+  bool setup_done = false;
+  // device counters
+  DevBuf d_counters;  // [0..1] FH counters (ull), [2] step, [3] nan_step, [4] ncalls, [5] flag|status
+  unsigned long long* fh_counters() const { return d_counters.as<unsigned long long>(); }
+  long long* d_step() const { return d_counters.as<long long>() + 2; }
+  long long* d_nan() const { return d_counters.as<long long>() + 3; }
+  long long* d_ncalls() const { return d_counters.as<long long>() + 4; }
+  int* d_flag() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 5); }
+  int* d_status() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 5) + 1; }
+  // graph
+  cudaGraphExec_t gexec = nullptr;
+  bool eager_done = false;
+
+  ~phafd_ctx() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (uref_h) cudaFreeHost(uref_h);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  size_t rsz() const { return precision == PHAFD_FP64 ? 8 : 4; }
+
+  void invalidate_graph() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    eager_done = false;
+  }
+
+  // ------------------------------------------------------------------ grid
+  void build_twiddles() {
+    for (int a = 0; a < 3; ++a) {
+      const int n = N[a];
+      for (int dir = 0; dir < 2; ++dir) {
+        const double sgn = dir == 0 ? -1.0 : 1.0;
+        std::vector<double> tbl(2 * (size_t)n);
+        for (int m = 0; m < n; ++m) {
+          long double ang = 2.0L * 3.141592653589793238462643383279502884L * m / n;
+          tbl[2 * m] = (double)std::cos(ang);
+          tbl[2 * m + 1] = sgn * (double)std::sin(ang);
+        }
+        if (precision == PHAFD_FP64) {
+          tw[a][dir].alloc(tbl.size() * 8);
+          CK(cudaMemcpy(tw[a][dir].p, tbl.data(), tbl.size() * 8, cudaMemcpyHostToDevice));
+        } else {
+          std::vector<float> f(tbl.begin(), tbl.end());
+          tw[a][dir].alloc(f.size() * 4);
+          CK(cudaMemcpy(tw[a][dir].p, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
+        }
+      }
+    }
+  }
+
+  void alloc_grid() {
+    const size_t r = nreal * rsz(), c = ncplx * 2 * rsz();
+    phi.alloc(r); gx.alloc(r); gy.alloc(r); gz.alloc(r); dep.alloc(r);
+    for (auto* b : {&phi, &gx, &gy, &gz, &dep}) b->zero(st);
+    phat[0].alloc(c); phat[1].alloc(c); muhat.alloc(c); w1.alloc(c);
+    wA.alloc(c); wB.alloc(c); wC.alloc(c); wD.alloc(c); wE.alloc(c);
+    for (auto* b : {&phat[0], &phat[1], &muhat, &w1, &wA, &wB, &wC, &wD, &wE}) b->zero(st);
+    build_twiddles();
+  }
+
+  template <typename T>
+  UpdateArgs<T> update_args(const cpx<T>* phi_old, const cpx<T>* mu_hat, cpx<T>* phi_new, double store_scale) {
+    UpdateArgs<T> u{};
+    u.phi_old = phi_old;
+    u.mu_hat = mu_hat;
+    u.phi_new = phi_new;
+    u.uref = uref.as<double2>();
+    u.mobility = c_mobility;
+    u.tvg = c_temp / c_volFH * c_gamma;
+    u.dt = dt;
+    u.norm = 1.0 / ((double)N[0] * N[2] * N[1]);  // conjugate_volfrac.cpp:76
+    const double invLcubed = 1.0 / (period[0] * period[1] * period[2]);
+    u.cpref = std::sqrt(12 * c_temp * c_mobility * invLcubed);
+    u.rpref = std::sqrt(24 * c_temp * c_mobility * invLcubed);
+    u.sqrtdt = std::sqrt(dt);
+    u.phi_scale = 1.0;
+    u.store_scale = store_scale;
+    u.qx = geom.kq[0];
+    u.qy = geom.kq[1];
+    u.qz = geom.kq[2];
+    u.noise = c_noise;
+    u.seed = (uint32_t)c_seed;
+    u.d_step = d_step();
+    u.Ny = N[1];
+    u.Nz = N[2];
+    u.Nxh = N[0] / 2 + 1;
+    return u;
+  }
+
+  static void chk(int rc, const char* what) {
+    if (rc == -2) throw std::runtime_error(std::string("unsupported FFT length in ") + what);
+    if (rc != 0) throw CudaError(std::string("launch failed: ") + what);
+  }
+
+  // r2c of a real field into `out` (unnormalised), optionally fused with FH
+  template <typename T>
+  void r2c(const T* in, const T* depp, cpx<T>* out, const FHArgs& fh) {
+    const cpx<T>* twf[3] = {tw[0][0].as<cpx<T>>(), tw[1][0].as<cpx<T>>(), tw[2][0].as<cpx<T>>()};
+    chk(GridOps<T>::xr2c(geom, in, depp, out, twf[0], fh, st), "x r2c");
+    chk(GridOps<T>::ypass(geom, -1, out, out, nullptr, twf[1], st), "y fft");
+    chk(GridOps<T>::zpass(geom, -1, out, out, nullptr, twf[2], nullptr, st), "z fft");
+  }
+
+  // from a spectrum S (z-ifft input) produce phi (scale sp, optional) and grad (scale sg)
+  template <typename T>
+  void inverse_chain(const cpx<T>* S, const UpdateArgs<T>* u, T* phi_out, T sp, T sg, bool grad, bool nan_check) {
+    const cpx<T>* twi[3] = {tw[0][1].as<cpx<T>>(), tw[1][1].as<cpx<T>>(), tw[2][1].as<cpx<T>>()};
+    cpx<T>* A = wA.as<cpx<T>>();
+    cpx<T>* B = wB.as<cpx<T>>();
+    cpx<T>* Cc = wC.as<cpx<T>>();
+    cpx<T>* D = wD.as<cpx<T>>();
+    cpx<T>* E = wE.as<cpx<T>>();
+    NanArgs nan{nan_check ? 1 : 0, d_nan(), d_step()};
+    NanArgs nonan{0, d_nan(), d_step()};
+    chk(GridOps<T>::zpass(geom, +1, S, A, grad ? B : nullptr, twi[2], u, st), "z ifft");
+    chk(GridOps<T>::ypass(geom, +1, A, Cc, grad ? D : nullptr, twi[1], st), "y ifft");
+    if (grad) chk(GridOps<T>::ypass(geom, +1, B, E, nullptr, twi[1], st), "y ifft");
+    if (phi_out && grad) {
+      chk(GridOps<T>::xc2r(geom, Cc, phi_out, sp, false, gx.as<T>(), sg, twi[0], nan, st), "x c2r");
+    } else if (phi_out) {
+      chk(GridOps<T>::xc2r(geom, Cc, phi_out, sp, false, nullptr, sg, twi[0], nan, st), "x c2r");
+    } else if (grad) {
+      chk(GridOps<T>::xc2r(geom, Cc, gx.as<T>(), sg, true, nullptr, sg, twi[0], nonan, st), "x c2r");
+    }
+    if (grad) {
+      chk(GridOps<T>::xc2r(geom, D, gy.as<T>(), sg, false, nullptr, sg, twi[0], nonan, st), "x c2r");
+      chk(GridOps<T>::xc2r(geom, E, gz.as<T>(), sg, false, nullptr, sg, twi[0], nonan, st), "x c2r");
+    }
+  }
+
+  // ------------------------------------------------------------------ beads
+  void fill_bead_args() {
+    BeadArgs& a = ba;
+    a.n = n;
+    a.x = bx.as<double>(); a.ux = bux.as<double>(); a.f = bf.as<double>(); a.xhold = bxhold.as<double>();
+    a.fchain = bfchain.as<double>(); a.tang = btang.as<double>();
+    a.image = bimage.as<int>(); a.type = btype.as<int>();
+    for (int d = 0; d < 3; ++d) {
+      a.boxlo[d] = boxlo[d]; a.boxhi[d] = boxhi[d]; a.period[d] = period[d];
+      a.N[d] = N[d];
+      a.dx[d] = gridset ? period[d] / N[d] : 1.0;
+    }
+    a.triggersq = 0.25 * skin * skin;
+    a.cutneigh = cutneigh;
+    a.cutneighsq = cutneigh * cutneigh;
+    a.flag = d_flag(); a.status = d_status(); a.ncalls = d_ncalls(); a.d_step = d_step();
+    a.bin_of = bin_of.as<int>(); a.bin_count = bin_count.as<int>(); a.bin_cursor = bin_cursor.as<int>();
+    a.bin_start = bin_start.as<int>(); a.sorted = sorted.as<int>(); a.scan_tmp = scan_tmp.as<int>();
+    a.nbr = have_lj ? nbr.as<int>() : nullptr;
+    a.nnbr = nnbr.as<int>();
+    a.gl = ga_style != PHAFD_GRIDATOM_NONE ? gl.as<uint32_t>() : nullptr;
+    a.ngl = ngl.as<int>();
+    a.zperiodic = zghost == PHAFD_ZGHOST_PERIODIC;
+    a.dragc = dragc.as<double>();
+    a.any_drag = !drags.empty();
+    a.sf_fix = sf_fix.as<int>(); a.sf_start = sf_start.as<int>(); a.sf_len = sf_len.as<int>();
+    a.sf = sf_par.as<SemiDev>();
+    a.any_semi = !semis.empty();
+  }
+
+  void setup_neighbor_structs() {
+    // bins: >= cutneigh wide, at least 3 per axis, about 2 bins per bead
+    const int target = std::max(3, (int)std::cbrt(2.0 * std::max(n, 1)) + 1);
+    long long nbins = 1;
+    for (int d = 0; d < 3; ++d) {
+      int nb = (int)std::floor(period[d] / cutneigh);
+      if (nb < 3) throw std::runtime_error("box must span at least three neighbor cutoffs per axis");
+      nb = std::min(nb, target);
+      ba.nb[d] = nb;
+      ba.bininv[d] = nb / period[d];
+      nbins *= nb;
+    }
+    ba.nbins = nbins;
+    bin_of.alloc(std::max(n, 1) * 4);
+    bin_count.alloc(nbins * 4);
+    bin_cursor.alloc(nbins * 4);
+    bin_start.alloc((nbins + 1) * 4);
+    sorted.alloc(std::max(n, 1) * 4);
+    scan_tmp.alloc(((nbins + 1023) / 1024 + 1) * 4);
+    ba.maxnb = 128;
+    if (have_lj) nbr.alloc((size_t)std::max(n, 1) * ba.maxnb * 4);
+    nnbr.alloc(std::max(n, 1) * 4);
+    int maxg = 1;
+    for (int d = 0; d < 3; ++d) {
+      const double dxd = gridset ? period[d] / N[d] : 1.0;
+      maxg *= (int)std::floor(2.0 * cutneigh / dxd) + 3;
+    }
+    ba.maxg = maxg;
+    if (ga_style != PHAFD_GRIDATOM_NONE) gl.alloc((size_t)std::max(n, 1) * maxg * 4);
+    ngl.alloc(std::max(n, 1) * 4);
+    nnbr.zero(st);
+    ngl.zero(st);
+  }
+
+  void upload_fix_tables() {
+    std::vector<double> dc(std::max(n, 1), 0.0);
+    for (auto& f : drags)
+      for (auto& r : f.first)
+        for (int j = r.start; j < r.end; ++j) {
+          if (dc[j] != 0.0) throw std::runtime_error("a bead may belong to one atom/drag fix only");
+          dc[j] = f.second;
+        }
+    dragc.alloc(dc.size() * 8);
+    CK(cudaMemcpy(dragc.p, dc.data(), dc.size() * 8, cudaMemcpyHostToDevice));
+    std::vector<int> fix(std::max(n, 1), -1), s0(std::max(n, 1), 0), ln(std::max(n, 1), 0);
+    std::vector<SemiDev> par;
+    for (size_t k = 0; k < semis.size(); ++k) {
+      const auto& p = semis[k].second;
+      par.push_back(SemiDev{p.bondlength, p.zeta_para, p.zeta_perp, p.bending, p.temp, p.kbond, (uint32_t)p.seed, p.noise});
+      for (auto& r : semis[k].first)
+        for (int j = r.start; j < r.end; ++j) {
+          if (fix[j] >= 0) throw std::runtime_error("a bead may belong to one semiflexible fix only");
+          fix[j] = (int)k; s0[j] = r.start; ln[j] = r.end - r.start;
+        }
+    }
+    sf_fix.alloc(fix.size() * 4); sf_start.alloc(s0.size() * 4); sf_len.alloc(ln.size() * 4);
+    CK(cudaMemcpy(sf_fix.p, fix.data(), fix.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sf_start.p, s0.data(), s0.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sf_len.p, ln.data(), ln.size() * 4, cudaMemcpyHostToDevice));
+    sf_par.alloc(std::max<size_t>(par.size(), 1) * sizeof(SemiDev));
+    if (!par.empty()) CK(cudaMemcpy(sf_par.p, par.data(), par.size() * sizeof(SemiDev), cudaMemcpyHostToDevice));
+    if (ntypes > 0) {
+      std::vector<double> g(3 * (size_t)ntypes, 0.0);
+      for (int t = 0; t < ntypes && !ga_cutsq.empty(); ++t) {
+        g[t] = ga_cutsq[t]; g[ntypes + t] = ga_eps[t]; g[2 * ntypes + t] = ga_phi[t];
+      }
+      ga_dev.alloc(g.size() * 8);
+      CK(cudaMemcpy(ga_dev.p, g.data(), g.size() * 8, cudaMemcpyHostToDevice));
+    }
+  }
+
+  template <typename T>
+  PairArgs<T> pair_args() {
+    PairArgs<T> p{};
+    p.lj = have_lj;
+    p.lj_cutsq = lj_cut * lj_cut;
+    p.lj1 = lj1;
+    p.lj2 = lj2;
+    p.ga_style = ga_style;
+    p.ga_cutsq = ga_dev.as<double>();
+    p.ga_eps = ga_dev.as<double>() + ntypes;
+    p.ga_phi = ga_dev.as<double>() + 2 * ntypes;
+    p.phi = phi.as<T>(); p.gx = gx.as<T>(); p.gy = gy.as<T>(); p.gz = gz.as<T>();
+    p.dep = dep.as<T>();
+    p.dv = gridset ? (period[0] / N[0]) * (period[1] / N[1]) * (period[2] / N[2]) : 1.0;
+    return p;
+  }
+
+  // ------------------------------------------------------------------ reference noise stream
+  // Draw order of Conjugate::update on one rank (conjugate.cpp:163-247):
+  // bulk (ky, kz, kx ascending), the kx = 0 and kx = Nx/2 planes
+  // (single + line_single), then the real points.  Stored per canonical mode.
+  void fill_reference_uniforms() {
+    const int Nx = N[0], Ny = N[1], Nz = N[2], Nxh = Nx / 2 + 1;
+    std::uniform_real_distribution<double> rd(-0.5, 0.5);
+    auto at = [&](int kx, int kz, int ky) -> double2& { return uref_h[((size_t)kx * Nz + kz) * Ny + ky]; };
+    auto two = [&](int ky, int kz, int kx) { double a = rd(c_gen); double b = rd(c_gen); at(kx, kz, ky) = make_double2(a, b); };
+    auto one = [&](int ky, int kz, int kx) { double a = rd(c_gen); at(kx, kz, ky) = make_double2(a, 0.0); };
+    for (int ky = 0; ky < Ny; ++ky)
+      for (int kz = 0; kz < Nz; ++kz)
+        for (int kx = 1; kx < Nxh - 1; ++kx) two(ky, kz, kx);
+    for (int kx = 0; kx < Nxh; kx += Nxh - 1) {
+      for (int kz = 1; kz < Nz / 2; ++kz) two(0, kz, kx);
+      for (int ky = 1; ky < Ny / 2; ++ky) for (int kz = 1; kz < Nz / 2; ++kz) two(ky, kz, kx);
+      for (int ky = Ny / 2 + 1; ky < Ny; ++ky) for (int kz = 1; kz < Nz / 2; ++kz) two(ky, kz, kx);
+      for (int kz = 1; kz < Nz / 2; ++kz) two(Ny / 2, kz, kx);
+      for (int ky = 1; ky < Ny / 2; ++ky) two(ky, 0, kx);
+      for (int ky = Ny / 2 + 1; ky < Ny; ++ky) two(ky, Nz / 2, kx);
+    }
+    one(0, Nz / 2, 0);
+    one(0, Nz / 2, Nxh - 1);
+    one(0, 0, Nxh - 1);
+    one(Ny / 2, 0, 0);
+    one(Ny / 2, Nz / 2, 0);
+    one(Ny / 2, Nz / 2, Nxh - 1);
+    one(Ny / 2, 0, Nxh - 1);
+  }
+
+  // ------------------------------------------------------------------ step
+  template <typename T>
+  void gradient_from_phi() {
+    FHArgs none{0, 0, fh_counters(), 0, nullptr};
+    r2c<T>(phi.as<T>(), nullptr, w1.as<cpx<T>>(), none);
+    inverse_chain<T>(w1.as<cpx<T>>(), nullptr, nullptr, (T)0, (T)(1.0 / (double)nreal), true, false);
+  }
+
+  template <typename T>
+  void enqueue_step() {
+    launch_step_begin(d_step(), st);
+    const bool resident = schedule == PHAFD_SCHEDULE_RESIDENT && have_conj;
+    // fixgrid_gradphi.cpp:45: "once" tests timestep == firststep after the
+    // increment, which never holds inside a run: only "every" recomputes
+    if (!resident && (have_conj || (have_gradphi && !gradphi_once))) gradient_from_phi<T>();
+    // neighbor
+    if (n > 0) launch_neighbor(ba, false, st);
+    // pairs (computed once: the reference's second pass reproduces the first, integrate.cpp:140-146)
+    PairArgs<T> pa = pair_args<T>();
+    if (n > 0 && (have_lj || ga_style != PHAFD_GRIDATOM_NONE)) launch_pair<T>(ba, pa, st);
+    // initial_integrate
+    launch_drag(ba, dt, st);
+    launch_chain_half(ba, 0, dt, st);
+    if (have_conj) {
+      FHArgs fh{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
+      // post_force + pre_final_integrate: mu = dep + FH(phi), r2c
+      r2c<T>(phi.as<T>(), dep.as<T>(), muhat.as<cpx<T>>(), fh);
+      if (n > 0 && ga_style != PHAFD_GRIDATOM_NONE) launch_dep_zero<T>(ba, dep.as<T>(), st);
+      // final_integrate + post_final_integrate
+      if (resident) {
+        // the state stays an unnormalised r2c spectrum: store N * update
+        UpdateArgs<T> u = update_args<T>(phat[cur].as<cpx<T>>(), muhat.as<cpx<T>>(), phat[1 - cur].as<cpx<T>>(),
+                                         (double)nreal);
+        inverse_chain<T>(nullptr, &u, phi.as<T>(), (T)1, (T)1, true, true);
+      } else {
+        UpdateArgs<T> u = update_args<T>(w1.as<cpx<T>>(), muhat.as<cpx<T>>(), phat[0].as<cpx<T>>(), 1.0);
+        inverse_chain<T>(nullptr, &u, phi.as<T>(), (T)1, (T)1, false, true);
+      }
+    }
+    launch_drag(ba, dt, st);
+    launch_chain_half(ba, 1, dt, st);
+  }
+
+  void step_once() {
+    if (precision == PHAFD_FP64) enqueue_step<double>();
+    else enqueue_step<float>();
+  }
+};
+
+// ====================================================================== helpers
+#define API_BEGIN(c)                     \
+  if (!(c)) return PHAFD_ERR_INVALID;    \
+  try {
+#define API_END(c)                                          \
+  return PHAFD_OK;                                          \
+  }                                                         \
+  catch (const CudaError& e) {                              \
+    (c)->err = e.what();                                    \
+    return PHAFD_ERR_CUDA;                                  \
+  }                                                         \
+  catch (const std::exception& e) {                         \
+    (c)->err = e.what();                                    \
+    return PHAFD_ERR_INVALID;                               \
+  }
+
+static void resident_spectrum_flip(phafd_ctx* c) { c->cur = 1 - c->cur; }
+
+template <typename T>
+static void copy_real_to_host(phafd_ctx* c, const DevBuf& b, double* host) {
+  std::vector<T> tmp(c->nreal);
+  CK(cudaMemcpyAsync(tmp.data(), b.p, c->nreal * sizeof(T), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (size_t i = 0; i < c->nreal; ++i) host[i] = (double)tmp[i];
+}
+
+template <typename T>
+static void copy_real_to_dev(phafd_ctx* c, DevBuf& b, const double* host) {
+  std::vector<T> tmp(host, host + c->nreal);
+  CK(cudaMemcpyAsync(b.p, tmp.data(), c->nreal * sizeof(T), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+}
+
+// device layout [kx][kz][ky] -> reference layout [ky][kz][kx], times `scale`
+template <typename T>
+static void copy_spec_to_host(phafd_ctx* c, const DevBuf& b, double* host, double scale) {
+  std::vector<T> tmp(2 * c->ncplx);
+  CK(cudaMemcpyAsync(tmp.data(), b.p, tmp.size() * sizeof(T), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  const int Nx = c->N[0], Ny = c->N[1], Nz = c->N[2], Nxh = Nx / 2 + 1;
+  for (int kx = 0; kx < Nxh; ++kx)
+    for (int kz = 0; kz < Nz; ++kz)
+      for (int ky = 0; ky < Ny; ++ky) {
+        const size_t s = ((size_t)kx * Nz + kz) * Ny + ky;
+        const size_t d = ((size_t)ky * Nz + kz) * Nxh + kx;
+        host[2 * d] = (double)tmp[2 * s] * scale;
+        host[2 * d + 1] = (double)tmp[2 * s + 1] * scale;
+      }
+}
+
+static int check_status(phafd_ctx* c) {
+  long long h[6];
+  CK(cudaMemcpyAsync(h, c->d_counters.p, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  int status = ((int*)&h[5])[1];
+  if (h[3] >= 0) {
+    c->err = "NAN encountered in phi. (step " + std::to_string(h[3]) + ")";
+    return PHAFD_ERR_NAN;
+  }
+  if (status & ST_OVERFLOW) {
+    c->err = "Neighbor list overflow";
+    return PHAFD_ERR_OVERFLOW;
+  }
+  if (status & ST_CONSTRAINT) {
+    c->err = "Failed to maintain polymer bond-length constraints.";
+    return PHAFD_ERR_CONSTRAINT;
+  }
+  return PHAFD_OK;
+}
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* phafd_build_info(void) {
+  return "libphafd_gpu: sm_103a; FFT lengths 16,32,64,96,128,160,256,512; FP32 and FP64 grid paths";
+}
+
+int phafd_ctx_create(phafd_ctx** out, int device, int precision) {
+  if (!out) return PHAFD_ERR_INVALID;
+  *out = nullptr;
+  if (precision != PHAFD_FP32 && precision != PHAFD_FP64) return PHAFD_ERR_INVALID;
+  phafd_ctx* c = new phafd_ctx();
+  c->device = device;
+  c->precision = precision;
+  try {
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    c->d_counters.alloc(6 * sizeof(long long));
+    long long init[6] = {0, 0, 0, -1, 0, 0};
+    CK(cudaMemcpy(c->d_counters.p, init, sizeof(init), cudaMemcpyHostToDevice));
+  } catch (const std::exception& e) {
+    delete c;
+    return PHAFD_ERR_CUDA;
+  }
+  *out = c;
+  return PHAFD_OK;
+}
+
+int phafd_ctx_destroy(phafd_ctx* c) {
+  if (!c) return PHAFD_ERR_INVALID;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  delete c;
+  return PHAFD_OK;
+}
+
+const char* phafd_last_error(phafd_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int phafd_set_zghost(phafd_ctx* c, int mode) {
+  API_BEGIN(c)
+  if (mode != PHAFD_ZGHOST_RANK1 && mode != PHAFD_ZGHOST_PERIODIC) throw std::invalid_argument("bad zghost mode");
+  c->zghost = mode;
+  c->invalidate_graph();
+  API_END(c)
+}
+
+int phafd_set_schedule(phafd_ctx* c, int schedule) {
+  API_BEGIN(c)
+  if (schedule != PHAFD_SCHEDULE_REFERENCE && schedule != PHAFD_SCHEDULE_RESIDENT) throw std::invalid_argument("bad schedule");
+  if (c->setup_done) throw std::runtime_error("schedule must be chosen before setup");
+  c->schedule = schedule;
+  API_END(c)
+}
+
+int phafd_set_keep_chempot(phafd_ctx* c, int keep) {
+  API_BEGIN(c)
+  c->keep_chempot = keep != 0;
+  if (c->keep_chempot && c->gridset && !c->mu.p) { c->mu.alloc(c->nreal * c->rsz()); c->mu.zero(c->st); }
+  c->invalidate_graph();
+  API_END(c)
+}
+
+int phafd_domain(phafd_ctx* c, const double* boxlo, const double* period) {
+  API_BEGIN(c)
+  for (int d = 0; d < 3; ++d) {
+    if (!(period[d] > 0)) throw std::invalid_argument("Bad arguments for domain_setup.");
+    c->boxlo[d] = boxlo[d];
+    c->period[d] = period[d];
+    c->boxhi[d] = boxlo[d] + period[d];
+  }
+  c->boxset = true;
+  API_END(c)
+}
+
+int phafd_grid_style(phafd_ctx* c, int nx, int ny, int nz) {
+  API_BEGIN(c)
+  if (!c->boxset) throw std::invalid_argument("CAnnot use command grid_style before domain box is set.");
+  if (!fft_size_supported(nx) || !fft_size_supported(ny) || !fft_size_supported(nz))
+    throw std::invalid_argument("grid sizes must be one of 16, 32, 64, 96, 128, 160, 256, 512");
+  CK(cudaSetDevice(c->device));
+  c->N[0] = nx; c->N[1] = ny; c->N[2] = nz;
+  c->nreal = (size_t)nx * ny * nz;
+  c->ncplx = (size_t)(nx / 2 + 1) * ny * nz;
+  c->geom.nx = nx; c->geom.ny = ny; c->geom.nz = nz; c->geom.nxh = nx / 2 + 1;
+  for (int d = 0; d < 3; ++d) c->geom.kq[d] = 2 * 3.141592 / c->period[d];  // domain.cpp:206-208
+  c->alloc_grid();
+  if (c->keep_chempot) { c->mu.alloc(c->nreal * c->rsz()); c->mu.zero(c->st); }
+  c->gridset = true;
+  API_END(c)
+}
+
+int phafd_grid_populate_constant(phafd_ctx* c, double average, double variance, int seed) {
+  API_BEGIN(c)
+  if (!c->gridset) throw std::invalid_argument("CAnnot use command grid_populate before grid_style is set.");
+  std::vector<double> h(c->nreal);
+  std::uniform_real_distribution<double> rd(-0.5, 0.5);
+  std::mt19937 gen;
+  gen.seed(make_unique_seed(seed));  // grid.cpp:120-131, 289-307
+  for (auto& v : h) v = average + variance * rd(gen);
+  if (c->precision == PHAFD_FP64) copy_real_to_dev<double>(c, c->phi, h.data());
+  else copy_real_to_dev<float>(c, c->phi, h.data());
+  c->populated = true;
+  API_END(c)
+}
+
+int phafd_grid_set(phafd_ctx* c, int field, const double* host) {
+  API_BEGIN(c)
+  if (!c->gridset) throw std::invalid_argument("grid not created");
+  DevBuf* b = field == PHAFD_FIELD_PHI ? &c->phi : field == PHAFD_FIELD_GRADX ? &c->gx
+            : field == PHAFD_FIELD_GRADY ? &c->gy : field == PHAFD_FIELD_GRADZ ? &c->gz : nullptr;
+  if (!b) throw std::invalid_argument("field cannot be set");
+  if (c->precision == PHAFD_FP64) copy_real_to_dev<double>(c, *b, host);
+  else copy_real_to_dev<float>(c, *b, host);
+  if (field == PHAFD_FIELD_PHI) c->populated = true;
+  API_END(c)
+}
+
+int phafd_grid_get(phafd_ctx* c, int field, double* host) {
+  API_BEGIN(c)
+  if (!c->gridset) throw std::invalid_argument("grid not created");
+  const bool f64 = c->precision == PHAFD_FP64;
+  if (field == PHAFD_FIELD_FT_PHI || field == PHAFD_FIELD_FT_CHEMPOT) {
+    const DevBuf* b;
+    double sc = 1.0;
+    if (field == PHAFD_FIELD_FT_CHEMPOT) b = &c->muhat;
+    else if (c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj) b = &c->phat[c->cur];
+    else if (c->have_conj && c->setup_done) { b = &c->phat[0]; sc = (double)c->nreal; }
+    else b = &c->w1;
+    if (f64) copy_spec_to_host<double>(c, *b, host, sc);
+    else copy_spec_to_host<float>(c, *b, host, sc);
+  } else {
+    const DevBuf* b = field == PHAFD_FIELD_PHI ? &c->phi : field == PHAFD_FIELD_GRADX ? &c->gx
+                    : field == PHAFD_FIELD_GRADY ? &c->gy : field == PHAFD_FIELD_GRADZ ? &c->gz
+                    : field == PHAFD_FIELD_CHEMPOT ? (c->chempot_from_mu ? &c->mu : &c->dep) : nullptr;
+    if (!b) throw std::invalid_argument("bad field");
+    if (f64) copy_real_to_host<double>(c, *b, host);
+    else copy_real_to_host<float>(c, *b, host);
+  }
+  API_END(c)
+}
+
+int phafd_atoms_create(phafd_ctx* c, int n, const int* tags, const int* mol, const int* types, const double* x) {
+  API_BEGIN(c)
+  if (n < 0) throw std::invalid_argument("negative bead count");
+  CK(cudaSetDevice(c->device));
+  c->n = n;
+  c->tags.assign(tags, tags + n);
+  c->types.assign(types, types + n);
+  c->mol.assign(mol ? mol : tags, (mol ? mol : tags) + n);
+  std::vector<int> sorted_tags(c->tags);
+  std::sort(sorted_tags.begin(), sorted_tags.end());
+  if (std::adjacent_find(sorted_tags.begin(), sorted_tags.end()) != sorted_tags.end())
+    throw std::runtime_error("duplicate IDs found on processor(s).");
+  int tmax = -1;
+  for (int t : c->types) tmax = std::max(tmax, t);
+  c->ntypes = tmax + 1;
+  const size_t nn = std::max(n, 1);
+  for (auto* b : {&c->bx, &c->bux, &c->bf, &c->bxhold, &c->bfchain, &c->btang}) { b->alloc(3 * nn * 8); b->zero(c->st); }
+  c->bimage.alloc(nn * 4);
+  c->btype.alloc(nn * 4);
+  if (n > 0) {
+    CK(cudaMemcpy(c->bx.p, x, 3 * (size_t)n * 8, cudaMemcpyHostToDevice));
+    std::vector<int> img(n, (512 << 20) | (512 << 10) | 512);  // Domain::set_image
+    CK(cudaMemcpy(c->bimage.p, img.data(), n * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->btype.p, types, n * 4, cudaMemcpyHostToDevice));
+  }
+  API_END(c)
+}
+
+int phafd_atoms_get(phafd_ctx* c, double* x, double* ux, double* f, int* images) {
+  API_BEGIN(c)
+  CK(cudaStreamSynchronize(c->st));
+  const size_t n = c->n;
+  if (n == 0) return PHAFD_OK;
+  if (x) CK(cudaMemcpy(x, c->bx.p, 3 * n * 8, cudaMemcpyDeviceToHost));
+  if (ux) CK(cudaMemcpy(ux, c->bux.p, 3 * n * 8, cudaMemcpyDeviceToHost));
+  if (f) CK(cudaMemcpy(f, c->bf.p, 3 * n * 8, cudaMemcpyDeviceToHost));
+  if (images) CK(cudaMemcpy(images, c->bimage.p, n * 4, cudaMemcpyDeviceToHost));
+  API_END(c)
+}
+
+int phafd_pair_gridatom(phafd_ctx* c, int style, double cut) {
+  API_BEGIN(c)
+  if (c->ntypes <= 0) throw std::runtime_error("Cannot create pair style before atoms are made.");
+  if (style < PHAFD_GRIDATOM_GAUSSIAN || style > PHAFD_GRIDATOM_LJISH_LINEAR) throw std::invalid_argument("Unrecognised pair style.");
+  c->ga_style = style;
+  c->ga_maxcut = cut;
+  c->ga_cutsq.assign(c->ntypes, cut * cut);  // pair_gridatom_gaussian.cpp:127-141
+  c->ga_eps.assign(c->ntypes, 1.0);
+  c->ga_phi.assign(c->ntypes, 0.1);
+  API_END(c)
+}
+
+int phafd_pair_gridatom_coeff(phafd_ctx* c, int type, int has_eps, double eps, int has_w, double nucwidth, int has_phi, double phit) {
+  API_BEGIN(c)
+  if (c->ga_style == PHAFD_GRIDATOM_NONE) throw std::runtime_error("pairCoeffs before a gridatom pair");
+  if (type < 0 || type >= c->ntypes) throw std::runtime_error("Pair grid/atom atom type out of range.");
+  if (has_eps) c->ga_eps[type] = eps;
+  if (has_w) {
+    if (nucwidth > c->ga_maxcut) throw std::runtime_error("nucwidth cannot be larger than maximum cut.");
+    c->ga_cutsq[type] = nucwidth * nucwidth;
+  }
+  if (has_phi) c->ga_phi[type] = phit;
+  API_END(c)
+}
+
+int phafd_pair_lj_cut(phafd_ctx* c, double cut, double eps, double sigma) {
+  API_BEGIN(c)
+  c->have_lj = true;  // pair_lj_cut.cpp:103-119
+  c->lj_cut = cut;
+  c->lj1 = 48 * eps * std::pow(sigma, 12.0);
+  c->lj2 = 24 * eps * std::pow(sigma, 6.0);
+  API_END(c)
+}
+
+int phafd_neighbor(phafd_ctx* c, double skin) {
+  API_BEGIN(c)
+  if (!c->gridset) throw std::runtime_error("Must call neighbor after subboxes are set (via grid style).");
+  c->skin = skin;  // neighbor.cpp:39-68
+  double cutoff = 0.0;
+  if (c->have_lj) cutoff = std::max(cutoff, c->lj_cut);
+  if (c->ga_style != PHAFD_GRIDATOM_NONE) cutoff = std::max(cutoff, c->ga_maxcut);
+  c->cutneigh = cutoff > 0.0 ? skin + cutoff : 0.0;
+  if (c->cutneigh <= 0.0) c->cutneigh = skin > 0 ? skin : 1.0;
+  c->neigh_set = true;
+  API_END(c)
+}
+
+int phafd_fix_conjugate_volfrac(phafd_ctx* c, int seed, double mobility, double temp, double volFH, double gamma, int noise) {
+  API_BEGIN(c)
+  if (!c->populated) throw std::runtime_error("Fix requires grid to be populated.");
+  if (noise != PHAFD_NOISE_OFF && noise != PHAFD_NOISE_REFERENCE && noise != PHAFD_NOISE_PHILOX) throw std::invalid_argument("bad noise mode");
+  c->have_conj = true;
+  c->c_seed = make_unique_seed(seed);  // fixgrid_conjugate.cpp:33
+  c->c_mobility = mobility; c->c_temp = temp; c->c_volFH = volFH; c->c_gamma = gamma;
+  c->c_noise = noise;
+  c->c_gen.seed(c->c_seed);  // conjugate_volfrac.cpp:64
+  if (noise == PHAFD_NOISE_REFERENCE) {
+    c->uref.alloc(c->ncplx * sizeof(double2));
+    c->uref.zero(c->st);
+    if (c->uref_h) cudaFreeHost(c->uref_h);
+    CK(cudaMallocHost(&c->uref_h, c->ncplx * sizeof(double2)));
+    std::memset(c->uref_h, 0, c->ncplx * sizeof(double2));
+  }
+  API_END(c)
+}
+
+int phafd_fix_floryhuggins(phafd_ctx* c, double temp, double volFH, double chi) {
+  API_BEGIN(c)
+  if (!c->populated) throw std::runtime_error("Fix requires grid to be populated.");
+  c->have_fh = true;
+  c->fh_temp = temp; c->fh_volFH = volFH; c->fh_chi = chi;
+  API_END(c)
+}
+
+int phafd_fix_gradphi(phafd_ctx* c, int once) {
+  API_BEGIN(c)
+  c->have_gradphi = true;
+  c->gradphi_once = once != 0;
+  API_END(c)
+}
+
+int phafd_fix_drag(phafd_ctx* c, int nranges, const int* starts, const int* ends, double drag) {
+  API_BEGIN(c)
+  std::vector<Range> r;
+  for (int k = 0; k < nranges; ++k) {
+    if (starts[k] < 0 || ends[k] > c->n || starts[k] > ends[k]) throw std::invalid_argument("bad group range");
+    r.push_back({starts[k], ends[k]});
+  }
+  c->drags.push_back({r, drag});
+  API_END(c)
+}
+
+int phafd_fix_semiflexible(phafd_ctx* c, int nranges, const int* starts, const int* ends, const phafd_semiflexible_params* p) {
+  API_BEGIN(c)
+  std::vector<Range> r;
+  for (int k = 0; k < nranges; ++k) {
+    if (starts[k] < 0 || ends[k] > c->n || starts[k] > ends[k]) throw std::invalid_argument("bad group range");
+    r.push_back({starts[k], ends[k]});
+  }
+  if (!(p->zeta_para > 0) || !(p->zeta_perp > 0)) throw std::invalid_argument("zeta must be positive");
+  c->semis.push_back({r, *p});
+  API_END(c)
+}
+
+int phafd_set_dt(phafd_ctx* c, double dt) {
+  API_BEGIN(c)
+  c->dt = dt;
+  c->invalidate_graph();
+  API_END(c)
+}
+
+int phafd_set_timestep(phafd_ctx* c, long long step) {
+  API_BEGIN(c)
+  c->timestep = c->firststep = step;
+  CK(cudaMemcpyAsync(c->d_step(), &c->timestep, sizeof(long long), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  API_END(c)
+}
+
+int phafd_setup(phafd_ctx* c) {
+  API_BEGIN(c)
+  CK(cudaSetDevice(c->device));
+  if (c->have_fh && !c->have_conj)
+    throw std::runtime_error("fix grid/floryhuggins/gpu runs fused with fix grid/conjugate/volfrac/gpu; define both");
+  if (!c->neigh_set && c->n > 0 && (c->have_lj || c->ga_style)) throw std::runtime_error("neighbor must be set before run");
+  if (c->have_conj && c->dt <= 0.0) throw std::runtime_error("Cannot run simulation without setting dt > 0.");
+  if (c->have_conj && c->geom.nx == 0) throw std::runtime_error("grid not created");
+  // FixAtomSemiFlexible::check_bonds, fixatom_semiflexible.cpp:114-140 (on positions as given)
+  if (!c->semis.empty()) {
+    std::vector<double> x(3 * (size_t)c->n);
+    CK(cudaMemcpy(x.data(), c->bx.p, x.size() * 8, cudaMemcpyDeviceToHost));
+    for (auto& f : c->semis)
+      for (auto& r : f.first)
+        for (int mu = r.start + 1; mu < r.end; ++mu) {
+          double d0 = x[3 * mu] - x[3 * (mu - 1)], d1 = x[3 * mu + 1] - x[3 * (mu - 1) + 1], d2 = x[3 * mu + 2] - x[3 * (mu - 1) + 2];
+          if (std::abs(std::sqrt(d0 * d0 + d1 * d1 + d2 * d2) - f.second.bondlength) > 1e-3)
+            throw std::runtime_error("Adjacent atom displacements do not match the FixAtomSemiFlexible bondlength specified.");
+        }
+  }
+  if (c->n > 0) {
+    if (!c->neigh_set) {  // no lists: bins only serve Domain::pbc on every step
+      c->cutneigh = std::min(c->period[0], std::min(c->period[1], c->period[2])) / 3.0;
+      c->skin = 0.0;
+    }
+    c->setup_neighbor_structs();
+    c->upload_fix_tables();
+    c->fill_bead_args();
+    launch_neighbor(c->ba, true, c->st);  // Integrate::setup: pbc, borders, build
+    c->bf.zero(c->st);
+  }
+  // field state
+  if (c->gridset && (c->have_conj || c->have_gradphi)) {
+    if (c->precision == PHAFD_FP64) {
+      if (c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj) {
+        FHArgs none{0, 0, c->fh_counters(), 0, nullptr};
+        c->r2c<double>(c->phi.as<double>(), nullptr, c->phat[c->cur].as<cpx<double>>(), none);
+        c->inverse_chain<double>(c->phat[c->cur].as<cpx<double>>(), nullptr, nullptr, 0.0, 1.0 / (double)c->nreal, true, false);
+      }
+    } else {
+      if (c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj) {
+        FHArgs none{0, 0, c->fh_counters(), 0, nullptr};
+        c->r2c<float>(c->phi.as<float>(), nullptr, c->phat[c->cur].as<cpx<float>>(), none);
+        c->inverse_chain<float>(c->phat[c->cur].as<cpx<float>>(), nullptr, nullptr, 0.0f, (float)(1.0 / (double)c->nreal), true, false);
+      }
+    }
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  c->invalidate_graph();
+  c->setup_done = true;
+  int rc = check_status(c);
+  if (rc) return rc;
+  API_END(c)
+}
+
+int phafd_run(phafd_ctx* c, int nsteps) {
+  API_BEGIN(c)
+  CK(cudaSetDevice(c->device));
+  if (!c->setup_done) {
+    int rc = phafd_setup(c);
+    if (rc) return rc;
+  }
+  const bool use_graph = c->c_noise != PHAFD_NOISE_REFERENCE || !c->have_conj;
+  const bool resident = c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj;
+  for (int s = 0; s < nsteps; ++s) {
+    if (c->have_conj && c->c_noise == PHAFD_NOISE_REFERENCE) {
+      CK(cudaStreamSynchronize(c->st));
+      c->fill_reference_uniforms();
+      CK(cudaMemcpyAsync(c->uref.p, c->uref_h, c->ncplx * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+    }
+    if (!use_graph || !c->eager_done) {
+      c->step_once();
+      CK(cudaGetLastError());
+      if (use_graph) c->eager_done = true;
+    } else {
+      if (resident && c->gexec && c->cur != c->graph_cur) {
+        c->step_once();  // bring the spectrum parity back to the captured one
+        CK(cudaGetLastError());
+        c->timestep += 1;
+        resident_spectrum_flip(c);
+        continue;
+      }
+      if (!c->gexec) {
+        // capture the two buffer parities of the resident schedule as one graph of two steps
+        c->graph_cur = c->cur;
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
+        c->step_once();
+        if (resident) { resident_spectrum_flip(c); c->step_once(); resident_spectrum_flip(c); }
+        CK(cudaStreamEndCapture(c->st, &g));
+        CK(cudaGraphInstantiate(&c->gexec, g, 0));
+        cudaGraphDestroy(g);
+      }
+      if (resident && s + 1 < nsteps) {
+        CK(cudaGraphLaunch(c->gexec, c->st));
+        ++s;
+        c->timestep += 2;
+        continue;  // the pair of steps leaves cur unchanged
+      }
+      // odd remainder (or reference schedule): one eager step
+      c->step_once();
+      CK(cudaGetLastError());
+    }
+    c->timestep += 1;
+    if (resident) resident_spectrum_flip(c);
+  }
+  CK(cudaStreamSynchronize(c->st));
+  if (c->keep_chempot && c->have_conj && nsteps > 0) c->chempot_from_mu = true;
+  int rc = check_status(c);
+  if (rc) return rc;
+  API_END(c)
+}
+
+int phafd_synchronize(phafd_ctx* c) {
+  API_BEGIN(c)
+  CK(cudaStreamSynchronize(c->st));
+  API_END(c)
+}
+
+int phafd_counters_get(phafd_ctx* c, phafd_counters* out) {
+  API_BEGIN(c)
+  long long h[6];
+  CK(cudaMemcpyAsync(h, c->d_counters.p, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  out->num_less_zero = h[0];
+  out->num_great_zero = h[1];
+  out->timestep = h[2];
+  out->nan_step = h[3];
+  out->neighbor_calls = h[4];
+  out->status = ((int*)&h[5])[1];
+  API_END(c)
+}
+
+int phafd_half_list_size(phafd_ctx* c, long long* nout) {
+  API_BEGIN(c)
+  CK(cudaStreamSynchronize(c->st));
+  long long tot = 0;
+  if (c->have_lj && c->n > 0) {
+    std::vector<int> nn(c->n), nb((size_t)c->n * c->ba.maxnb);
+    CK(cudaMemcpy(nn.data(), c->nnbr.p, c->n * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(nb.data(), c->nbr.p, nb.size() * 4, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < c->n; ++i)
+      for (int k = 0; k < nn[i]; ++k) if ((nb[(size_t)i * c->ba.maxnb + k] >> 5) > i) ++tot;
+  }
+  *nout = tot;
+  API_END(c)
+}
+
+int phafd_half_list(phafd_ctx* c, int* out3) {
+  API_BEGIN(c)
+  CK(cudaStreamSynchronize(c->st));
+  if (c->have_lj && c->n > 0) {
+    std::vector<int> nn(c->n), nb((size_t)c->n * c->ba.maxnb);
+    CK(cudaMemcpy(nn.data(), c->nnbr.p, c->n * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(nb.data(), c->nbr.p, nb.size() * 4, cudaMemcpyDeviceToHost));
+    size_t m = 0;
+    for (int i = 0; i < c->n; ++i)
+      for (int k = 0; k < nn[i]; ++k) {
+        const int e = nb[(size_t)i * c->ba.maxnb + k], j = e >> 5;
+        if (j <= i) continue;  // each unordered pair once
+        out3[3 * m] = c->tags[i];
+        out3[3 * m + 1] = c->tags[j];
+        out3[3 * m + 2] = e & 31;
+        ++m;
+      }
+  }
+  API_END(c)
+}
+
+int phafd_grid_list_size(phafd_ctx* c, long long* nout) {
+  API_BEGIN(c)
+  CK(cudaStreamSynchronize(c->st));
+  long long tot = 0;
+  if (c->ga_style != PHAFD_GRIDATOM_NONE && c->n > 0) {
+    std::vector<int> nn(c->n);
+    CK(cudaMemcpy(nn.data(), c->ngl.p, c->n * 4, cudaMemcpyDeviceToHost));
+    for (int v : nn) tot += v;
+  }
+  *nout = tot;
+  API_END(c)
+}
+
+int phafd_grid_list(phafd_ctx* c, int* out3) {
+  API_BEGIN(c)
+  CK(cudaStreamSynchronize(c->st));
+  if (c->ga_style != PHAFD_GRIDATOM_NONE && c->n > 0) {
+    std::vector<int> nn(c->n);
+    std::vector<uint32_t> g((size_t)c->n * c->ba.maxg);
+    CK(cudaMemcpy(nn.data(), c->ngl.p, c->n * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(g.data(), c->gl.p, g.size() * 4, cudaMemcpyDeviceToHost));
+    size_t m = 0;
+    for (int i = 0; i < c->n; ++i)
+      for (int k = 0; k < nn[i]; ++k) {
+        const uint32_t e = g[(size_t)i * c->ba.maxg + k];
+        out3[3 * m] = (int)(e >> 5);
+        out3[3 * m + 1] = c->tags[i];
+        out3[3 * m + 2] = (int)(e & 31u);
+        ++m;
+      }
+  }
+  API_END(c)
+}
+
+int phafd_stage_gradient(phafd_ctx* c) {
+  API_BEGIN(c)
+  if (c->precision == PHAFD_FP64) c->gradient_from_phi<double>();
+  else c->gradient_from_phi<float>();
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  API_END(c)
+}
+
+int phafd_stage_borders_and_build(phafd_ctx* c) {
+  API_BEGIN(c)
+  if (c->n == 0) return PHAFD_OK;
+  if (c->ba.nbins == 0) {
+    c->setup_neighbor_structs();
+    c->upload_fix_tables();
+  }
+  c->fill_bead_args();
+  launch_neighbor(c->ba, true, c->st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  int rc = check_status(c);
+  if (rc) return rc;
+  API_END(c)
+}
+
+int phafd_stage_pairs(phafd_ctx* c) {
+  API_BEGIN(c)
+  if (c->n == 0) return PHAFD_OK;
+  c->fill_bead_args();
+  if (c->precision == PHAFD_FP64) {
+    c->dep.zero(c->st);
+    launch_pair<double>(c->ba, c->pair_args<double>(), c->st);
+  } else {
+    c->dep.zero(c->st);
+    launch_pair<float>(c->ba, c->pair_args<float>(), c->st);
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  API_END(c)
+}
+
+}  // extern "C"

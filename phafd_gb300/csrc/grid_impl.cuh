@@ -1,0 +1,445 @@
+// Grid-side kernels of the particle-field step, templated on the arithmetic
+// type T (float or double).  Included once per type by grid_f32.cu and
+// grid_f64.cu.
+//
+// Layouts (all in HBM, resident for the whole run)
+//   real field   R[z][y][x]                       x fastest
+//   spectrum     C[kx][kz][ky], kx in [0, Nx/2]    ky fastest
+//   after x pass C[kx][z][y]; after y pass C[kx][z][ky]
+//
+// A 3D r2c is three passes (x rows -> y lines -> z columns); a c2r runs them
+// backwards.  Every pass moves one tile HBM -> shared memory -> HBM with the
+// pointwise stages of the step fused into its load or store:
+//   x-forward : Flory-Huggins mu + bead deposit (fixgrid_floryhuggins.cpp:71-83)
+//   z pass    : Model-B update with the Hermitian planes and the real points
+//               (conjugate.cpp:163-327, conjugate_volfrac.cpp:89-144)
+//   y / z / x : the spectral derivative i*dq*m (fixgrid_conjugate.cpp:80-105)
+//   x-inverse : the 1/N of the gradient and the NaN check of phi(0,0,0)
+#pragma once
+#include "fft.cuh"
+#include "internal.h"
+
+namespace phafd {
+
+template <typename T>
+PHAFD_D cpx<T> deriv(cpx<T> a, T dq, int m) {
+  // fixgrid_conjugate.cpp:101-103: phi_hat * (0, dq) * m
+  const T mm = (T)m;
+  return mk<T>(-(a.y * dq) * mm, (a.x * dq) * mm);
+}
+
+// number of lines a CTA transforms for axis length N, so that N*NL/16 = 256
+template <int N>
+__host__ __device__ constexpr int lines_for() {
+  int t = 4096 / N, p = 1;
+  while (p * 2 <= t) p *= 2;
+  return p > 32 ? 32 : (p < 4 ? 4 : p);
+}
+
+// -------------------------------------------------------------------- x r2c
+template <typename T, int N, int LB, int PRO>
+__global__ void __launch_bounds__(N * LB / 16)
+k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict__ out,
+       const cpx<T>* __restrict__ tw, int Ny, int Nz, FHArgs fh) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
+  constexpr int NT = N * LB / 16, STR = LB + 1;
+  const int z = blockIdx.y;
+  const int y0 = blockIdx.x * 2 * LB;
+  unsigned long long nless = 0, ngreat = 0;
+  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+    const int l = idx / N, x = idx % N;
+    T v[2] = {(T)0, (T)0};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int y = y0 + 2 * l + h;
+      if (y < Ny) {
+        const size_t o = ((size_t)z * Ny + y) * N + x;
+        T p = in0[o];
+        if constexpr (PRO == 1) {
+          if (fh.enabled) {
+            // fixgrid_floryhuggins.cpp:72-82
+            if (p <= (T)0) { p = -p; nless++; }
+            else if (p >= (T)1) { p = (T)1 - (p - (T)1); ngreat++; }
+            p = dep[o] + (T)fh.tv * (log(p / ((T)1 - p)) + (T)fh.chi * ((T)1 - (T)2 * p));
+          } else {
+            p = dep[o];
+          }
+          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[o] = p;
+        }
+        v[h] = p;
+      }
+    }
+    s[x * STR + l] = mk<T>(v[0], v[1]);
+  }
+  if constexpr (PRO == 1) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      nless += __shfl_down_sync(0xffffffffu, nless, off);
+      ngreat += __shfl_down_sync(0xffffffffu, ngreat, off);
+    }
+    if ((threadIdx.x & 31) == 0 && (nless | ngreat)) {
+      if (nless) atomicAdd(fh.counters + 0, nless);
+      if (ngreat) atomicAdd(fh.counters + 1, ngreat);
+    }
+  }
+  __syncthreads();
+  fft::run<T, N, LB, -1>(s, tw);
+  for (int idx = threadIdx.x; idx < LB * (N / 2 + 1); idx += NT) {
+    const int l = idx % LB, k = idx / LB;
+    const cpx<T> zk = s[k * STR + l];
+    const cpx<T> zm = conjg(s[((N - k) % N) * STR + l]);
+    const cpx<T> a = scale(zk + zm, (T)0.5);
+    const cpx<T> d = zk - zm;
+    const cpx<T> b = mk<T>((T)0.5 * d.y, (T)-0.5 * d.x);
+    const int y = y0 + 2 * l;
+    const size_t o = ((size_t)k * Nz + z) * Ny + y;
+    if (y < Ny) out[o] = a;
+    if (y + 1 < Ny) out[o + 1] = b;
+  }
+}
+
+// -------------------------------------------------------------------- x c2r
+// out0 = c2r(m0 * in) * s0 with m0 = i dqx kx if MUL0 else 1
+// out1 = c2r(i dqx kx * in) * s1          (NOUT == 2)
+template <typename T, int N, int LB, bool MUL0, int NOUT>
+__global__ void __launch_bounds__(N * LB * NOUT / 16)
+k_xc2r(const cpx<T>* __restrict__ in, T* __restrict__ out0, T* __restrict__ out1, T s0, T s1, T dq,
+       const cpx<T>* __restrict__ tw, int Ny, int Nz, NanArgs nan) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
+  constexpr int NL = LB * NOUT;
+  constexpr int NT = N * NL / 16, STR = NL + 1;
+  const int z = blockIdx.y;
+  const int y0 = blockIdx.x * 2 * LB;
+  for (int idx = threadIdx.x; idx < LB * (N / 2 + 1); idx += NT) {
+    const int l = idx % LB, k = idx / LB;
+    const int y = y0 + 2 * l;
+    const size_t o = ((size_t)k * Nz + z) * Ny + y;
+    cpx<T> A = mk<T>(0, 0), B = mk<T>(0, 0);
+    if (y < Ny) A = in[o];
+    if (y + 1 < Ny) B = in[o + 1];
+#pragma unroll
+    for (int q = 0; q < NOUT; ++q) {
+      cpx<T> a = A, b = B;
+      if (q == 1 || MUL0) { a = deriv(a, dq, k); b = deriv(b, dq, k); }
+      if (k == 0 || k == N / 2) { a.y = (T)0; b.y = (T)0; }
+      s[k * STR + q * LB + l] = mk<T>(a.x - b.y, a.y + b.x);
+      if (k > 0 && k < N / 2) s[(N - k) * STR + q * LB + l] = mk<T>(a.x + b.y, b.x - a.y);
+    }
+  }
+  __syncthreads();
+  fft::run<T, N, NL, +1>(s, tw);
+  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+    const int x = idx % N, l = idx / N;
+#pragma unroll
+    for (int q = 0; q < NOUT; ++q) {
+      const cpx<T> v = s[x * STR + q * LB + l];
+      T* out = q == 0 ? out0 : out1;
+      const T sc = q == 0 ? s0 : s1;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int y = y0 + 2 * l + h;
+        if (y < Ny) {
+          const T val = (h == 0 ? v.x : v.y) * sc;
+          out[((size_t)z * Ny + y) * N + x] = val;
+          if (q == 0 && nan.check && z == 0 && y == 0 && x == 0 && isnan(val))
+            atomicCAS(reinterpret_cast<unsigned long long*>(nan.nan_step), (unsigned long long)-1LL,
+                      (unsigned long long)(*nan.d_step));
+        }
+      }
+    }
+  }
+}
+
+// -------------------------------------------------------------------- y pass
+// lines contiguous: in[line * N + e]; out0 = FFT_S(in), out1 = FFT_S(i dq m(e) in)
+template <typename T, int N, int LB, int S, int NOUT>
+__global__ void __launch_bounds__(N * LB * NOUT / 16)
+k_ypass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __restrict__ tw, long long nlines) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
+  constexpr int NL = LB * NOUT;
+  constexpr int NT = N * NL / 16, STR = NL + 1;
+  const long long line0 = (long long)blockIdx.x * LB;
+  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+    const int l = idx / N, e = idx % N;
+    cpx<T> v = mk<T>(0, 0);
+    if (line0 + l < nlines) v = in[(line0 + l) * N + e];
+    s[e * STR + l] = v;
+    if constexpr (NOUT == 2) s[e * STR + LB + l] = deriv(v, dq, wrap_index(e, N));
+  }
+  __syncthreads();
+  fft::run<T, N, NL, S>(s, tw);
+  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+    const int l = idx / N, e = idx % N;
+    if (line0 + l < nlines) {
+      out0[(line0 + l) * N + e] = s[e * STR + l];
+      if constexpr (NOUT == 2) out1[(line0 + l) * N + e] = s[e * STR + LB + l];
+    }
+  }
+}
+
+// -------------------------------------------------------------------- update
+// One mode of ConjugateVolFrac::complex_update / real_update / origin_update
+// (conjugate_volfrac.cpp:89-144) with the Hermitian bookkeeping of
+// Conjugate::update for one rank (conjugate.cpp:163-327).  (kx, ky, kz) are
+// this project's indices: the reference's (i, j, k) = (ky, kz, kx).
+template <typename T>
+PHAFD_D cpx<T> update_mode(const UpdateArgs<T>& u, int kx, int ky, int kz, size_t o) {
+  const int Ny = u.Ny, Nz = u.Nz, Nxh = u.Nxh;
+  const bool plane = (kx == 0 || kx == Nxh - 1);
+  int cy = ky, cz = kz;  // canonical mode whose update this element takes
+  bool mirror = false, real = false, origin = false;
+  if (plane) {
+    const bool ry = (ky == 0 || ky == Ny / 2), rz = (kz == 0 || kz == Nz / 2);
+    if (ry && rz) {
+      real = true;
+      origin = (kx == 0 && ky == 0 && kz == 0);
+    } else {
+      const bool canon = (kz >= 1 && kz < Nz / 2) || (kz == 0 && ky >= 1 && ky < Ny / 2) ||
+                         (kz == Nz / 2 && ky > Ny / 2);
+      if (!canon) {
+        mirror = true;
+        cy = (Ny - ky) % Ny;
+        cz = (Nz - kz) % Nz;
+      }
+    }
+  }
+  const size_t oc = mirror ? ((size_t)kx * Nz + cz) * Ny + cy : o;
+  cpx<T> ph = u.phi_old[oc];
+  ph = scale(ph, (T)u.phi_scale);
+  if (origin) return scale(ph, (T)u.norm);
+  const cpx<T> mu = u.mu_hat[oc];
+  const T qx = (T)u.qx * (T)kx;
+  const T qy = (T)u.qy * (T)wrap_index(cy, Ny);
+  const T qz = (T)u.qz * (T)wrap_index(cz, Nz);
+  const T q2 = qx * qx + qz * qz + qy * qy;  // reference order: qx^2 + q(kz)^2 + q(ky)^2
+  const T pre = (T)u.mobility * q2 * (T)u.dt;
+  const T g = (T)u.tvg * q2;
+  const cpx<T> inner = mk<T>(mu.x + g * ph.x, mu.y + g * ph.y);
+  cpx<T> r = mk<T>((ph.x - pre * inner.x) * (T)u.norm, (ph.y - pre * inner.y) * (T)u.norm);
+  double u0 = 0.0, u1 = 0.0;
+  if (u.noise == PHAFD_NOISE_REFERENCE) {
+    const double2 w = u.uref[((size_t)kx * Nz + cz) * Ny + cy];
+    u0 = w.x; u1 = w.y;
+  } else if (u.noise == PHAFD_NOISE_PHILOX) {
+    const uint32_t st = (uint32_t)(*u.d_step);
+    u0 = field_noise_u(kx, cy, cz, 0, Ny, Nz, st, u.seed);
+    if (!real) u1 = field_noise_u(kx, cy, cz, 1, Ny, Nz, st, u.seed);
+  }
+  const T sq = sqrt(q2);
+  if (real) {
+    r.x += (T)u.rpref * sq * (T)u.sqrtdt * (T)u0;
+  } else {
+    const T a = (T)u.cpref * sq * (T)u.sqrtdt;
+    r.x += a * (T)u0;
+    r.y += a * (T)u1;
+  }
+  return mirror ? conjg(r) : r;
+}
+
+// -------------------------------------------------------------------- z pass
+// tile = (kx, ky in [c0, c0+LB)), transform along kz with stride Ny.
+// UPD: the loaded element is replaced by its Model-B update, stored to
+// u.phi_new, then transformed.
+template <typename T, int N, int LB, int S, int NOUT, bool UPD>
+__global__ void __launch_bounds__(N * LB * NOUT / 16)
+k_zpass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __restrict__ tw, int Ny,
+        UpdateArgs<T> u) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
+  constexpr int NL = LB * NOUT;
+  constexpr int NT = N * NL / 16, STR = NL + 1;
+  const int kx = blockIdx.y;
+  const int c0 = blockIdx.x * LB;
+  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+    const int c = idx % LB, e = idx / LB;
+    const int ky = c0 + c;
+    cpx<T> v = mk<T>(0, 0);
+    if (ky < Ny) {
+      const size_t o = ((size_t)kx * N + e) * Ny + ky;
+      if constexpr (UPD) {
+        v = update_mode(u, kx, ky, e, o);
+        u.phi_new[o] = scale(v, (T)u.store_scale);
+      } else {
+        v = in[o];
+      }
+    }
+    s[e * STR + c] = v;
+    if constexpr (NOUT == 2) s[e * STR + LB + c] = deriv(v, dq, wrap_index(e, N));
+  }
+  __syncthreads();
+  fft::run<T, N, NL, S>(s, tw);
+  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+    const int c = idx % LB, e = idx / LB;
+    const int ky = c0 + c;
+    if (ky < Ny) {
+      const size_t o = ((size_t)kx * N + e) * Ny + ky;
+      out0[o] = s[e * STR + c];
+      if constexpr (NOUT == 2) out1[o] = s[e * STR + LB + c];
+    }
+  }
+}
+
+// -------------------------------------------------------------------- launchers
+// Opt a kernel into more than 48 KB of dynamic shared memory; done once per
+// kernel so that graph capture never sees the attribute call.
+template <typename Kern>
+static int set_smem(Kern k, size_t bytes) {
+  static size_t done = 0;
+  if (bytes > 48 * 1024 && bytes > done) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return -1;
+    done = bytes;
+  }
+  return 0;
+}
+
+template <typename T, int N>
+struct Axis {
+  static constexpr int NLT = lines_for<N>();
+
+  static int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
+                  cudaStream_t st) {
+    constexpr int LB = NLT;
+    const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
+    dim3 grid((g.ny + 2 * LB - 1) / (2 * LB), g.nz);
+    if (dep) {
+      auto k = k_xr2c<T, N, LB, 1>;
+      if (set_smem(k, sm)) return -1;
+      k<<<grid, N * LB / 16, sm, st>>>(in, dep, out, tw, g.ny, g.nz, fh);
+    } else {
+      auto k = k_xr2c<T, N, LB, 0>;
+      if (set_smem(k, sm)) return -1;
+      k<<<grid, N * LB / 16, sm, st>>>(in, dep, out, tw, g.ny, g.nz, fh);
+    }
+    return 0;
+  }
+
+  static int xc2r(const Geom& g, const cpx<T>* in, T* out0, T s0, bool mul0, T* out1, T s1, const cpx<T>* tw,
+                  const NanArgs& nan, cudaStream_t st) {
+    const T dq = (T)g.kq[0];
+    if (out1) {
+      constexpr int LB = NLT / 2 >= 1 ? NLT / 2 : 1;
+      const size_t sm = (size_t)N * (2 * LB + 1) * sizeof(cpx<T>);
+      dim3 grid((g.ny + 2 * LB - 1) / (2 * LB), g.nz);
+      if (mul0) return -1;
+      auto k = k_xc2r<T, N, LB, false, 2>;
+      if (set_smem(k, sm)) return -1;
+      k<<<grid, N * LB * 2 / 16, sm, st>>>(in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
+    } else {
+      constexpr int LB = NLT;
+      const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
+      dim3 grid((g.ny + 2 * LB - 1) / (2 * LB), g.nz);
+      if (mul0) {
+        auto k = k_xc2r<T, N, LB, true, 1>;
+        if (set_smem(k, sm)) return -1;
+        k<<<grid, N * LB / 16, sm, st>>>(in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
+      } else {
+        auto k = k_xc2r<T, N, LB, false, 1>;
+        if (set_smem(k, sm)) return -1;
+        k<<<grid, N * LB / 16, sm, st>>>(in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
+      }
+    }
+    return 0;
+  }
+
+  template <int S>
+  static int ypass(const Geom& g, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw, cudaStream_t st) {
+    const long long nlines = (long long)g.nxh * g.nz;
+    const T dq = (T)g.kq[1];
+    if (out1) {
+      constexpr int LB = NLT / 2 >= 1 ? NLT / 2 : 1;
+      const size_t sm = (size_t)N * (2 * LB + 1) * sizeof(cpx<T>);
+      auto k = k_ypass<T, N, LB, S, 2>;
+      if (set_smem(k, sm)) return -1;
+      k<<<(unsigned)((nlines + LB - 1) / LB), N * LB * 2 / 16, sm, st>>>(in, out0, out1, dq, tw, nlines);
+    } else {
+      constexpr int LB = NLT;
+      const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
+      auto k = k_ypass<T, N, LB, S, 1>;
+      if (set_smem(k, sm)) return -1;
+      k<<<(unsigned)((nlines + LB - 1) / LB), N * LB / 16, sm, st>>>(in, out0, out1, dq, tw, nlines);
+    }
+    return 0;
+  }
+
+  template <int S, bool UPD>
+  static int zpass(const Geom& g, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
+                   const UpdateArgs<T>& u, cudaStream_t st) {
+    const T dq = (T)g.kq[2];
+    if (out1) {
+      constexpr int LB = NLT / 2 >= 1 ? NLT / 2 : 1;
+      const size_t sm = (size_t)N * (2 * LB + 1) * sizeof(cpx<T>);
+      dim3 grid((g.ny + LB - 1) / LB, g.nxh);
+      auto k = k_zpass<T, N, LB, S, 2, UPD>;
+      if (set_smem(k, sm)) return -1;
+      k<<<grid, N * LB * 2 / 16, sm, st>>>(in, out0, out1, dq, tw, g.ny, u);
+    } else {
+      constexpr int LB = NLT;
+      const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
+      dim3 grid((g.ny + LB - 1) / LB, g.nxh);
+      auto k = k_zpass<T, N, LB, S, 1, UPD>;
+      if (set_smem(k, sm)) return -1;
+      k<<<grid, N * LB / 16, sm, st>>>(in, out0, out1, dq, tw, g.ny, u);
+    }
+    return 0;
+  }
+};
+
+#define PHAFD_FOR_SIZES(M) M(16) M(32) M(64) M(96) M(128) M(160) M(256) M(512)
+
+template <typename T>
+int GridOps<T>::xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
+                     cudaStream_t st) {
+  switch (g.nx) {
+#define CASE(n) case n: return Axis<T, n>::xr2c(g, in, dep, out, tw, fh, st);
+    PHAFD_FOR_SIZES(CASE)
+#undef CASE
+  }
+  return -2;
+}
+
+template <typename T>
+int GridOps<T>::xc2r(const Geom& g, const cpx<T>* in, T* out0, T s0, bool mul0, T* out1, T s1, const cpx<T>* tw,
+                     const NanArgs& nan, cudaStream_t st) {
+  switch (g.nx) {
+#define CASE(n) case n: return Axis<T, n>::xc2r(g, in, out0, s0, mul0, out1, s1, tw, nan, st);
+    PHAFD_FOR_SIZES(CASE)
+#undef CASE
+  }
+  return -2;
+}
+
+template <typename T>
+int GridOps<T>::ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
+                      cudaStream_t st) {
+  switch (g.ny) {
+#define CASE(n)                                                                   \
+  case n:                                                                         \
+    return sign < 0 ? Axis<T, n>::template ypass<-1>(g, in, out0, out1, tw, st)   \
+                    : Axis<T, n>::template ypass<+1>(g, in, out0, out1, tw, st);
+    PHAFD_FOR_SIZES(CASE)
+#undef CASE
+  }
+  return -2;
+}
+
+template <typename T>
+int GridOps<T>::zpass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
+                      const UpdateArgs<T>* u, cudaStream_t st) {
+  UpdateArgs<T> dummy{};
+  switch (g.nz) {
+#define CASE(n)                                                                                   \
+  case n:                                                                                         \
+    if (u) return Axis<T, n>::template zpass<+1, true>(g, in, out0, out1, tw, *u, st);            \
+    return sign < 0 ? Axis<T, n>::template zpass<-1, false>(g, in, out0, out1, tw, dummy, st)     \
+                    : Axis<T, n>::template zpass<+1, false>(g, in, out0, out1, tw, dummy, st);
+    PHAFD_FOR_SIZES(CASE)
+#undef CASE
+  }
+  return -2;
+}
+
+}  // namespace phafd

@@ -1,0 +1,57 @@
+// Internal declarations shared by the translation units of libphafd_gpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "common.cuh"
+#include "../../include/phafd_gpu.h"
+
+namespace phafd {
+
+struct Geom {
+  int nx, ny, nz, nxh;
+  double kq[3];  // 2*3.141592/L per physical axis (domain.cpp:206-208)
+};
+
+struct FHArgs {
+  double tv;   // temp / volFH
+  double chi;
+  unsigned long long* counters;  // [0] phi <= 0 reflections, [1] phi >= 1 reflections
+  int enabled;                   // 0: mu = deposit only (no fix grid/floryhuggins)
+  void* mu_out;                  // optional: materialised chempot (T*)
+};
+
+struct NanArgs {
+  int check;
+  long long* nan_step;
+  const long long* d_step;
+};
+
+template <typename T>
+struct UpdateArgs {
+  const cpx<T>* phi_old;
+  const cpx<T>* mu_hat;
+  cpx<T>* phi_new;
+  const double2* uref;
+  double mobility, tvg, dt, norm, cpref, rpref, sqrtdt, phi_scale, store_scale;
+  double qx, qy, qz;
+  int noise;
+  uint32_t seed;
+  const long long* d_step;
+  int Ny, Nz, Nxh;
+};
+
+template <typename T>
+struct GridOps {
+  static int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
+                  cudaStream_t st);
+  static int xc2r(const Geom& g, const cpx<T>* in, T* out0, T s0, bool mul0, T* out1, T s1, const cpx<T>* tw,
+                  const NanArgs& nan, cudaStream_t st);
+  static int ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
+                   cudaStream_t st);
+  static int zpass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
+                   const UpdateArgs<T>* u, cudaStream_t st);
+};
+
+bool fft_size_supported(int n);
+
+}  // namespace phafd

@@ -1,0 +1,272 @@
+"""ctypes binding of libphafd_gpu.so (the C ABI in include/phafd_gpu.h).
+
+`PhafdGPU` mirrors the reference's input-script commands one method per
+command (input.cpp:48-299).  There is no CPU fallback: if the library is
+missing or fails to load, construction raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libphafd_gpu.so")
+
+FIELD = {"phi": 0, "chempot": 1, "gradx": 2, "grady": 3, "gradz": 4, "ft_phi": 5, "ft_chempot": 6}
+GRIDATOM = {"none": 0, "gaussian": 1, "LJish": 2, "LJish/linear": 3}
+NOISE = {"off": 0, "reference": 1, "philox": 2}
+ZGHOST = {"rank1": 0, "periodic": 1}
+SCHEDULE = {"reference": 0, "resident": 1}
+ERRORS = {-1: "invalid", -2: "cuda", -3: "nan", -4: "overflow", -5: "constraint", -6: "unsupported", -7: "nomem"}
+
+# every symbol declared in include/phafd_gpu.h
+EXPORTS = [
+    "phafd_ctx_create", "phafd_ctx_destroy", "phafd_last_error", "phafd_build_info",
+    "phafd_domain", "phafd_grid_style", "phafd_grid_populate_constant", "phafd_grid_set", "phafd_grid_get",
+    "phafd_set_zghost", "phafd_set_schedule", "phafd_set_keep_chempot",
+    "phafd_atoms_create", "phafd_atoms_get",
+    "phafd_pair_gridatom", "phafd_pair_gridatom_coeff", "phafd_pair_lj_cut",
+    "phafd_neighbor",
+    "phafd_fix_conjugate_volfrac", "phafd_fix_floryhuggins", "phafd_fix_gradphi", "phafd_fix_drag",
+    "phafd_fix_semiflexible",
+    "phafd_set_dt", "phafd_set_timestep", "phafd_setup", "phafd_run", "phafd_counters_get", "phafd_synchronize",
+    "phafd_half_list_size", "phafd_half_list", "phafd_grid_list_size", "phafd_grid_list",
+    "phafd_stage_gradient", "phafd_stage_borders_and_build", "phafd_stage_pairs",
+]
+
+
+class SemiParams(C.Structure):
+    _fields_ = [("bondlength", C.c_double), ("zeta_para", C.c_double), ("zeta_perp", C.c_double),
+                ("bending", C.c_double), ("temp", C.c_double), ("kbond", C.c_double),
+                ("seed", C.c_int), ("noise", C.c_int)]
+
+
+class Counters(C.Structure):
+    _fields_ = [("num_less_zero", C.c_longlong), ("num_great_zero", C.c_longlong),
+                ("neighbor_calls", C.c_longlong), ("timestep", C.c_longlong),
+                ("status", C.c_longlong), ("nan_step", C.c_longlong)]
+
+
+class PhafdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%s)" % (msg, ERRORS.get(code, code)))
+        self.code = code
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load libphafd_gpu.so; raise if it is absent (no fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("libphafd_gpu.so not built: run __graft_entry__.build() (expected %s)" % p)
+    L = C.CDLL(p)
+    dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+    ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+    vp = C.c_void_p
+    sig = {
+        "phafd_ctx_create": [C.POINTER(vp), C.c_int, C.c_int],
+        "phafd_ctx_destroy": [vp],
+        "phafd_set_zghost": [vp, C.c_int],
+        "phafd_set_schedule": [vp, C.c_int],
+        "phafd_set_keep_chempot": [vp, C.c_int],
+        "phafd_domain": [vp, dp, dp],
+        "phafd_grid_style": [vp, C.c_int, C.c_int, C.c_int],
+        "phafd_grid_populate_constant": [vp, C.c_double, C.c_double, C.c_int],
+        "phafd_grid_set": [vp, C.c_int, dp],
+        "phafd_grid_get": [vp, C.c_int, dp],
+        "phafd_atoms_create": [vp, C.c_int, ip, ip, ip, dp],
+        "phafd_atoms_get": [vp, dp, dp, dp, ip],
+        "phafd_pair_gridatom": [vp, C.c_int, C.c_double],
+        "phafd_pair_gridatom_coeff": [vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double],
+        "phafd_pair_lj_cut": [vp, C.c_double, C.c_double, C.c_double],
+        "phafd_neighbor": [vp, C.c_double],
+        "phafd_fix_conjugate_volfrac": [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int],
+        "phafd_fix_floryhuggins": [vp, C.c_double, C.c_double, C.c_double],
+        "phafd_fix_gradphi": [vp, C.c_int],
+        "phafd_fix_drag": [vp, C.c_int, ip, ip, C.c_double],
+        "phafd_fix_semiflexible": [vp, C.c_int, ip, ip, C.POINTER(SemiParams)],
+        "phafd_set_dt": [vp, C.c_double],
+        "phafd_set_timestep": [vp, C.c_longlong],
+        "phafd_setup": [vp],
+        "phafd_run": [vp, C.c_int],
+        "phafd_counters_get": [vp, C.POINTER(Counters)],
+        "phafd_synchronize": [vp],
+        "phafd_half_list_size": [vp, C.POINTER(C.c_longlong)],
+        "phafd_half_list": [vp, ip],
+        "phafd_grid_list_size": [vp, C.POINTER(C.c_longlong)],
+        "phafd_grid_list": [vp, ip],
+        "phafd_stage_gradient": [vp],
+        "phafd_stage_borders_and_build": [vp],
+        "phafd_stage_pairs": [vp],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.phafd_last_error.argtypes = [vp]
+    L.phafd_last_error.restype = C.c_char_p
+    L.phafd_build_info.argtypes = []
+    L.phafd_build_info.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+class PhafdGPU:
+    """One simulation context on one GPU.  precision: 32 or 64."""
+
+    def __init__(self, precision=64, device=0, schedule="resident"):
+        self._L = load()
+        self._c = C.c_void_p()
+        rc = self._L.phafd_ctx_create(C.byref(self._c), device, precision)
+        if rc != 0:
+            raise PhafdError(rc, "phafd_ctx_create failed (device %d)" % device)
+        self.precision = precision
+        self.shape = None
+        self.n = 0
+        self.set_schedule(schedule)
+
+    def close(self):
+        if getattr(self, "_c", None):
+            self._L.phafd_ctx_destroy(self._c)
+            self._c = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _call(self, name, *args):
+        rc = getattr(self._L, name)(self._c, *args)
+        if rc != 0:
+            raise PhafdError(rc, self._L.phafd_last_error(self._c).decode())
+        return rc
+
+    # ---- commands
+    def set_zghost(self, mode):
+        self._call("phafd_set_zghost", ZGHOST[mode])
+
+    def set_schedule(self, schedule):
+        self._call("phafd_set_schedule", SCHEDULE[schedule])
+
+    def set_keep_chempot(self, keep=True):
+        self._call("phafd_set_keep_chempot", int(keep))
+
+    def domain(self, boxlo, period):
+        self._call("phafd_domain", np.asarray(boxlo, np.float64), np.asarray(period, np.float64))
+
+    def grid_style(self, nx, ny, nz):
+        self._call("phafd_grid_style", nx, ny, nz)
+        self.shape = (nz, ny, nx)
+
+    def grid_populate_constant(self, average, variance, seed):
+        self._call("phafd_grid_populate_constant", average, variance, seed)
+
+    def grid_set(self, field, arr):
+        self._call("phafd_grid_set", FIELD[field], np.ascontiguousarray(arr, np.float64).reshape(-1))
+
+    def grid_get(self, field):
+        nz, ny, nx = self.shape
+        if field.startswith("ft_"):
+            out = np.zeros((ny, nz, nx // 2 + 1), np.complex128)
+            self._call("phafd_grid_get", FIELD[field], out.view(np.float64).reshape(-1))
+        else:
+            out = np.zeros(self.shape, np.float64)
+            self._call("phafd_grid_get", FIELD[field], out.reshape(-1))
+        return out
+
+    def atoms_create(self, tags, mol, types, x):
+        self.n = len(tags)
+        self._call("phafd_atoms_create", self.n, np.asarray(tags, np.int32), np.asarray(mol, np.int32),
+                   np.asarray(types, np.int32), np.ascontiguousarray(x, np.float64).reshape(-1))
+
+    def atoms_get(self):
+        n = max(self.n, 1)
+        x = np.zeros((n, 3)); ux = np.zeros((n, 3)); f = np.zeros((n, 3)); im = np.zeros(n, np.int32)
+        self._call("phafd_atoms_get", x.reshape(-1), ux.reshape(-1), f.reshape(-1), im)
+        return x[:self.n], ux[:self.n], f[:self.n], im[:self.n]
+
+    def pair_gridatom(self, style, cut):
+        self._call("phafd_pair_gridatom", GRIDATOM[style], cut)
+
+    def pair_gridatom_coeff(self, t, epsilon=None, nucwidth=None, phi=None):
+        self._call("phafd_pair_gridatom_coeff", t, epsilon is not None, epsilon or 0.0,
+                   nucwidth is not None, nucwidth or 0.0, phi is not None, phi or 0.0)
+
+    def pair_lj_cut(self, cut, eps, sigma):
+        self._call("phafd_pair_lj_cut", cut, eps, sigma)
+
+    def neighbor(self, skin):
+        self._call("phafd_neighbor", skin)
+
+    def fix_conjugate_volfrac(self, seed, mobility=1.0, temp=1.0, volFH=1.0, gamma=1.0, noise="philox"):
+        self._call("phafd_fix_conjugate_volfrac", seed, mobility, temp, volFH, gamma, NOISE[noise])
+
+    def fix_floryhuggins(self, temp=1.0, volFH=1.0, chi=1.0):
+        self._call("phafd_fix_floryhuggins", temp, volFH, chi)
+
+    def fix_gradphi(self, once=False):
+        self._call("phafd_fix_gradphi", int(once))
+
+    def fix_drag(self, ranges, drag):
+        s = np.array([r[0] for r in ranges], np.int32); e = np.array([r[1] for r in ranges], np.int32)
+        self._call("phafd_fix_drag", len(ranges), s, e, drag)
+
+    def fix_semiflexible(self, ranges, bondlength=1.0, zeta_para=1.0, zeta_perp=1.0, bending=0.0,
+                         temp=0.0, kbond=100.0, seed=0, noise="philox"):
+        s = np.array([r[0] for r in ranges], np.int32); e = np.array([r[1] for r in ranges], np.int32)
+        p = SemiParams(bondlength, zeta_para, zeta_perp, bending, temp, kbond, seed, NOISE[noise])
+        self._call("phafd_fix_semiflexible", len(ranges), s, e, C.byref(p))
+
+    def set_dt(self, dt):
+        self._call("phafd_set_dt", dt)
+
+    def set_timestep(self, ts):
+        self._call("phafd_set_timestep", ts)
+
+    def setup(self):
+        self._call("phafd_setup")
+
+    def run(self, nsteps):
+        self._call("phafd_run", nsteps)
+
+    def synchronize(self):
+        self._call("phafd_synchronize")
+
+    def counters(self):
+        c = Counters()
+        self._call("phafd_counters_get", C.byref(c))
+        return {k: getattr(c, k) for k, _ in Counters._fields_}
+
+    # ---- stage hooks / inspection
+    def stage_gradient(self):
+        self._call("phafd_stage_gradient")
+
+    def stage_borders_and_build(self):
+        self._call("phafd_stage_borders_and_build")
+
+    def stage_pairs(self):
+        self._call("phafd_stage_pairs")
+
+    def half_list(self):
+        n = C.c_longlong()
+        self._call("phafd_half_list_size", C.byref(n))
+        out = np.zeros(3 * max(n.value, 1), np.int32)
+        self._call("phafd_half_list", out)
+        return out[:3 * n.value].reshape(n.value, 3)
+
+    def grid_list(self):
+        n = C.c_longlong()
+        self._call("phafd_grid_list_size", C.byref(n))
+        out = np.zeros(3 * max(n.value, 1), np.int32)
+        self._call("phafd_grid_list", out)
+        return out[:3 * n.value].reshape(n.value, 3)
+
+
+def build_info():
+    return load().phafd_build_info().decode()

@@ -1,0 +1,161 @@
+"""CUDA path against the FP64 oracle, through the C ABI (libphafd_gpu.so).
+
+Tolerances: FP64 path 1e-10 relative (field and bead positions), FP32 path
+2e-5 relative on single transforms; neighbor lists bit-exact as sets.
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from phafd_gb300 import workloads as W
+from tests.helpers import canon_grid, canon_half, rel_err, small_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu(precision=64, schedule="resident"):
+    from phafd_gb300.gpu import PhafdGPU
+    return PhafdGPU(precision=precision, schedule=schedule)
+
+
+@pytest.mark.parametrize("precision,tol", [(64, 1e-12), (32, 2e-5)])
+@pytest.mark.parametrize("shape", [(16, 16, 16), (32, 32, 32), (64, 64, 64), (16, 32, 64), (96, 32, 160), (128, 16, 16)])
+def test_gradient_matches_oracle(gpu_lib, precision, tol, shape):
+    nz, ny, nx = shape
+    rng = np.random.default_rng(nx + 7 * ny + 13 * nz)
+    phi = 0.4 + 0.1 * rng.standard_normal(shape)
+    L = [nx * 0.7, ny * 1.1, nz * 0.9]
+    o = Oracle(); g = gpu(precision)
+    for d in (o, g):
+        d.domain([-1.0, -2.0, -3.0], L)
+        d.grid_style(nx, ny, nz)
+        d.grid_set("phi", phi)
+        d.stage_gradient()
+    for f in ("gradx", "grady", "gradz"):
+        assert rel_err(g.grid_get(f), o.grid_get(f)) < tol, f
+
+
+@pytest.mark.parametrize("zghost", ["periodic", "rank1"])
+def test_neighbor_lists_match_oracle_as_sets(gpu_lib, zghost):
+    o = Oracle(); g = gpu(64)
+    for d in (o, g):
+        small_scene(d, n=32, L=32.0, nbeads=600, zghost=zghost, seed=11)
+        d.setup()
+    assert canon_half(g.half_list()) == canon_half(o.half_list())
+    assert canon_grid(g.grid_list()) == canon_grid(o.grid_list())
+
+
+@pytest.mark.parametrize("style", ["gaussian", "LJish", "LJish/linear"])
+def test_pair_forces_and_deposit_match_oracle(gpu_lib, style):
+    o = Oracle(); g = gpu(64)
+    for d in (o, g):
+        small_scene(d, n=32, L=32.0, nbeads=300, style=style, seed=5, amp=0.3)
+        d.setup()
+        d.stage_gradient()
+        d.stage_borders_and_build()
+        d.stage_pairs()
+    _, _, fo, _ = o.atoms_get()
+    _, _, fg, _ = g.atoms_get()
+    assert rel_err(fg, fo) < 1e-12
+    assert rel_err(g.grid_get("chempot"), o.grid_get("chempot")) < 1e-12
+
+
+def _full_scene(d, noise, zghost="periodic", chi=2.5, steps_dt=1e-3):
+    cfg = dict(W.CONFIGS["32cube_64beads"])
+    cfg["field_noise"] = noise
+    cfg["dt"] = steps_dt
+    cfg["bead_temp"] = 1.0 if noise != "off" else 0.0
+    cfg["chi"] = chi
+    W.apply(d, cfg, zghost=zghost)
+    return cfg
+
+
+@pytest.mark.parametrize("schedule", ["reference", "resident"])
+@pytest.mark.parametrize("noise", ["off", "reference", "philox"])
+def test_fp64_steps_match_oracle(gpu_lib, schedule, noise):
+    o = Oracle(); g = gpu(64, schedule)
+    for d in (o, g):
+        _full_scene(d, noise)
+        d.setup()
+        d.run(30)
+    xo, uxo, fo, imo = o.atoms_get()
+    xg, uxg, fg, img = g.atoms_get()
+    assert np.array_equal(imo, img)
+    assert rel_err(g.grid_get("phi"), o.grid_get("phi")) < 1e-10
+    assert np.abs(xg - xo).max() < 1e-10 * np.abs(xo).max()
+    assert np.abs(uxg - uxo).max() < 1e-10 * np.abs(uxo).max()
+    assert rel_err(fg, fo) < 1e-9
+    co, cg = o.counters(), g.counters()
+    assert cg["neighbor_calls"] == co["neighbor_calls"]
+    assert (cg["num_less_zero"], cg["num_great_zero"]) == (co["num_less_zero"], co["num_great_zero"])
+
+
+@pytest.mark.parametrize("zghost", ["rank1", "periodic"])
+def test_fp64_drag_fix_matches_oracle(gpu_lib, zghost):
+    o = Oracle(); g = gpu(64, "reference")
+    for d in (o, g):
+        cfg = dict(W.CONFIGS["32cube_64beads"])
+        W.apply(d, cfg, semiflexible=False, drag=1.0, zghost=zghost)
+        d.setup()
+        d.run(25)
+    xo, *_ = o.atoms_get()
+    xg, *_ = g.atoms_get()
+    assert np.abs(xg - xo).max() < 1e-10 * np.abs(xo).max()
+    assert rel_err(g.grid_get("phi"), o.grid_get("phi")) < 1e-10
+
+
+def test_fp32_path_error_against_oracle(gpu_lib):
+    """FP32 production path vs the FP64 oracle: max |dphi| and S(k)."""
+    o = Oracle(); g = gpu(32, "resident")
+    for d in (o, g):
+        _full_scene(d, "philox")
+        d.setup()
+        d.run(30)
+    po, pg = o.grid_get("phi"), g.grid_get("phi")
+    assert np.abs(pg - po).max() < 1e-4
+    sk_o = np.abs(np.fft.rfftn(po)) ** 2
+    sk_g = np.abs(np.fft.rfftn(pg)) ** 2
+    k = np.sqrt(sum(np.meshgrid(*(np.fft.fftfreq(32) if i < 2 else np.fft.rfftfreq(32) for i in range(3)),
+                                indexing="ij")[i] ** 2 for i in range(3)))
+    shells = np.minimum((k * 32).astype(int), 16)
+    so = np.bincount(shells.ravel(), sk_o.ravel())[1:]
+    sg = np.bincount(shells.ravel(), sk_g.ravel())[1:]
+    assert np.max(np.abs(sg - so) / so) < 1e-4
+
+
+def test_fp32_mass_mode_exact(gpu_lib):
+    g = gpu(32, "resident")
+    _full_scene(g, "philox")
+    g.setup()
+    m0 = g.grid_get("ft_phi")[0, 0, 0]
+    g.run(40)
+    assert g.grid_get("ft_phi")[0, 0, 0] == m0
+
+
+def test_nan_is_reported(gpu_lib):
+    g = gpu(64, "resident")
+    cfg = dict(W.CONFIGS["32cube_64beads"])
+    W.apply(g, cfg)
+    phi = np.full((32, 32, 32), 0.5)
+    phi[3, 4, 5] = np.nan
+    g.grid_set("phi", phi)
+    g.setup()
+    from phafd_gb300.gpu import PhafdError
+    with pytest.raises(PhafdError, match="NAN"):
+        g.run(2)
+
+
+def test_neighbor_overflow_is_reported(gpu_lib):
+    g = gpu(64)
+    g.domain([0.0] * 3, [16.0] * 3)
+    g.grid_style(16, 16, 16)
+    g.grid_populate_constant(0.5, 0.0, 1)
+    rng = np.random.default_rng(0)
+    x = 8.0 + 0.4 * rng.random((200, 3))  # 200 beads inside one cutoff sphere
+    n = len(x)
+    g.atoms_create(np.arange(1, n + 1), np.zeros(n), np.zeros(n), x)
+    g.pair_lj_cut(2 ** (1 / 6), 1.0, 1.0)
+    g.neighbor(0.3)
+    from phafd_gb300.gpu import PhafdError
+    with pytest.raises(PhafdError, match="overflow"):
+        g.setup()
