@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Throughput of the particle-field step on GB300.
+
+Workload: 256^3 grid (box 256, spacing 1) + 64 semiflexible chains x 500
+beads = 32,000 beads, kT = 1, dt = 1e-4 (synthetic, seeded; no dataset).
+A "step" is one full timestep of the hot path: neighbor check/rebuild,
+lj/cut + gridatom/gaussian pair forces and mu deposit, chain integration,
+Flory-Huggins mu, r2c(mu), Model-B update with conserved noise, c2r to phi
+and grad phi.  Grid arithmetic FP32, bead positions FP64.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+N > 1 runs under torchrun: every rank advances an independent replica (its
+own seeds) on its own GPU with no data-path collective ("replicas only");
+value = steps of all ranks / max-over-ranks time.
+
+--impl reference times the reference's CPU algorithm (the FP64 oracle
+restatement: the reference itself cannot be built here) on the same
+workload, rank 0 only.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "steps/s at 256^3 grid+32k beads, fraction of HBM roofline; learned vs plain"
+WORKLOAD = "256cube_32kbeads"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default=WORKLOAD)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--profile-steps", type=int, default=5)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = []
+        smax = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def stage_bytes(cfg, s):
+    """Compulsory HBM bytes of each stage of the resident step, per step.
+    N real nodes, Nc complex modes, s bytes per real (4 in FP32)."""
+    n = cfg["n"]
+    N = n ** 3
+    Nc = (n // 2 + 1) * n * n
+    return {
+        "x_r2c_fh": 2 * s * N + 2 * s * Nc,   # read phi, deposit; write x-transformed mu
+        "y_fft": 4 * s * Nc,                  # read + write one spectrum
+        "z_fft": 4 * s * Nc,
+        "z_update_ifft": 10 * s * Nc,         # read mu_hat, phi_hat; write phi_hat', A, B
+        "y_ifft": 10 * s * Nc,                # read A, B; write C, D, E
+        "x_c2r": 6 * s * Nc + 4 * s * N,     # read C, D, E; write phi, dphi/dx, dphi/dy, dphi/dz
+    }
+
+
+def ncu_traffic():
+    """DRAM bytes per step of each stage from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "ncu_dram_bytes_256cube.txt")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            parts = line.split()
+            if len(parts) == 2 and not line.startswith("#"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
+def make_chains(cfg, rank):
+    from phafd_gb300 import workloads as W
+    return W.random_walk_chains(cfg["nchains"], cfg["chain_len"], cfg["origin"], cfg["L"],
+                                cfg["chain_seed"] + 1000 * rank, cfg["bond"])
+
+
+def replica_cfg(cfg, rank):
+    c = dict(cfg)
+    c["grid_seed"] = cfg["grid_seed"] + 1000 * rank
+    c["chain_seed"] = cfg["chain_seed"] + 1000 * rank
+    return c
+
+
+def cpu_baseline_oracle(cfg, chains, nsteps):
+    """The reference's algorithm (FP64 oracle restatement, one core) on a
+    bounded sample of the workload: set-up untimed, then `nsteps` steps."""
+    from oracle.oracle import Oracle
+    from phafd_gb300 import workloads as W
+    o = Oracle()
+    W.apply(o, cfg, chains=chains)
+    o.setup()
+    t0 = time.perf_counter()
+    o.run(nsteps)
+    dt = time.perf_counter() - t0
+    return nsteps / dt, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from phafd_gb300 import workloads as W
+    from oracle import build as OB
+    OB.build()
+    cfg = replica_cfg(W.CONFIGS[args.workload], 0)
+    chains = make_chains(cfg, 0)
+    timed = max(1, min(args.steps, 3))
+    warm = 1 if args.warmup > 0 else 0
+    from oracle.oracle import Oracle
+    o = Oracle()
+    W.apply(o, cfg, chains=chains)
+    o.setup()
+    if warm:
+        o.run(warm)
+    t0 = time.perf_counter()
+    o.run(timed)
+    dt = time.perf_counter() - t0
+    v = timed / dt
+    sample = "%d timed steps of %s after set-up and %d warm-up step(s); FP64 oracle restatement of the reference's one-rank CPU path" % (timed, args.workload, warm)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": timed, "warmup": warm, "ms_per_step": 1000.0 * dt / timed, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "grid": [cfg["n"]] * 3, "beads": W.nbeads(cfg),
+                   "parallelism": "1 process, 1 thread"},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    rank, world, local = dist_env()
+    import numpy as np
+    from phafd_gb300 import build as B
+    B.build()
+    from phafd_gb300 import workloads as W
+    from phafd_gb300.gpu import PhafdGPU
+
+    torch_dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        torch_dist = dist
+
+    def barrier():
+        if torch_dist:
+            torch_dist.barrier()
+
+    def max_over_ranks(v):
+        if not torch_dist:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        torch_dist.all_reduce(t, op=torch_dist.ReduceOp.MAX)
+        return float(t.item())
+
+    cfg = replica_cfg(W.CONFIGS[args.workload], rank)
+    chains = make_chains(cfg, rank)
+    g = PhafdGPU(precision=32, device=local, schedule="resident")
+    W.apply(g, cfg, chains=chains)
+    g.setup()
+    g.run(max(args.warmup, 3))
+
+    # stage profile (eager steps with events between stages; not the timed region)
+    prof = g.profile_stages(args.profile_steps)
+    g.run(2)
+
+    sampler = ClockSampler(local)
+    barrier()
+    g.synchronize()
+    sampler.start()
+    ms = g.run_timed(args.steps)
+    g.synchronize()
+    clocks = sampler.stop()
+    barrier()
+    ms_max = max_over_ranks(ms)
+    counters = g.counters()
+
+    value = world * args.steps / (ms_max / 1000.0)
+    peak, peak_kind = measured_peak()
+    s = 4
+    sb = stage_bytes(cfg, s)
+    grid_stages = {k: prof[k] for k in sb}
+    dom = max(grid_stages, key=grid_stages.get)
+    achieved = sb[dom] / (prof[dom] / 1000.0) / 1e9
+    traffic = ncu_traffic().get(dom)
+    bstep = W.algorithmic_bytes_per_step(cfg, s)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": sb[dom], "launch_ms": prof[dom]}
+    step_roofline = {"bytes_per_step": bstep, "achieved": bstep / (ms_max / args.steps / 1000.0) / 1e9,
+                     "peak": peak, "unit": "GB/s"}
+    step_roofline["frac"] = step_roofline["achieved"] / peak
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "grid": [cfg["n"]] * 3, "beads": W.nbeads(cfg),
+                   "schedule": "resident", "bead_positions": "f64",
+                   "parallelism": "replicas x%d" % world,
+                   "l2": "working set ~0.9 GB > 129 MB L2 (no flush needed)"},
+        "roofline": roofline,
+        "step_roofline": step_roofline,
+        "stage_ms": prof,
+        "clocks": clocks,
+        "gpu_launches": int(counters.get("kernels_per_step", 0)) * args.steps if counters.get("kernels_per_step") else None,
+        "neighbor_calls": counters["neighbor_calls"],
+    }
+
+    # end to end through the public C ABI with host buffers: upload the
+    # state from host memory, then per step one phafd_run(ctx, 1) and a read
+    # of the step's bead result (x, ux, F, images); finally read phi back
+    if not args.no_e2e:
+        k = max(10, min(args.steps, 100))
+        phi_host = np.ascontiguousarray(g.grid_get("phi"))
+        xs = chains[0]
+        e = PhafdGPU(precision=32, device=local, schedule="resident")
+        t0 = time.perf_counter()
+        W.apply(e, cfg, chains=chains)
+        e.grid_set("phi", phi_host)
+        e.setup()
+        for _ in range(k):
+            e.run(1)
+            e.atoms_get()
+        out = e.grid_get("phi")
+        t1 = time.perf_counter()
+        nb = W.nbeads(cfg)
+        h2d = (phi_host.size * 4 + xs.size * 8 + nb * 12) / k
+        d2h = nb * (3 * 8 * 3 + 4) + out.size * 4 / k
+        e2e_v = world * k / max_over_ranks(t1 - t0)
+        line["e2e"] = {"value": e2e_v, "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
+                       "d2h_bytes_per_step": int(d2h),
+                       "note": "state uploaded once from host arrays, %d steps each followed by a bead read, phi read at the end; includes set-up" % k}
+        e.close()
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, dt = cpu_baseline_oracle(cfg, chains, 3)
+        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                                "sample": "3 steps of %s (FP64 oracle restatement, one core) after its set-up" % args.workload}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    if torch_dist:
+        torch_dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -89,6 +89,7 @@ typedef struct phafd_counters {
   long long timestep;        /* Integrate::timestep                                    */
   long long status;          /* sticky PHAFD_ERR_* raised on the device, 0 if none     */
   long long nan_step;        /* first step whose phi(0,0,0) was NaN, -1 if none        */
+  long long kernels_per_step; /* kernel launches of one step in the captured graph, 0 before capture */
 } phafd_counters;
 
 typedef struct phafd_ctx phafd_ctx;
@@ -138,6 +139,12 @@ int phafd_setup(phafd_ctx* ctx);                                  /* Integrate::
 int phafd_run(phafd_ctx* ctx, int nsteps);                        /* Integrate::run, integrate.cpp:90-219 */
 int phafd_counters_get(phafd_ctx* ctx, phafd_counters* out);      /* Integrate::finalise counters, integrate.cpp:418-443 */
 int phafd_synchronize(phafd_ctx* ctx);
+int phafd_run_timed(phafd_ctx* ctx, int nsteps, double* ms);      /* run, timed by CUDA events on the context's stream */
+/* per-stage device time over `nsteps` eager steps (events between stage
+ * groups): 0 gradient (reference schedule), 1 neighbor, 2 pairs, 3 bead
+ * integration, 4 x r2c + Flory-Huggins, 5 y fft, 6 z fft, 7 z pass with the
+ * Model-B update, 8 y ifft, 9 x c2r; stage_ms has nstage entries */
+int phafd_profile_stages(phafd_ctx* ctx, int nsteps, double* stage_ms, int nstage);
 
 /* ---- neighbor-list export (NeighList ilist/firstneigh, neigh_list.hpp) ----
  * half list: (tag_i, tag_j, image code of j relative to i)

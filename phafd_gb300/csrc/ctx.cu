@@ -138,6 +138,17 @@ struct phafd_ctx {
   // graph
   cudaGraphExec_t gexec = nullptr;
   bool eager_done = false;
+  long long kernels_per_step = 0;
+  // stage profiling (eager steps only): event after each stage group
+  bool profiling = false;
+  std::vector<std::pair<int, cudaEvent_t>> marks;
+  void mark(int stage) {
+    if (!profiling) return;
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    CK(cudaEventRecord(e, st));
+    marks.push_back({stage, e});
+  }
 
   ~phafd_ctx() {
     if (gexec) cudaGraphExecDestroy(gexec);
@@ -226,8 +237,11 @@ struct phafd_ctx {
   void r2c(const T* in, const T* depp, cpx<T>* out, const FHArgs& fh) {
     const cpx<T>* twf[3] = {tw[0][0].as<cpx<T>>(), tw[1][0].as<cpx<T>>(), tw[2][0].as<cpx<T>>()};
     chk(GridOps<T>::xr2c(geom, in, depp, out, twf[0], fh, st), "x r2c");
+    mark(4);
     chk(GridOps<T>::ypass(geom, -1, out, out, nullptr, twf[1], st), "y fft");
+    mark(5);
     chk(GridOps<T>::zpass(geom, -1, out, out, nullptr, twf[2], nullptr, st), "z fft");
+    mark(6);
   }
 
   // from a spectrum S (z-ifft input) produce phi (scale sp, optional) and grad (scale sg)
@@ -242,8 +256,10 @@ struct phafd_ctx {
     NanArgs nan{nan_check ? 1 : 0, d_nan(), d_step()};
     NanArgs nonan{0, d_nan(), d_step()};
     chk(GridOps<T>::zpass(geom, +1, S, A, grad ? B : nullptr, twi[2], u, st), "z ifft");
+    mark(7);
     chk(GridOps<T>::ypass(geom, +1, A, Cc, grad ? D : nullptr, twi[1], st), "y ifft");
     if (grad) chk(GridOps<T>::ypass(geom, +1, B, E, nullptr, twi[1], st), "y ifft");
+    mark(8);
     if (phi_out && grad) {
       chk(GridOps<T>::xc2r(geom, Cc, phi_out, sp, false, gx.as<T>(), sg, twi[0], nan, st), "x c2r");
     } else if (phi_out) {
@@ -255,6 +271,7 @@ struct phafd_ctx {
       chk(GridOps<T>::xc2r(geom, D, gy.as<T>(), sg, false, nullptr, sg, twi[0], nonan, st), "x c2r");
       chk(GridOps<T>::xc2r(geom, E, gz.as<T>(), sg, false, nullptr, sg, twi[0], nonan, st), "x c2r");
     }
+    mark(9);
   }
 
   // ------------------------------------------------------------------ beads
@@ -415,19 +432,24 @@ struct phafd_ctx {
 
   template <typename T>
   void enqueue_step() {
+    mark(-1);
     launch_step_begin(d_step(), st);
     const bool resident = schedule == PHAFD_SCHEDULE_RESIDENT && have_conj;
     // fixgrid_gradphi.cpp:45: "once" tests timestep == firststep after the
     // increment, which never holds inside a run: only "every" recomputes
     if (!resident && (have_conj || (have_gradphi && !gradphi_once))) gradient_from_phi<T>();
+    mark(0);
     // neighbor
     if (n > 0) launch_neighbor(ba, false, st);
+    mark(1);
     // pairs (computed once: the reference's second pass reproduces the first, integrate.cpp:140-146)
     PairArgs<T> pa = pair_args<T>();
     if (n > 0 && (have_lj || ga_style != PHAFD_GRIDATOM_NONE)) launch_pair<T>(ba, pa, st);
+    mark(2);
     // initial_integrate
     launch_drag(ba, dt, st);
     launch_chain_half(ba, 0, dt, st);
+    mark(3);
     if (have_conj) {
       FHArgs fh{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
       // post_force + pre_final_integrate: mu = dep + FH(phi), r2c
@@ -446,6 +468,7 @@ struct phafd_ctx {
     }
     launch_drag(ba, dt, st);
     launch_chain_half(ba, 1, dt, st);
+    mark(3);
   }
 
   void step_once() {
@@ -915,6 +938,17 @@ int phafd_run(phafd_ctx* c, int nsteps) {
         c->step_once();
         if (resident) { resident_spectrum_flip(c); c->step_once(); resident_spectrum_flip(c); }
         CK(cudaStreamEndCapture(c->st, &g));
+        size_t nnodes = 0;
+        CK(cudaGraphGetNodes(g, nullptr, &nnodes));
+        std::vector<cudaGraphNode_t> nodes(nnodes);
+        if (nnodes) CK(cudaGraphGetNodes(g, nodes.data(), &nnodes));
+        long long nk = 0;
+        for (auto nd : nodes) {
+          cudaGraphNodeType ty;
+          CK(cudaGraphNodeGetType(nd, &ty));
+          if (ty == cudaGraphNodeTypeKernel) ++nk;
+        }
+        c->kernels_per_step = nk / (resident ? 2 : 1);
         CK(cudaGraphInstantiate(&c->gexec, g, 0));
         cudaGraphDestroy(g);
       }
@@ -938,6 +972,62 @@ int phafd_run(phafd_ctx* c, int nsteps) {
   API_END(c)
 }
 
+int phafd_run_timed(phafd_ctx* c, int nsteps, double* ms) {
+  API_BEGIN(c)
+  CK(cudaSetDevice(c->device));
+  if (!c->setup_done) {
+    int rc = phafd_setup(c);
+    if (rc) return rc;
+  }
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaEventRecord(e0, c->st));
+  int rc = phafd_run(c, nsteps);
+  CK(cudaEventRecord(e1, c->st));
+  CK(cudaEventSynchronize(e1));
+  float f = 0;
+  CK(cudaEventElapsedTime(&f, e0, e1));
+  *ms = f;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  API_END(c)
+}
+
+int phafd_profile_stages(phafd_ctx* c, int nsteps, double* stage_ms, int nstage) {
+  API_BEGIN(c)
+  CK(cudaSetDevice(c->device));
+  if (!c->setup_done) {
+    int rc = phafd_setup(c);
+    if (rc) return rc;
+  }
+  if (c->have_conj && c->c_noise == PHAFD_NOISE_REFERENCE) throw std::runtime_error("profiling needs device noise");
+  for (int k = 0; k < nstage; ++k) stage_ms[k] = 0.0;
+  const bool resident = c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj;
+  for (int s = 0; s < nsteps; ++s) {
+    c->profiling = true;
+    c->step_once();
+    c->profiling = false;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->st));
+    for (size_t k = 1; k < c->marks.size(); ++k) {
+      float f = 0;
+      CK(cudaEventElapsedTime(&f, c->marks[k - 1].second, c->marks[k].second));
+      const int id = c->marks[k].first;
+      if (id >= 0 && id < nstage) stage_ms[id] += f;
+    }
+    for (auto& m : c->marks) cudaEventDestroy(m.second);
+    c->marks.clear();
+    c->timestep += 1;
+    if (resident) resident_spectrum_flip(c);
+  }
+  int rc = check_status(c);
+  if (rc) return rc;
+  API_END(c)
+}
+
 int phafd_synchronize(phafd_ctx* c) {
   API_BEGIN(c)
   CK(cudaStreamSynchronize(c->st));
@@ -955,6 +1045,7 @@ int phafd_counters_get(phafd_ctx* c, phafd_counters* out) {
   out->nan_step = h[3];
   out->neighbor_calls = h[4];
   out->status = ((int*)&h[5])[1];
+  out->kernels_per_step = c->kernels_per_step;
   API_END(c)
 }
 

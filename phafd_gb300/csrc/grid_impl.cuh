@@ -16,6 +16,9 @@
 //   y / z / x : the spectral derivative i*dq*m (fixgrid_conjugate.cpp:80-105)
 //   x-inverse : the 1/N of the gradient and the NaN check of phi(0,0,0)
 #pragma once
+#include <mutex>
+#include <unordered_map>
+
 #include "fft.cuh"
 #include "internal.h"
 
@@ -287,11 +290,15 @@ k_zpass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
 // kernel so that graph capture never sees the attribute call.
 template <typename Kern>
 static int set_smem(Kern k, size_t bytes) {
-  static size_t done = 0;
-  if (bytes > 48 * 1024 && bytes > done) {
+  if (bytes <= 48 * 1024) return 0;
+  static std::mutex mu;
+  static std::unordered_map<const void*, size_t> done;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& d = done[reinterpret_cast<const void*>(k)];
+  if (bytes > d) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return -1;
-    done = bytes;
+    d = bytes;
   }
   return 0;
 }

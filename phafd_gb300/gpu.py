@@ -30,6 +30,7 @@ EXPORTS = [
     "phafd_fix_conjugate_volfrac", "phafd_fix_floryhuggins", "phafd_fix_gradphi", "phafd_fix_drag",
     "phafd_fix_semiflexible",
     "phafd_set_dt", "phafd_set_timestep", "phafd_setup", "phafd_run", "phafd_counters_get", "phafd_synchronize",
+    "phafd_run_timed", "phafd_profile_stages",
     "phafd_half_list_size", "phafd_half_list", "phafd_grid_list_size", "phafd_grid_list",
     "phafd_stage_gradient", "phafd_stage_borders_and_build", "phafd_stage_pairs",
 ]
@@ -44,7 +45,7 @@ class SemiParams(C.Structure):
 class Counters(C.Structure):
     _fields_ = [("num_less_zero", C.c_longlong), ("num_great_zero", C.c_longlong),
                 ("neighbor_calls", C.c_longlong), ("timestep", C.c_longlong),
-                ("status", C.c_longlong), ("nan_step", C.c_longlong)]
+                ("status", C.c_longlong), ("nan_step", C.c_longlong), ("kernels_per_step", C.c_longlong)]
 
 
 class PhafdError(RuntimeError):
@@ -96,6 +97,8 @@ def load(path=None):
         "phafd_run": [vp, C.c_int],
         "phafd_counters_get": [vp, C.POINTER(Counters)],
         "phafd_synchronize": [vp],
+        "phafd_run_timed": [vp, C.c_int, C.POINTER(C.c_double)],
+        "phafd_profile_stages": [vp, C.c_int, dp, C.c_int],
         "phafd_half_list_size": [vp, C.POINTER(C.c_longlong)],
         "phafd_half_list": [vp, ip],
         "phafd_grid_list_size": [vp, C.POINTER(C.c_longlong)],
@@ -237,6 +240,21 @@ class PhafdGPU:
 
     def synchronize(self):
         self._call("phafd_synchronize")
+
+    def run_timed(self, nsteps):
+        """Run `nsteps` steps; return device milliseconds (CUDA events on
+        the library's stream)."""
+        ms = C.c_double()
+        self._call("phafd_run_timed", nsteps, C.byref(ms))
+        return ms.value
+
+    STAGES = ["gradient", "neighbor", "pairs", "bead_integrate", "x_r2c_fh", "y_fft", "z_fft",
+              "z_update_ifft", "y_ifft", "x_c2r"]
+
+    def profile_stages(self, nsteps):
+        out = np.zeros(len(self.STAGES))
+        self._call("phafd_profile_stages", nsteps, out, len(out))
+        return dict(zip(self.STAGES, (out / nsteps).tolist()))
 
     def counters(self):
         c = Counters()

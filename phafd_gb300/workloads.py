@@ -78,28 +78,39 @@ def random_walk_chains(nchains, length, boxlo, L, seed, bond=1.0, min_sep=1.0, m
 
     xs = []
     for c in range(nchains):
-        for attempt in range(max_tries):
-            start = boxlo + rng.random(3) * L
-            if ok(start, ()):
-                break
-        chain = [start]
-        idx0 = len(xs)
-        buckets.setdefault(key(start), []).append((idx0, start))
-        xs.append(start)
-        for b in range(1, length):
-            prev = chain[-1]
+        for restart in range(max_tries):
+            idx0 = len(xs)
             for attempt in range(max_tries):
-                v = rng.standard_normal(3)
-                v /= np.linalg.norm(v)
-                p = prev + bond * v
-                # unit bond length to round-off
-                if ok(p, {len(xs) - 1}):
+                start = boxlo + rng.random(3) * L
+                if ok(start, ()):
                     break
-            else:
-                raise RuntimeError("could not grow a self-avoiding chain")
-            chain.append(p)
-            buckets.setdefault(key(p), []).append((len(xs), p))
-            xs.append(p)
+            chain = [start]
+            buckets.setdefault(key(start), []).append((idx0, start))
+            xs.append(start)
+            grown = True
+            for b in range(1, length):
+                prev = chain[-1]
+                for attempt in range(max_tries):
+                    v = rng.standard_normal(3)
+                    v /= np.linalg.norm(v)
+                    p = prev + bond * v
+                    if ok(p, {len(xs) - 1}):
+                        break
+                else:
+                    grown = False
+                    break
+                chain.append(p)
+                buckets.setdefault(key(p), []).append((len(xs), p))
+                xs.append(p)
+            if grown:
+                break
+            # trapped: remove this chain and grow it again from a new start
+            for idx in range(idx0, len(xs)):
+                kk = key(xs[idx])
+                buckets[kk] = [e for e in buckets[kk] if e[0] != idx]
+            del xs[idx0:]
+        else:
+            raise RuntimeError("could not grow a self-avoiding chain")
     x = np.array(xs, dtype=np.float64)
     n = len(x)
     tags = np.arange(1, n + 1, dtype=np.int32)
