@@ -19,7 +19,7 @@ import numpy as np
 _COMMON = dict(
     lj_cut=2.0 ** (1.0 / 6.0), lj_eps=1.0, lj_sigma=1.0,
     ga_style="gaussian", ga_cut=1.0, ga_eps=1.0, ga_width=1.0, ga_phi=0.1,
-    gamma=1.0, mobility=1.0, temp=1.0, volFH=1.0,
+    gamma=1.0, mobility=1.0, temp=1.0, volFH=1.0, field_temp=0.01,
     bond=1.0, kbond=100.0, bending=10.0, zeta=1.0,
     dt=1e-4, skin=0.3, amp=0.02,
 )
@@ -145,8 +145,15 @@ def apply(driver, cfg, chains=None, semiflexible=True, drag=None, zghost="period
                                 seed=cfg["chain_seed"] + 100, noise="philox" if cfg["bead_temp"] > 0 else "off")
     if drag is not None:
         driver.fix_drag(ranges, drag)
-    driver.fix_conjugate_volfrac(cfg["grid_seed"] + 10, mobility=cfg["mobility"], temp=cfg["temp"],
-                                 volFH=cfg["volFH"], gamma=cfg["gamma"], noise=cfg["field_noise"])
+    # The conjugate fix's temp sets both the conserved-noise amplitude and the
+    # gradient coefficient kappa = temp/volFH*gamma (conjugate_volfrac.cpp:80-108).
+    # The noise runs at field_temp while gamma is rescaled so that kappa keeps
+    # its value temp/volFH*gamma: at field temp 1 on a unit-spacing grid the
+    # explicit update is driven through the Flory-Huggins log singularity
+    # within a few dozen steps of dt = 1e-4.
+    driver.fix_conjugate_volfrac(cfg["grid_seed"] + 10, mobility=cfg["mobility"], temp=cfg["field_temp"],
+                                 volFH=cfg["volFH"], gamma=cfg["gamma"] * cfg["temp"] / cfg["field_temp"],
+                                 noise=cfg["field_noise"])
     driver.fix_floryhuggins(temp=cfg["temp"], volFH=cfg["volFH"], chi=cfg["chi"])
     driver.set_dt(cfg["dt"])
     return chains

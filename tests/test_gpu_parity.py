@@ -60,7 +60,7 @@ def test_pair_forces_and_deposit_match_oracle(gpu_lib, style):
     assert rel_err(g.grid_get("chempot"), o.grid_get("chempot")) < 1e-12
 
 
-def _full_scene(d, noise, zghost="periodic", chi=2.5, steps_dt=1e-3):
+def _full_scene(d, noise, zghost="periodic", chi=2.5, steps_dt=5e-4):
     cfg = dict(W.CONFIGS["32cube_64beads"])
     cfg["field_noise"] = noise
     cfg["dt"] = steps_dt
@@ -159,3 +159,25 @@ def test_neighbor_overflow_is_reported(gpu_lib):
     from phafd_gb300.gpu import PhafdError
     with pytest.raises(PhafdError, match="overflow"):
         g.setup()
+
+
+def test_64cube_200beads_1000_steps_fp64(gpu_lib):
+    """The FP64 parity workload: 64^3 grid, one 200-bead chain, noise off,
+    1000 steps of dt = 1e-4: per-node phi and per-bead positions within 1e-10
+    relative of the oracle, total concentration conserved."""
+    cfg = W.CONFIGS["64cube_200beads"]
+    o = Oracle(); g = gpu(64, "resident")
+    chains = None
+    for d in (o, g):
+        chains = W.apply(d, cfg, chains=chains)
+        d.setup()
+    m0 = o.grid_get("phi").sum()
+    for d in (o, g):
+        d.run(cfg["steps"])
+    po, pg = o.grid_get("phi"), g.grid_get("phi")
+    xo, uxo, _, _ = o.atoms_get()
+    xg, uxg, _, _ = g.atoms_get()
+    assert rel_err(pg, po) < 1e-10
+    assert np.abs(uxg - uxo).max() < 1e-10 * np.abs(uxo).max()
+    assert np.abs(xg - xo).max() < 1e-10 * np.abs(xo).max()
+    assert abs(pg.sum() - m0) < 1e-10 * abs(m0)
