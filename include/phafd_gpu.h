@@ -160,6 +160,22 @@ int phafd_stage_gradient(phafd_ctx* ctx);          /* FixGridConjugate::start_of
 int phafd_stage_borders_and_build(phafd_ctx* ctx); /* Domain::pbc + CommBrick::borders + Neighbor::build */
 int phafd_stage_pairs(phafd_ctx* ctx);             /* Fs = 0, chempot = 0, pair->compute(), reverse_comm */
 
+/* ---- allocation-free gradient (no counterpart in the reference) ----
+ * grad phi of a device-resident phi for callers that cannot allocate device
+ * memory inside a time step (a host code that owns the device heap, or one
+ * that forbids cudaMalloc/cudaFree mid-step because they synchronise the
+ * device).  phi, gradx, grady, gradz are caller-owned device arrays
+ * [z][y][x] of FP64; period is a host array of the three box lengths;
+ * stream is a cudaStream_t (NULL = default stream).  Same result as
+ * phafd_stage_gradient (fixgrid_gradphi.cpp:42-99).  The scratch spectra
+ * live in a fixed 6.5 MB device array inside the library, so every axis must
+ * be 16, 32 or 64 points (larger: PHAFD_ERR_UNSUPPORTED, nothing done).  All
+ * calls share that array: calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's device address; make it before any
+ * stream capture on that device.  Allocates no device memory. */
+int phafd_gradphi_noalloc(const double* phi, double* gradx, double* grady, double* gradz, int nx, int ny, int nz,
+                          const double* period, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libphafd_gpu.so")
 EXE = os.path.join(OUT, "phafd_gpu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
-CU_SOURCES = ["ctx.cu", "bead_kernels.cu", "grid_f32.cu", "grid_f64.cu"]
+CU_SOURCES = ["ctx.cu", "bead_kernels.cu", "grid_f32.cu", "grid_f64.cu", "noalloc.cu"]
 
 
 def nvcc():

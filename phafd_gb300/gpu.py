@@ -33,6 +33,7 @@ EXPORTS = [
     "phafd_run_timed", "phafd_profile_stages",
     "phafd_half_list_size", "phafd_half_list", "phafd_grid_list_size", "phafd_grid_list",
     "phafd_stage_gradient", "phafd_stage_borders_and_build", "phafd_stage_pairs",
+    "phafd_gradphi_noalloc",
 ]
 
 
@@ -115,6 +116,8 @@ def load(path=None):
     L.phafd_last_error.restype = C.c_char_p
     L.phafd_build_info.argtypes = []
     L.phafd_build_info.restype = C.c_char_p
+    L.phafd_gradphi_noalloc.argtypes = [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, dp, vp]
+    L.phafd_gradphi_noalloc.restype = C.c_int
     _lib = L
     return L
 
