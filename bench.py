@@ -126,8 +126,7 @@ def stage_bytes(cfg, s):
     return {
         "x_r2c_fh": 2 * s * N + 2 * s * Nc,   # read phi, deposit; write x-transformed mu
         "y_fft": 4 * s * Nc,                  # read + write one spectrum
-        "z_fft": 4 * s * Nc,
-        "z_update_ifft": 10 * s * Nc,         # read mu_hat, phi_hat; write phi_hat', A, B
+        "z_update_ifft": 10 * s * Nc,         # read mu (x,y done), phi_hat; write phi_hat', A, B
         "y_ifft": 10 * s * Nc,                # read A, B; write C, D, E
         "x_c2r": 6 * s * Nc + 4 * s * N,     # read C, D, E; write phi, dphi/dx, dphi/dy, dphi/dz
     }

@@ -136,24 +136,41 @@ __global__ void k_scan_block(BeadArgs a) {
   if (i < a.nbins) a.bin_start[i] = incl - v + warp_sums[w];
 }
 
+// exclusive scan of the per-block sums: one block of 1024 threads, each
+// thread owning a contiguous chunk of the sums
 __global__ void k_scan_sums(BeadArgs a, int nblocks) {
   if (!*a.flag) return;
-  // single warp, sequential over chunks of 32
-  const int lane = threadIdx.x;
-  int carry = 0;
-  for (int c = 0; c < nblocks; c += 32) {
-    const int idx = c + lane;
-    int v = idx < nblocks ? a.scan_tmp[idx] : 0;
-    int incl = v;
+  __shared__ int warp_sums[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int chunk = (nblocks + 1023) / 1024;
+  const int b0 = t * chunk, b1 = min(b0 + chunk, nblocks);
+  int local = 0;
+  for (int b = b0; b < b1; ++b) local += a.scan_tmp[b];
+  int incl = local;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    int v = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += v;
+  }
+  if (lane == 31) warp_sums[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int s = warp_sums[lane], si = s;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-      int t = __shfl_up_sync(0xffffffffu, incl, off);
-      if (lane >= off) incl += t;
+      int v = __shfl_up_sync(0xffffffffu, si, off);
+      if (lane >= off) si += v;
     }
-    if (idx < nblocks) a.scan_tmp[idx] = carry + incl - v;
-    carry += __shfl_sync(0xffffffffu, incl, 31);
+    warp_sums[lane] = si - s;
+    if (lane == 31) a.bin_start[a.nbins] = si;
   }
-  if (lane == 0) a.bin_start[a.nbins] = carry;
+  __syncthreads();
+  int run = incl - local + warp_sums[w];
+  for (int b = b0; b < b1; ++b) {
+    const int v = a.scan_tmp[b];
+    a.scan_tmp[b] = run;
+    run += v;
+  }
 }
 
 __global__ void k_scan_add(BeadArgs a) {
@@ -230,17 +247,16 @@ __global__ void k_build(BeadArgs a) {
     if (cnt > a.maxnb) { atomicOr(a.status, ST_OVERFLOW); cnt = a.maxnb; }
     a.nnbr[i] = cnt;
   }
-  // ---- grid list: nodes within cutneigh of each periodic image of bead i
+  // ---- grid list: nodes within cutneigh of each periodic image of bead i.
+  // Candidate rows are pruned to the cutoff sphere with a margin; membership
+  // is decided by the exact test in the reference's operand order.
   if (a.gl) {
-    int lo3[3], hi3[3];
-    for (int d = 0; d < 3; ++d) {
-      const double u = (xi[d] - a.boxlo[d]) / a.dx[d];
-      const double r = a.cutneigh / a.dx[d];
-      lo3[d] = (int)floor(u - r) - 1;
-      hi3[d] = (int)ceil(u + r) + 1;
-    }
+    const double cutsq = a.cutneighsq;
+    const double margin = 1e-9 * cutsq;
     int cnt = 0;
-    for (int kz = lo3[2]; kz <= hi3[2]; ++kz) {
+    const double uz = (xi[2] - a.boxlo[2]) / a.dx[2];
+    const int kz0 = (int)floor(uz - a.cutneigh / a.dx[2]) - 1, kz1 = (int)ceil(uz + a.cutneigh / a.dx[2]) + 1;
+    for (int kz = kz0; kz <= kz1; ++kz) {
       int wz = kz, sz = 0;
       if (wz < 0) { wz += a.N[2]; sz = 1; } else if (wz >= a.N[2]) { wz -= a.N[2]; sz = -1; }
       if (wz < 0 || wz >= a.N[2]) continue;
@@ -248,14 +264,24 @@ __global__ void k_build(BeadArgs a) {
       const double zt = __dadd_rn(__dmul_rn((double)wz, a.dx[2]), a.boxlo[2]);
       const double bz = sz ? __dadd_rn(xi[2], sz > 0 ? a.period[2] : -a.period[2]) : xi[2];
       const double dz = __dsub_rn(zt, bz);
-      for (int ky = lo3[1]; ky <= hi3[1]; ++ky) {
+      const double remz = cutsq - dz * dz;
+      if (remz < -margin) continue;
+      const double ry = sqrt(fmax(remz, 0.0)) / a.dx[1];
+      const double uy = (xi[1] - a.boxlo[1]) / a.dx[1];
+      const int ky0 = (int)floor(uy - ry) - 1, ky1 = (int)ceil(uy + ry) + 1;
+      for (int ky = ky0; ky <= ky1; ++ky) {
         int wy = ky, sy = 0;
         if (wy < 0) { wy += a.N[1]; sy = 1; } else if (wy >= a.N[1]) { wy -= a.N[1]; sy = -1; }
         if (wy < 0 || wy >= a.N[1]) continue;
         const double yt = __dadd_rn(__dmul_rn((double)wy, a.dx[1]), a.boxlo[1]);
         const double by_ = sy ? __dadd_rn(xi[1], sy > 0 ? a.period[1] : -a.period[1]) : xi[1];
         const double dy = __dsub_rn(yt, by_);
-        for (int kx = lo3[0]; kx <= hi3[0]; ++kx) {
+        const double remy = remz - dy * dy;
+        if (remy < -margin) continue;
+        const double rx = sqrt(fmax(remy, 0.0)) / a.dx[0];
+        const double ux = (xi[0] - a.boxlo[0]) / a.dx[0];
+        const int kx0 = (int)floor(ux - rx) - 1, kx1 = (int)ceil(ux + rx) + 1;
+        for (int kx = kx0; kx <= kx1; ++kx) {
           int wx = kx, sx = 0;
           if (wx < 0) { wx += a.N[0]; sx = 1; } else if (wx >= a.N[0]) { wx -= a.N[0]; sx = -1; }
           if (wx < 0 || wx >= a.N[0]) continue;
@@ -263,7 +289,7 @@ __global__ void k_build(BeadArgs a) {
           const double bx_ = sx ? __dadd_rn(xi[0], sx > 0 ? a.period[0] : -a.period[0]) : xi[0];
           const double dxx = __dsub_rn(xt, bx_);
           const double rsq = __dadd_rn(__dadd_rn(__dmul_rn(dxx, dxx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-          if (rsq <= a.cutneighsq) {
+          if (rsq <= cutsq) {
             const uint32_t node = (uint32_t)(((long long)wz * a.N[1] + wy) * a.N[0] + wx);
             const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
             if (cnt < a.maxg) a.gl[(size_t)i * a.maxg + cnt] = (node << 5) | (uint32_t)code;
@@ -291,13 +317,24 @@ __global__ void k_build_done(BeadArgs a) {
 __global__ void k_step_begin(long long* d_step) { *d_step += 1; }
 
 // ---- pair forces: lj/cut over the bead list, gridatom over the grid list.
-// Each bead sums its own force (no atomics on F).  The mu deposit of the
-// gridatom styles goes to `dep` with atomics.
+// PAIR_TPB threads share one bead (its list entries are split among them,
+// then shuffle-reduced), so no atomics on F.  The mu deposit of the gridatom
+// styles goes to `dep` with atomics.
+//
+// Distances.  FP64: the reference's operand order (x_i - (x_j + s);
+// (k dx + lo) - (x + s)).  FP32: bead-bead separations are formed in FP64
+// and rounded once; bead-node separations come from the bead's position in
+// grid units split once per step into an integer part and a fraction, so the
+// per-entry arithmetic is (small integer - fraction) * dx in FP32.
+constexpr int PAIR_TPB = 4;
+
 template <typename T>
 __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  const double xi0 = a.x[3 * i], xi1 = a.x[3 * i + 1], xi2 = a.x[3 * i + 2];
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gtid / PAIR_TPB, sub = gtid % PAIR_TPB;
+  const bool live = i < a.n;
+  const int ii = live ? i : 0;
+  const double xi0 = a.x[3 * ii], xi1 = a.x[3 * ii + 1], xi2 = a.x[3 * ii + 2];
   // Kahan-compensated sums (exact no-ops in double beyond round-off)
   T f[3] = {0, 0, 0}, c[3] = {0, 0, 0};
   auto add = [&](int d, T v) {
@@ -306,9 +343,9 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
     c[d] = (t - f[d]) - y;
     f[d] = t;
   };
-  if (p.lj && a.nbr) {
+  if (live && p.lj && a.nbr) {
     const int cnt = a.nnbr[i];
-    for (int k = 0; k < cnt; ++k) {
+    for (int k = sub; k < cnt; k += PAIR_TPB) {
       const int e = a.nbr[(size_t)i * a.maxnb + k];
       const int j = e >> 5, code = e & 31;
       const double d0 = xi0 - (a.x[3 * j] + img_shift(code, 0, a));
@@ -327,22 +364,37 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
       }
     }
   }
-  if (p.ga_style != PHAFD_GRIDATOM_NONE && a.gl) {
+  if (live && p.ga_style != PHAFD_GRIDATOM_NONE && a.gl) {
     const int cnt = a.ngl[i];
     const int t = a.type[i];
     const T cutsq = (T)p.ga_cutsq[t], eps = (T)p.ga_eps[t], phit = (T)p.ga_phi[t];
-    for (int k = 0; k < cnt; ++k) {
+    // bead position in grid units: integer part + fraction (FP32 path)
+    int gi[3];
+    T gf[3], dxf[3];
+    const double xi[3] = {xi0, xi1, xi2};
+    for (int d = 0; d < 3; ++d) {
+      const double ud = (xi[d] - a.boxlo[d]) / a.dx[d];
+      const double fl = floor(ud);
+      gi[d] = (int)fl;
+      gf[d] = (T)(ud - fl);
+      dxf[d] = (T)a.dx[d];
+    }
+    for (int k = sub; k < cnt; k += PAIR_TPB) {
       const uint32_t e = a.gl[(size_t)i * a.maxg + k];
       const uint32_t node = e >> 5;
       const int code = (int)(e & 31u);
-      const int gx = (int)(node % (uint32_t)a.N[0]);
-      const int gy = (int)((node / (uint32_t)a.N[0]) % (uint32_t)a.N[1]);
-      const int gz = (int)(node / ((uint32_t)a.N[0] * (uint32_t)a.N[1]));
-      // node coordinate k*dx + boxlo without contraction (npair_grid_bin.cpp:76-88)
-      const double d0 = __dadd_rn(__dmul_rn((double)gx, a.dx[0]), a.boxlo[0]) - (xi0 + img_shift(code, 0, a));
-      const double d1 = __dadd_rn(__dmul_rn((double)gy, a.dx[1]), a.boxlo[1]) - (xi1 + img_shift(code, 1, a));
-      const double d2 = __dadd_rn(__dmul_rn((double)gz, a.dx[2]), a.boxlo[2]) - (xi2 + img_shift(code, 2, a));
-      const T dx = (T)d0, dy = (T)d1, dz = (T)d2;
+      const int g3[3] = {(int)(node % (uint32_t)a.N[0]), (int)((node / (uint32_t)a.N[0]) % (uint32_t)a.N[1]),
+                         (int)(node / ((uint32_t)a.N[0] * (uint32_t)a.N[1]))};
+      T dd[3];
+      if constexpr (sizeof(T) == 8) {
+        // node coordinate k*dx + boxlo without contraction (npair_grid_bin.cpp:76-88)
+        for (int d = 0; d < 3; ++d)
+          dd[d] = __dadd_rn(__dmul_rn((double)g3[d], a.dx[d]), a.boxlo[d]) - (xi[d] + img_shift(code, d, a));
+      } else {
+        const int sc[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+        for (int d = 0; d < 3; ++d) dd[d] = ((T)(g3[d] - gi[d] - sc[d] * a.N[d]) - gf[d]) * dxf[d];
+      }
+      const T dx = dd[0], dy = dd[1], dz = dd[2];
       T rsq = dx * dx + dy * dy + dz * dz;
       const bool inside = (p.ga_style == PHAFD_GRIDATOM_GAUSSIAN) ? (rsq <= cutsq) : (rsq < cutsq);
       if (!inside) continue;
@@ -372,9 +424,19 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
       add(2, -p.gz[node] * expfac);
     }
   }
-  a.f[3 * i] = (double)f[0];
-  a.f[3 * i + 1] = (double)f[1];
-  a.f[3 * i + 2] = (double)f[2];
+  // combine the PAIR_TPB partial sums of a bead (adjacent lanes)
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    T v = f[d] - c[d];
+#pragma unroll
+    for (int off = 1; off < PAIR_TPB; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    f[d] = v;
+  }
+  if (live && sub == 0) {
+    a.f[3 * i] = (double)f[0];
+    a.f[3 * i + 1] = (double)f[1];
+    a.f[3 * i + 2] = (double)f[2];
+  }
 }
 
 // zero the nodes a bead may have deposited on (sparse reset of dep)
@@ -396,7 +458,10 @@ __global__ void k_drag(BeadArgs a, double dt) {
     a.x[3 * i + d] = __dadd_rn(a.x[3 * i + d], __dmul_rn(__dmul_rn(__dmul_rn(dr, a.f[3 * i + d]), dt), 0.5));
 }
 
-// chain model (no reference counterpart; the oracle's oracle_chain_force)
+// chain model (no reference counterpart; the oracle's oracle_chain_force).
+// Bond vectors are differences of FP64 positions taken in FP64, then the
+// force arithmetic runs in T; positions stay FP64.
+template <typename T>
 __global__ void k_chain_force(BeadArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -405,69 +470,77 @@ __global__ void k_chain_force(BeadArgs a) {
   const SemiDev& P = a.sf[fi];
   const int base = a.sf_start[i], n = a.sf_len[i], b = i - base;
   const double* u = a.ux + 3 * (size_t)base;
-  double f[3] = {0, 0, 0};
+  auto bond = [&](int q, T r[3]) {  // u[q+1] - u[q]
+    for (int d = 0; d < 3; ++d) r[d] = (T)(u[3 * (q + 1) + d] - u[3 * q + d]);
+  };
+  const T kb = (T)P.kbond, b0 = (T)P.bondlength, kap = (T)P.bending;
+  T f[3] = {0, 0, 0};
   for (int side = 0; side < 2; ++side) {
     const int q = side == 0 ? b - 1 : b;
     if (q < 0 || q + 1 >= n) continue;
-    const double r[3] = {u[3 * (q + 1)] - u[3 * q], u[3 * (q + 1) + 1] - u[3 * q + 1], u[3 * (q + 1) + 2] - u[3 * q + 2]};
-    const double len = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-    const double g = P.kbond * (len - P.bondlength) / len;
-    const double sgn = (q == b) ? 1.0 : -1.0;
+    T r[3];
+    bond(q, r);
+    const T len = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    const T g = kb * (len - b0) / len;
+    const T sgn = (q == b) ? (T)1 : (T)-1;
     for (int d = 0; d < 3; ++d) f[d] += sgn * g * r[d];
   }
   if (P.bending != 0.0) {
     for (int cc = b - 1; cc <= b + 1; ++cc) {
       if (cc < 1 || cc + 1 >= n) continue;
-      double ra[3], rb[3];
+      T ra[3], rb[3];
+      bond(cc - 1, ra);
+      bond(cc, rb);
+      const T la = sqrt(ra[0] * ra[0] + ra[1] * ra[1] + ra[2] * ra[2]);
+      const T lb = sqrt(rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2]);
+      const T cs = (ra[0] * rb[0] + ra[1] * rb[1] + ra[2] * rb[2]) / (la * lb);
       for (int d = 0; d < 3; ++d) {
-        ra[d] = u[3 * cc + d] - u[3 * (cc - 1) + d];
-        rb[d] = u[3 * (cc + 1) + d] - u[3 * cc + d];
-      }
-      const double la = sqrt(ra[0] * ra[0] + ra[1] * ra[1] + ra[2] * ra[2]);
-      const double lb = sqrt(rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2]);
-      const double cs = (ra[0] * rb[0] + ra[1] * rb[1] + ra[2] * rb[2]) / (la * lb);
-      for (int d = 0; d < 3; ++d) {
-        const double dca = rb[d] / (la * lb) - cs * ra[d] / (la * la);
-        const double dcb = ra[d] / (la * lb) - cs * rb[d] / (lb * lb);
-        if (b == cc - 1) f[d] += P.bending * (-dca);
-        else if (b == cc) f[d] += P.bending * (dca - dcb);
-        else f[d] += P.bending * dcb;
+        const T dca = rb[d] / (la * lb) - cs * ra[d] / (la * la);
+        const T dcb = ra[d] / (la * lb) - cs * rb[d] / (lb * lb);
+        if (b == cc - 1) f[d] += kap * (-dca);
+        else if (b == cc) f[d] += kap * (dca - dcb);
+        else f[d] += kap * dcb;
       }
     }
   }
   const int lo = b > 0 ? b - 1 : b, hi = b + 1 < n ? b + 1 : b;
-  const double tv[3] = {u[3 * hi] - u[3 * lo], u[3 * hi + 1] - u[3 * lo + 1], u[3 * hi + 2] - u[3 * lo + 2]};
-  const double tl = sqrt(tv[0] * tv[0] + tv[1] * tv[1] + tv[2] * tv[2]);
+  T tv[3];
+  for (int d = 0; d < 3; ++d) tv[d] = (T)(u[3 * hi + d] - u[3 * lo + d]);
+  const T tl = sqrt(tv[0] * tv[0] + tv[1] * tv[1] + tv[2] * tv[2]);
   for (int d = 0; d < 3; ++d) {
-    a.fchain[3 * i + d] = f[d];
-    a.tang[3 * i + d] = tl > 0 ? tv[d] / tl : 0.0;
+    a.fchain[3 * i + d] = (double)f[d];
+    a.tang[3 * i + d] = (double)(tl > 0 ? tv[d] / tl : (T)0);
   }
 }
 
+template <typename T>
 __global__ void k_chain_move(BeadArgs a, int half, double dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const int fi = a.sf_fix[i];
   if (fi < 0) return;
   const SemiDev& P = a.sf[fi];
-  double xi[3] = {0, 0, 0};
+  T xi[3] = {0, 0, 0};
   if (P.noise == PHAFD_NOISE_PHILOX && P.temp > 0) bead_gauss(P.seed, (uint64_t)(*a.d_step), half, i, xi);
-  const double* fc = a.fchain + 3 * (size_t)i;
-  const double* fp = a.f + 3 * (size_t)i;
-  const double* t = a.tang + 3 * (size_t)i;
-  const double h = 0.5 * dt;
-  const double ft[3] = {fc[0] + fp[0], fc[1] + fp[1], fc[2] + fp[2]};
-  const double tf = t[0] * ft[0] + t[1] * ft[1] + t[2] * ft[2];
-  const double tx = t[0] * xi[0] + t[1] * xi[1] + t[2] * xi[2];
-  const double aa = 1.0 / P.zeta_perp, bpar = 1.0 / P.zeta_para - 1.0 / P.zeta_perp;
-  const double sa = 1.0 / sqrt(P.zeta_perp), sb = 1.0 / sqrt(P.zeta_para) - 1.0 / sqrt(P.zeta_perp);
-  const double amp = sqrt(2.0 * P.temp * h);
+  T fc[3], fp[3], t[3];
+  for (int d = 0; d < 3; ++d) {
+    fc[d] = (T)a.fchain[3 * (size_t)i + d];
+    fp[d] = (T)a.f[3 * (size_t)i + d];
+    t[d] = (T)a.tang[3 * (size_t)i + d];
+  }
+  const T h = (T)(0.5 * dt);
+  const T ft[3] = {fc[0] + fp[0], fc[1] + fp[1], fc[2] + fp[2]};
+  const T tf = t[0] * ft[0] + t[1] * ft[1] + t[2] * ft[2];
+  const T tx = t[0] * xi[0] + t[1] * xi[1] + t[2] * xi[2];
+  const T aa = (T)(1.0 / P.zeta_perp), bpar = (T)(1.0 / P.zeta_para - 1.0 / P.zeta_perp);
+  const T sa = (T)(1.0 / sqrt(P.zeta_perp)), sb = (T)(1.0 / sqrt(P.zeta_para) - 1.0 / sqrt(P.zeta_perp));
+  const T amp = (T)sqrt(2.0 * P.temp * 0.5 * dt);
   const int im = a.image[i];
   const int box[3] = {(im & IMGMASK) - IMGMAX, (im >> IMGBITS & IMGMASK) - IMGMAX, (im >> IMG2BITS) - IMGMAX};
   bool bad = false;
   for (int d = 0; d < 3; ++d) {
-    const double disp = h * (aa * ft[d] + bpar * tf * t[d]) + amp * (sa * xi[d] + sb * tx * t[d]);
-    const double nu = a.ux[3 * i + d] + disp;
+    const T disp = h * (aa * ft[d] + bpar * tf * t[d]) + amp * (sa * xi[d] + sb * tx * t[d]);
+    const double nu = a.ux[3 * i + d] + (double)disp;
     a.ux[3 * i + d] = nu;
     a.x[3 * i + d] = __dsub_rn(nu, __dmul_rn((double)box[d], a.period[d]));  // Domain::map, domain.cpp:180-193
     bad |= !isfinite(nu);
@@ -490,7 +563,7 @@ void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st) {
   k_bin_count<<<nblk(a.n, T), T, 0, st>>>(a);
   const int nblocks = (int)((a.nbins + 1023) / 1024);
   k_scan_block<<<nblocks, 1024, 0, st>>>(a);
-  k_scan_sums<<<1, 32, 0, st>>>(a, nblocks);
+  k_scan_sums<<<1, 1024, 0, st>>>(a, nblocks);
   k_scan_add<<<nblocks, 1024, 0, st>>>(a);
   k_bin_fill<<<nblk(a.n, T), T, 0, st>>>(a);
   k_bin_sort<<<nblk(a.nbins, T) > 4096 ? 4096 : nblk(a.nbins, T), T, 0, st>>>(a);
@@ -501,7 +574,7 @@ void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st) {
 template <typename T>
 void launch_pair(const BeadArgs& a, const PairArgs<T>& p, cudaStream_t st) {
   if (a.n == 0) return;
-  k_pair<T><<<nblk(a.n, 128), 128, 0, st>>>(a, p);
+  k_pair<T><<<nblk((long long)a.n * PAIR_TPB, 128), 128, 0, st>>>(a, p);
 }
 template void launch_pair<float>(const BeadArgs&, const PairArgs<float>&, cudaStream_t);
 template void launch_pair<double>(const BeadArgs&, const PairArgs<double>&, cudaStream_t);
@@ -519,10 +592,13 @@ void launch_drag(const BeadArgs& a, double dt, cudaStream_t st) {
   k_drag<<<nblk(a.n, 256), 256, 0, st>>>(a, dt);
 }
 
+template <typename T>
 void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st) {
   if (a.n == 0 || !a.any_semi) return;
-  k_chain_force<<<nblk(a.n, 128), 128, 0, st>>>(a);
-  k_chain_move<<<nblk(a.n, 128), 128, 0, st>>>(a, half, dt);
+  k_chain_force<T><<<nblk(a.n, 128), 128, 0, st>>>(a);
+  k_chain_move<T><<<nblk(a.n, 128), 128, 0, st>>>(a, half, dt);
 }
+template void launch_chain_half<float>(const BeadArgs&, int, double, cudaStream_t);
+template void launch_chain_half<double>(const BeadArgs&, int, double, cudaStream_t);
 
 }  // namespace phafd

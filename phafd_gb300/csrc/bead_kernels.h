@@ -59,6 +59,6 @@ void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st);
 template <typename T> void launch_pair(const BeadArgs& a, const PairArgs<T>& p, cudaStream_t st);
 template <typename T> void launch_dep_zero(const BeadArgs& a, T* dep, cudaStream_t st);
 void launch_drag(const BeadArgs& a, double dt, cudaStream_t st);
-void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st);
+template <typename T> void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st);
 
 }  // namespace phafd

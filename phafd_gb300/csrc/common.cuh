@@ -44,17 +44,27 @@ PHAFD_HD double u53(uint32_t a, uint32_t b) {
   return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
 }
 
-// Uniform in [-0.5, 0.5) for component `comp` of the canonical mode
-// (kx, ky, kz) at `step`: the oracle's philox_u.
-PHAFD_D double field_noise_u(int kx, int ky, int kz, int comp, int Ny, int Nz, uint32_t step, uint32_t seed) {
+// Philox words of the canonical mode (kx, ky, kz) at `step`: the oracle's
+// philox_u draws u53(c0, c1) - 0.5 and u53(c2, c3) - 0.5 from them.
+PHAFD_D void field_noise_words(int kx, int ky, int kz, int Ny, int Nz, uint32_t step, uint32_t seed, uint32_t c[4]) {
   const uint64_t idx = ((uint64_t)kx * Nz + kz) * Ny + ky;
-  uint32_t c[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), step, 0x46494c44u};
+  c[0] = (uint32_t)idx; c[1] = (uint32_t)(idx >> 32); c[2] = step; c[3] = 0x46494c44u;
   philox4x32_10(c, seed, 0x434f4e4au);
-  return (comp == 0 ? u53(c[0], c[1]) : u53(c[2], c[3])) - 0.5;
+}
+// the two uniforms in [-0.5, 0.5) in precision T: 53 bits for double (the
+// oracle's values exactly); for float the top 24 of those 53 bits
+PHAFD_D void field_noise_pair(const uint32_t c[4], double& u0, double& u1) {
+  u0 = u53(c[0], c[1]) - 0.5;
+  u1 = u53(c[2], c[3]) - 0.5;
+}
+PHAFD_D void field_noise_pair(const uint32_t c[4], float& u0, float& u1) {
+  u0 = (float)(c[0] >> 8) * 5.9604644775390625e-8f - 0.5f;
+  u1 = (float)(c[2] >> 8) * 5.9604644775390625e-8f - 0.5f;
 }
 
 // Three standard normals for bead `bead`, half-step `half` of `step`
-// (Box-Muller on Philox words): the oracle's oracle_bead_gauss.
+// (Box-Muller on Philox words): the oracle's oracle_bead_gauss.  The float
+// version uses the top 24 bits of the same uniforms.
 PHAFD_D void bead_gauss(uint32_t seed, uint64_t step, int half, int bead, double xi[3]) {
   double g[4];
 #pragma unroll
@@ -66,6 +76,23 @@ PHAFD_D void bead_gauss(uint32_t seed, uint64_t step, int half, int bead, double
     const double r = sqrt(-2.0 * log(1.0 - u1));
     double s, co;
     sincos(6.283185307179586 * u2, &s, &co);
+    g[2 * call] = r * co;
+    g[2 * call + 1] = r * s;
+  }
+  xi[0] = g[0]; xi[1] = g[1]; xi[2] = g[2];
+}
+PHAFD_D void bead_gauss(uint32_t seed, uint64_t step, int half, int bead, float xi[3]) {
+  float g[4];
+#pragma unroll
+  for (int call = 0; call < 2; ++call) {
+    uint32_t c[4] = {(uint32_t)bead, (uint32_t)step, (uint32_t)(step >> 32) * 2u + (uint32_t)half,
+                     0x4245414Du + (uint32_t)call};
+    philox4x32_10(c, seed, 0x53454d49u);
+    const float u1 = (float)(c[0] >> 8) * 5.9604644775390625e-8f;
+    const float u2 = (float)(c[2] >> 8) * 5.9604644775390625e-8f;
+    const float r = sqrtf(-2.0f * logf(1.0f - u1));
+    float s, co;
+    sincosf(6.2831853f * u2, &s, &co);
     g[2 * call] = r * co;
     g[2 * call + 1] = r * s;
   }

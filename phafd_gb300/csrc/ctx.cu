@@ -205,19 +205,19 @@ struct phafd_ctx {
     u.mu_hat = mu_hat;
     u.phi_new = phi_new;
     u.uref = uref.as<double2>();
-    u.mobility = c_mobility;
-    u.tvg = c_temp / c_volFH * c_gamma;
-    u.dt = dt;
-    u.norm = 1.0 / ((double)N[0] * N[2] * N[1]);  // conjugate_volfrac.cpp:76
+    u.mobility = (T)c_mobility;
+    u.tvg = (T)(c_temp / c_volFH * c_gamma);
+    u.dt = (T)dt;
+    u.norm = (T)(1.0 / ((double)N[0] * N[2] * N[1]));  // conjugate_volfrac.cpp:76
     const double invLcubed = 1.0 / (period[0] * period[1] * period[2]);
-    u.cpref = std::sqrt(12 * c_temp * c_mobility * invLcubed);
-    u.rpref = std::sqrt(24 * c_temp * c_mobility * invLcubed);
-    u.sqrtdt = std::sqrt(dt);
-    u.phi_scale = 1.0;
-    u.store_scale = store_scale;
-    u.qx = geom.kq[0];
-    u.qy = geom.kq[1];
-    u.qz = geom.kq[2];
+    u.cpref = (T)std::sqrt(12 * c_temp * c_mobility * invLcubed);
+    u.rpref = (T)std::sqrt(24 * c_temp * c_mobility * invLcubed);
+    u.sqrtdt = (T)std::sqrt(dt);
+    u.phi_scale = (T)1.0;
+    u.store_scale = (T)store_scale;
+    u.qx = (T)geom.kq[0];
+    u.qy = (T)geom.kq[1];
+    u.qz = (T)geom.kq[2];
     u.noise = c_noise;
     u.seed = (uint32_t)c_seed;
     u.d_step = d_step();
@@ -244,9 +244,9 @@ struct phafd_ctx {
     mark(6);
   }
 
-  // from a spectrum S (z-ifft input) produce phi (scale sp, optional) and grad (scale sg)
+  // y inverse and x c2r of A (and B): phi (scale sp, optional) and grad (scale sg)
   template <typename T>
-  void inverse_chain(const cpx<T>* S, const UpdateArgs<T>* u, T* phi_out, T sp, T sg, bool grad, bool nan_check) {
+  void yx_inverse(T* phi_out, T sp, T sg, bool grad, bool nan_check) {
     const cpx<T>* twi[3] = {tw[0][1].as<cpx<T>>(), tw[1][1].as<cpx<T>>(), tw[2][1].as<cpx<T>>()};
     cpx<T>* A = wA.as<cpx<T>>();
     cpx<T>* B = wB.as<cpx<T>>();
@@ -255,8 +255,6 @@ struct phafd_ctx {
     cpx<T>* E = wE.as<cpx<T>>();
     NanArgs nan{nan_check ? 1 : 0, d_nan(), d_step()};
     NanArgs nonan{0, d_nan(), d_step()};
-    chk(GridOps<T>::zpass(geom, +1, S, A, grad ? B : nullptr, twi[2], u, st), "z ifft");
-    mark(7);
     chk(GridOps<T>::ypass(geom, +1, A, Cc, grad ? D : nullptr, twi[1], st), "y ifft");
     if (grad) chk(GridOps<T>::ypass(geom, +1, B, E, nullptr, twi[1], st), "y ifft");
     mark(8);
@@ -272,6 +270,15 @@ struct phafd_ctx {
       chk(GridOps<T>::xc2r(geom, E, gz.as<T>(), sg, false, nullptr, sg, twi[0], nonan, st), "x c2r");
     }
     mark(9);
+  }
+
+  // from a spectrum S (z-ifft input) produce phi (scale sp, optional) and grad (scale sg)
+  template <typename T>
+  void inverse_chain(const cpx<T>* S, const UpdateArgs<T>* u, T* phi_out, T sp, T sg, bool grad, bool nan_check) {
+    const cpx<T>* twi2 = tw[2][1].as<cpx<T>>();
+    chk(GridOps<T>::zpass(geom, +1, S, wA.as<cpx<T>>(), grad ? wB.as<cpx<T>>() : nullptr, twi2, u, st), "z ifft");
+    mark(7);
+    yx_inverse<T>(phi_out, sp, sg, grad, nan_check);
   }
 
   // ------------------------------------------------------------------ beads
@@ -305,16 +312,27 @@ struct phafd_ctx {
   }
 
   void setup_neighbor_structs() {
-    // bins: >= cutneigh wide, at least 3 per axis, about 2 bins per bead
-    const int target = std::max(3, (int)std::cbrt(2.0 * std::max(n, 1)) + 1);
+    // bins: at least one cutoff wide (the 27-bin stencil then covers the
+    // cutoff sphere) and at most 128 per axis, at least 3 per axis
     long long nbins = 1;
+    int nbd[3];
     for (int d = 0; d < 3; ++d) {
-      int nb = (int)std::floor(period[d] / cutneigh);
-      if (nb < 3) throw std::runtime_error("box must span at least three neighbor cutoffs per axis");
-      nb = std::min(nb, target);
-      ba.nb[d] = nb;
-      ba.bininv[d] = nb / period[d];
-      nbins *= nb;
+      nbd[d] = std::min(128, (int)std::floor(period[d] / cutneigh));
+      if (nbd[d] < 3) throw std::runtime_error("box must span at least three neighbor cutoffs per axis");
+      nbins *= nbd[d];
+    }
+    const long long cap = 1LL << 25;
+    if (nbins > cap) {
+      const double shrink = std::cbrt((double)cap / (double)nbins);
+      nbins = 1;
+      for (int d = 0; d < 3; ++d) {
+        nbd[d] = std::max(3, (int)std::floor(nbd[d] * shrink));
+        nbins *= nbd[d];
+      }
+    }
+    for (int d = 0; d < 3; ++d) {
+      ba.nb[d] = nbd[d];
+      ba.bininv[d] = nbd[d] / period[d];
     }
     ba.nbins = nbins;
     bin_of.alloc(std::max(n, 1) * 4);
@@ -448,26 +466,39 @@ struct phafd_ctx {
     mark(2);
     // initial_integrate
     launch_drag(ba, dt, st);
-    launch_chain_half(ba, 0, dt, st);
+    launch_chain_half<T>(ba, 0, dt, st);
     mark(3);
     if (have_conj) {
       FHArgs fh{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
-      // post_force + pre_final_integrate: mu = dep + FH(phi), r2c
-      r2c<T>(phi.as<T>(), dep.as<T>(), muhat.as<cpx<T>>(), fh);
-      if (n > 0 && ga_style != PHAFD_GRIDATOM_NONE) launch_dep_zero<T>(ba, dep.as<T>(), st);
-      // final_integrate + post_final_integrate
       if (resident) {
+        // post_force + pre_final_integrate fused into the x r2c, y fft; then
+        // z fft + update + z ifft in one pass (planes finished separately)
+        const cpx<T>* twf[3] = {tw[0][0].as<cpx<T>>(), tw[1][0].as<cpx<T>>(), tw[2][0].as<cpx<T>>()};
+        cpx<T>* W1 = w1.as<cpx<T>>();
+        chk(GridOps<T>::xr2c(geom, phi.as<T>(), dep.as<T>(), W1, twf[0], fh, st), "x r2c");
+        mark(4);
+        chk(GridOps<T>::ypass(geom, -1, W1, W1, nullptr, twf[1], st), "y fft");
+        mark(5);
+        if (n > 0 && ga_style != PHAFD_GRIDATOM_NONE) launch_dep_zero<T>(ba, dep.as<T>(), st);
+        mark(6);
         // the state stays an unnormalised r2c spectrum: store N * update
         UpdateArgs<T> u = update_args<T>(phat[cur].as<cpx<T>>(), muhat.as<cpx<T>>(), phat[1 - cur].as<cpx<T>>(),
                                          (double)nreal);
-        inverse_chain<T>(nullptr, &u, phi.as<T>(), (T)1, (T)1, true, true);
+        chk(GridOps<T>::zfused(geom, W1, muhat.as<cpx<T>>(), wA.as<cpx<T>>(), wB.as<cpx<T>>(), twf[2],
+                               tw[2][1].as<cpx<T>>(), u, keep_chempot ? 1 : 0, st), "z fused");
+        chk(GridOps<T>::zpass_planes(geom, wA.as<cpx<T>>(), wB.as<cpx<T>>(), tw[2][1].as<cpx<T>>(), u, st), "z planes");
+        mark(7);
+        yx_inverse<T>(phi.as<T>(), (T)1, (T)1, true, true);
       } else {
+        // post_force + pre_final_integrate: mu = dep + FH(phi), r2c
+        r2c<T>(phi.as<T>(), dep.as<T>(), muhat.as<cpx<T>>(), fh);
+        if (n > 0 && ga_style != PHAFD_GRIDATOM_NONE) launch_dep_zero<T>(ba, dep.as<T>(), st);
         UpdateArgs<T> u = update_args<T>(w1.as<cpx<T>>(), muhat.as<cpx<T>>(), phat[0].as<cpx<T>>(), 1.0);
         inverse_chain<T>(nullptr, &u, phi.as<T>(), (T)1, (T)1, false, true);
       }
     }
     launch_drag(ba, dt, st);
-    launch_chain_half(ba, 1, dt, st);
+    launch_chain_half<T>(ba, 1, dt, st);
     mark(3);
   }
 

@@ -127,15 +127,14 @@ PHAFD_D void dft(cpx<T>* v) {
 }
 
 // One Stockham stage, then recurse on the rest.  tw = W_N^m table for sign S.
-template <typename T, int N, int NL, int S, int NS>
+// Transforms lines [0, NL) of a buffer with row stride STR using NT threads.
+template <typename T, int N, int NL, int S, int NS, int NT, int STR>
 PHAFD_D void stages(cpx<T>* s, const cpx<T>* __restrict__ tw) {
   if constexpr (NS < N) {
     constexpr int R = pick(N / NS);
     constexpr int NB = N / R;                   // butterflies per line
-    constexpr int NT = N * NL / 16;             // threads in the CTA
     constexpr int TOT = NB * NL;                // butterflies in the CTA
     constexpr int PER = (TOT + NT - 1) / NT;    // butterflies per thread
-    constexpr int STR = NL + 1;
     constexpr int TWS = N / (NS * R);
     cpx<T> v[PER][R];
     const int tid = threadIdx.x;
@@ -166,14 +165,20 @@ PHAFD_D void stages(cpx<T>* s, const cpx<T>* __restrict__ tw) {
       }
     }
     __syncthreads();
-    stages<T, N, NL, S, NS * R>(s, tw);
+    stages<T, N, NL, S, NS * R, NT, STR>(s, tw);
   }
 }
 
-// Transform all NL lines in s (layout above).  Caller syncs before.
+// Transform all NL lines in s (layout above) with N*NL/16 threads.  Caller syncs before.
 template <typename T, int N, int NL, int S>
 PHAFD_D void run(cpx<T>* s, const cpx<T>* __restrict__ tw) {
-  stages<T, N, NL, S, 1>(s, tw);
+  stages<T, N, NL, S, 1, N * NL / 16, NL + 1>(s, tw);
+}
+
+// Transform lines [0, NL) of a buffer with row stride STR using NT threads.
+template <typename T, int N, int NL, int S, int NT, int STR>
+PHAFD_D void run_sub(cpx<T>* s, const cpx<T>* __restrict__ tw) {
+  stages<T, N, NL, S, 1, NT, STR>(s, tw);
 }
 
 template <int N, int NL>

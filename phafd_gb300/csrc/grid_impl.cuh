@@ -24,6 +24,12 @@
 
 namespace phafd {
 
+// Loop over the TOTAL elements of a tile with NT threads: a fixed trip count
+// the compiler unrolls, so all global loads of a thread are in flight at once.
+#define TILE_LOOP(idx, TOTAL, NT)                                                           \
+  _Pragma("unroll") for (int it_##idx = 0; it_##idx < ((TOTAL) + (NT)-1) / (NT); ++it_##idx) \
+    if (const int idx = (int)threadIdx.x + it_##idx * (NT); ((TOTAL) % (NT)) == 0 || idx < (TOTAL))
+
 template <typename T>
 PHAFD_D cpx<T> deriv(cpx<T> a, T dq, int m) {
   // fixgrid_conjugate.cpp:101-103: phi_hat * (0, dq) * m
@@ -50,7 +56,7 @@ k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict_
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * LB;
   unsigned long long nless = 0, ngreat = 0;
-  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+  TILE_LOOP(idx, LB * N, NT) {
     const int l = idx / N, x = idx % N;
     T v[2] = {(T)0, (T)0};
 #pragma unroll
@@ -88,7 +94,7 @@ k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict_
   }
   __syncthreads();
   fft::run<T, N, LB, -1>(s, tw);
-  for (int idx = threadIdx.x; idx < LB * (N / 2 + 1); idx += NT) {
+  TILE_LOOP(idx, LB * (N / 2 + 1), NT) {
     const int l = idx % LB, k = idx / LB;
     const cpx<T> zk = s[k * STR + l];
     const cpx<T> zm = conjg(s[((N - k) % N) * STR + l]);
@@ -115,7 +121,7 @@ k_xc2r(const cpx<T>* __restrict__ in, T* __restrict__ out0, T* __restrict__ out1
   constexpr int NT = N * NL / 16, STR = NL + 1;
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * LB;
-  for (int idx = threadIdx.x; idx < LB * (N / 2 + 1); idx += NT) {
+  TILE_LOOP(idx, LB * (N / 2 + 1), NT) {
     const int l = idx % LB, k = idx / LB;
     const int y = y0 + 2 * l;
     const size_t o = ((size_t)k * Nz + z) * Ny + y;
@@ -133,7 +139,7 @@ k_xc2r(const cpx<T>* __restrict__ in, T* __restrict__ out0, T* __restrict__ out1
   }
   __syncthreads();
   fft::run<T, N, NL, +1>(s, tw);
-  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+  TILE_LOOP(idx, LB * N, NT) {
     const int x = idx % N, l = idx / N;
 #pragma unroll
     for (int q = 0; q < NOUT; ++q) {
@@ -165,7 +171,7 @@ k_ypass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
   constexpr int NL = LB * NOUT;
   constexpr int NT = N * NL / 16, STR = NL + 1;
   const long long line0 = (long long)blockIdx.x * LB;
-  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+  TILE_LOOP(idx, LB * N, NT) {
     const int l = idx / N, e = idx % N;
     cpx<T> v = mk<T>(0, 0);
     if (line0 + l < nlines) v = in[(line0 + l) * N + e];
@@ -174,7 +180,7 @@ k_ypass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
   }
   __syncthreads();
   fft::run<T, N, NL, S>(s, tw);
-  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+  TILE_LOOP(idx, LB * N, NT) {
     const int l = idx / N, e = idx % N;
     if (line0 + l < nlines) {
       out0[(line0 + l) * N + e] = s[e * STR + l];
@@ -188,6 +194,39 @@ k_ypass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
 // (conjugate_volfrac.cpp:89-144) with the Hermitian bookkeeping of
 // Conjugate::update for one rank (conjugate.cpp:163-327).  (kx, ky, kz) are
 // this project's indices: the reference's (i, j, k) = (ky, kz, kx).
+// Model-B update of one mode from its old spectrum value ph (unnormalised)
+// and mu_hat value mu; (cy, cz) is the canonical mode that owns the noise.
+template <typename T>
+PHAFD_D cpx<T> update_value(const UpdateArgs<T>& u, int kx, int cy, int cz, cpx<T> ph, cpx<T> mu, bool real) {
+  const int Ny = u.Ny, Nz = u.Nz;
+  const T qx = u.qx * (T)kx;
+  const T qy = u.qy * (T)wrap_index(cy, Ny);
+  const T qz = u.qz * (T)wrap_index(cz, Nz);
+  const T q2 = qx * qx + qz * qz + qy * qy;  // reference order: qx^2 + q(kz)^2 + q(ky)^2
+  const T pre = u.mobility * q2 * u.dt;
+  const T g = u.tvg * q2;
+  const cpx<T> inner = mk<T>(mu.x + g * ph.x, mu.y + g * ph.y);
+  cpx<T> r = mk<T>((ph.x - pre * inner.x) * u.norm, (ph.y - pre * inner.y) * u.norm);
+  T u0 = 0, u1 = 0;
+  if (u.noise == PHAFD_NOISE_REFERENCE) {
+    const double2 w = u.uref[((size_t)kx * Nz + cz) * Ny + cy];
+    u0 = (T)w.x; u1 = (T)w.y;
+  } else if (u.noise == PHAFD_NOISE_PHILOX) {
+    uint32_t c[4];
+    field_noise_words(kx, cy, cz, Ny, Nz, (uint32_t)(*u.d_step), u.seed, c);
+    field_noise_pair(c, u0, u1);
+  }
+  const T sq = sqrt(q2);
+  if (real) {
+    r.x += u.rpref * sq * u.sqrtdt * u0;
+  } else {
+    const T a = u.cpref * sq * u.sqrtdt;
+    r.x += a * u0;
+    r.y += a * u1;
+  }
+  return r;
+}
+
 template <typename T>
 PHAFD_D cpx<T> update_mode(const UpdateArgs<T>& u, int kx, int ky, int kz, size_t o) {
   const int Ny = u.Ny, Nz = u.Nz, Nxh = u.Nxh;
@@ -211,34 +250,9 @@ PHAFD_D cpx<T> update_mode(const UpdateArgs<T>& u, int kx, int ky, int kz, size_
   }
   const size_t oc = mirror ? ((size_t)kx * Nz + cz) * Ny + cy : o;
   cpx<T> ph = u.phi_old[oc];
-  ph = scale(ph, (T)u.phi_scale);
-  if (origin) return scale(ph, (T)u.norm);
-  const cpx<T> mu = u.mu_hat[oc];
-  const T qx = (T)u.qx * (T)kx;
-  const T qy = (T)u.qy * (T)wrap_index(cy, Ny);
-  const T qz = (T)u.qz * (T)wrap_index(cz, Nz);
-  const T q2 = qx * qx + qz * qz + qy * qy;  // reference order: qx^2 + q(kz)^2 + q(ky)^2
-  const T pre = (T)u.mobility * q2 * (T)u.dt;
-  const T g = (T)u.tvg * q2;
-  const cpx<T> inner = mk<T>(mu.x + g * ph.x, mu.y + g * ph.y);
-  cpx<T> r = mk<T>((ph.x - pre * inner.x) * (T)u.norm, (ph.y - pre * inner.y) * (T)u.norm);
-  double u0 = 0.0, u1 = 0.0;
-  if (u.noise == PHAFD_NOISE_REFERENCE) {
-    const double2 w = u.uref[((size_t)kx * Nz + cz) * Ny + cy];
-    u0 = w.x; u1 = w.y;
-  } else if (u.noise == PHAFD_NOISE_PHILOX) {
-    const uint32_t st = (uint32_t)(*u.d_step);
-    u0 = field_noise_u(kx, cy, cz, 0, Ny, Nz, st, u.seed);
-    if (!real) u1 = field_noise_u(kx, cy, cz, 1, Ny, Nz, st, u.seed);
-  }
-  const T sq = sqrt(q2);
-  if (real) {
-    r.x += (T)u.rpref * sq * (T)u.sqrtdt * (T)u0;
-  } else {
-    const T a = (T)u.cpref * sq * (T)u.sqrtdt;
-    r.x += a * (T)u0;
-    r.y += a * (T)u1;
-  }
+  ph = scale(ph, u.phi_scale);
+  if (origin) return scale(ph, u.norm);
+  const cpx<T> r = update_value(u, kx, cy, cz, ph, u.mu_hat[oc], real);
   return mirror ? conjg(r) : r;
 }
 
@@ -249,14 +263,14 @@ PHAFD_D cpx<T> update_mode(const UpdateArgs<T>& u, int kx, int ky, int kz, size_
 template <typename T, int N, int LB, int S, int NOUT, bool UPD>
 __global__ void __launch_bounds__(N * LB * NOUT / 16)
 k_zpass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __restrict__ tw, int Ny,
-        UpdateArgs<T> u) {
+        UpdateArgs<T> u, int planes_only) {
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = LB * NOUT;
   constexpr int NT = N * NL / 16, STR = NL + 1;
-  const int kx = blockIdx.y;
+  const int kx = planes_only ? (blockIdx.y == 0 ? 0 : u.Nxh - 1) : (int)blockIdx.y;
   const int c0 = blockIdx.x * LB;
-  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+  TILE_LOOP(idx, LB * N, NT) {
     const int c = idx % LB, e = idx / LB;
     const int ky = c0 + c;
     cpx<T> v = mk<T>(0, 0);
@@ -264,7 +278,7 @@ k_zpass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
       const size_t o = ((size_t)kx * N + e) * Ny + ky;
       if constexpr (UPD) {
         v = update_mode(u, kx, ky, e, o);
-        u.phi_new[o] = scale(v, (T)u.store_scale);
+        u.phi_new[o] = scale(v, u.store_scale);
       } else {
         v = in[o];
       }
@@ -274,13 +288,73 @@ k_zpass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
   }
   __syncthreads();
   fft::run<T, N, NL, S>(s, tw);
-  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+  TILE_LOOP(idx, LB * N, NT) {
     const int c = idx % LB, e = idx / LB;
     const int ky = c0 + c;
     if (ky < Ny) {
       const size_t o = ((size_t)kx * N + e) * Ny + ky;
       out0[o] = s[e * STR + c];
       if constexpr (NOUT == 2) out1[o] = s[e * STR + LB + c];
+    }
+  }
+}
+
+// ------------------------------------------------------- z fft + update + z ifft
+// One tile (kx, ky in [c0, c0+LB)) of the spectrum after the x and y passes
+// of mu: forward z FFT -> mu_hat in shared memory; Model-B update against
+// phi_hat (global) for the bulk modes (1 <= kx < Nx/2), phi_hat' stored;
+// z inverse FFT of phi_hat' and of i qz phi_hat' -> out0, out1.  Tiles of the
+// kx = 0 and kx = Nx/2 planes, whose modes pair with mirror modes in other
+// tiles, only store mu_hat; k_zpass<planes_only> finishes them.
+template <typename T, int N, int LB>
+__global__ void __launch_bounds__(N * LB * 2 / 16)
+k_zfused(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __restrict__ out0,
+         cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny,
+         UpdateArgs<T> u, int store_mu) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
+  constexpr int NL = 2 * LB;
+  constexpr int NT = N * NL / 16, STR = NL + 1;
+  const int kx = blockIdx.y;
+  const int c0 = blockIdx.x * LB;
+  const bool plane = (kx == 0 || kx == u.Nxh - 1);
+  TILE_LOOP(idx, LB * N, NT) {
+    const int c = idx % LB, e = idx / LB;
+    const int ky = c0 + c;
+    s[e * STR + c] = ky < Ny ? muin[((size_t)kx * N + e) * Ny + ky] : mk<T>(0, 0);
+  }
+  __syncthreads();
+  fft::run_sub<T, N, LB, -1, NT, STR>(s, twf);
+  if (plane || store_mu) {
+    TILE_LOOP(idx, LB * N, NT) {
+      const int c = idx % LB, e = idx / LB;
+      const int ky = c0 + c;
+      if (ky < Ny) muhat[((size_t)kx * N + e) * Ny + ky] = s[e * STR + c];
+    }
+  }
+  if (plane) return;  // uniform per CTA
+  TILE_LOOP(idx, LB * N, NT) {
+    const int c = idx % LB, e = idx / LB;
+    const int ky = c0 + c;
+    cpx<T> v = mk<T>(0, 0);
+    if (ky < Ny) {
+      const size_t o = ((size_t)kx * N + e) * Ny + ky;
+      const cpx<T> ph = scale(u.phi_old[o], u.phi_scale);
+      v = update_value(u, kx, ky, e, ph, s[e * STR + c], false);
+      u.phi_new[o] = scale(v, u.store_scale);
+    }
+    s[e * STR + c] = v;
+    s[e * STR + LB + c] = deriv(v, dq, wrap_index(e, N));
+  }
+  __syncthreads();
+  fft::run<T, N, NL, +1>(s, twi);
+  TILE_LOOP(idx, LB * N, NT) {
+    const int c = idx % LB, e = idx / LB;
+    const int ky = c0 + c;
+    if (ky < Ny) {
+      const size_t o = ((size_t)kx * N + e) * Ny + ky;
+      out0[o] = s[e * STR + c];
+      out1[o] = s[e * STR + LB + c];
     }
   }
 }
@@ -374,23 +448,35 @@ struct Axis {
 
   template <int S, bool UPD>
   static int zpass(const Geom& g, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
-                   const UpdateArgs<T>& u, cudaStream_t st) {
+                   const UpdateArgs<T>& u, cudaStream_t st, int planes_only = 0) {
     const T dq = (T)g.kq[2];
+    const unsigned gy = planes_only ? 2u : (unsigned)g.nxh;
     if (out1) {
       constexpr int LB = NLT / 2 >= 1 ? NLT / 2 : 1;
       const size_t sm = (size_t)N * (2 * LB + 1) * sizeof(cpx<T>);
-      dim3 grid((g.ny + LB - 1) / LB, g.nxh);
+      dim3 grid((g.ny + LB - 1) / LB, gy);
       auto k = k_zpass<T, N, LB, S, 2, UPD>;
       if (set_smem(k, sm)) return -1;
-      k<<<grid, N * LB * 2 / 16, sm, st>>>(in, out0, out1, dq, tw, g.ny, u);
+      k<<<grid, N * LB * 2 / 16, sm, st>>>(in, out0, out1, dq, tw, g.ny, u, planes_only);
     } else {
       constexpr int LB = NLT;
       const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
-      dim3 grid((g.ny + LB - 1) / LB, g.nxh);
+      dim3 grid((g.ny + LB - 1) / LB, gy);
       auto k = k_zpass<T, N, LB, S, 1, UPD>;
       if (set_smem(k, sm)) return -1;
-      k<<<grid, N * LB / 16, sm, st>>>(in, out0, out1, dq, tw, g.ny, u);
+      k<<<grid, N * LB / 16, sm, st>>>(in, out0, out1, dq, tw, g.ny, u, planes_only);
     }
+    return 0;
+  }
+
+  static int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
+                    const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st) {
+    constexpr int LB = NLT / 2 >= 1 ? NLT / 2 : 1;
+    const size_t sm = (size_t)N * (2 * LB + 1) * sizeof(cpx<T>);
+    dim3 grid((g.ny + LB - 1) / LB, g.nxh);
+    auto k = k_zfused<T, N, LB>;
+    if (set_smem(k, sm)) return -1;
+    k<<<grid, N * LB * 2 / 16, sm, st>>>(muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu);
     return 0;
   }
 };
@@ -427,6 +513,28 @@ int GridOps<T>::ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, c
   case n:                                                                         \
     return sign < 0 ? Axis<T, n>::template ypass<-1>(g, in, out0, out1, tw, st)   \
                     : Axis<T, n>::template ypass<+1>(g, in, out0, out1, tw, st);
+    PHAFD_FOR_SIZES(CASE)
+#undef CASE
+  }
+  return -2;
+}
+
+template <typename T>
+int GridOps<T>::zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
+                       const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st) {
+  switch (g.nz) {
+#define CASE(n) case n: return Axis<T, n>::zfused(g, muin, muhat, out0, out1, twf, twi, u, store_mu, st);
+    PHAFD_FOR_SIZES(CASE)
+#undef CASE
+  }
+  return -2;
+}
+
+template <typename T>
+int GridOps<T>::zpass_planes(const Geom& g, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw, const UpdateArgs<T>& u,
+                             cudaStream_t st) {
+  switch (g.nz) {
+#define CASE(n) case n: return Axis<T, n>::template zpass<+1, true>(g, nullptr, out0, out1, tw, u, st, 1);
     PHAFD_FOR_SIZES(CASE)
 #undef CASE
   }

@@ -32,8 +32,8 @@ struct UpdateArgs {
   const cpx<T>* mu_hat;
   cpx<T>* phi_new;
   const double2* uref;
-  double mobility, tvg, dt, norm, cpref, rpref, sqrtdt, phi_scale, store_scale;
-  double qx, qy, qz;
+  T mobility, tvg, dt, norm, cpref, rpref, sqrtdt, phi_scale, store_scale;
+  T qx, qy, qz;
   int noise;
   uint32_t seed;
   const long long* d_step;
@@ -50,6 +50,12 @@ struct GridOps {
                    cudaStream_t st);
   static int zpass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
                    const UpdateArgs<T>* u, cudaStream_t st);
+  // forward z FFT of mu + update + z inverse FFT (bulk kx); plane tiles store mu_hat only
+  static int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
+                    const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st);
+  // update + z inverse FFT of the kx = 0 and kx = Nx/2 planes (reads mu_hat)
+  static int zpass_planes(const Geom& g, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw, const UpdateArgs<T>& u,
+                          cudaStream_t st);
 };
 
 bool fft_size_supported(int n);
