@@ -109,6 +109,7 @@ int phafd_grid_get(phafd_ctx* ctx, int field, double* host);         /* download
 int phafd_set_zghost(phafd_ctx* ctx, int mode);                      /* CommBrick::borders z swaps, comm_brick.cpp:283-352 */
 int phafd_set_schedule(phafd_ctx* ctx, int schedule);
 int phafd_set_keep_chempot(phafd_ctx* ctx, int keep);               /* also store mu = deposit + FH (grid->chempot) each step */
+int phafd_set_plane_fusion(phafd_ctx* ctx, int on);                 /* x and y passes fused per z-plane in thread-block clusters (Nx == Ny) */
 
 /* ---- beads (atom_style / atom_populate, atom.cpp:26-110,219-252) ---- */
 int phafd_atoms_create(phafd_ctx* ctx, int n, const int* tags, const int* mol, const int* types, const double* x);

@@ -90,6 +90,7 @@ struct phafd_ctx {
   int schedule = PHAFD_SCHEDULE_RESIDENT;
   bool keep_chempot = false;
   bool chempot_from_mu = false;
+  bool use_plane = false;  // plane-fused x/y passes where they apply (phafd_set_plane_fusion)
   int graph_cur = 0;
   DevBuf phi, gx, gy, gz, dep, mu;
   DevBuf phat[2], muhat, w1, wA, wB, wC, wD, wE;
@@ -270,6 +271,24 @@ struct phafd_ctx {
       chk(GridOps<T>::xc2r(geom, E, gz.as<T>(), sg, false, nullptr, sg, twi[0], nonan, st), "x c2r");
     }
     mark(9);
+  }
+
+  // plane-fused y ifft + x c2r of A (phi, dphi/dx; dphi/dy) and B (dphi/dz);
+  // false when the plane path does not apply to this grid
+  template <typename T>
+  bool yx_fused() {
+    const cpx<T>* twy = tw[1][1].as<cpx<T>>();
+    const cpx<T>* twx = tw[0][1].as<cpx<T>>();
+    NanArgs nan{1, d_nan(), d_step()};
+    NanArgs nonan{0, d_nan(), d_step()};
+    const int rc = GridOps<T>::yx_inv(geom, wA.as<cpx<T>>(), phi.as<T>(), (T)1, false, gx.as<T>(), (T)1, twy, twx, nan, st);
+    if (rc == -3) return false;
+    chk(rc, "yx inv");
+    chk(GridOps<T>::yx_inv(geom, wA.as<cpx<T>>(), gy.as<T>(), (T)1, true, nullptr, (T)1, twy, twx, nonan, st), "yx inv");
+    mark(8);
+    chk(GridOps<T>::yx_inv(geom, wB.as<cpx<T>>(), gz.as<T>(), (T)1, false, nullptr, (T)1, twy, twx, nonan, st), "yx inv");
+    mark(9);
+    return true;
   }
 
   // from a spectrum S (z-ifft input) produce phi (scale sp, optional) and grad (scale sg)
@@ -475,9 +494,15 @@ struct phafd_ctx {
         // z fft + update + z ifft in one pass (planes finished separately)
         const cpx<T>* twf[3] = {tw[0][0].as<cpx<T>>(), tw[1][0].as<cpx<T>>(), tw[2][0].as<cpx<T>>()};
         cpx<T>* W1 = w1.as<cpx<T>>();
-        chk(GridOps<T>::xr2c(geom, phi.as<T>(), dep.as<T>(), W1, twf[0], fh, st), "x r2c");
-        mark(4);
-        chk(GridOps<T>::ypass(geom, -1, W1, W1, nullptr, twf[1], st), "y fft");
+        const int prc = use_plane ? GridOps<T>::xy_fwd(geom, phi.as<T>(), dep.as<T>(), W1, twf[0], twf[1], fh, st) : -3;
+        if (prc == -3) {
+          chk(GridOps<T>::xr2c(geom, phi.as<T>(), dep.as<T>(), W1, twf[0], fh, st), "x r2c");
+          mark(4);
+          chk(GridOps<T>::ypass(geom, -1, W1, W1, nullptr, twf[1], st), "y fft");
+        } else {
+          chk(prc, "xy fwd");
+          mark(4);
+        }
         mark(5);
         if (n > 0 && ga_style != PHAFD_GRIDATOM_NONE) launch_dep_zero<T>(ba, dep.as<T>(), st);
         mark(6);
@@ -488,7 +513,7 @@ struct phafd_ctx {
                                tw[2][1].as<cpx<T>>(), u, keep_chempot ? 1 : 0, st), "z fused");
         chk(GridOps<T>::zpass_planes(geom, wA.as<cpx<T>>(), wB.as<cpx<T>>(), tw[2][1].as<cpx<T>>(), u, st), "z planes");
         mark(7);
-        yx_inverse<T>(phi.as<T>(), (T)1, (T)1, true, true);
+        if (!use_plane || !yx_fused<T>()) yx_inverse<T>(phi.as<T>(), (T)1, (T)1, true, true);
       } else {
         // post_force + pre_final_integrate: mu = dep + FH(phi), r2c
         r2c<T>(phi.as<T>(), dep.as<T>(), muhat.as<cpx<T>>(), fh);
@@ -629,6 +654,13 @@ int phafd_set_schedule(phafd_ctx* c, int schedule) {
   if (schedule != PHAFD_SCHEDULE_REFERENCE && schedule != PHAFD_SCHEDULE_RESIDENT) throw std::invalid_argument("bad schedule");
   if (c->setup_done) throw std::runtime_error("schedule must be chosen before setup");
   c->schedule = schedule;
+  API_END(c)
+}
+
+int phafd_set_plane_fusion(phafd_ctx* c, int on) {
+  API_BEGIN(c)
+  c->use_plane = on != 0;
+  c->invalidate_graph();
   API_END(c)
 }
 

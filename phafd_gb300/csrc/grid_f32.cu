@@ -1,5 +1,5 @@
 // Single-precision instantiation of the grid kernels.
-#include "grid_impl.cuh"
+#include "plane_impl.cuh"
 namespace phafd {
 template struct GridOps<float>;
 }

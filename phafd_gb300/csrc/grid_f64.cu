@@ -1,5 +1,5 @@
 // Double-precision instantiation of the grid kernels.
-#include "grid_impl.cuh"
+#include "plane_impl.cuh"
 namespace phafd {
 template struct GridOps<double>;
 bool fft_size_supported(int n) {

@@ -53,6 +53,12 @@ struct GridOps {
   // forward z FFT of mu + update + z inverse FFT (bulk kx); plane tiles store mu_hat only
   static int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
                     const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st);
+  // plane-fused x r2c + y fft (returns -3 when the plane path does not apply)
+  static int xy_fwd(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* twx, const cpx<T>* twy,
+                    const FHArgs& fh, cudaStream_t st);
+  // plane-fused y ifft (optionally times i qy) + x c2r to out0 (plain) and out1 (i qx)
+  static int yx_inv(const Geom& g, const cpx<T>* in, T* out0, T s0, bool ymul, T* out1, T s1, const cpx<T>* twy,
+                    const cpx<T>* twx, const NanArgs& nan, cudaStream_t st);
   // update + z inverse FFT of the kx = 0 and kx = Nx/2 planes (reads mu_hat)
   static int zpass_planes(const Geom& g, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw, const UpdateArgs<T>& u,
                           cudaStream_t st);
