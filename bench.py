@@ -154,10 +154,26 @@ def make_chains(cfg, rank):
 
 
 def replica_cfg(cfg, rank):
+    """Rank r advances an independent replica: the same workload with its own seeds."""
     c = dict(cfg)
     c["grid_seed"] = cfg["grid_seed"] + 1000 * rank
     c["chain_seed"] = cfg["chain_seed"] + 1000 * rank
     return c
+
+
+def max_over_ranks(value, dist=None, device=None):
+    """The slowest rank's time (all_reduce MAX); the value itself at N = 1."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, steps, ms_max):
+    """Whole-job steps/s: every rank advanced `steps` steps of its own replica."""
+    return world * steps / (ms_max / 1000.0)
 
 
 def cpu_baseline_oracle(cfg, chains, nsteps):
@@ -229,13 +245,8 @@ def run_gpu(args):
         if torch_dist:
             torch_dist.barrier()
 
-    def max_over_ranks(v):
-        if not torch_dist:
-            return v
-        import torch
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        torch_dist.all_reduce(t, op=torch_dist.ReduceOp.MAX)
-        return float(t.item())
+    def ranks_max(v):
+        return max_over_ranks(v, torch_dist, "cuda")
 
     cfg = replica_cfg(W.CONFIGS[args.workload], rank)
     chains = make_chains(cfg, rank)
@@ -256,10 +267,10 @@ def run_gpu(args):
     g.synchronize()
     clocks = sampler.stop()
     barrier()
-    ms_max = max_over_ranks(ms)
+    ms_max = ranks_max(ms)
     counters = g.counters()
 
-    value = world * args.steps / (ms_max / 1000.0)
+    value = job_throughput(world, args.steps, ms_max)
     peak, peak_kind = measured_peak()
     s = 4
     sb = stage_bytes(cfg, s)
@@ -311,7 +322,7 @@ def run_gpu(args):
         nb = W.nbeads(cfg)
         h2d = (phi_host.size * 4 + xs.size * 8 + nb * 12) / k
         d2h = nb * (3 * 8 * 3 + 4) + out.size * 4 / k
-        e2e_v = world * k / max_over_ranks(t1 - t0)
+        e2e_v = world * k / ranks_max(t1 - t0)
         line["e2e"] = {"value": e2e_v, "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h),
                        "note": "state uploaded once from host arrays, %d steps each followed by a bead read, phi read at the end; includes set-up" % k}
