@@ -955,12 +955,16 @@ struct oracle_ctx {
     sqrtdt = std::sqrt(dt);
   }
 
-  // Philox noise for a canonical mode (kx, ky, kz); same function on the GPU
+  // Philox noise for a canonical mode (kx, ky, kz); same function on the GPU.
+  // One Philox4x32-10 call serves the mode pair (kz, kz ^ 16): words (c0, c1)
+  // for the mode with bit 4 of kz clear, (c2, c3) for the other; each word
+  // gives a 24-bit uniform, exact in float and double.
   double philox_u(int kx, int ky, int kz, int comp) const {
-    uint64_t idx = ((uint64_t)kx * N[2] + kz) * N[1] + ky;
+    uint64_t idx = ((uint64_t)kx * N[2] + (kz & ~16)) * N[1] + ky;
     uint32_t ctr[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), (uint32_t)timestep, 0x46494c44u};
     Philox::gen(ctr, (uint32_t)c_seed, 0x434f4e4au);
-    return (comp == 0 ? u53(ctr[0], ctr[1]) : u53(ctr[2], ctr[3])) - 0.5;
+    const int w = ((kz >> 4) & 1) * 2 + comp;
+    return (double)(ctr[w] >> 8) * (1.0 / 16777216.0) - 0.5;
   }
 
   double draw(int i, int j, int k, int comp) {

@@ -44,22 +44,25 @@ PHAFD_HD double u53(uint32_t a, uint32_t b) {
   return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
 }
 
-// Philox words of the canonical mode (kx, ky, kz) at `step`: the oracle's
-// philox_u draws u53(c0, c1) - 0.5 and u53(c2, c3) - 0.5 from them.
+// Field noise of the canonical mode (kx, ky, kz) at `step`: the oracle's
+// philox_u.  One Philox4x32-10 call serves the mode pair (kz, kz ^ 16):
+// words (c0, c1) for the mode with bit 4 of kz clear, (c2, c3) for the other;
+// each word gives a 24-bit uniform in [-0.5, 0.5), exact in float and double.
 PHAFD_D void field_noise_words(int kx, int ky, int kz, int Ny, int Nz, uint32_t step, uint32_t seed, uint32_t c[4]) {
-  const uint64_t idx = ((uint64_t)kx * Nz + kz) * Ny + ky;
+  const uint64_t idx = ((uint64_t)kx * Nz + (kz & ~16)) * Ny + ky;
   c[0] = (uint32_t)idx; c[1] = (uint32_t)(idx >> 32); c[2] = step; c[3] = 0x46494c44u;
   philox4x32_10(c, seed, 0x434f4e4au);
 }
-// the two uniforms in [-0.5, 0.5) in precision T: 53 bits for double (the
-// oracle's values exactly); for float the top 24 of those 53 bits
-PHAFD_D void field_noise_pair(const uint32_t c[4], double& u0, double& u1) {
-  u0 = u53(c[0], c[1]) - 0.5;
-  u1 = u53(c[2], c[3]) - 0.5;
+template <typename T>
+PHAFD_D T noise_u24(uint32_t w) {
+  return (T)(w >> 8) * (T)5.9604644775390625e-8 - (T)0.5;
 }
-PHAFD_D void field_noise_pair(const uint32_t c[4], float& u0, float& u1) {
-  u0 = (float)(c[0] >> 8) * 5.9604644775390625e-8f - 0.5f;
-  u1 = (float)(c[2] >> 8) * 5.9604644775390625e-8f - 0.5f;
+// the two uniforms of mode kz from the words of its pair
+template <typename T>
+PHAFD_D void field_noise_pair(const uint32_t c[4], int kz, T& u0, T& u1) {
+  const int s = (kz >> 4) & 1;
+  u0 = noise_u24<T>(c[2 * s]);
+  u1 = noise_u24<T>(c[2 * s + 1]);
 }
 
 // Three standard normals for bead `bead`, half-step `half` of `step`
@@ -97,6 +100,36 @@ PHAFD_D void bead_gauss(uint32_t seed, uint64_t step, int half, int bead, float 
     g[2 * call + 1] = r * s;
   }
   xi[0] = g[0]; xi[1] = g[1]; xi[2] = g[2];
+}
+
+// Asynchronous global -> shared copies (cp.async): issued without staging
+// through registers, so a thread can have its whole share of a tile in
+// flight at once.  commit() closes a group, wait<n>() waits until at most n
+// groups are pending.
+PHAFD_D void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+PHAFD_D void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+PHAFD_D void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+PHAFD_D void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+PHAFD_D void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+template <typename T>
+PHAFD_D void cp_async_elem(cpx<T>* smem, const cpx<T>* gmem) {
+  if constexpr (sizeof(T) == 4) cp_async8(smem, gmem);
+  else cp_async16(smem, gmem);
+}
+template <typename T>
+PHAFD_D void cp_async_real(T* smem, const T* gmem) {
+  if constexpr (sizeof(T) == 4) cp_async4(smem, gmem);
+  else cp_async8(smem, gmem);
 }
 
 // signed wavenumber index, reference convention (fixgrid_conjugate.cpp:80-95):

@@ -1,5 +1,6 @@
 // Double-precision instantiation of the grid kernels.
 #include "plane_impl.cuh"
+#include "reg256.cuh"
 namespace phafd {
 template struct GridOps<double>;
 bool fft_size_supported(int n) {

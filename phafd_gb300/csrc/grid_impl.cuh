@@ -30,6 +30,11 @@ namespace phafd {
   _Pragma("unroll") for (int it_##idx = 0; it_##idx < ((TOTAL) + (NT)-1) / (NT); ++it_##idx) \
     if (const int idx = (int)threadIdx.x + it_##idx * (NT); ((TOTAL) % (NT)) == 0 || idx < (TOTAL))
 
+// ln(p / (1 - p)) of fixgrid_floryhuggins.cpp:81: FP64 as written; FP32 as
+// the difference of two hardware logarithms (relative error ~1e-6)
+PHAFD_D double fh_log_ratio(double p) { return log(p / (1.0 - p)); }
+PHAFD_D float fh_log_ratio(float p) { return __logf(p) - __logf(1.0f - p); }
+
 template <typename T>
 PHAFD_D cpx<T> deriv(cpx<T> a, T dq, int m) {
   // fixgrid_conjugate.cpp:101-103: phi_hat * (0, dq) * m
@@ -53,33 +58,54 @@ k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict_
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NT = N * LB / 16, STR = LB + 1;
+  cpx<T>* sd = s + (size_t)N * STR;  // deposit rows, same layout (PRO == 1)
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * LB;
   unsigned long long nless = 0, ngreat = 0;
+  // rows 2l and 2l+1 of the tile land as the real and imaginary parts of line l
   TILE_LOOP(idx, LB * N, NT) {
     const int l = idx / N, x = idx % N;
-    T v[2] = {(T)0, (T)0};
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int y = y0 + 2 * l + h;
+      T* dst = reinterpret_cast<T*>(&s[x * STR + l]) + h;
+      T* dstd = reinterpret_cast<T*>(&sd[x * STR + l]) + h;
       if (y < Ny) {
         const size_t o = ((size_t)z * Ny + y) * N + x;
-        T p = in0[o];
-        if constexpr (PRO == 1) {
+        cp_async_real(dst, in0 + o);
+        if constexpr (PRO == 1) cp_async_real(dstd, dep + o);
+      } else {
+        *dst = (T)0;
+        if constexpr (PRO == 1) *dstd = (T)0;
+      }
+    }
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  if constexpr (PRO == 1) {
+    TILE_LOOP(idx, LB * N, NT) {
+      const int l = idx / N, x = idx % N;
+      T* v = reinterpret_cast<T*>(&s[x * STR + l]);
+      const T* dd = reinterpret_cast<const T*>(&sd[x * STR + l]);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int y = y0 + 2 * l + h;
+        if (y < Ny) {
+          T p = v[h];
           if (fh.enabled) {
             // fixgrid_floryhuggins.cpp:72-82
             if (p <= (T)0) { p = -p; nless++; }
             else if (p >= (T)1) { p = (T)1 - (p - (T)1); ngreat++; }
-            p = dep[o] + (T)fh.tv * (log(p / ((T)1 - p)) + (T)fh.chi * ((T)1 - (T)2 * p));
+            p = dd[h] + (T)fh.tv * (fh_log_ratio(p) + (T)fh.chi * ((T)1 - (T)2 * p));
           } else {
-            p = dep[o];
+            p = dd[h];
           }
-          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[o] = p;
+          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[((size_t)z * Ny + y) * N + x] = p;
+          v[h] = p;
         }
-        v[h] = p;
       }
     }
-    s[x * STR + l] = mk<T>(v[0], v[1]);
   }
   if constexpr (PRO == 1) {
 #pragma unroll
@@ -197,7 +223,8 @@ k_ypass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
 // Model-B update of one mode from its old spectrum value ph (unnormalised)
 // and mu_hat value mu; (cy, cz) is the canonical mode that owns the noise.
 template <typename T>
-PHAFD_D cpx<T> update_value(const UpdateArgs<T>& u, int kx, int cy, int cz, cpx<T> ph, cpx<T> mu, bool real) {
+PHAFD_D cpx<T> update_value(const UpdateArgs<T>& u, int kx, int cy, int cz, cpx<T> ph, cpx<T> mu, bool real,
+                            const uint32_t* words = nullptr) {
   const int Ny = u.Ny, Nz = u.Nz;
   const T qx = u.qx * (T)kx;
   const T qy = u.qy * (T)wrap_index(cy, Ny);
@@ -213,8 +240,9 @@ PHAFD_D cpx<T> update_value(const UpdateArgs<T>& u, int kx, int cy, int cz, cpx<
     u0 = (T)w.x; u1 = (T)w.y;
   } else if (u.noise == PHAFD_NOISE_PHILOX) {
     uint32_t c[4];
-    field_noise_words(kx, cy, cz, Ny, Nz, (uint32_t)(*u.d_step), u.seed, c);
-    field_noise_pair(c, u0, u1);
+    if (words) { c[0] = words[0]; c[1] = words[1]; c[2] = words[2]; c[3] = words[3]; }
+    else field_noise_words(kx, cy, cz, Ny, Nz, (uint32_t)(*u.d_step), u.seed, c);
+    field_noise_pair(c, cz, u0, u1);
   }
   const T sq = sqrt(q2);
   if (real) {
@@ -318,11 +346,24 @@ k_zfused(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __
   const int kx = blockIdx.y;
   const int c0 = blockIdx.x * LB;
   const bool plane = (kx == 0 || kx == u.Nxh - 1);
+  cpx<T>* sph = s + (size_t)N * STR;  // phi_hat tile, [kz][c]
+  // two async groups: mu (needed first) and phi_hat (needed after the forward FFT)
   TILE_LOOP(idx, LB * N, NT) {
     const int c = idx % LB, e = idx / LB;
     const int ky = c0 + c;
-    s[e * STR + c] = ky < Ny ? muin[((size_t)kx * N + e) * Ny + ky] : mk<T>(0, 0);
+    if (ky < Ny) cp_async_elem(&s[e * STR + c], &muin[((size_t)kx * N + e) * Ny + ky]);
+    else s[e * STR + c] = mk<T>(0, 0);
   }
+  cp_async_commit();
+  if (!plane) {
+    TILE_LOOP(idx, LB * N, NT) {
+      const int c = idx % LB, e = idx / LB;
+      const int ky = c0 + c;
+      if (ky < Ny) cp_async_elem(&sph[e * LB + c], &u.phi_old[((size_t)kx * N + e) * Ny + ky]);
+    }
+  }
+  cp_async_commit();
+  cp_async_wait<1>();
   __syncthreads();
   fft::run_sub<T, N, LB, -1, NT, STR>(s, twf);
   if (plane || store_mu) {
@@ -333,13 +374,15 @@ k_zfused(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __
     }
   }
   if (plane) return;  // uniform per CTA
+  cp_async_wait<0>();
+  __syncthreads();
   TILE_LOOP(idx, LB * N, NT) {
     const int c = idx % LB, e = idx / LB;
     const int ky = c0 + c;
     cpx<T> v = mk<T>(0, 0);
     if (ky < Ny) {
       const size_t o = ((size_t)kx * N + e) * Ny + ky;
-      const cpx<T> ph = scale(u.phi_old[o], u.phi_scale);
+      const cpx<T> ph = scale(sph[e * LB + c], u.phi_scale);
       v = update_value(u, kx, ky, e, ph, s[e * STR + c], false);
       u.phi_new[o] = scale(v, u.store_scale);
     }
@@ -384,7 +427,7 @@ struct Axis {
   static int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
                   cudaStream_t st) {
     constexpr int LB = NLT;
-    const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
+    const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>) * (dep ? 2 : 1);
     dim3 grid((g.ny + 2 * LB - 1) / (2 * LB), g.nz);
     if (dep) {
       auto k = k_xr2c<T, N, LB, 1>;
@@ -472,7 +515,7 @@ struct Axis {
   static int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
                     const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st) {
     constexpr int LB = NLT / 2 >= 1 ? NLT / 2 : 1;
-    const size_t sm = (size_t)N * (2 * LB + 1) * sizeof(cpx<T>);
+    const size_t sm = (size_t)N * (3 * LB + 1) * sizeof(cpx<T>);
     dim3 grid((g.ny + LB - 1) / LB, g.nxh);
     auto k = k_zfused<T, N, LB>;
     if (set_smem(k, sm)) return -1;
@@ -519,9 +562,16 @@ int GridOps<T>::ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, c
   return -2;
 }
 
+namespace r256 {
+template <typename T>
+int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
+           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st);
+}
+
 template <typename T>
 int GridOps<T>::zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
                        const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st) {
+  if (g.nz == 256) return r256::zfused<T>(g, muin, muhat, out0, out1, twf, twi, u, store_mu, st);
   switch (g.nz) {
 #define CASE(n) case n: return Axis<T, n>::zfused(g, muin, muhat, out0, out1, twf, twi, u, store_mu, st);
     PHAFD_FOR_SIZES(CASE)

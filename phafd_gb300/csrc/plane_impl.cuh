@@ -157,7 +157,7 @@ k_xy_fwd(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restric
         if (fh.enabled) {
           if (q <= (T)0) { q = -q; nless++; }
           else if (q >= (T)1) { q = (T)1 - (q - (T)1); ngreat++; }
-          q = dep[o] + (T)fh.tv * (log(q / ((T)1 - q)) + (T)fh.chi * ((T)1 - (T)2 * q));
+          q = dep[o] + (T)fh.tv * (fh_log_ratio(q) + (T)fh.chi * ((T)1 - (T)2 * q));
         } else {
           q = dep[o];
         }

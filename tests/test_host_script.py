@@ -115,10 +115,13 @@ def test_script_run_matches_binding(exe, tmp_path, gpu_lib):
     assert "Run time =" in r.stdout and "chempot had phi < 0" in r.stdout
     phi_script = np.fromfile(tmp_path / "phi.bin", dtype=np.float64).reshape(32, 32, 32)
     from phafd_gb300.gpu import PhafdGPU
-    cfg = dict(W.CONFIGS["32cube_64beads"], dt=5e-4)
+    cfg = dict(W.CONFIGS["32cube_64beads"], dt=5e-4, field_noise="philox")  # package gpu default noise
     g = PhafdGPU(precision=32)
     W.apply(g, cfg, chains=chains)
     g.set_timestep(0)
     g.setup()
     g.run(20)
-    assert np.array_equal(g.grid_get("phi"), phi_script)
+    # same commands, same library; the bead deposit is summed with float
+    # atomics, so two runs agree to FP32 round-off, not bit for bit
+    ref = g.grid_get("phi")
+    assert np.abs(ref - phi_script).max() < 1e-5 * np.abs(ref).max()
