@@ -102,6 +102,12 @@ __global__ void k_bin_count(BeadArgs a) {
   const int bz = bin_coord(a.x[3 * i + 2], a.boxlo[2], a.bininv[2], a.nb[2]);
   const int b = (bz * a.nb[1] + by) * a.nb[0] + bx;
   a.bin_of[i] = b;
+  if (a.bin_off) {
+    const double bs[3] = {a.period[0] / a.nb[0], a.period[1] / a.nb[1], a.period[2] / a.nb[2]};
+    a.bin_off[i] = make_float4((float)(a.x[3 * i] - (a.boxlo[0] + bx * bs[0])),
+                               (float)(a.x[3 * i + 1] - (a.boxlo[1] + by * bs[1])),
+                               (float)(a.x[3 * i + 2] - (a.boxlo[2] + bz * bs[2])), 0.f);
+  }
   atomicAdd(&a.bin_count[b], 1);
 }
 
@@ -302,6 +308,111 @@ __global__ void k_build(BeadArgs a) {
     a.ngl[i] = cnt;
   }
   // neighbor.cpp:106-109
+  a.xhold[3 * i] = xi[0];
+  a.xhold[3 * i + 1] = xi[1];
+  a.xhold[3 * i + 2] = xi[2];
+}
+
+// FP32 list build (production precision): the same stencil scans with
+// distances formed from bin-relative float offsets (bead list) and from the
+// bead position in grid units split into an integer part and a fraction
+// (grid list); the cutoff carries a 1e-5 relative margin, so the lists are
+// supersets of the exact ones (the extra pairs lie beyond every interaction
+// cutoff, which the pair kernel tests again each step).
+__global__ void k_build_fp32(BeadArgs a) {
+  if (!*a.flag) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const float cut2 = (float)(a.cutneighsq * (1.0 + 1e-5));
+  if (a.nbr) {
+    const int b = a.bin_of[i];
+    const int bx = b % a.nb[0], by = (b / a.nb[0]) % a.nb[1], bz = b / (a.nb[0] * a.nb[1]);
+    const float4 oi = a.bin_off[i];
+    const float bs[3] = {(float)(a.period[0] / a.nb[0]), (float)(a.period[1] / a.nb[1]), (float)(a.period[2] / a.nb[2])};
+    int cnt = 0;
+    for (int dz = -1; dz <= 1; ++dz) {
+      int cz = bz + dz, sz = 0;
+      if (cz < 0) { cz += a.nb[2]; sz = -1; } else if (cz >= a.nb[2]) { cz -= a.nb[2]; sz = 1; }
+      if (sz != 0 && !a.zperiodic) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        int cy = by + dy, sy = 0;
+        if (cy < 0) { cy += a.nb[1]; sy = -1; } else if (cy >= a.nb[1]) { cy -= a.nb[1]; sy = 1; }
+        for (int dx = -1; dx <= 1; ++dx) {
+          int cx = bx + dx, sx = 0;
+          if (cx < 0) { cx += a.nb[0]; sx = -1; } else if (cx >= a.nb[0]) { cx -= a.nb[0]; sx = 1; }
+          const int nbn = (cz * a.nb[1] + cy) * a.nb[0] + cx;
+          const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
+          // x_i - (x_j + s L) = (b_i - b_j' ) bs + off_i - off_j, with b_j' = c + s nb
+          const float ex = (float)(bx - (cx + sx * a.nb[0])) * bs[0] + oi.x;
+          const float ey = (float)(by - (cy + sy * a.nb[1])) * bs[1] + oi.y;
+          const float ez = (float)(bz - (cz + sz * a.nb[2])) * bs[2] + oi.z;
+          for (int p = a.bin_start[nbn]; p < a.bin_start[nbn + 1]; ++p) {
+            const int j = a.sorted[p];
+            if (j == i && code == 13) continue;
+            const float4 oj = a.bin_off[j];
+            const float d0 = ex - oj.x, d1 = ey - oj.y, d2 = ez - oj.z;
+            if (d0 * d0 + d1 * d1 + d2 * d2 <= cut2) {
+              if (cnt < a.maxnb) a.nbr[(size_t)i * a.maxnb + cnt] = (j << 5) | code;
+              ++cnt;
+            }
+          }
+        }
+      }
+    }
+    if (cnt > a.maxnb) { atomicOr(a.status, ST_OVERFLOW); cnt = a.maxnb; }
+    a.nnbr[i] = cnt;
+  }
+  const double xi[3] = {a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2]};
+  if (a.gl) {
+    int gi[3];
+    float gf[3], dxf[3];
+    for (int d = 0; d < 3; ++d) {
+      const double ud = (xi[d] - a.boxlo[d]) / a.dx[d];
+      const double fl = floor(ud);
+      gi[d] = (int)fl;
+      gf[d] = (float)(ud - fl);
+      dxf[d] = (float)a.dx[d];
+    }
+    const float cut = (float)a.cutneigh * 1.00001f;
+    int cnt = 0;
+    const int rz = (int)ceilf(cut / dxf[2]) + 1;
+    for (int oz = -rz; oz <= rz; ++oz) {
+      const int kz = gi[2] + oz;
+      int wz = kz, sz = 0;
+      if (wz < 0) { wz += a.N[2]; sz = 1; } else if (wz >= a.N[2]) { wz -= a.N[2]; sz = -1; }
+      if (wz < 0 || wz >= a.N[2]) continue;
+      if (sz != 0 && !a.zperiodic) continue;
+      const float dz = ((float)oz - gf[2]) * dxf[2];
+      const float remz = cut2 - dz * dz;
+      if (remz < 0.f) continue;
+      const int ry = (int)ceilf(sqrtf(remz) / dxf[1]) + 1;
+      for (int oy = -ry; oy <= ry; ++oy) {
+        const int ky = gi[1] + oy;
+        int wy = ky, sy = 0;
+        if (wy < 0) { wy += a.N[1]; sy = 1; } else if (wy >= a.N[1]) { wy -= a.N[1]; sy = -1; }
+        if (wy < 0 || wy >= a.N[1]) continue;
+        const float dy = ((float)oy - gf[1]) * dxf[1];
+        const float remy = remz - dy * dy;
+        if (remy < 0.f) continue;
+        const int rx = (int)ceilf(sqrtf(remy) / dxf[0]) + 1;
+        for (int ox = -rx; ox <= rx; ++ox) {
+          const int kx = gi[0] + ox;
+          int wx = kx, sx = 0;
+          if (wx < 0) { wx += a.N[0]; sx = 1; } else if (wx >= a.N[0]) { wx -= a.N[0]; sx = -1; }
+          if (wx < 0 || wx >= a.N[0]) continue;
+          const float dxx = ((float)ox - gf[0]) * dxf[0];
+          if (dxx * dxx + dy * dy + dz * dz <= cut2) {
+            const uint32_t node = (uint32_t)(((long long)wz * a.N[1] + wy) * a.N[0] + wx);
+            const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
+            if (cnt < a.maxg) a.gl[(size_t)i * a.maxg + cnt] = (node << 5) | (uint32_t)code;
+            ++cnt;
+          }
+        }
+      }
+    }
+    if (cnt > a.maxg) { atomicOr(a.status, ST_OVERFLOW); cnt = a.maxg; }
+    a.ngl[i] = cnt;
+  }
   a.xhold[3 * i] = xi[0];
   a.xhold[3 * i + 1] = xi[1];
   a.xhold[3 * i + 2] = xi[2];
@@ -567,7 +678,8 @@ void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st) {
   k_scan_add<<<nblocks, 1024, 0, st>>>(a);
   k_bin_fill<<<nblk(a.n, T), T, 0, st>>>(a);
   k_bin_sort<<<nblk(a.nbins, T) > 4096 ? 4096 : nblk(a.nbins, T), T, 0, st>>>(a);
-  k_build<<<nblk(a.n, 128), 128, 0, st>>>(a);
+  if (a.fp32_lists) k_build_fp32<<<nblk(a.n, 128), 128, 0, st>>>(a);
+  else k_build<<<nblk(a.n, 128), 128, 0, st>>>(a);
   k_build_done<<<1, 1, 0, st>>>(a);
 }
 

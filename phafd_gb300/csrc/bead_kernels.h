@@ -25,6 +25,8 @@ struct BeadArgs {
   double bininv[3];
   long long nbins;
   int *bin_of, *bin_count, *bin_cursor, *bin_start, *sorted, *scan_tmp;
+  float4* bin_off;   // position minus the corner of its bin (FP32 lists)
+  int fp32_lists;    // 1: list membership in FP32 with a superset margin
   // lists
   int* nbr;
   int* nnbr;

@@ -80,6 +80,8 @@ struct phafd_ctx {
   std::string err;
   int device = 0, precision = PHAFD_FP32;
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;           // bead branch, forked from st inside a step
+  cudaEvent_t ev_fork = nullptr, ev_dep = nullptr, ev_join = nullptr;
   // domain / grid
   bool boxset = false, gridset = false, populated = false;
   double boxlo[3] = {0, 0, 0}, boxhi[3] = {0, 0, 0}, period[3] = {0, 0, 0};
@@ -102,7 +104,7 @@ struct phafd_ctx {
   int n = 0, ntypes = 0;
   std::vector<int> tags, types, mol;
   DevBuf bx, bux, bf, bxhold, bfchain, btang, bimage, btype;
-  DevBuf bin_of, bin_count, bin_cursor, bin_start, sorted, scan_tmp;
+  DevBuf bin_of, bin_count, bin_cursor, bin_start, sorted, scan_tmp, bin_off;
   DevBuf nbr, nnbr, gl, ngl;
   DevBuf dragc, sf_fix, sf_start, sf_len, sf_par;
   BeadArgs ba{};
@@ -154,6 +156,8 @@ struct phafd_ctx {
   ~phafd_ctx() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (uref_h) cudaFreeHost(uref_h);
+    for (cudaEvent_t e : {ev_fork, ev_dep, ev_join}) if (e) cudaEventDestroy(e);
+    if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -318,6 +322,8 @@ struct phafd_ctx {
     a.flag = d_flag(); a.status = d_status(); a.ncalls = d_ncalls(); a.d_step = d_step();
     a.bin_of = bin_of.as<int>(); a.bin_count = bin_count.as<int>(); a.bin_cursor = bin_cursor.as<int>();
     a.bin_start = bin_start.as<int>(); a.sorted = sorted.as<int>(); a.scan_tmp = scan_tmp.as<int>();
+    a.fp32_lists = precision == PHAFD_FP32 ? 1 : 0;
+    a.bin_off = a.fp32_lists ? bin_off.as<float4>() : nullptr;
     a.nbr = have_lj ? nbr.as<int>() : nullptr;
     a.nnbr = nnbr.as<int>();
     a.gl = ga_style != PHAFD_GRIDATOM_NONE ? gl.as<uint32_t>() : nullptr;
@@ -359,6 +365,7 @@ struct phafd_ctx {
     bin_cursor.alloc(nbins * 4);
     bin_start.alloc((nbins + 1) * 4);
     sorted.alloc(std::max(n, 1) * 4);
+    bin_off.alloc((size_t)std::max(n, 1) * sizeof(float4));
     scan_tmp.alloc(((nbins + 1023) / 1024 + 1) * 4);
     ba.maxnb = 128;
     if (have_lj) nbr.alloc((size_t)std::max(n, 1) * ba.maxnb * 4);
@@ -483,9 +490,20 @@ struct phafd_ctx {
     PairArgs<T> pa = pair_args<T>();
     if (n > 0 && (have_lj || ga_style != PHAFD_GRIDATOM_NONE)) launch_pair<T>(ba, pa, st);
     mark(2);
+    // Bead integration needs only F: off the profiling path it runs on a
+    // second stream, a parallel branch of the step, while the field passes run.
+    const bool fork = !profiling && n > 0;
+    cudaStream_t bs = fork ? st2 : st;
+    if (fork) {
+      CK(cudaEventRecord(ev_fork, st));
+      CK(cudaStreamWaitEvent(st2, ev_fork, 0));
+    }
     // initial_integrate
-    launch_drag(ba, dt, st);
-    launch_chain_half<T>(ba, 0, dt, st);
+    launch_drag(ba, dt, bs);
+    launch_chain_half<T>(ba, 0, dt, bs);
+    // final_integrate of the beads (independent of the field update)
+    launch_drag(ba, dt, bs);
+    launch_chain_half<T>(ba, 1, dt, bs);
     mark(3);
     if (have_conj) {
       FHArgs fh{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
@@ -498,13 +516,14 @@ struct phafd_ctx {
         if (prc == -3) {
           chk(GridOps<T>::xr2c(geom, phi.as<T>(), dep.as<T>(), W1, twf[0], fh, st), "x r2c");
           mark(4);
+          dep_reset<T>(fork);
           chk(GridOps<T>::ypass(geom, -1, W1, W1, nullptr, twf[1], st), "y fft");
         } else {
           chk(prc, "xy fwd");
           mark(4);
+          dep_reset<T>(fork);
         }
         mark(5);
-        if (n > 0 && ga_style != PHAFD_GRIDATOM_NONE) launch_dep_zero<T>(ba, dep.as<T>(), st);
         mark(6);
         // the state stays an unnormalised r2c spectrum: store N * update
         UpdateArgs<T> u = update_args<T>(phat[cur].as<cpx<T>>(), muhat.as<cpx<T>>(), phat[1 - cur].as<cpx<T>>(),
@@ -517,14 +536,29 @@ struct phafd_ctx {
       } else {
         // post_force + pre_final_integrate: mu = dep + FH(phi), r2c
         r2c<T>(phi.as<T>(), dep.as<T>(), muhat.as<cpx<T>>(), fh);
-        if (n > 0 && ga_style != PHAFD_GRIDATOM_NONE) launch_dep_zero<T>(ba, dep.as<T>(), st);
+        dep_reset<T>(fork);
         UpdateArgs<T> u = update_args<T>(w1.as<cpx<T>>(), muhat.as<cpx<T>>(), phat[0].as<cpx<T>>(), 1.0);
         inverse_chain<T>(nullptr, &u, phi.as<T>(), (T)1, (T)1, false, true);
       }
     }
-    launch_drag(ba, dt, st);
-    launch_chain_half<T>(ba, 1, dt, st);
-    mark(3);
+    if (fork) {  // join the bead branch before the next step
+      CK(cudaEventRecord(ev_join, st2));
+      CK(cudaStreamWaitEvent(st, ev_join, 0));
+    }
+  }
+
+  // zero the deposit nodes once the x pass has consumed them: on the bead
+  // branch when forked, so it overlaps the field passes
+  template <typename T>
+  void dep_reset(bool fork) {
+    if (n == 0 || ga_style == PHAFD_GRIDATOM_NONE) return;
+    if (fork) {
+      CK(cudaEventRecord(ev_dep, st));
+      CK(cudaStreamWaitEvent(st2, ev_dep, 0));
+      launch_dep_zero<T>(ba, dep.as<T>(), st2);
+    } else {
+      launch_dep_zero<T>(ba, dep.as<T>(), st);
+    }
   }
 
   void step_once() {
@@ -620,6 +654,10 @@ int phafd_ctx_create(phafd_ctx** out, int device, int precision) {
   try {
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_dep, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     c->d_counters.alloc(6 * sizeof(long long));
     long long init[6] = {0, 0, 0, -1, 0, 0};
     CK(cudaMemcpy(c->d_counters.p, init, sizeof(init), cudaMemcpyHostToDevice));

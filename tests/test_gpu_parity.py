@@ -208,3 +208,17 @@ def test_plane_fused_steps_match_oracle(gpu_lib, precision, n, tol, plane):
     xo = o.atoms_get()[0]
     xg = g.atoms_get()[0]
     assert np.abs(xg - xo).max() < (1e-10 if precision == 64 else 1e-6) * np.abs(xo).max()
+
+
+@pytest.mark.parametrize("zghost", ["periodic", "rank1"])
+def test_fp32_lists_are_tight_supersets(gpu_lib, zghost):
+    """FP32 contexts build their lists in FP32 with a 1e-5 relative cutoff
+    margin: every exact pair is present and extras are at most a trace."""
+    o = Oracle(); g = gpu(32)
+    for d in (o, g):
+        small_scene(d, n=32, L=32.0, nbeads=600, zghost=zghost, seed=11)
+        d.setup()
+    for got, want in ((canon_half(g.half_list()), canon_half(o.half_list())),
+                      (canon_grid(g.grid_list()), canon_grid(o.grid_list()))):
+        assert want <= got
+        assert len(got - want) <= max(2, len(want) // 1000)
