@@ -138,6 +138,8 @@ int phafd_set_dt(phafd_ctx* ctx, double dt);                      /* "dt" comman
 int phafd_set_timestep(phafd_ctx* ctx, long long step);           /* "timestep" command */
 int phafd_setup(phafd_ctx* ctx);                                  /* Integrate::setup, integrate.cpp:33-88 */
 int phafd_run(phafd_ctx* ctx, int nsteps);                        /* Integrate::run, integrate.cpp:90-219 */
+int phafd_run_async(phafd_ctx* ctx, int nsteps);                  /* enqueue the steps and return; phafd_synchronize
+                                                                     waits and reports device status (replicas overlap) */
 int phafd_counters_get(phafd_ctx* ctx, phafd_counters* out);      /* Integrate::finalise counters, integrate.cpp:418-443 */
 int phafd_synchronize(phafd_ctx* ctx);
 int phafd_run_timed(phafd_ctx* ctx, int nsteps, double* ms);      /* run, timed by CUDA events on the context's stream */

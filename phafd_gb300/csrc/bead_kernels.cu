@@ -643,9 +643,9 @@ __global__ void k_chain_move(BeadArgs a, int half, double dt) {
   const T ft[3] = {fc[0] + fp[0], fc[1] + fp[1], fc[2] + fp[2]};
   const T tf = t[0] * ft[0] + t[1] * ft[1] + t[2] * ft[2];
   const T tx = t[0] * xi[0] + t[1] * xi[1] + t[2] * xi[2];
-  const T aa = (T)(1.0 / P.zeta_perp), bpar = (T)(1.0 / P.zeta_para - 1.0 / P.zeta_perp);
-  const T sa = (T)(1.0 / sqrt(P.zeta_perp)), sb = (T)(1.0 / sqrt(P.zeta_para) - 1.0 / sqrt(P.zeta_perp));
-  const T amp = (T)sqrt(2.0 * P.temp * 0.5 * dt);
+  const T aa = (T)P.inv_perp, bpar = (T)P.dinv;
+  const T sa = (T)P.sinv_perp, sb = (T)P.dsinv;
+  const T amp = sqrt((T)(P.temp * dt));  // sqrt(2 T h), h = dt/2
   const int im = a.image[i];
   const int box[3] = {(im & IMGMASK) - IMGMAX, (im >> IMGBITS & IMGMASK) - IMGMAX, (im >> IMG2BITS) - IMGMAX};
   bool bad = false;

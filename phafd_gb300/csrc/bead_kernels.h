@@ -8,6 +8,10 @@ struct SemiDev {
   double bondlength, zeta_para, zeta_perp, bending, temp, kbond;
   uint32_t seed;
   int noise;
+  // per-fix constants of the displacement, precomputed on the host:
+  // 1/zeta_perp, 1/zeta_para - 1/zeta_perp, their square-root forms, and
+  // sqrt(2 T h) is formed with h = dt/2 on the device
+  double inv_perp, dinv, sinv_perp, dsinv;
 };
 
 struct BeadArgs {

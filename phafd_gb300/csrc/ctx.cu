@@ -396,7 +396,13 @@ struct phafd_ctx {
     std::vector<SemiDev> par;
     for (size_t k = 0; k < semis.size(); ++k) {
       const auto& p = semis[k].second;
-      par.push_back(SemiDev{p.bondlength, p.zeta_para, p.zeta_perp, p.bending, p.temp, p.kbond, (uint32_t)p.seed, p.noise});
+      SemiDev d{p.bondlength, p.zeta_para, p.zeta_perp, p.bending, p.temp, p.kbond, (uint32_t)p.seed, p.noise,
+                0, 0, 0, 0};
+      d.inv_perp = 1.0 / p.zeta_perp;
+      d.dinv = 1.0 / p.zeta_para - 1.0 / p.zeta_perp;
+      d.sinv_perp = 1.0 / std::sqrt(p.zeta_perp);
+      d.dsinv = 1.0 / std::sqrt(p.zeta_para) - 1.0 / std::sqrt(p.zeta_perp);
+      par.push_back(d);
       for (auto& r : semis[k].first)
         for (int j = r.start; j < r.end; ++j) {
           if (fix[j] >= 0) throw std::runtime_error("a bead may belong to one semiflexible fix only");
@@ -1004,6 +1010,8 @@ int phafd_setup(phafd_ctx* c) {
   API_END(c)
 }
 
+static void enqueue_run(phafd_ctx* c, int nsteps);
+
 int phafd_run(phafd_ctx* c, int nsteps) {
   API_BEGIN(c)
   CK(cudaSetDevice(c->device));
@@ -1011,6 +1019,30 @@ int phafd_run(phafd_ctx* c, int nsteps) {
     int rc = phafd_setup(c);
     if (rc) return rc;
   }
+  enqueue_run(c, nsteps);
+  CK(cudaStreamSynchronize(c->st));
+  if (c->keep_chempot && c->have_conj && nsteps > 0) c->chempot_from_mu = true;
+  int rc = check_status(c);
+  if (rc) return rc;
+  API_END(c)
+}
+
+int phafd_run_async(phafd_ctx* c, int nsteps) {
+  API_BEGIN(c)
+  CK(cudaSetDevice(c->device));
+  if (!c->setup_done) {
+    int rc = phafd_setup(c);
+    if (rc) return rc;
+  }
+  if (c->have_conj && c->c_noise == PHAFD_NOISE_REFERENCE)
+    throw std::runtime_error("the reference noise stream is generated on the host: use phafd_run");
+  enqueue_run(c, nsteps);
+  if (c->keep_chempot && c->have_conj && nsteps > 0) c->chempot_from_mu = true;
+  API_END(c)
+}
+
+static void enqueue_run(phafd_ctx* c, int nsteps) {
+  {
   const bool use_graph = c->c_noise != PHAFD_NOISE_REFERENCE || !c->have_conj;
   const bool resident = c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj;
   for (int s = 0; s < nsteps; ++s) {
@@ -1066,11 +1098,7 @@ int phafd_run(phafd_ctx* c, int nsteps) {
     c->timestep += 1;
     if (resident) resident_spectrum_flip(c);
   }
-  CK(cudaStreamSynchronize(c->st));
-  if (c->keep_chempot && c->have_conj && nsteps > 0) c->chempot_from_mu = true;
-  int rc = check_status(c);
-  if (rc) return rc;
-  API_END(c)
+  }
 }
 
 int phafd_run_timed(phafd_ctx* c, int nsteps, double* ms) {
@@ -1132,6 +1160,8 @@ int phafd_profile_stages(phafd_ctx* c, int nsteps, double* stage_ms, int nstage)
 int phafd_synchronize(phafd_ctx* c) {
   API_BEGIN(c)
   CK(cudaStreamSynchronize(c->st));
+  int rc = check_status(c);
+  if (rc) return rc;
   API_END(c)
 }
 

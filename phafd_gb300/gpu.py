@@ -29,7 +29,8 @@ EXPORTS = [
     "phafd_neighbor",
     "phafd_fix_conjugate_volfrac", "phafd_fix_floryhuggins", "phafd_fix_gradphi", "phafd_fix_drag",
     "phafd_fix_semiflexible",
-    "phafd_set_dt", "phafd_set_timestep", "phafd_setup", "phafd_run", "phafd_counters_get", "phafd_synchronize",
+    "phafd_set_dt", "phafd_set_timestep", "phafd_setup", "phafd_run", "phafd_run_async", "phafd_counters_get",
+    "phafd_synchronize",
     "phafd_run_timed", "phafd_profile_stages",
     "phafd_half_list_size", "phafd_half_list", "phafd_grid_list_size", "phafd_grid_list",
     "phafd_stage_gradient", "phafd_stage_borders_and_build", "phafd_stage_pairs",
@@ -97,6 +98,7 @@ def load(path=None):
         "phafd_set_timestep": [vp, C.c_longlong],
         "phafd_setup": [vp],
         "phafd_run": [vp, C.c_int],
+        "phafd_run_async": [vp, C.c_int],
         "phafd_counters_get": [vp, C.POINTER(Counters)],
         "phafd_synchronize": [vp],
         "phafd_run_timed": [vp, C.c_int, C.POINTER(C.c_double)],
@@ -244,6 +246,11 @@ class PhafdGPU:
 
     def run(self, nsteps):
         self._call("phafd_run", nsteps)
+
+    def run_async(self, nsteps):
+        """Enqueue `nsteps` steps and return; synchronize() waits and raises on
+        a device-side failure."""
+        self._call("phafd_run_async", nsteps)
 
     def synchronize(self):
         self._call("phafd_synchronize")
