@@ -38,6 +38,7 @@ extern "C" {
 #define PHAFD_ERR_CONSTRAINT -5   /* chain step failed (non-finite / stretch)*/
 #define PHAFD_ERR_UNSUPPORTED -6  /* size or option not built                */
 #define PHAFD_ERR_NOMEM -7
+#define PHAFD_ERR_TIMEOUT -8      /* a bounded device wait gave up           */
 
 /* ---- precision of the grid path ---- */
 #define PHAFD_FP64 64
@@ -90,6 +91,7 @@ typedef struct phafd_counters {
   long long status;          /* sticky PHAFD_ERR_* raised on the device, 0 if none     */
   long long nan_step;        /* first step whose phi(0,0,0) was NaN, -1 if none        */
   long long kernels_per_step; /* kernel launches of one step in the captured graph, 0 before capture */
+  long long kernels_per_rebuild; /* launches added by a neighbor rebuild inside the graph          */
 } phafd_counters;
 
 typedef struct phafd_ctx phafd_ctx;
@@ -148,6 +150,37 @@ int phafd_run_timed(phafd_ctx* ctx, int nsteps, double* ms);      /* run, timed 
  * integration, 4 x r2c + Flory-Huggins, 5 y fft, 6 z fft, 7 z pass with the
  * Model-B update, 8 y ifft, 9 x c2r; stage_ms has nstage entries */
 int phafd_profile_stages(phafd_ctx* ctx, int nsteps, double* stage_ms, int nstage);
+
+/* ---- spectra (compute complex, compute_complex.cpp:54-91) ----
+ * quant: real, imag, modulus |F| or norm |F|^2 of ft_phi / ft_chempot times
+ * 1/(dx dy dz) (squared for norm), one value per mode in the reference's
+ * transposed layout [ky][kz][kx], kx in [0, Nx/2] */
+#define PHAFD_COMPLEX_REAL 0
+#define PHAFD_COMPLEX_IMAG 1
+#define PHAFD_COMPLEX_MODULUS 2
+#define PHAFD_COMPLEX_NORM 3
+int phafd_compute_complex(phafd_ctx* ctx, int field, int quant, double* out);
+/* structure factor of the current phi (no reference counterpart: the shell
+ * average of compute complex ft_phi norm): S[b] = mean of |phi_hat(q)|^2 / N
+ * over the modes with b <= |q| / dq < b + 1, dq = 2 pi / L of the x axis,
+ * q != 0, every mode of the full spectrum counted once (the half spectrum
+ * with its mirror modes).  counts[b] = modes in shell b (may be NULL). */
+int phafd_structure_factor(phafd_ctx* ctx, int nbins, double* sk, long long* counts);
+
+/* ---- learned macro step support (no reference counterpart) ----
+ * nsub > 1 makes each step a macro step: the Model-B update of nsub
+ * linearised substeps (dmu/dphi = f2 about the mean, the rest of mu frozen at
+ * the step's start), beads moved with nsub * dt; nsub = 1 restores the plain
+ * step.  phafd_grid_device returns the device address of a real field (FP32
+ * or FP64 as the context); phafd_deposit_density writes to the device array
+ * rho (nx*ny*nz, context precision) the sum over beads of the gridatom shape
+ * function (pair_gridatom_*.cpp without epsilon and the phi factor);
+ * phafd_grid_add_device adds scale * src (device, context precision) to phi
+ * and re-derives the spectrum and gradient the next step starts from. */
+int phafd_set_linear_substeps(phafd_ctx* ctx, int nsub, double f2);
+int phafd_grid_device(phafd_ctx* ctx, int field, void** dev);
+int phafd_deposit_density(phafd_ctx* ctx, void* rho);
+int phafd_grid_add_device(phafd_ctx* ctx, const void* src, double scale);
 
 /* ---- neighbor-list export (NeighList ilist/firstneigh, neigh_list.hpp) ----
  * half list: (tag_i, tag_j, image code of j relative to i)

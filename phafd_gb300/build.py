@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libphafd_gpu.so")
 EXE = os.path.join(OUT, "phafd_gpu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
-CU_SOURCES = ["ctx.cu", "bead_kernels.cu", "grid_f32.cu", "grid_f64.cu", "noalloc.cu"]
+CU_SOURCES = ["ctx.cu", "bead_kernels.cu", "grid_f32.cu", "grid_f64.cu", "noalloc.cu", "fno.cu"]
 
 
 def nvcc():
@@ -42,6 +42,7 @@ def _newer(target, deps):
 def _headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     hs.append(os.path.join(ROOT, "include", "phafd_gpu.h"))
+    hs.append(os.path.join(ROOT, "include", "phafd_fno.h"))
     return hs
 
 

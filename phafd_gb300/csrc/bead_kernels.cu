@@ -39,14 +39,34 @@ __device__ __forceinline__ int bin_coord(double x, double lo, double inv, int nb
 }  // namespace
 
 // neighbor.cpp:79-97
-__global__ void k_check(BeadArgs a) {
+// With use_cond the last block to finish (threadfence pattern) copies the
+// flag into the graph conditional that gates the rebuild body.
+__global__ void k_check(BeadArgs a, cudaGraphConditionalHandle h, int use_cond) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  const double d0 = a.x[3 * i] - a.xhold[3 * i];
-  const double d1 = a.x[3 * i + 1] - a.xhold[3 * i + 1];
-  const double d2 = a.x[3 * i + 2] - a.xhold[3 * i + 2];
-  const double rsq = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
-  if (rsq > a.triggersq) *a.flag = 1;
+  if (i < a.n) {
+    const double d0 = a.x[3 * i] - a.xhold[3 * i];
+    const double d1 = a.x[3 * i + 1] - a.xhold[3 * i + 1];
+    const double d2 = a.x[3 * i + 2] - a.xhold[3 * i + 2];
+    const double rsq = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+    if (rsq > a.triggersq) {
+      atomicOr(a.flag, 1);
+      __threadfence();
+    }
+  }
+  if (!use_cond) return;
+  __shared__ int last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(a.check_done, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    const int f = atomicOr(a.flag, 0);
+    *a.check_done = 0;
+    cudaGraphSetConditional(h, f ? 1u : 0u);
+  }
 }
 
 // domain.cpp:102-163 then Domain::unmap
@@ -550,6 +570,42 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
   }
 }
 
+// rho[node] += shape of the gridatom coupling (epsilon 1, no phi factor) of
+// every bead within its cutoff: the bead-density input of the learned
+// propagator.  One thread per bead, FP64 separations rounded once.
+template <typename T>
+__global__ void k_density(BeadArgs a, PairArgs<T> p, T* rho) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n || !a.gl || p.ga_style == PHAFD_GRIDATOM_NONE) return;
+  const double xi[3] = {a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2]};
+  const int cnt = a.ngl[i];
+  const T cutsq = (T)p.ga_cutsq[a.type[i]];
+  for (int k = 0; k < cnt; ++k) {
+    const uint32_t e = a.gl[(size_t)i * a.maxg + k];
+    const uint32_t node = e >> 5;
+    const int code = (int)(e & 31u);
+    const int g3[3] = {(int)(node % (uint32_t)a.N[0]), (int)((node / (uint32_t)a.N[0]) % (uint32_t)a.N[1]),
+                       (int)(node / ((uint32_t)a.N[0] * (uint32_t)a.N[1]))};
+    T dd[3];
+    for (int d = 0; d < 3; ++d) dd[d] = (T)((double)g3[d] * a.dx[d] + a.boxlo[d] - (xi[d] + img_shift(code, d, a)));
+    T rsq = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
+    const bool inside = (p.ga_style == PHAFD_GRIDATOM_GAUSSIAN) ? (rsq <= cutsq) : (rsq < cutsq);
+    if (!inside) continue;
+    rsq = rsq / cutsq;
+    const T v = p.ga_style == PHAFD_GRIDATOM_GAUSSIAN ? (exp(-rsq / (T)2.0) - exp((T)-0.5)) * exp((T)0.5)
+                                                      : exp((T)-1. / ((T)1 - rsq) + (T)1);
+    atomicAdd(rho + node, v);
+  }
+}
+
+template <typename T>
+void launch_density(const BeadArgs& a, const PairArgs<T>& p, T* rho, cudaStream_t st) {
+  if (a.n == 0) return;
+  k_density<T><<<(unsigned)((a.n + 127) / 128), 128, 0, st>>>(a, p, rho);
+}
+template void launch_density<float>(const BeadArgs&, const PairArgs<float>&, float*, cudaStream_t);
+template void launch_density<double>(const BeadArgs&, const PairArgs<double>&, double*, cudaStream_t);
+
 // zero the nodes a bead may have deposited on (sparse reset of dep)
 template <typename T>
 __global__ void k_dep_zero(BeadArgs a, T* dep) {
@@ -664,11 +720,21 @@ static inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) 
 
 void launch_step_begin(long long* d_step, cudaStream_t st) { k_step_begin<<<1, 1, 0, st>>>(d_step); }
 
+void launch_neighbor_check(const BeadArgs& a, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
+  if (a.n == 0) return;
+  k_check<<<nblk(a.n, 256), 256, 0, st>>>(a, h, use_cond);
+}
+
 void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st) {
   if (a.n == 0) return;
-  const int T = 256;
   if (force) cudaMemsetAsync(a.flag, 0xff, sizeof(int), st);
-  else k_check<<<nblk(a.n, T), T, 0, st>>>(a);
+  else launch_neighbor_check(a, 0, 0, st);
+  launch_rebuild(a, st);
+}
+
+void launch_rebuild(const BeadArgs& a, cudaStream_t st) {
+  if (a.n == 0) return;
+  const int T = 256;
   k_pbc<<<nblk(a.n, T), T, 0, st>>>(a);
   k_bin_clear<<<nblk(a.nbins, T) > 4096 ? 4096 : nblk(a.nbins, T), T, 0, st>>>(a);
   k_bin_count<<<nblk(a.n, T), T, 0, st>>>(a);

@@ -21,6 +21,7 @@ struct BeadArgs {
   double boxlo[3], boxhi[3], period[3];
   double triggersq, cutneigh, cutneighsq;
   int* flag;            // rebuild requested (device)
+  int* check_done;      // blocks of k_check finished (last one sets the graph condition)
   int* status;          // sticky ST_* bits
   long long* ncalls;    // Neighbor::ncalls
   const long long* d_step;
@@ -62,8 +63,13 @@ struct PairArgs {
 
 void launch_step_begin(long long* d_step, cudaStream_t st);
 void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st);
+// the two halves of launch_neighbor: the displacement check (optionally
+// setting a graph conditional to the rebuild flag) and the rebuild kernels
+void launch_neighbor_check(const BeadArgs& a, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
+void launch_rebuild(const BeadArgs& a, cudaStream_t st);
 template <typename T> void launch_pair(const BeadArgs& a, const PairArgs<T>& p, cudaStream_t st);
 template <typename T> void launch_dep_zero(const BeadArgs& a, T* dep, cudaStream_t st);
+template <typename T> void launch_density(const BeadArgs& a, const PairArgs<T>& p, T* rho, cudaStream_t st);
 void launch_drag(const BeadArgs& a, double dt, cudaStream_t st);
 template <typename T> void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st);
 

@@ -74,6 +74,61 @@ int make_unique_seed(int baseseed) {  // utility.cpp:213-235, rank 0
   return integer_dist(gen);
 }
 
+// phi += scale * src
+template <typename T>
+__global__ void k_axpy(T* __restrict__ y, const T* __restrict__ x, T scale, long long n) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    y[k] += scale * x[k];
+}
+
+// shell sums of |F|^2 over the half spectrum [kx][kz][ky]; modes with
+// 0 < kx < Nx/2 stand for their mirror too (weight 2)
+template <typename T>
+__global__ void k_shells(const cpx<T>* __restrict__ F, int Nx, int Ny, int Nz, double dqx, double dqy, double dqz,
+                         double binw, int nbins, double* __restrict__ sum, unsigned long long* __restrict__ cnt) {
+  extern __shared__ double sh[];
+  double* ss = sh;
+  unsigned long long* sc = reinterpret_cast<unsigned long long*>(sh + nbins);
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) { ss[b] = 0.0; sc[b] = 0ull; }
+  __syncthreads();
+  const int Nxh = Nx / 2 + 1;
+  const long long total = (long long)Nxh * Nz * Ny;
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < total; m += (long long)gridDim.x * blockDim.x) {
+    const int ky = (int)(m % Ny), kz = (int)((m / Ny) % Nz), kx = (int)(m / ((long long)Ny * Nz));
+    if (kx == 0 && ky == 0 && kz == 0) continue;
+    const double qx = dqx * kx, qy = dqy * wrap_index(ky, Ny), qz = dqz * wrap_index(kz, Nz);
+    const int b = (int)(sqrt(qx * qx + qy * qy + qz * qz) / binw);
+    if (b >= nbins) continue;
+    const int w = (kx == 0 || 2 * kx == Nx) ? 1 : 2;
+    const cpx<T> f = F[m];
+    atomicAdd(ss + b, (double)w * ((double)f.x * f.x + (double)f.y * f.y));
+    atomicAdd(sc + b, (unsigned long long)w);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
+    if (sc[b]) {
+      atomicAdd(sum + b, ss[b]);
+      atomicAdd(cnt + b, sc[b]);
+    }
+  }
+}
+
+// kernel nodes at the top level of a graph (the bodies of conditional
+// nodes, which run only when switched on, are not counted)
+long long count_kernels(cudaGraph_t g) {
+  size_t nnodes = 0;
+  CK(cudaGraphGetNodes(g, nullptr, &nnodes));
+  std::vector<cudaGraphNode_t> nodes(nnodes);
+  if (nnodes) CK(cudaGraphGetNodes(g, nodes.data(), &nnodes));
+  long long nk = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType ty;
+    CK(cudaGraphNodeGetType(nd, &ty));
+    if (ty == cudaGraphNodeTypeKernel) ++nk;
+  }
+  return nk;
+}
+
 }  // namespace
 
 struct phafd_ctx {
@@ -81,7 +136,10 @@ struct phafd_ctx {
   int device = 0, precision = PHAFD_FP32;
   cudaStream_t st = nullptr;
   cudaStream_t st2 = nullptr;           // bead branch, forked from st inside a step
+  cudaStream_t st3 = nullptr;           // Hermitian-plane branch, forked from st inside a step
+  cudaStream_t stc = nullptr;           // capture of the conditional rebuild body only
   cudaEvent_t ev_fork = nullptr, ev_dep = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_pl_fork = nullptr, ev_pl_join = nullptr;
   // domain / grid
   bool boxset = false, gridset = false, populated = false;
   double boxlo[3] = {0, 0, 0}, boxhi[3] = {0, 0, 0}, period[3] = {0, 0, 0};
@@ -93,6 +151,8 @@ struct phafd_ctx {
   bool keep_chempot = false;
   bool chempot_from_mu = false;
   bool use_plane = false;  // plane-fused x/y passes where they apply (phafd_set_plane_fusion)
+  int nsub = 1;            // substeps of one step (phafd_set_linear_substeps)
+  double f2_lin = 0.0;     // dmu/dphi of the linearisation
   int graph_cur = 0;
   DevBuf phi, gx, gy, gz, dep, mu;
   DevBuf phat[2], muhat, w1, wA, wB, wC, wD, wE;
@@ -131,17 +191,20 @@ struct phafd_ctx {
   long long timestep = 0, firststep = 0;
   bool setup_done = false;
   // device counters
-  DevBuf d_counters;  // [0..1] FH counters (ull), [2] step, [3] nan_step, [4] ncalls, [5] flag|status
+  DevBuf d_counters;  // [0..1] FH counters (ull), [2] step, [3] nan_step, [4] ncalls, [5] flag|status,
+                      // [6] blocks of the neighbor check done
   unsigned long long* fh_counters() const { return d_counters.as<unsigned long long>(); }
   long long* d_step() const { return d_counters.as<long long>() + 2; }
   long long* d_nan() const { return d_counters.as<long long>() + 3; }
   long long* d_ncalls() const { return d_counters.as<long long>() + 4; }
   int* d_flag() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 5); }
   int* d_status() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 5) + 1; }
+  int* d_check_done() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 6); }
   // graph
   cudaGraphExec_t gexec = nullptr;
   bool eager_done = false;
   long long kernels_per_step = 0;
+  long long rebuild_kernels = 0;  // kernels of the conditional rebuild body
   // stage profiling (eager steps only): event after each stage group
   bool profiling = false;
   std::vector<std::pair<int, cudaEvent_t>> marks;
@@ -156,7 +219,9 @@ struct phafd_ctx {
   ~phafd_ctx() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (uref_h) cudaFreeHost(uref_h);
-    for (cudaEvent_t e : {ev_fork, ev_dep, ev_join}) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {ev_fork, ev_dep, ev_join, ev_pl_fork, ev_pl_join}) if (e) cudaEventDestroy(e);
+    if (stc) cudaStreamDestroy(stc);
+    if (st3) cudaStreamDestroy(st3);
     if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
   }
@@ -229,6 +294,8 @@ struct phafd_ctx {
     u.Ny = N[1];
     u.Nz = N[2];
     u.Nxh = N[0] / 2 + 1;
+    u.nsub = nsub;
+    u.f2 = (T)f2_lin;
     return u;
   }
 
@@ -320,6 +387,7 @@ struct phafd_ctx {
     a.cutneigh = cutneigh;
     a.cutneighsq = cutneigh * cutneigh;
     a.flag = d_flag(); a.status = d_status(); a.ncalls = d_ncalls(); a.d_step = d_step();
+    a.check_done = d_check_done();
     a.bin_of = bin_of.as<int>(); a.bin_count = bin_count.as<int>(); a.bin_cursor = bin_cursor.as<int>();
     a.bin_start = bin_start.as<int>(); a.sorted = sorted.as<int>(); a.scan_tmp = scan_tmp.as<int>();
     a.fp32_lists = precision == PHAFD_FP32 ? 1 : 0;
@@ -490,7 +558,7 @@ struct phafd_ctx {
     if (!resident && (have_conj || (have_gradphi && !gradphi_once))) gradient_from_phi<T>();
     mark(0);
     // neighbor
-    if (n > 0) launch_neighbor(ba, false, st);
+    if (n > 0) neighbor_stage();
     mark(1);
     // pairs (computed once: the reference's second pass reproduces the first, integrate.cpp:140-146)
     PairArgs<T> pa = pair_args<T>();
@@ -505,11 +573,13 @@ struct phafd_ctx {
       CK(cudaStreamWaitEvent(st2, ev_fork, 0));
     }
     // initial_integrate
-    launch_drag(ba, dt, bs);
-    launch_chain_half<T>(ba, 0, dt, bs);
+    // (a macro step of nsub substeps moves the beads with nsub * dt)
+    const double bdt = dt * nsub;
+    launch_drag(ba, bdt, bs);
+    launch_chain_half<T>(ba, 0, bdt, bs);
     // final_integrate of the beads (independent of the field update)
-    launch_drag(ba, dt, bs);
-    launch_chain_half<T>(ba, 1, dt, bs);
+    launch_drag(ba, bdt, bs);
+    launch_chain_half<T>(ba, 1, bdt, bs);
     mark(3);
     if (have_conj) {
       FHArgs fh{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
@@ -534,9 +604,21 @@ struct phafd_ctx {
         // the state stays an unnormalised r2c spectrum: store N * update
         UpdateArgs<T> u = update_args<T>(phat[cur].as<cpx<T>>(), muhat.as<cpx<T>>(), phat[1 - cur].as<cpx<T>>(),
                                          (double)nreal);
+        // the two Hermitian planes (kx = 0, Nx/2) on a parallel branch, the
+        // bulk planes on the main stream
+        cudaStream_t ps = fork ? st3 : st;
+        if (fork) {
+          CK(cudaEventRecord(ev_pl_fork, st));
+          CK(cudaStreamWaitEvent(st3, ev_pl_fork, 0));
+        }
+        chk(GridOps<T>::zfwd_planes(geom, W1, muhat.as<cpx<T>>(), twf[2], ps), "z planes fwd");
+        chk(GridOps<T>::zpass_planes(geom, wA.as<cpx<T>>(), wB.as<cpx<T>>(), tw[2][1].as<cpx<T>>(), u, ps), "z planes");
         chk(GridOps<T>::zfused(geom, W1, muhat.as<cpx<T>>(), wA.as<cpx<T>>(), wB.as<cpx<T>>(), twf[2],
-                               tw[2][1].as<cpx<T>>(), u, keep_chempot ? 1 : 0, st), "z fused");
-        chk(GridOps<T>::zpass_planes(geom, wA.as<cpx<T>>(), wB.as<cpx<T>>(), tw[2][1].as<cpx<T>>(), u, st), "z planes");
+                               tw[2][1].as<cpx<T>>(), u, keep_chempot ? 1 : 0, 1, st), "z fused");
+        if (fork) {
+          CK(cudaEventRecord(ev_pl_join, st3));
+          CK(cudaStreamWaitEvent(st, ev_pl_join, 0));
+        }
         mark(7);
         if (!use_plane || !yx_fused<T>()) yx_inverse<T>(phi.as<T>(), (T)1, (T)1, true, true);
       } else {
@@ -551,6 +633,39 @@ struct phafd_ctx {
       CK(cudaEventRecord(ev_join, st2));
       CK(cudaStreamWaitEvent(st, ev_join, 0));
     }
+  }
+
+  // Neighbor::decide + build.  Inside a graph capture the rebuild kernels
+  // form the body of a conditional node that the check kernel switches on,
+  // so a step without a rebuild runs one kernel here instead of eleven.
+  void neighbor_stage() {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    if (cs != cudaStreamCaptureStatusActive) {
+      launch_neighbor(ba, false, st);
+      return;
+    }
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+    launch_neighbor_check(ba, h, 1, st);
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p));
+    CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(stc, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    launch_rebuild(ba, stc);
+    cudaGraph_t unused = nullptr;
+    CK(cudaStreamEndCapture(stc, &unused));
+    rebuild_kernels = count_kernels(body);
   }
 
   // zero the deposit nodes once the x pass has consumed them: on the bead
@@ -661,11 +776,12 @@ int phafd_ctx_create(phafd_ctx** out, int device, int precision) {
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&c->ev_dep, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
-    c->d_counters.alloc(6 * sizeof(long long));
-    long long init[6] = {0, 0, 0, -1, 0, 0};
+    CK(cudaStreamCreateWithFlags(&c->st3, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->stc, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&c->ev_fork, &c->ev_dep, &c->ev_join, &c->ev_pl_fork, &c->ev_pl_join})
+      CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    c->d_counters.alloc(7 * sizeof(long long));
+    long long init[7] = {0, 0, 0, -1, 0, 0, 0};
     CK(cudaMemcpy(c->d_counters.p, init, sizeof(init), cudaMemcpyHostToDevice));
   } catch (const std::exception& e) {
     delete c;
@@ -1071,17 +1187,7 @@ static void enqueue_run(phafd_ctx* c, int nsteps) {
         c->step_once();
         if (resident) { resident_spectrum_flip(c); c->step_once(); resident_spectrum_flip(c); }
         CK(cudaStreamEndCapture(c->st, &g));
-        size_t nnodes = 0;
-        CK(cudaGraphGetNodes(g, nullptr, &nnodes));
-        std::vector<cudaGraphNode_t> nodes(nnodes);
-        if (nnodes) CK(cudaGraphGetNodes(g, nodes.data(), &nnodes));
-        long long nk = 0;
-        for (auto nd : nodes) {
-          cudaGraphNodeType ty;
-          CK(cudaGraphNodeGetType(nd, &ty));
-          if (ty == cudaGraphNodeTypeKernel) ++nk;
-        }
-        c->kernels_per_step = nk / (resident ? 2 : 1);
+        c->kernels_per_step = count_kernels(g) / (resident ? 2 : 1);
         CK(cudaGraphInstantiate(&c->gexec, g, 0));
         cudaGraphDestroy(g);
       }
@@ -1177,6 +1283,7 @@ int phafd_counters_get(phafd_ctx* c, phafd_counters* out) {
   out->neighbor_calls = h[4];
   out->status = ((int*)&h[5])[1];
   out->kernels_per_step = c->kernels_per_step;
+  out->kernels_per_rebuild = c->rebuild_kernels;
   API_END(c)
 }
 
@@ -1272,6 +1379,125 @@ int phafd_stage_borders_and_build(phafd_ctx* c) {
   CK(cudaStreamSynchronize(c->st));
   int rc = check_status(c);
   if (rc) return rc;
+  API_END(c)
+}
+
+int phafd_compute_complex(phafd_ctx* c, int field, int quant, double* out) {
+  API_BEGIN(c)
+  if (!c->gridset) throw std::invalid_argument("grid not created");
+  if (field != PHAFD_FIELD_FT_PHI && field != PHAFD_FIELD_FT_CHEMPOT)
+    throw std::invalid_argument("Invalid array to compute in compute modulus.");
+  if (quant < PHAFD_COMPLEX_REAL || quant > PHAFD_COMPLEX_NORM) throw std::invalid_argument("Invalid argument in compute complex.");
+  std::vector<double> spec(2 * c->ncplx);
+  int rc = phafd_grid_get(c, field, spec.data());
+  if (rc) return rc;
+  // compute_complex.cpp:50: prefac = 1 / (dx dy dz)
+  const double prefac = 1.0 / ((c->period[0] / c->N[0]) * (c->period[1] / c->N[1]) * (c->period[2] / c->N[2]));
+  for (size_t m = 0; m < c->ncplx; ++m) {
+    const double re = spec[2 * m], im = spec[2 * m + 1];
+    switch (quant) {
+      case PHAFD_COMPLEX_REAL: out[m] = re * prefac; break;
+      case PHAFD_COMPLEX_IMAG: out[m] = im * prefac; break;
+      case PHAFD_COMPLEX_MODULUS: out[m] = std::sqrt(re * re + im * im) * prefac; break;
+      default: out[m] = (re * re + im * im) * prefac * prefac; break;
+    }
+  }
+  API_END(c)
+}
+
+int phafd_structure_factor(phafd_ctx* c, int nbins, double* sk, long long* counts) {
+  API_BEGIN(c)
+  if (!c->gridset || nbins <= 0 || !sk) throw std::invalid_argument("structure factor: grid and bins needed");
+  CK(cudaSetDevice(c->device));
+  DevBuf acc;
+  acc.alloc((size_t)nbins * 16);
+  acc.zero(c->st);
+  double* dsum = acc.as<double>();
+  unsigned long long* dcnt = reinterpret_cast<unsigned long long*>(dsum + nbins);
+  FHArgs none{0, 0, c->fh_counters(), 0, nullptr};
+  const double tp = 2.0 * M_PI;
+  const size_t shm = (size_t)nbins * 16;
+  if (c->precision == PHAFD_FP64) {
+    c->r2c<double>(c->phi.as<double>(), nullptr, c->w1.as<cpx<double>>(), none);
+    k_shells<double><<<1024, 256, shm, c->st>>>(c->w1.as<cpx<double>>(), c->N[0], c->N[1], c->N[2], tp / c->period[0],
+                                                tp / c->period[1], tp / c->period[2], tp / c->period[0], nbins, dsum, dcnt);
+  } else {
+    c->r2c<float>(c->phi.as<float>(), nullptr, c->w1.as<cpx<float>>(), none);
+    k_shells<float><<<1024, 256, shm, c->st>>>(c->w1.as<cpx<float>>(), c->N[0], c->N[1], c->N[2], tp / c->period[0],
+                                               tp / c->period[1], tp / c->period[2], tp / c->period[0], nbins, dsum, dcnt);
+  }
+  CK(cudaGetLastError());
+  std::vector<double> hs(nbins);
+  std::vector<unsigned long long> hc(nbins);
+  CK(cudaMemcpyAsync(hs.data(), dsum, nbins * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(hc.data(), dcnt, nbins * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int b = 0; b < nbins; ++b) {
+    sk[b] = hc[b] ? hs[b] / (double)hc[b] / (double)c->nreal : 0.0;
+    if (counts) counts[b] = (long long)hc[b];
+  }
+  API_END(c)
+}
+
+int phafd_set_linear_substeps(phafd_ctx* c, int nsub, double f2) {
+  API_BEGIN(c)
+  if (nsub < 1) throw std::invalid_argument("substeps must be >= 1");
+  if (nsub > 1 && c->c_noise == PHAFD_NOISE_REFERENCE)
+    throw std::invalid_argument("macro steps draw Philox noise (the reference stream has one draw per substep)");
+  c->nsub = nsub;
+  c->f2_lin = f2;
+  c->invalidate_graph();
+  API_END(c)
+}
+
+int phafd_grid_device(phafd_ctx* c, int field, void** dev) {
+  API_BEGIN(c)
+  if (!c->gridset || !dev) throw std::invalid_argument("grid not created");
+  const DevBuf* b = field == PHAFD_FIELD_PHI ? &c->phi : field == PHAFD_FIELD_GRADX ? &c->gx
+                  : field == PHAFD_FIELD_GRADY ? &c->gy : field == PHAFD_FIELD_GRADZ ? &c->gz
+                  : field == PHAFD_FIELD_CHEMPOT ? &c->dep : nullptr;
+  if (!b) throw std::invalid_argument("bad field");
+  *dev = b->p;
+  API_END(c)
+}
+
+int phafd_deposit_density(phafd_ctx* c, void* rho) {
+  API_BEGIN(c)
+  if (!c->gridset || !rho) throw std::invalid_argument("grid not created");
+  if (!c->setup_done) throw std::invalid_argument("density needs the neighbor lists of setup");
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemsetAsync(rho, 0, c->nreal * c->rsz(), c->st));
+  if (c->n > 0 && c->ga_style != PHAFD_GRIDATOM_NONE) {
+    c->fill_bead_args();
+    if (c->precision == PHAFD_FP64) launch_density<double>(c->ba, c->pair_args<double>(), (double*)rho, c->st);
+    else launch_density<float>(c->ba, c->pair_args<float>(), (float*)rho, c->st);
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  API_END(c)
+}
+
+int phafd_grid_add_device(phafd_ctx* c, const void* src, double scale) {
+  API_BEGIN(c)
+  if (!c->gridset || !src) throw std::invalid_argument("grid not created");
+  CK(cudaSetDevice(c->device));
+  const bool resident = c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj && c->setup_done;
+  FHArgs none{0, 0, c->fh_counters(), 0, nullptr};
+  if (c->precision == PHAFD_FP64) {
+    k_axpy<double><<<1024, 256, 0, c->st>>>(c->phi.as<double>(), (const double*)src, scale, (long long)c->nreal);
+    if (resident) {
+      c->r2c<double>(c->phi.as<double>(), nullptr, c->phat[c->cur].as<cpx<double>>(), none);
+      c->inverse_chain<double>(c->phat[c->cur].as<cpx<double>>(), nullptr, nullptr, 0.0, 1.0 / (double)c->nreal, true, false);
+    }
+  } else {
+    k_axpy<float><<<1024, 256, 0, c->st>>>(c->phi.as<float>(), (const float*)src, (float)scale, (long long)c->nreal);
+    if (resident) {
+      c->r2c<float>(c->phi.as<float>(), nullptr, c->phat[c->cur].as<cpx<float>>(), none);
+      c->inverse_chain<float>(c->phat[c->cur].as<cpx<float>>(), nullptr, nullptr, 0.0f, (float)(1.0 / (double)c->nreal), true, false);
+    }
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
   API_END(c)
 }
 

@@ -1,0 +1,1474 @@
+// Spectral neural operator of the learned field propagator (no reference
+// counterpart; the network is described in include/phafd_fno.h).
+//
+// Data layout in HBM
+//   activations      BF16 [node][32]           node = (z * Ny + y) * Nx + x
+//   x-stage partials FP32 [row][half][32][16]  row = z * Ny + y, half = x / 128,
+//                                              16 = (kx, re/im) for kx < 8
+//   y-stage          FP32 complex [z][ky'][kx][32]
+//   retained modes   FP32 complex [mode][32],  mode = (kz' * 16 + ky') * 8 + kx
+//   x-inverse input  BF16 [row][32][16]        (K-major B rows of the tiles)
+//
+// Tensor-core tiles.  A CTA owns 4 rows x 128 nodes (one x-half).  Its
+// activation tile lives in shared memory in one layout that serves three
+// operand roles (tc05.cuh):
+//   element (tile i, x, c) at (x % 8) * 16 + (c % 8) * 2 + (4 i + c / 8) * 128 + (x / 8) * 2048
+//   - K-major A of tile i (M = x, K = c):          start 512 i, LBO 128, SBO 2048
+//   - MN-major A of all tiles (M = (i, c), K = x):  start 0, MN groups 128, K groups 2048
+//   - MN-major B of tile j (N = c, K = x):          start 512 j, MN groups 128, K groups 2048
+// so the per-node channel GEMM (D_i = A_i W^T + G Yx_i), the x-stage
+// truncated DFT of the result (D2 = V^T F^T over 4 rows) and the weight
+// gradients (D = delta^T v) are all single tcgen05.mma chains without any
+// shared-memory transpose.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "tc05.cuh"
+#include "../../include/phafd_fno.h"
+
+namespace phafd {
+namespace fno {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int C = 32;      // channels
+constexpr int NKX = 8;     // retained kx
+constexpr int NK = 16;     // retained ky', kz'
+constexpr int KR = 16;     // (kx, re/im) rows of the x stage
+constexpr int NMODE = NK * NK * NKX;
+constexpr int TX = 128;    // nodes of a tile along x
+constexpr int TPC = 4;     // tiles (rows) per CTA
+constexpr int NTH = 128;   // threads per tile CTA
+
+// flat parameter vector
+constexpr size_t OFF_P = 0, OFF_PB = 512;
+constexpr size_t LSZ = 1024 + 32 + (size_t)NMODE * C * C * 2;
+constexpr size_t OFF_L0 = 544;
+__host__ __device__ constexpr size_t layer_off(int l) { return OFF_L0 + (size_t)l * LSZ; }
+constexpr size_t OFF_Q1 = OFF_L0 + 4 * LSZ, OFF_Q1B = OFF_Q1 + 1024, OFF_Q2 = OFF_Q1B + 32, OFF_Q2B = OFF_Q2 + 32;
+constexpr size_t NPARAM = OFF_Q2B + 1;
+
+// shared-memory map of the tile kernels (bytes); the second activation tile
+// T1 exists only in the training kernels
+constexpr uint32_t SM_T0 = 0;                  // activation tile, 32 KB
+constexpr uint32_t SM_ASP = 32768;             // A spectral part [x][16], 4 KB
+constexpr uint32_t SM_BM = SM_ASP + 4096;      // B main [32][<=32], 2 KB
+constexpr uint32_t SM_BM2 = SM_BM + 2048;      // second B main (projection backward), 2 KB
+constexpr uint32_t SM_BS = SM_BM2 + 2048;      // B spectral, 4 x [32][16], 4 KB
+constexpr uint32_t SM_B2 = SM_BS + 4096;       // B of the x-stage DFT [16][128], 4 KB
+constexpr uint32_t SM_BAR = SM_B2 + 4096;      // mbarrier + TMEM address
+constexpr uint32_t SM_INF = SM_BAR + 64;       // 48 KB: 4 CTAs (4 x 128 TMEM columns) per SM
+constexpr uint32_t SM_T1 = SM_BAR + 1024;      // second activation tile, 32 KB
+constexpr uint32_t SM_TRAIN = SM_T1 + 32768;   // 81 KB: 2 CTAs (2 x 256 TMEM columns) per SM
+
+PHAFD_D uint32_t tile_off(int i, int x, int c) {
+  return (uint32_t)((x & 7) * 16 + (c & 7) * 2 + (i * 4 + (c >> 3)) * 128 + (x >> 3) * 2048);
+}
+PHAFD_D uint64_t kdesc(uint32_t saddr, uint32_t sbo) { return tc::sdesc(saddr, 128, sbo); }
+// MN-major operand with MN-group stride mno and K-group stride ko
+PHAFD_D uint64_t mndesc(uint32_t saddr, uint32_t mno, uint32_t ko, int swap) {
+  return swap ? tc::sdesc(saddr, mno, ko) : tc::sdesc(saddr, ko, mno);
+}
+
+// GELU, tanh form, and its derivative
+PHAFD_D float gelu(float x) {
+  const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
+  return 0.5f * x * (1.f + tanhf(u));
+}
+PHAFD_D float gelu_d(float x) {
+  const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
+  const float t = tanhf(u);
+  return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * 0.7978845608028654f * (1.f + 0.134145f * x * x);
+}
+
+struct Dims {
+  int Nx, Ny, Nz, H;  // H = Nx / 128
+  long long rows;     // Nz * Ny
+  long long nodes;
+};
+
+struct Status {
+  int* err;  // device flag: nonzero after a bounded wait gave up
+};
+
+// ------------------------------------------------------------------ CTA plumbing
+struct Tile {
+  unsigned char* sm;
+  uint32_t sbase;
+  uint64_t* bar;
+  uint32_t* taddr_slot;
+  int rg, h;
+  long long node0[TPC];
+  long long row[TPC];
+};
+
+PHAFD_D void tile_begin(Tile& t, unsigned char* sm, const Dims& d, uint32_t ncols) {
+  t.sm = sm;
+  t.sbase = tc::smem_u32(sm);
+  t.bar = reinterpret_cast<uint64_t*>(sm + SM_BAR);
+  t.taddr_slot = reinterpret_cast<uint32_t*>(sm + SM_BAR + 16);
+  t.rg = blockIdx.x / d.H;
+  t.h = blockIdx.x % d.H;
+#pragma unroll
+  for (int i = 0; i < TPC; ++i) {
+    t.row[i] = (long long)t.rg * TPC + i;
+    t.node0[i] = t.row[i] * d.Nx + (long long)t.h * TX;
+  }
+  if (threadIdx.x == 0) {
+    tc::mbar_init(t.bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (threadIdx.x < 32) {
+    tc::tmem_alloc(t.taddr_slot, ncols);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+}
+
+PHAFD_D void tile_end(Tile& t, uint32_t ncols) {
+  tc::fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc::fence_after();
+    tc::tmem_dealloc(*t.taddr_slot, ncols);
+  }
+}
+
+// wait for the MMAs committed as phase `ph`; on timeout flag the error.
+// Every thread of the CTA calls it; the result is made uniform so that the
+// barriers behind a failed wait are skipped by all threads alike.
+PHAFD_D bool mma_wait(Tile& t, uint32_t ph, const Status& s) {
+  const bool mine = tc::mbar_wait(t.bar, ph);
+  if (!mine) atomicExch(s.err, 1);
+  const bool ok = __syncthreads_and(mine) != 0;
+  tc::fence_after();
+  return ok;
+}
+
+// all threads: make shared-memory operand writes (st.shared and completed
+// cp.async) visible to the tensor core, then barrier
+PHAFD_D void operands_ready() {
+  cp_async_wait<0>();
+  tc::fence_async_smem();
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+}
+
+// ---- loads into shared memory (cp.async, all threads)
+// activation tiles [node][32] -> unified layout at `dst`
+PHAFD_D void load_act(unsigned char* dst, const bf16* act, const Tile& t) {
+  for (int q = threadIdx.x; q < TPC * TX * 4; q += NTH) {
+    const int i = q >> 9, x = (q >> 2) & (TX - 1), g = q & 3;
+    cp_async16(dst + tile_off(i, x, 8 * g), act + (size_t)(t.node0[i] + x) * C + 8 * g);
+  }
+}
+// K-major matrix of `rows` rows and K columns (row-major [rows][K] in HBM)
+PHAFD_D void load_kmajor(unsigned char* dst, const bf16* src, int rows, int K) {
+  const int kc = K / 8;
+  for (int q = threadIdx.x; q < rows * kc; q += NTH) {
+    const int r = q / kc, c = q % kc;
+    cp_async16(dst + (r & 7) * 16 + c * 128 + (r >> 3) * (K * 16), src + (size_t)r * K + 8 * c);
+  }
+}
+// x-half of a [16][Nx] table as K-major B (N = 16 rows, K = 128 x)
+PHAFD_D void load_b2(unsigned char* dst, const bf16* tab, const Dims& d, int h) {
+  for (int q = threadIdx.x; q < KR * (TX / 8); q += NTH) {
+    const int r = q / (TX / 8), c = q % (TX / 8);
+    cp_async16(dst + (r & 7) * 16 + c * 128 + (r >> 3) * 2048, tab + (size_t)r * d.Nx + h * TX + 8 * c);
+  }
+}
+// x-half of a [Nx][16] table as K-major A (M = 128 x, K = 16)
+PHAFD_D void load_aspec(unsigned char* dst, const bf16* tab, int h) {
+  for (int q = threadIdx.x; q < TX * 2; q += NTH) {
+    const int x = q >> 1, c = q & 1;
+    cp_async16(dst + (x & 7) * 16 + c * 128 + (x >> 3) * 256, tab + (size_t)(h * TX + x) * KR + 8 * c);
+  }
+}
+// per-row spectral B parts [row][32][16] of the 4 tiles
+PHAFD_D void load_bspec(unsigned char* dst, const bf16* rows16, const Tile& t) {
+  for (int q = threadIdx.x; q < TPC * C * 2; q += NTH) {
+    const int i = q >> 6, n = (q >> 1) & 31, c = q & 1;
+    cp_async16(dst + i * 1024 + (n & 7) * 16 + c * 128 + (n >> 3) * 256,
+               rows16 + ((size_t)t.row[i] * C + n) * KR + 8 * c);
+  }
+}
+
+// ---- MMA issue (one thread)
+// D_i (cols 32 i) = A_i (K-major, K = 16 * ksteps) * B^T, + Aspec * Bspec_i^T
+PHAFD_D void issue_main(const Tile& t, uint32_t tmem, uint32_t a_off, uint32_t b_off, int ksteps, bool spec) {
+  const uint32_t id = tc::idesc_bf16(128, 32, 0, 0);
+  const uint32_t bsbo = (uint32_t)ksteps * 256;  // K * 16 bytes
+  for (int i = 0; i < TPC; ++i) {
+    const uint32_t d = tmem + 32 * i;
+    for (int s = 0; s < ksteps; ++s)
+      tc::mma(d, kdesc(t.sbase + a_off + 512 * i + 256 * s, 2048), kdesc(t.sbase + b_off + 256 * s, bsbo), id, s > 0);
+    if (spec) tc::mma(d, kdesc(t.sbase + SM_ASP, 256), kdesc(t.sbase + SM_BS + 1024 * i, 256), id, 1);
+  }
+}
+// D (cols 0..15) = V^T F^T: A = all tiles MN-major at a_off, B = SM_B2 (K-major, N = 16)
+PHAFD_D void issue_xdft(const Tile& t, uint32_t tmem, uint32_t a_off, int swap) {
+  const uint32_t id = tc::idesc_bf16(128, 16, 1, 0);
+  for (int s = 0; s < TX / 16; ++s)
+    tc::mma(tmem, mndesc(t.sbase + a_off + 4096 * s, 128, 2048, swap), kdesc(t.sbase + SM_B2 + 256 * s, 2048), id,
+            s > 0);
+}
+// D_j (cols col0 + 32 j) = A^T B_j: A = all tiles MN-major at a_off (M = (i, r)),
+// B_j = tile j MN-major at b_off (N = nb channels, K = x)
+PHAFD_D void issue_wgrad(const Tile& t, uint32_t tmem, uint32_t col0, uint32_t a_off, uint32_t b_off, int nb,
+                         int swap) {
+  const uint32_t id = tc::idesc_bf16(128, nb, 1, 1);
+  for (int j = 0; j < TPC; ++j)
+    for (int s = 0; s < TX / 16; ++s)
+      tc::mma(tmem + col0 + 32 * j, mndesc(t.sbase + a_off + 4096 * s, 128, 2048, swap),
+              mndesc(t.sbase + b_off + 512 * j + 4096 * s, 128, 2048, swap), id, s > 0);
+}
+
+// ---- epilogue pieces
+PHAFD_D uint32_t lane_addr(uint32_t tmem, uint32_t col) {
+  return tmem + ((uint32_t)(32 * (threadIdx.x >> 5)) << 16) + col;
+}
+PHAFD_D void tmem_row32(uint32_t tmem, uint32_t col, float* v) {
+  tc::tmem_ld16(lane_addr(tmem, col), v);
+  tc::tmem_ld16(lane_addr(tmem, col + 16), v + 16);
+}
+// 32 FP32 -> 32 BF16: HBM row (64 B) and/or the unified tile
+PHAFD_D void store_row(bf16* g, unsigned char* tile, int i, int x, const float* v) {
+  uint4 q[4];
+  uint32_t* w = reinterpret_cast<uint32_t*>(q);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    __nv_bfloat162 p = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+    w[k] = *reinterpret_cast<uint32_t*>(&p);
+  }
+  if (g) {
+    uint4* gp = reinterpret_cast<uint4*>(g);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) gp[k] = q[k];
+  }
+  if (tile) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) *reinterpret_cast<uint4*>(tile + tile_off(i, x, 8 * k)) = q[k];
+  }
+}
+PHAFD_D void load_row(const bf16* g, float* v) {
+  const uint4* gp = reinterpret_cast<const uint4*>(g);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    uint4 q = gp[k];
+    const __nv_bfloat162* p = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float2 f = __bfloat1622float2(p[e]);
+      v[8 * k + 2 * e] = f.x;
+      v[8 * k + 2 * e + 1] = f.y;
+    }
+  }
+}
+// lane (i, c): 16 x-stage DFT values of row i, channel c -> [row][half][c][16]
+PHAFD_D void store_xdft(float* out, uint32_t tmem, const Tile& t, const Dims& d) {
+  float v[16];
+  tc::tmem_ld16(lane_addr(tmem, 0), v);
+  const int i = threadIdx.x >> 5, c = threadIdx.x & 31;
+  float4* o = reinterpret_cast<float4*>(out + (((size_t)t.row[i] * d.H + t.h) * C + c) * KR);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+}
+// lane (i, r): weight-gradient rows of tile i (cols col0 + 32 i, nb wide),
+// summed over the 4 tiles through `scratch` (16 KB) and added to g[r][0..nb)
+PHAFD_D void reduce_wgrad(float* g, uint32_t tmem, uint32_t col0, int nb, float* scratch) {
+  const int i = threadIdx.x >> 5, r = threadIdx.x & 31;
+  float v[32];
+  tc::tmem_ld16(lane_addr(tmem, col0 + 32 * i), v);
+  if (nb > 16) tc::tmem_ld16(lane_addr(tmem, col0 + 32 * i + 16), v + 16);
+  for (int k = 0; k < nb; ++k) scratch[(i * 32 + r) * 33 + k] = v[k];
+  __syncthreads();
+  for (int q = threadIdx.x; q < 32 * nb; q += NTH) {
+    const int rr = q / nb, k = q % nb;
+    float s = 0.f;
+#pragma unroll
+    for (int ii = 0; ii < TPC; ++ii) s += scratch[(ii * 32 + rr) * 33 + k];
+    atomicAdd(g + rr * nb + k, s);
+  }
+  __syncthreads();
+}
+// block sum of 32 per-thread values (one per channel) added to g[32]
+PHAFD_D void reduce_vec32(float* g, const float* v, float* scratch) {
+  for (int k = 0; k < 32; ++k) {
+    float s = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) scratch[(threadIdx.x >> 5) * 32 + k] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float s = 0.f;
+    for (int w = 0; w < NTH / 32; ++w) s += scratch[w * 32 + threadIdx.x];
+    atomicAdd(g + threadIdx.x, s);
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ kernels
+struct LiftIn {
+  const float *phi, *rho;
+  float chi_n, n0, n1, n2, n3;  // (phi - n0) / n1, (rho - n2) / n3; chi_n already normalised
+};
+PHAFD_D void lift_inputs(const LiftIn& in, long long node, float* v) {
+  v[0] = (in.phi[node] - in.n0) / in.n1;
+  v[1] = (in.rho[node] - in.n2) / in.n3;
+  v[2] = in.chi_n;
+#pragma unroll
+  for (int k = 3; k < 16; ++k) v[k] = 0.f;
+}
+// 16 lift inputs of node x of tile i into the unified tile (channels 0..15)
+PHAFD_D void store_inputs(unsigned char* tile, int i, int x, const float* v) {
+  uint4 q[2];
+  uint32_t* w = reinterpret_cast<uint32_t*>(q);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    __nv_bfloat162 p = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+    w[k] = *reinterpret_cast<uint32_t*>(&p);
+  }
+  *reinterpret_cast<uint4*>(tile + tile_off(i, x, 0)) = q[0];
+  *reinterpret_cast<uint4*>(tile + tile_off(i, x, 8)) = q[1];
+}
+
+// v0 = P in + pb; x-stage DFT of v0
+__global__ void __launch_bounds__(NTH) k_lift(LiftIn in, const bf16* __restrict__ Pb, const float* __restrict__ pb,
+                                               const bf16* __restrict__ Ftab, bf16* __restrict__ v0,
+                                               float* __restrict__ vx, Dims d, int swap, Status st) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  Tile t;
+  tile_begin(t, sm, d, 128);
+  const uint32_t tmem = *t.taddr_slot;
+  load_kmajor(sm + SM_BM, Pb, 32, 16);
+  load_b2(sm + SM_B2, Ftab, d, t.h);
+  cp_async_commit();
+  const int x = threadIdx.x;
+  for (int i = 0; i < TPC; ++i) {
+    float v[16];
+    lift_inputs(in, t.node0[i] + x, v);
+    store_inputs(sm + SM_T0, i, x, v);
+  }
+  operands_ready();
+  if (threadIdx.x == 0) {
+    issue_main(t, tmem, SM_T0, SM_BM, 1, false);
+    tc::commit(t.bar);
+  }
+  if (mma_wait(t, 0, st)) {
+    for (int i = 0; i < TPC; ++i) {
+      float v[32];
+      tmem_row32(tmem, 32 * i, v);
+#pragma unroll
+      for (int c = 0; c < 32; ++c) v[c] += pb[c];
+      store_row(v0 + (size_t)(t.node0[i] + x) * C, sm + SM_T0, i, x, v);
+    }
+    operands_ready();
+    if (threadIdx.x == 0) {
+      issue_xdft(t, tmem, SM_T0, swap);
+      tc::commit(t.bar);
+    }
+    if (mma_wait(t, 1, st)) store_xdft(vx, tmem, t, d);
+  }
+  tile_end(t, 128);
+}
+
+// v_out = act(W v_in + b + G Yx); optional pre-activation; x-stage DFT of v_out
+template <bool ACT, bool XDFT, bool SAVE_PRE>
+__global__ void __launch_bounds__(NTH) k_layer(const bf16* __restrict__ vin, const bf16* __restrict__ Wb,
+                                                const float* __restrict__ b, const bf16* __restrict__ Gtab,
+                                                const bf16* __restrict__ yx, const bf16* __restrict__ Ftab,
+                                                bf16* __restrict__ vout, bf16* __restrict__ pre,
+                                                float* __restrict__ vx, Dims d, int swap, Status st) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  Tile t;
+  tile_begin(t, sm, d, 128);
+  const uint32_t tmem = *t.taddr_slot;
+  load_act(sm + SM_T0, vin, t);
+  load_kmajor(sm + SM_BM, Wb, 32, 32);
+  load_aspec(sm + SM_ASP, Gtab, t.h);
+  load_bspec(sm + SM_BS, yx, t);
+  if (XDFT) load_b2(sm + SM_B2, Ftab, d, t.h);
+  cp_async_commit();
+  operands_ready();
+  if (threadIdx.x == 0) {
+    issue_main(t, tmem, SM_T0, SM_BM, 2, true);
+    tc::commit(t.bar);
+  }
+  const int x = threadIdx.x;
+  if (mma_wait(t, 0, st)) {
+    for (int i = 0; i < TPC; ++i) {
+      float v[32];
+      tmem_row32(tmem, 32 * i, v);
+      const size_t o = (size_t)(t.node0[i] + x) * C;
+#pragma unroll
+      for (int c = 0; c < 32; ++c) v[c] += b[c];
+      if (SAVE_PRE) store_row(pre + o, nullptr, i, x, v);
+      if (ACT) {
+#pragma unroll
+        for (int c = 0; c < 32; ++c) v[c] = gelu(v[c]);
+      }
+      store_row(vout + o, XDFT ? sm + SM_T0 : nullptr, i, x, v);
+    }
+    if (XDFT) {
+      operands_ready();
+      if (threadIdx.x == 0) {
+        issue_xdft(t, tmem, SM_T0, swap);
+        tc::commit(t.bar);
+      }
+      if (mma_wait(t, 1, st)) store_xdft(vx, tmem, t, d);
+    }
+  }
+  tile_end(t, 128);
+}
+
+// projection, inference: out = q2 . GELU(Q1 v4 + q1b) + q2b; sum(out) in FP64
+__global__ void __launch_bounds__(NTH) k_proj(const bf16* __restrict__ v4, const bf16* __restrict__ Q1b,
+                                               const float* __restrict__ q1b, const float* __restrict__ q2, float q2b,
+                                               float* __restrict__ out, double* __restrict__ sum, Dims d, Status st) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  Tile t;
+  tile_begin(t, sm, d, 128);
+  const uint32_t tmem = *t.taddr_slot;
+  load_act(sm + SM_T0, v4, t);
+  load_kmajor(sm + SM_BM, Q1b, 32, 32);
+  cp_async_commit();
+  operands_ready();
+  if (threadIdx.x == 0) {
+    issue_main(t, tmem, SM_T0, SM_BM, 2, false);
+    tc::commit(t.bar);
+  }
+  const int x = threadIdx.x;
+  double acc = 0.0;
+  if (mma_wait(t, 0, st)) {
+    for (int i = 0; i < TPC; ++i) {
+      float v[32];
+      tmem_row32(tmem, 32 * i, v);
+      float o = q2b;
+#pragma unroll
+      for (int k = 0; k < 32; ++k) o += q2[k] * gelu(v[k] + q1b[k]);
+      out[t.node0[i] + x] = o;
+      acc += (double)o;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
+  tile_end(t, 128);
+}
+
+// correction = scale * (out - mean(out))
+__global__ void k_center(const float* __restrict__ out, const double* __restrict__ sum, float scale, float* corr,
+                         long long n) {
+  const float mean = (float)(*sum / (double)n);
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    corr[k] = scale * (out[k] - mean);
+}
+
+// ---- training
+struct Grads {
+  float *P, *pb, *W, *b, *Q1, *q1b, *q2, *q2b;  // W, b of the layer at hand
+};
+
+// projection forward + loss + backward to delta4 = dL/dv4 (layer 4 has no
+// activation), dQ1, dq1b, dq2, dq2b; x-stage G-DFT of delta4
+__global__ void __launch_bounds__(NTH) k_proj_train(const bf16* __restrict__ v4, const bf16* __restrict__ Q1b,
+                                                     const bf16* __restrict__ Q1tb, const float* __restrict__ q1b,
+                                                     const float* __restrict__ q2, float q2b,
+                                                     const float* __restrict__ target, const bf16* __restrict__ Gt,
+                                                     bf16* __restrict__ delta4, float* __restrict__ dyx, Grads g,
+                                                     double* __restrict__ loss, Dims d, int swap, Status st) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  Tile t;
+  tile_begin(t, sm, d, 256);
+  const uint32_t tmem = *t.taddr_slot;
+  load_act(sm + SM_T0, v4, t);
+  load_kmajor(sm + SM_BM, Q1b, 32, 32);
+  load_kmajor(sm + SM_BM2, Q1tb, 32, 32);
+  load_b2(sm + SM_B2, Gt, d, t.h);
+  cp_async_commit();
+  operands_ready();
+  if (threadIdx.x == 0) {
+    issue_main(t, tmem, SM_T0, SM_BM, 2, false);
+    tc::commit(t.bar);
+  }
+  const int x = threadIdx.x;
+  const float inv_n = 1.f / (float)d.nodes;
+  double lsum = 0.0;
+  float dq2[32], dq1b[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) { dq2[k] = 0.f; dq1b[k] = 0.f; }
+  float dq2b = 0.f;
+  bool ok = mma_wait(t, 0, st);
+  if (ok) {
+    for (int i = 0; i < TPC; ++i) {
+      float v[32];
+      tmem_row32(tmem, 32 * i, v);
+      float o = q2b;
+#pragma unroll
+      for (int k = 0; k < 32; ++k) o += q2[k] * gelu(v[k] + q1b[k]);
+      const float e = o - target[t.node0[i] + x];
+      lsum += (double)e * (double)e;
+      const float gr = 2.f * e * inv_n;
+      dq2b += gr;
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const float p = v[k] + q1b[k];
+        dq2[k] += gr * gelu(p);
+        v[k] = gr * q2[k] * gelu_d(p);  // dL/dpre_h
+        dq1b[k] += v[k];
+      }
+      store_row(nullptr, sm + SM_T1, i, x, v);
+    }
+  }
+  // g4 = dpre_h Q1 (cols 0..127); dQ1 = dpre_h^T v4 (cols 128..255)
+  operands_ready();
+  if (ok && threadIdx.x == 0) {
+    issue_main(t, tmem, SM_T1, SM_BM2, 2, false);
+    issue_wgrad(t, tmem, 128, SM_T1, SM_T0, 32, swap);
+    tc::commit(t.bar);
+  }
+  ok = ok && mma_wait(t, 1, st);
+  if (ok) {
+    for (int i = 0; i < TPC; ++i) {
+      float v[32];
+      tmem_row32(tmem, 32 * i, v);
+      store_row(delta4 + (size_t)(t.node0[i] + x) * C, nullptr, i, x, v);
+    }
+  }
+  // v4 tile no longer needed: delta4 into T0 after the MMAs that read it
+  __syncthreads();
+  if (ok) {
+    for (int i = 0; i < TPC; ++i) {
+      float v[32];
+      tmem_row32(tmem, 32 * i, v);
+      store_row(nullptr, sm + SM_T0, i, x, v);
+    }
+    reduce_wgrad(g.Q1, tmem, 128, 32, reinterpret_cast<float*>(sm + SM_T1));
+  }
+  operands_ready();
+  if (ok && threadIdx.x == 0) {
+    issue_xdft(t, tmem, SM_T0, swap);
+    tc::commit(t.bar);
+  }
+  ok = ok && mma_wait(t, 0, st);
+  if (ok) store_xdft(dyx, tmem, t, d);
+  __syncthreads();
+  float* scratch = reinterpret_cast<float*>(sm + SM_T1);
+  reduce_vec32(g.q2, dq2, scratch);
+  reduce_vec32(g.q1b, dq1b, scratch);
+  {
+    float s = dq2b;
+    double l = lsum;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+      l += __shfl_xor_sync(0xffffffffu, l, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(g.q2b, s);
+      atomicAdd(loss, l * (double)inv_n);
+    }
+  }
+  tile_end(t, 256);
+}
+
+// backward through layer l: g = delta W + F^T dVx (cols 0..127); dW = delta^T
+// v_prev (cols 128..255); db = sum delta.  Then delta_prev = g * GELU'(pre_prev)
+// (or g itself below the first layer), its G-DFT (XDFT), or the lift
+// gradient dP = g^T in, dpb = sum g (LIFT).
+template <bool GELU_PREV, bool XDFT, bool LIFT>
+__global__ void __launch_bounds__(NTH) k_layer_bwd(const bf16* __restrict__ delta, const bf16* __restrict__ vprev,
+                                                    const bf16* __restrict__ preprev, const bf16* __restrict__ Wtb,
+                                                    const bf16* __restrict__ Fttab, const bf16* __restrict__ dvx,
+                                                    const bf16* __restrict__ Gt, bf16* __restrict__ delta_out,
+                                                    float* __restrict__ dyx, LiftIn in, Grads g, Dims d, int swap,
+                                                    Status st) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  Tile t;
+  tile_begin(t, sm, d, 256);
+  const uint32_t tmem = *t.taddr_slot;
+  load_act(sm + SM_T1, delta, t);
+  load_act(sm + SM_T0, vprev, t);
+  load_kmajor(sm + SM_BM, Wtb, 32, 32);
+  load_aspec(sm + SM_ASP, Fttab, t.h);
+  load_bspec(sm + SM_BS, dvx, t);
+  if (XDFT) load_b2(sm + SM_B2, Gt, d, t.h);
+  cp_async_commit();
+  operands_ready();
+  if (threadIdx.x == 0) {
+    issue_main(t, tmem, SM_T1, SM_BM, 2, true);
+    issue_wgrad(t, tmem, 128, SM_T1, SM_T0, 32, swap);
+    tc::commit(t.bar);
+  }
+  const int x = threadIdx.x;
+  // db from the delta tile (read before it is overwritten)
+  float db[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) db[c] = 0.f;
+  bool ok = mma_wait(t, 0, st);
+  if (ok) {
+    for (int i = 0; i < TPC; ++i) {
+      const unsigned char* tile = sm + SM_T1;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        uint4 q = *reinterpret_cast<const uint4*>(tile + tile_off(i, x, 8 * k));
+        const __nv_bfloat162* p = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float2 f = __bfloat1622float2(p[e]);
+          db[8 * k + 2 * e] += f.x;
+          db[8 * k + 2 * e + 1] += f.y;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  float dpb[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) dpb[c] = 0.f;
+  if (ok) {
+    for (int i = 0; i < TPC; ++i) {
+      float v[32];
+      tmem_row32(tmem, 32 * i, v);
+      const size_t o = (size_t)(t.node0[i] + x) * C;
+      if (GELU_PREV) {
+        float p[32];
+        load_row(preprev + o, p);
+#pragma unroll
+        for (int c = 0; c < 32; ++c) v[c] *= gelu_d(p[c]);
+      }
+      if (LIFT) {
+#pragma unroll
+        for (int c = 0; c < 32; ++c) dpb[c] += v[c];
+      }
+      store_row(delta_out ? delta_out + o : nullptr, sm + SM_T1, i, x, v);
+    }
+    reduce_wgrad(g.W, tmem, 128, 32, reinterpret_cast<float*>(sm + SM_T0));
+  }
+  reduce_vec32(g.b, db, reinterpret_cast<float*>(sm + SM_T0));
+  if (XDFT) {
+    operands_ready();
+    if (ok && threadIdx.x == 0) {
+      issue_xdft(t, tmem, SM_T1, swap);
+      tc::commit(t.bar);
+    }
+    ok = ok && mma_wait(t, 1, st);
+    if (ok) store_xdft(dyx, tmem, t, d);
+  }
+  if (LIFT) {
+    // inputs of the lift as MN-major B tiles (16 channels) in T0
+    __syncthreads();
+    for (int i = 0; i < TPC; ++i) {
+      float v[16];
+      lift_inputs(in, t.node0[i] + x, v);
+      store_inputs(sm + SM_T0, i, x, v);
+    }
+    operands_ready();
+    if (ok && threadIdx.x == 0) {
+      issue_wgrad(t, tmem, 128, SM_T1, SM_T0, 16, swap);
+      tc::commit(t.bar);
+    }
+    ok = ok && mma_wait(t, 1, st);
+    if (ok) reduce_wgrad(g.P, tmem, 128, 16, reinterpret_cast<float*>(sm + SM_T0));
+    reduce_vec32(g.pb, dpb, reinterpret_cast<float*>(sm + SM_T0));
+  }
+  tile_end(t, 256);
+}
+
+// ------------------------------------------------------------------ y and z stages (FP32)
+// forward DFT along y of the x-stage partials (summed over halves):
+// out[z][ky'][kx][c] = sum_y in(z, y, kx, c) e^{-2 pi i ky y / Ny}
+__global__ void __launch_bounds__(256) k_ydft(const float* __restrict__ in, const float2* __restrict__ ey,
+                                              float2* __restrict__ out, Dims d) {
+  extern __shared__ float2 sey[];  // [16][Ny]
+  for (int q = threadIdx.x; q < NK * d.Ny; q += 256) sey[q] = ey[q];
+  __syncthreads();
+  const int z = blockIdx.x;
+  const int kx = threadIdx.x & 7, c = threadIdx.x >> 3;
+  float2 acc[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) acc[k] = make_float2(0.f, 0.f);
+  for (int y = 0; y < d.Ny; ++y) {
+    const size_t row = (size_t)z * d.Ny + y;
+    float2 v = make_float2(0.f, 0.f);
+    for (int h = 0; h < d.H; ++h) {
+      const float2 w = *reinterpret_cast<const float2*>(in + ((row * d.H + h) * C + c) * KR + 2 * kx);
+      v.x += w.x;
+      v.y += w.y;
+    }
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const float2 e = sey[k * d.Ny + y];
+      acc[k].x += v.x * e.x - v.y * e.y;
+      acc[k].y += v.x * e.y + v.y * e.x;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NK; ++k) out[(((size_t)z * NK + k) * NKX + kx) * C + c] = acc[k];
+}
+
+// inverse DFT along y: out[row][c][2 kx + ri] = sum_ky' in[z][ky'][kx][c] e^{+2 pi i ky y / Ny}
+__global__ void __launch_bounds__(256) k_yidft(const float2* __restrict__ in, const float2* __restrict__ ey,
+                                               bf16* __restrict__ out, Dims d) {
+  extern __shared__ float2 sey[];
+  for (int q = threadIdx.x; q < NK * d.Ny; q += 256) sey[q] = ey[q];
+  __syncthreads();
+  const int z = blockIdx.x;
+  const int kx = threadIdx.x & 7, c = threadIdx.x >> 3;
+  float2 a[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) a[k] = in[(((size_t)z * NK + k) * NKX + kx) * C + c];
+  for (int y = 0; y < d.Ny; ++y) {
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const float2 e = sey[k * d.Ny + y];  // e^{-i}: use its conjugate
+      re += a[k].x * e.x + a[k].y * e.y;
+      im += a[k].y * e.x - a[k].x * e.y;
+    }
+    const size_t row = (size_t)z * d.Ny + y;
+    *reinterpret_cast<__nv_bfloat162*>(out + (row * C + c) * KR + 2 * kx) = __floats2bfloat162_rn(re, im);
+  }
+}
+
+// z DFT (scaled by 1/N) -> retained modes (saved), channel mixing with R,
+// inverse z DFT.  One CTA per (ky', kx).
+__global__ void __launch_bounds__(256) k_zmix(const float2* __restrict__ in, const float2* __restrict__ ez,
+                                              const bf16* __restrict__ Rb, float2* __restrict__ vhat,
+                                              float2* __restrict__ out, float inv_n, Dims d) {
+  extern __shared__ float2 s[];
+  float2* sv = s;                     // [Nz][32]
+  float2* sez = sv + d.Nz * C;        // [16][Nz]
+  float2* sh = sez + NK * d.Nz;       // [16][32] modes
+  float2* sy = sh + NK * C;           // [16][32] mixed
+  const int ky = blockIdx.x / NKX, kx = blockIdx.x % NKX;
+  for (int q = threadIdx.x; q < d.Nz * C; q += 256) {
+    const int z = q / C, c = q % C;
+    sv[q] = in[(((size_t)z * NK + ky) * NKX + kx) * C + c];
+  }
+  for (int q = threadIdx.x; q < NK * d.Nz; q += 256) sez[q] = ez[q];
+  __syncthreads();
+  for (int q = threadIdx.x; q < NK * C; q += 256) {
+    const int kz = q / C, c = q % C;
+    float re = 0.f, im = 0.f;
+    for (int z = 0; z < d.Nz; ++z) {
+      const float2 v = sv[z * C + c], e = sez[kz * d.Nz + z];
+      re += v.x * e.x - v.y * e.y;
+      im += v.x * e.y + v.y * e.x;
+    }
+    const float2 h = make_float2(re * inv_n, im * inv_n);
+    sh[q] = h;
+    if (vhat) vhat[((size_t)(kz * NK + ky) * NKX + kx) * C + c] = h;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < NK * C; q += 256) {
+    const int kz = q / C, co = q % C;
+    const size_t m = (size_t)(kz * NK + ky) * NKX + kx;
+    const __nv_bfloat162* r = reinterpret_cast<const __nv_bfloat162*>(Rb + (m * C + co) * C * 2);
+    float re = 0.f, im = 0.f;
+    for (int ci = 0; ci < C; ++ci) {
+      const float2 w = __bfloat1622float2(r[ci]);
+      const float2 v = sh[kz * C + ci];
+      re += w.x * v.x - w.y * v.y;
+      im += w.x * v.y + w.y * v.x;
+    }
+    sy[q] = make_float2(re, im);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < d.Nz * C; q += 256) {
+    const int z = q / C, c = q % C;
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int kz = 0; kz < NK; ++kz) {
+      const float2 v = sy[kz * C + c], e = sez[kz * d.Nz + z];  // conj(e)
+      re += v.x * e.x + v.y * e.y;
+      im += v.y * e.x - v.x * e.y;
+    }
+    out[(((size_t)z * NK + ky) * NKX + kx) * C + c] = make_float2(re, im);
+  }
+}
+
+// adjoint of k_zmix: dY = z DFT of in (no scale); gR += dY conj(vhat);
+// dV = sum_co conj(R) dY; out = (1/N) inverse z DFT of dV
+__global__ void __launch_bounds__(256) k_zmix_adj(const float2* __restrict__ in, const float2* __restrict__ ez,
+                                                  const bf16* __restrict__ Rb, const float2* __restrict__ vhat,
+                                                  float* __restrict__ gR, float2* __restrict__ out, float inv_n,
+                                                  Dims d) {
+  extern __shared__ float2 s[];
+  float2* sv = s;
+  float2* sez = sv + d.Nz * C;
+  float2* sdy = sez + NK * d.Nz;   // [16][32]
+  float2* sdv = sdy + NK * C;      // [16][32]
+  float2* sh = sdv + NK * C;       // [16][32] saved modes
+  const int ky = blockIdx.x / NKX, kx = blockIdx.x % NKX;
+  for (int q = threadIdx.x; q < d.Nz * C; q += 256) {
+    const int z = q / C, c = q % C;
+    sv[q] = in[(((size_t)z * NK + ky) * NKX + kx) * C + c];
+  }
+  for (int q = threadIdx.x; q < NK * d.Nz; q += 256) sez[q] = ez[q];
+  for (int q = threadIdx.x; q < NK * C; q += 256) {
+    const int kz = q / C, c = q % C;
+    sh[q] = vhat[((size_t)(kz * NK + ky) * NKX + kx) * C + c];
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < NK * C; q += 256) {
+    const int kz = q / C, c = q % C;
+    float re = 0.f, im = 0.f;
+    for (int z = 0; z < d.Nz; ++z) {
+      const float2 v = sv[z * C + c], e = sez[kz * d.Nz + z];
+      re += v.x * e.x - v.y * e.y;
+      im += v.x * e.y + v.y * e.x;
+    }
+    sdy[q] = make_float2(re, im);
+  }
+  __syncthreads();
+  // gR[m][co][ci] += dY[co] conj(V[ci])
+  for (int q = threadIdx.x; q < NK * C * C; q += 256) {
+    const int kz = q / (C * C), co = (q / C) % C, ci = q % C;
+    const size_t m = (size_t)(kz * NK + ky) * NKX + kx;
+    const float2 gy = sdy[kz * C + co], v = sh[kz * C + ci];
+    float* p = gR + ((m * C + co) * C + ci) * 2;
+    p[0] += gy.x * v.x + gy.y * v.y;
+    p[1] += gy.y * v.x - gy.x * v.y;
+  }
+  // dV[ci] = sum_co conj(R[co][ci]) dY[co]
+  for (int q = threadIdx.x; q < NK * C; q += 256) {
+    const int kz = q / C, ci = q % C;
+    const size_t m = (size_t)(kz * NK + ky) * NKX + kx;
+    float re = 0.f, im = 0.f;
+    for (int co = 0; co < C; ++co) {
+      const float2 w = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(Rb + ((m * C + co) * C + ci) * 2));
+      const float2 gy = sdy[kz * C + co];
+      re += w.x * gy.x + w.y * gy.y;
+      im += w.x * gy.y - w.y * gy.x;
+    }
+    sdv[q] = make_float2(re, im);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < d.Nz * C; q += 256) {
+    const int z = q / C, c = q % C;
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int kz = 0; kz < NK; ++kz) {
+      const float2 v = sdv[kz * C + c], e = sez[kz * d.Nz + z];
+      re += v.x * e.x + v.y * e.y;
+      im += v.y * e.x - v.x * e.y;
+    }
+    out[(((size_t)z * NK + ky) * NKX + kx) * C + c] = make_float2(re * inv_n, im * inv_n);
+  }
+}
+
+// ------------------------------------------------------------------ parameters
+// BF16 operand copies of the FP32 master parameters
+__global__ void k_refresh(const float* __restrict__ p, bf16* Pb, bf16* Wb, bf16* Wtb, bf16* Rb, bf16* Q1b,
+                          bf16* Q1tb) {
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k = tid; k < 512; k += stride) Pb[k] = __float2bfloat16_rn(p[OFF_P + k]);
+  for (long long k = tid; k < 4 * 1024; k += stride) {
+    const int l = (int)(k / 1024), r = (int)(k % 1024), o = r / 32, i = r % 32;
+    const float w = p[layer_off(l) + r];
+    Wb[k] = __float2bfloat16_rn(w);
+    Wtb[l * 1024 + i * 32 + o] = __float2bfloat16_rn(w);
+  }
+  for (long long k = tid; k < 1024; k += stride) {
+    const int o = (int)(k / 32), i = (int)(k % 32);
+    const float w = p[OFF_Q1 + k];
+    Q1b[k] = __float2bfloat16_rn(w);
+    Q1tb[i * 32 + o] = __float2bfloat16_rn(w);
+  }
+  const long long nr = (long long)NMODE * C * C * 2;
+  for (long long k = tid; k < 4 * nr; k += stride) {
+    const int l = (int)(k / nr);
+    Rb[k] = __float2bfloat16_rn(p[layer_off(l) + 1056 + (k % nr)]);
+  }
+}
+
+__global__ void k_adam(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       long long n, float lr, float b1, float b2, float eps, float c1, float c2, float gscale) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const float gr = g[k] * gscale;
+    const float mk = b1 * m[k] + (1.f - b1) * gr;
+    const float vk = b2 * v[k] + (1.f - b2) * gr * gr;
+    m[k] = mk;
+    v[k] = vk;
+    p[k] -= lr * (mk * c1) / (sqrtf(vk * c2) + eps);
+    g[k] = 0.f;
+  }
+}
+
+// ------------------------------------------------------------------ self-test
+// One CTA: exact small-integer products through every operand layout used
+// above.  out1[128][64]: tiles 0 and 2 times W (K-major A and B); out2[128][16]:
+// MN-major A over the 4 tiles times a K-major table; out3[128][32]: MN-major A
+// times the MN-major tile 1.
+PHAFD_HD float st_val(int i, int x, int c) { return (float)((i * 7 + x * 3 + c * 5) % 5 - 2); }
+PHAFD_HD float st_w(int n, int k) { return (float)((n * 3 + k * 7) % 5 - 2); }
+PHAFD_HD float st_f(int n, int x) { return (float)((n * 5 + x * 3) % 7 - 3); }
+
+__global__ void __launch_bounds__(NTH) k_selftest(float* out1, float* out2, float* out3, int swap, Status st) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  Dims d{TX, 4, 1, 1, 4, 4 * TX};
+  Tile t;
+  tile_begin(t, sm, d, 256);
+  const uint32_t tmem = *t.taddr_slot;
+  const int x = threadIdx.x;
+  for (int i = 0; i < TPC; ++i) {
+    float v[32];
+    for (int c = 0; c < 32; ++c) v[c] = st_val(i, x, c);
+    store_row(nullptr, sm + SM_T0, i, x, v);
+  }
+  for (int q = threadIdx.x; q < 32 * 32; q += NTH) {
+    const int n = q / 32, k = q % 32;
+    *reinterpret_cast<bf16*>(sm + SM_BM + (n & 7) * 16 + (k & 7) * 2 + (k >> 3) * 128 + (n >> 3) * 512) =
+        __float2bfloat16_rn(st_w(n, k));
+  }
+  for (int q = threadIdx.x; q < KR * TX; q += NTH) {
+    const int n = q / TX, k = q % TX;
+    *reinterpret_cast<bf16*>(sm + SM_B2 + (n & 7) * 16 + (k & 7) * 2 + (k >> 3) * 128 + (n >> 3) * 2048) =
+        __float2bfloat16_rn(st_f(n, k));
+  }
+  operands_ready();
+  if (threadIdx.x == 0) {
+    const uint32_t id = tc::idesc_bf16(128, 32, 0, 0);
+    for (int u = 0; u < 2; ++u) {
+      const int i = 2 * u;
+      for (int s = 0; s < 2; ++s)
+        tc::mma(tmem + 32 * u, kdesc(t.sbase + SM_T0 + 512 * i + 256 * s, 2048), kdesc(t.sbase + SM_BM + 256 * s, 512),
+                id, s > 0);
+    }
+    issue_xdft(t, tmem + 64, SM_T0, swap);
+    const uint32_t id3 = tc::idesc_bf16(128, 32, 1, 1);
+    for (int s = 0; s < TX / 16; ++s)
+      tc::mma(tmem + 96, mndesc(t.sbase + SM_T0 + 4096 * s, 128, 2048, swap),
+              mndesc(t.sbase + SM_T0 + 512 * 1 + 4096 * s, 128, 2048, swap), id3, s > 0);
+    tc::commit(t.bar);
+  }
+  if (mma_wait(t, 0, st)) {
+    float v[32];
+    tmem_row32(tmem, 0, v);
+    for (int c = 0; c < 32; ++c) out1[x * 64 + c] = v[c];
+    tmem_row32(tmem, 32, v);
+    for (int c = 0; c < 32; ++c) out1[x * 64 + 32 + c] = v[c];
+    tc::tmem_ld16(lane_addr(tmem, 64), v);
+    for (int c = 0; c < 16; ++c) out2[x * 16 + c] = v[c];
+    tmem_row32(tmem, 96, v);
+    for (int c = 0; c < 32; ++c) out3[x * 32 + c] = v[c];
+  }
+  tile_end(t, 256);
+}
+
+}  // namespace fno
+}  // namespace phafd
+
+// ====================================================================== host
+using namespace phafd;
+using namespace phafd::fno;
+
+namespace {
+
+#define FCK(x)                                                                                        \
+  do {                                                                                                \
+    cudaError_t e_ = (x);                                                                             \
+    if (e_ != cudaSuccess) throw std::runtime_error(std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct Dbuf {
+  void* p = nullptr;
+  size_t n = 0;
+  void alloc(size_t bytes) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = bytes;
+    if (bytes) FCK(cudaMalloc(&p, bytes));
+  }
+  ~Dbuf() {
+    if (p) cudaFree(p);
+  }
+  template <typename T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+uint16_t bf16_bits(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  const uint32_t lsb = (u >> 16) & 1u;
+  u += 0x7FFFu + lsb;  // round to nearest even
+  return (uint16_t)(u >> 16);
+}
+
+// the MN-major descriptor order, found once per device by the self-test
+std::mutex g_swap_mu;
+int g_swap[64];
+bool g_swap_known[64];
+
+int run_selftest(int device, int result[2], int* swap_out) {
+  FCK(cudaSetDevice(device));
+  Dbuf o1, o2, o3, err;
+  o1.alloc(128 * 64 * 4);
+  o2.alloc(128 * 16 * 4);
+  o3.alloc(128 * 32 * 4);
+  err.alloc(4);
+  FCK(cudaFuncSetAttribute(k_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM_TRAIN));
+  std::vector<float> e1(128 * 64), e2(128 * 16), e3(128 * 32);
+  for (int x = 0; x < 128; ++x) {
+    for (int u = 0; u < 2; ++u)
+      for (int n = 0; n < 32; ++n) {
+        float s = 0;
+        for (int c = 0; c < 32; ++c) s += st_val(2 * u, x, c) * st_w(n, c);
+        e1[x * 64 + 32 * u + n] = s;
+      }
+  }
+  for (int m = 0; m < 128; ++m) {
+    const int i = m / 32, c = m % 32;
+    for (int n = 0; n < 16; ++n) {
+      float s = 0;
+      for (int x = 0; x < 128; ++x) s += st_val(i, x, c) * st_f(n, x);
+      e2[m * 16 + n] = s;
+    }
+    for (int n = 0; n < 32; ++n) {
+      float s = 0;
+      for (int x = 0; x < 128; ++x) s += st_val(i, x, c) * st_val(1, x, n);
+      e3[m * 32 + n] = s;
+    }
+  }
+  result[0] = 0;
+  result[1] = 0;
+  *swap_out = -1;
+  std::vector<float> h1(128 * 64), h2(128 * 16), h3(128 * 32);
+  for (int swap = 0; swap < 2; ++swap) {
+    FCK(cudaMemset(err.p, 0, 4));
+    FCK(cudaMemset(o1.p, 0, o1.n));
+    FCK(cudaMemset(o2.p, 0, o2.n));
+    FCK(cudaMemset(o3.p, 0, o3.n));
+    k_selftest<<<1, NTH, SM_TRAIN>>>(o1.as<float>(), o2.as<float>(), o3.as<float>(), swap, Status{err.as<int>()});
+    FCK(cudaGetLastError());
+    FCK(cudaDeviceSynchronize());
+    int herr = 0;
+    FCK(cudaMemcpy(&herr, err.p, 4, cudaMemcpyDeviceToHost));
+    if (herr) return PHAFD_ERR_TIMEOUT;
+    FCK(cudaMemcpy(h1.data(), o1.p, o1.n, cudaMemcpyDeviceToHost));
+    FCK(cudaMemcpy(h2.data(), o2.p, o2.n, cudaMemcpyDeviceToHost));
+    FCK(cudaMemcpy(h3.data(), o3.p, o3.n, cudaMemcpyDeviceToHost));
+    const bool k_ok = h1 == e1;
+    const bool mn_ok = h2 == e2 && h3 == e3;
+    if (k_ok) result[0] = 1;
+    if (k_ok && mn_ok) {
+      result[1] = 1;
+      *swap_out = swap;
+      break;
+    }
+  }
+  return PHAFD_OK;
+}
+
+int mn_swap_for(int device) {
+  std::lock_guard<std::mutex> lk(g_swap_mu);
+  if (device < 0 || device >= 64) return -1;
+  if (!g_swap_known[device]) {
+    int res[2], sw = -1;
+    if (run_selftest(device, res, &sw) != PHAFD_OK) return -1;
+    g_swap[device] = sw;
+    g_swap_known[device] = true;
+  }
+  return g_swap[device];
+}
+
+}  // namespace
+
+struct phafd_fno {
+  std::string err;
+  int device = 0, swap = 0;
+  bool train = false;
+  Dims d{};
+  float norm[8] = {0.45f, 0.05f, 0.f, 1.f, 3.f, 0.3f, 1.f, 0.f};
+  cudaStream_t st = nullptr;
+  Dbuf params, grad, adam_m, adam_v;
+  Dbuf Pb, Wb, Wtb, Rb, Q1b, Q1tb;
+  Dbuf F, Gt, G, Ft, ey, ez;
+  Dbuf act[5], pre[3], delta[2];
+  Dbuf vx, vxy, yxy, yx, vhat[4], out, sum, loss, errf;
+  long long adam_t = 0;
+
+  size_t smem_ey() const { return (size_t)NK * d.Ny * sizeof(float2); }
+  size_t smem_z(int extra) const { return ((size_t)d.Nz * C + (size_t)NK * d.Nz + (size_t)extra * NK * C) * sizeof(float2); }
+
+  void tables() {
+    const int Nx = d.Nx;
+    std::vector<uint16_t> f(KR * Nx), gt(KR * Nx), g(Nx * KR), ft(Nx * KR);
+    for (int kx = 0; kx < NKX; ++kx)
+      for (int x = 0; x < Nx; ++x) {
+        const double th = 2.0 * M_PI * (double)((long long)kx * x % Nx) / Nx;
+        const double w = kx == 0 ? 1.0 : 2.0;
+        const float c = (float)std::cos(th), s = (float)std::sin(th);
+        f[(2 * kx) * Nx + x] = bf16_bits(c);
+        f[(2 * kx + 1) * Nx + x] = bf16_bits(-s);
+        ft[x * KR + 2 * kx] = bf16_bits(c);
+        ft[x * KR + 2 * kx + 1] = bf16_bits(-s);
+        g[x * KR + 2 * kx] = bf16_bits((float)(w * c));
+        g[x * KR + 2 * kx + 1] = bf16_bits((float)(-w * s));
+        gt[(2 * kx) * Nx + x] = bf16_bits((float)(w * c));
+        gt[(2 * kx + 1) * Nx + x] = bf16_bits((float)(-w * s));
+      }
+    F.alloc(f.size() * 2);
+    Gt.alloc(gt.size() * 2);
+    G.alloc(g.size() * 2);
+    Ft.alloc(ft.size() * 2);
+    FCK(cudaMemcpy(F.p, f.data(), f.size() * 2, cudaMemcpyHostToDevice));
+    FCK(cudaMemcpy(Gt.p, gt.data(), gt.size() * 2, cudaMemcpyHostToDevice));
+    FCK(cudaMemcpy(G.p, g.data(), g.size() * 2, cudaMemcpyHostToDevice));
+    FCK(cudaMemcpy(Ft.p, ft.data(), ft.size() * 2, cudaMemcpyHostToDevice));
+    auto twid = [](int n) {
+      std::vector<float2> e(NK * n);
+      for (int k = 0; k < NK; ++k) {
+        const int kk = k < NK / 2 ? k : k - NK;
+        for (int y = 0; y < n; ++y) {
+          const long long ph = (((long long)kk * y) % n + n) % n;
+          const double th = 2.0 * M_PI * (double)ph / n;
+          e[k * n + y] = make_float2((float)std::cos(th), (float)-std::sin(th));
+        }
+      }
+      return e;
+    };
+    auto hy = twid(d.Ny), hz = twid(d.Nz);
+    ey.alloc(hy.size() * sizeof(float2));
+    ez.alloc(hz.size() * sizeof(float2));
+    FCK(cudaMemcpy(ey.p, hy.data(), ey.n, cudaMemcpyHostToDevice));
+    FCK(cudaMemcpy(ez.p, hz.data(), ez.n, cudaMemcpyHostToDevice));
+  }
+
+  void refresh() {
+    k_refresh<<<1024, 256, 0, st>>>(params.as<float>(), Pb.as<bf16>(), Wb.as<bf16>(), Wtb.as<bf16>(), Rb.as<bf16>(),
+                                    Q1b.as<bf16>(), Q1tb.as<bf16>());
+    FCK(cudaGetLastError());
+  }
+
+  const bf16* W(int l) const { return Wb.as<bf16>() + l * 1024; }
+  const bf16* Wt(int l) const { return Wtb.as<bf16>() + l * 1024; }
+  const bf16* R(int l) const { return Rb.as<bf16>() + (size_t)l * NMODE * C * C * 2; }
+  const float* P(size_t off) const { return params.as<float>() + off; }
+  Status status() const { return Status{errf.as<int>()}; }
+  unsigned ntiles() const { return (unsigned)(d.rows / TPC * d.H); }
+  float inv_n() const { return 1.f / (float)d.nodes; }
+
+  // spectral branch of layer l: x-stage partials in vx -> x-inverse input in yx
+  void spectral(int l, bool save) {
+    k_ydft<<<d.Nz, 256, smem_ey(), st>>>(vx.as<float>(), ey.as<float2>(), vxy.as<float2>(), d);
+    k_zmix<<<NK * NKX, 256, smem_z(2), st>>>(vxy.as<float2>(), ez.as<float2>(), R(l),
+                                             save ? vhat[l].as<float2>() : nullptr, yxy.as<float2>(), inv_n(), d);
+    k_yidft<<<d.Nz, 256, smem_ey(), st>>>(yxy.as<float2>(), ey.as<float2>(), yx.as<bf16>(), d);
+  }
+
+  LiftIn lift_in(const float* phi, const float* rho, float chi) const {
+    return LiftIn{phi, rho, (chi - norm[4]) / norm[5], norm[0], norm[1], norm[2], norm[3]};
+  }
+
+  // forward through the four layers; training keeps v0..v4 and pre1..pre3
+  void forward(const float* phi, const float* rho, float chi, bool training) {
+    const Status s = status();
+    bf16* v[5];
+    for (int k = 0; k < 5; ++k) v[k] = training ? act[k].as<bf16>() : act[k & 1].as<bf16>();
+    k_lift<<<ntiles(), NTH, SM_INF, st>>>(lift_in(phi, rho, chi), Pb.as<bf16>(), P(OFF_PB), F.as<bf16>(), v[0],
+                                            vx.as<float>(), d, swap, s);
+    for (int l = 0; l < 4; ++l) {
+      spectral(l, training);
+      const float* b = P(layer_off(l) + 1024);
+      bf16* pr = training && l < 3 ? pre[l].as<bf16>() : nullptr;
+      if (l < 3) {
+        if (training)
+          k_layer<true, true, true><<<ntiles(), NTH, SM_INF, st>>>(v[l], W(l), b, G.as<bf16>(), yx.as<bf16>(),
+                                                                     F.as<bf16>(), v[l + 1], pr, vx.as<float>(), d,
+                                                                     swap, s);
+        else
+          k_layer<true, true, false><<<ntiles(), NTH, SM_INF, st>>>(v[l], W(l), b, G.as<bf16>(), yx.as<bf16>(),
+                                                                      F.as<bf16>(), v[l + 1], pr, vx.as<float>(), d,
+                                                                      swap, s);
+      } else {
+        k_layer<false, false, false><<<ntiles(), NTH, SM_INF, st>>>(v[l], W(l), b, G.as<bf16>(), yx.as<bf16>(),
+                                                                      F.as<bf16>(), v[l + 1], nullptr, vx.as<float>(),
+                                                                      d, swap, s);
+      }
+    }
+    FCK(cudaGetLastError());
+  }
+
+  Grads grads(int l) const {
+    float* g = grad.as<float>();
+    Grads r;
+    r.P = g + OFF_P;
+    r.pb = g + OFF_PB;
+    r.W = l >= 0 ? g + layer_off(l) : nullptr;
+    r.b = l >= 0 ? g + layer_off(l) + 1024 : nullptr;
+    r.Q1 = g + OFF_Q1;
+    r.q1b = g + OFF_Q1B;
+    r.q2 = g + OFF_Q2;
+    r.q2b = g + OFF_Q2B;
+    return r;
+  }
+
+  void backward(const float* phi, const float* rho, float chi, const float* target) {
+    const Status s = status();
+    float q2b = 0;
+    FCK(cudaMemcpyAsync(&q2b, P(OFF_Q2B), 4, cudaMemcpyDeviceToHost, st));
+    FCK(cudaStreamSynchronize(st));
+    FCK(cudaMemsetAsync(loss.p, 0, 8, st));
+    // delta4 into delta[0], its G-DFT partials into vx
+    k_proj_train<<<ntiles(), NTH, SM_TRAIN, st>>>(act[4].as<bf16>(), Q1b.as<bf16>(), Q1tb.as<bf16>(), P(OFF_Q1B),
+                                                  P(OFF_Q2), q2b, target, Gt.as<bf16>(), delta[0].as<bf16>(),
+                                                  vx.as<float>(), grads(-1), loss.as<double>(), d, swap, s);
+    const LiftIn in = lift_in(phi, rho, chi);
+    int cur = 0;
+    for (int l = 3; l >= 0; --l) {
+      // adjoint spectral chain: dYx partials (vx) -> dVx (yx)
+      k_ydft<<<d.Nz, 256, smem_ey(), st>>>(vx.as<float>(), ey.as<float2>(), vxy.as<float2>(), d);
+      float* gR = grad.as<float>() + layer_off(l) + 1056;
+      k_zmix_adj<<<NK * NKX, 256, smem_z(3), st>>>(vxy.as<float2>(), ez.as<float2>(), R(l), vhat[l].as<float2>(), gR,
+                                                   yxy.as<float2>(), inv_n(), d);
+      k_yidft<<<d.Nz, 256, smem_ey(), st>>>(yxy.as<float2>(), ey.as<float2>(), yx.as<bf16>(), d);
+      const bf16* dl = delta[cur].as<bf16>();
+      bf16* dout = delta[1 - cur].as<bf16>();
+      if (l > 0)
+        k_layer_bwd<true, true, false><<<ntiles(), NTH, SM_TRAIN, st>>>(
+            dl, act[l].as<bf16>(), pre[l - 1].as<bf16>(), Wt(l), Ft.as<bf16>(), yx.as<bf16>(), Gt.as<bf16>(), dout,
+            vx.as<float>(), in, grads(l), d, swap, s);
+      else
+        k_layer_bwd<false, false, true><<<ntiles(), NTH, SM_TRAIN, st>>>(
+            dl, act[0].as<bf16>(), nullptr, Wt(0), Ft.as<bf16>(), yx.as<bf16>(), Gt.as<bf16>(), nullptr,
+            vx.as<float>(), in, grads(0), d, swap, s);
+      cur = 1 - cur;
+    }
+    FCK(cudaGetLastError());
+  }
+
+  void check_err() {
+    int h = 0;
+    FCK(cudaMemcpyAsync(&h, errf.p, 4, cudaMemcpyDeviceToHost, st));
+    FCK(cudaStreamSynchronize(st));
+    if (h) throw std::runtime_error("tensor-core wait timed out");
+  }
+};
+
+namespace {
+template <typename K>
+void smem_attr(K k, size_t bytes) {
+  FCK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+}  // namespace
+
+#define FAPI_BEGIN(f)                 \
+  if (!(f)) return PHAFD_ERR_INVALID; \
+  try {                               \
+    FCK(cudaSetDevice((f)->device));
+#define FAPI_END(f)                     \
+  }                                     \
+  catch (const std::exception& e) {     \
+    (f)->err = e.what();                \
+    return PHAFD_ERR_CUDA;              \
+  }                                     \
+  return PHAFD_OK;
+
+extern "C" {
+
+size_t phafd_fno_param_count(void) { return NPARAM; }
+
+int phafd_fno_selftest(int device, int result[2]) {
+  if (!result) return PHAFD_ERR_INVALID;
+  try {
+    int sw = -1;
+    return run_selftest(device, result, &sw);
+  } catch (const std::exception&) {
+    return PHAFD_ERR_CUDA;
+  }
+}
+
+int phafd_fno_create(phafd_fno** out, int device, int nx, int ny, int nz, int train) {
+  if (!out) return PHAFD_ERR_INVALID;
+  *out = nullptr;
+  if (nx < TX || nx % TX || ny < NK || nz < NK || ((long long)nz * ny) % TPC) return PHAFD_ERR_UNSUPPORTED;
+  phafd_fno* f = new phafd_fno();
+  f->device = device;
+  f->train = train != 0;
+  f->d = Dims{nx, ny, nz, nx / TX, (long long)nz * ny, (long long)nz * ny * nx};
+  try {
+    FCK(cudaSetDevice(device));
+    const int sw = mn_swap_for(device);
+    if (sw < 0) {
+      delete f;
+      return PHAFD_ERR_UNSUPPORTED;
+    }
+    f->swap = sw;
+    FCK(cudaStreamCreateWithFlags(&f->st, cudaStreamNonBlocking));
+    f->params.alloc(NPARAM * 4);
+    FCK(cudaMemset(f->params.p, 0, f->params.n));
+    f->Pb.alloc(512 * 2);
+    f->Wb.alloc(4 * 1024 * 2);
+    f->Wtb.alloc(4 * 1024 * 2);
+    f->Rb.alloc((size_t)4 * NMODE * C * C * 2 * 2);
+    f->Q1b.alloc(1024 * 2);
+    f->Q1tb.alloc(1024 * 2);
+    f->tables();
+    const size_t nact = (size_t)f->d.nodes * C * 2;
+    const int nkeep = f->train ? 5 : 2;
+    for (int k = 0; k < nkeep; ++k) f->act[k].alloc(nact);
+    f->vx.alloc((size_t)f->d.rows * f->d.H * C * KR * 4);
+    f->vxy.alloc((size_t)nz * NK * NKX * C * sizeof(float2));
+    f->yxy.alloc((size_t)nz * NK * NKX * C * sizeof(float2));
+    f->yx.alloc((size_t)f->d.rows * C * KR * 2);
+    f->out.alloc((size_t)f->d.nodes * 4);
+    f->sum.alloc(8);
+    f->loss.alloc(8);
+    f->errf.alloc(4);
+    FCK(cudaMemset(f->errf.p, 0, 4));
+    if (f->train) {
+      for (int k = 0; k < 3; ++k) f->pre[k].alloc(nact);
+      for (int k = 0; k < 2; ++k) f->delta[k].alloc(nact);
+      for (int k = 0; k < 4; ++k) f->vhat[k].alloc((size_t)NMODE * C * sizeof(float2));
+      f->grad.alloc(NPARAM * 4);
+      f->adam_m.alloc(NPARAM * 4);
+      f->adam_v.alloc(NPARAM * 4);
+      FCK(cudaMemset(f->grad.p, 0, f->grad.n));
+      FCK(cudaMemset(f->adam_m.p, 0, f->adam_m.n));
+      FCK(cudaMemset(f->adam_v.p, 0, f->adam_v.n));
+    }
+    smem_attr(k_lift, SM_INF);
+    smem_attr(k_layer<true, true, true>, SM_INF);
+    smem_attr(k_layer<true, true, false>, SM_INF);
+    smem_attr(k_layer<false, false, false>, SM_INF);
+    smem_attr(k_proj, SM_INF);
+    smem_attr(k_proj_train, SM_TRAIN);
+    smem_attr(k_layer_bwd<true, true, false>, SM_TRAIN);
+    smem_attr(k_layer_bwd<false, false, true>, SM_TRAIN);
+    smem_attr(k_ydft, f->smem_ey());
+    smem_attr(k_yidft, f->smem_ey());
+    smem_attr(k_zmix, f->smem_z(2));
+    smem_attr(k_zmix_adj, f->smem_z(3));
+    f->refresh();
+    FCK(cudaStreamSynchronize(f->st));
+  } catch (const std::exception& e) {
+    delete f;
+    return PHAFD_ERR_CUDA;
+  }
+  *out = f;
+  return PHAFD_OK;
+}
+
+int phafd_fno_destroy(phafd_fno* f) {
+  if (!f) return PHAFD_ERR_INVALID;
+  cudaSetDevice(f->device);
+  if (f->st) cudaStreamSynchronize(f->st);
+  if (f->st) cudaStreamDestroy(f->st);
+  delete f;
+  return PHAFD_OK;
+}
+
+const char* phafd_fno_last_error(phafd_fno* f) { return f ? f->err.c_str() : "null network"; }
+
+int phafd_fno_set_params(phafd_fno* f, const float* p, size_t n) {
+  if (!f || !p || n != NPARAM) return PHAFD_ERR_INVALID;
+  FAPI_BEGIN(f)
+  FCK(cudaMemcpyAsync(f->params.p, p, NPARAM * 4, cudaMemcpyHostToDevice, f->st));
+  f->refresh();
+  FCK(cudaStreamSynchronize(f->st));
+  FAPI_END(f)
+}
+
+int phafd_fno_get_params(phafd_fno* f, float* p, size_t n) {
+  if (!f || !p || n != NPARAM) return PHAFD_ERR_INVALID;
+  FAPI_BEGIN(f)
+  FCK(cudaMemcpyAsync(p, f->params.p, NPARAM * 4, cudaMemcpyDeviceToHost, f->st));
+  FCK(cudaStreamSynchronize(f->st));
+  FAPI_END(f)
+}
+
+int phafd_fno_set_norm(phafd_fno* f, const float norm[8]) {
+  if (!f || !norm) return PHAFD_ERR_INVALID;
+  if (norm[1] == 0.f || norm[3] == 0.f || norm[5] == 0.f) return PHAFD_ERR_INVALID;
+  std::memcpy(f->norm, norm, sizeof(f->norm));
+  return PHAFD_OK;
+}
+
+int phafd_fno_infer(phafd_fno* f, const float* phi, const float* rho, float chi, float* corr, void* stream) {
+  if (!f || !phi || !rho || !corr) return PHAFD_ERR_INVALID;
+  FAPI_BEGIN(f)
+  cudaStream_t cs = stream ? (cudaStream_t)stream : f->st;
+  cudaEvent_t ev;
+  if (stream) {  // order against the caller's stream
+    FCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    FCK(cudaEventRecord(ev, cs));
+    FCK(cudaStreamWaitEvent(f->st, ev, 0));
+    cudaEventDestroy(ev);
+  }
+  f->forward(phi, rho, chi, false);
+  FCK(cudaMemsetAsync(f->sum.p, 0, 8, f->st));
+  k_proj<<<f->ntiles(), NTH, SM_INF, f->st>>>(f->act[0].as<bf16>(), f->Q1b.as<bf16>(), f->P(OFF_Q1B),
+                                                 f->P(OFF_Q2), 0.f, f->out.as<float>(), f->sum.as<double>(), f->d,
+                                                 f->status());
+  // q2b cancels in out - mean(out)
+  k_center<<<1024, 256, 0, f->st>>>(f->out.as<float>(), f->sum.as<double>(), f->norm[6], corr, f->d.nodes);
+  FCK(cudaGetLastError());
+  if (stream) {
+    FCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    FCK(cudaEventRecord(ev, f->st));
+    FCK(cudaStreamWaitEvent(cs, ev, 0));
+    cudaEventDestroy(ev);
+  } else {
+    f->check_err();
+  }
+  FAPI_END(f)
+}
+
+int phafd_fno_zero_grad(phafd_fno* f) {
+  if (!f || !f->train) return PHAFD_ERR_INVALID;
+  FAPI_BEGIN(f)
+  FCK(cudaMemsetAsync(f->grad.p, 0, f->grad.n, f->st));
+  FAPI_END(f)
+}
+
+int phafd_fno_forward_backward(phafd_fno* f, const float* phi, const float* rho, float chi, const float* target,
+                               double* loss) {
+  if (!f || !f->train || !phi || !rho || !target) return PHAFD_ERR_INVALID;
+  FAPI_BEGIN(f)
+  f->forward(phi, rho, chi, true);
+  f->backward(phi, rho, chi, target);
+  f->check_err();
+  if (loss) FCK(cudaMemcpy(loss, f->loss.p, 8, cudaMemcpyDeviceToHost));
+  FAPI_END(f)
+}
+
+int phafd_fno_get_grad(phafd_fno* f, float* g, size_t n) {
+  if (!f || !f->train || !g || n != NPARAM) return PHAFD_ERR_INVALID;
+  FAPI_BEGIN(f)
+  FCK(cudaMemcpyAsync(g, f->grad.p, NPARAM * 4, cudaMemcpyDeviceToHost, f->st));
+  FCK(cudaStreamSynchronize(f->st));
+  FAPI_END(f)
+}
+
+int phafd_fno_adam_step(phafd_fno* f, float lr, float beta1, float beta2, float eps, int nbatch) {
+  if (!f || !f->train || nbatch <= 0) return PHAFD_ERR_INVALID;
+  FAPI_BEGIN(f)
+  f->adam_t += 1;
+  const float c1 = 1.f / (1.f - std::pow(beta1, (float)f->adam_t));
+  const float c2 = 1.f / (1.f - std::pow(beta2, (float)f->adam_t));
+  k_adam<<<2048, 256, 0, f->st>>>(f->params.as<float>(), f->grad.as<float>(), f->adam_m.as<float>(),
+                                  f->adam_v.as<float>(), (long long)NPARAM, lr, beta1, beta2, eps, c1, c2,
+                                  1.f / (float)nbatch);
+  f->refresh();
+  FCK(cudaStreamSynchronize(f->st));
+  FAPI_END(f)
+}
+
+}  // extern "C"

@@ -232,8 +232,25 @@ PHAFD_D cpx<T> update_value(const UpdateArgs<T>& u, int kx, int cy, int cz, cpx<
   const T q2 = qx * qx + qz * qz + qy * qy;  // reference order: qx^2 + q(kz)^2 + q(ky)^2
   const T pre = u.mobility * q2 * u.dt;
   const T g = u.tvg * q2;
-  const cpx<T> inner = mk<T>(mu.x + g * ph.x, mu.y + g * ph.y);
-  cpx<T> r = mk<T>((ph.x - pre * inner.x) * u.norm, (ph.y - pre * inner.y) * u.norm);
+  cpx<T> r;
+  T namp = (T)1;
+  if (u.nsub > 1) {
+    // a = 1 - pre (f2 + g) per substep: phi' = a^K phi - S_K pre (mu - f2 phi),
+    // S_K = sum_{s<K} a^s; the noise of K substeps has variance sum a^(2s)
+    const T a = (T)1 - pre * (u.f2 + g);
+    T ak = (T)1, sk = (T)0, s2 = (T)0;
+    for (int k = 0; k < u.nsub; ++k) {
+      sk += ak;
+      s2 += ak * ak;
+      ak *= a;
+    }
+    const cpx<T> src = mk<T>(mu.x - u.f2 * ph.x, mu.y - u.f2 * ph.y);
+    r = mk<T>((ak * ph.x - sk * pre * src.x) * u.norm, (ak * ph.y - sk * pre * src.y) * u.norm);
+    namp = sqrt(s2);
+  } else {
+    const cpx<T> inner = mk<T>(mu.x + g * ph.x, mu.y + g * ph.y);
+    r = mk<T>((ph.x - pre * inner.x) * u.norm, (ph.y - pre * inner.y) * u.norm);
+  }
   T u0 = 0, u1 = 0;
   if (u.noise == PHAFD_NOISE_REFERENCE) {
     const double2 w = u.uref[((size_t)kx * Nz + cz) * Ny + cy];
@@ -246,9 +263,9 @@ PHAFD_D cpx<T> update_value(const UpdateArgs<T>& u, int kx, int cy, int cz, cpx<
   }
   const T sq = sqrt(q2);
   if (real) {
-    r.x += u.rpref * sq * u.sqrtdt * u0;
+    r.x += u.rpref * sq * u.sqrtdt * u0 * namp;
   } else {
-    const T a = u.cpref * sq * u.sqrtdt;
+    const T a = u.cpref * sq * u.sqrtdt * namp;
     r.x += a * u0;
     r.y += a * u1;
   }
@@ -333,17 +350,19 @@ k_zpass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
 // phi_hat (global) for the bulk modes (1 <= kx < Nx/2), phi_hat' stored;
 // z inverse FFT of phi_hat' and of i qz phi_hat' -> out0, out1.  Tiles of the
 // kx = 0 and kx = Nx/2 planes, whose modes pair with mirror modes in other
-// tiles, only store mu_hat; k_zpass<planes_only> finishes them.
+// tiles, only store mu_hat; k_zpass<planes_only> finishes them.  With
+// kx0 = 1 the grid covers the bulk planes only and the Hermitian planes are
+// transformed by k_zpass<planes_only> on a parallel branch.
 template <typename T, int N, int LB>
 __global__ void __launch_bounds__(N * LB * 2 / 16)
 k_zfused(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __restrict__ out0,
          cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny,
-         UpdateArgs<T> u, int store_mu) {
+         UpdateArgs<T> u, int store_mu, int kx0) {
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = 2 * LB;
   constexpr int NT = N * NL / 16, STR = NL + 1;
-  const int kx = blockIdx.y;
+  const int kx = (int)blockIdx.y + kx0;
   const int c0 = blockIdx.x * LB;
   const bool plane = (kx == 0 || kx == u.Nxh - 1);
   cpx<T>* sph = s + (size_t)N * STR;  // phi_hat tile, [kz][c]
@@ -493,6 +512,7 @@ struct Axis {
   static int zpass(const Geom& g, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
                    const UpdateArgs<T>& u, cudaStream_t st, int planes_only = 0) {
     const T dq = (T)g.kq[2];
+    if (planes_only && u.Nxh != g.nxh) return -1;  // kx of the second plane comes from u.Nxh
     const unsigned gy = planes_only ? 2u : (unsigned)g.nxh;
     if (out1) {
       constexpr int LB = NLT / 2 >= 1 ? NLT / 2 : 1;
@@ -513,13 +533,16 @@ struct Axis {
   }
 
   static int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
-                    const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st) {
+                    const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only,
+                    cudaStream_t st) {
     constexpr int LB = NLT / 2 >= 1 ? NLT / 2 : 1;
     const size_t sm = (size_t)N * (3 * LB + 1) * sizeof(cpx<T>);
-    dim3 grid((g.ny + LB - 1) / LB, g.nxh);
+    const int kx0 = bulk_only ? 1 : 0;
+    if (g.nxh - 2 * kx0 <= 0) return 0;
+    dim3 grid((g.ny + LB - 1) / LB, g.nxh - 2 * kx0);
     auto k = k_zfused<T, N, LB>;
     if (set_smem(k, sm)) return -1;
-    k<<<grid, N * LB * 2 / 16, sm, st>>>(muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu);
+    k<<<grid, N * LB * 2 / 16, sm, st>>>(muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
     return 0;
   }
 };
@@ -565,15 +588,16 @@ int GridOps<T>::ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, c
 namespace r256 {
 template <typename T>
 int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
-           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st);
+           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only, cudaStream_t st);
 }
 
 template <typename T>
 int GridOps<T>::zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
-                       const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st) {
-  if (g.nz == 256) return r256::zfused<T>(g, muin, muhat, out0, out1, twf, twi, u, store_mu, st);
+                       const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only,
+                       cudaStream_t st) {
+  if (g.nz == 256) return r256::zfused<T>(g, muin, muhat, out0, out1, twf, twi, u, store_mu, bulk_only, st);
   switch (g.nz) {
-#define CASE(n) case n: return Axis<T, n>::zfused(g, muin, muhat, out0, out1, twf, twi, u, store_mu, st);
+#define CASE(n) case n: return Axis<T, n>::zfused(g, muin, muhat, out0, out1, twf, twi, u, store_mu, bulk_only, st);
     PHAFD_FOR_SIZES(CASE)
 #undef CASE
   }
@@ -585,6 +609,18 @@ int GridOps<T>::zpass_planes(const Geom& g, cpx<T>* out0, cpx<T>* out1, const cp
                              cudaStream_t st) {
   switch (g.nz) {
 #define CASE(n) case n: return Axis<T, n>::template zpass<+1, true>(g, nullptr, out0, out1, tw, u, st, 1);
+    PHAFD_FOR_SIZES(CASE)
+#undef CASE
+  }
+  return -2;
+}
+
+template <typename T>
+int GridOps<T>::zfwd_planes(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, const cpx<T>* tw, cudaStream_t st) {
+  UpdateArgs<T> none{};
+  none.Ny = g.ny; none.Nz = g.nz; none.Nxh = g.nxh;  // the plane kernel takes kx = Nx/2 from Nxh
+  switch (g.nz) {
+#define CASE(n) case n: return Axis<T, n>::template zpass<-1, false>(g, muin, muhat, nullptr, tw, none, st, 1);
     PHAFD_FOR_SIZES(CASE)
 #undef CASE
   }

@@ -38,6 +38,10 @@ struct UpdateArgs {
   uint32_t seed;
   const long long* d_step;
   int Ny, Nz, Nxh;
+  // nsub > 1: nsub linearised substeps with the nonlinear part of mu frozen
+  // (the base propagator of the learned macro step); f2 = dmu/dphi at the mean
+  int nsub;
+  T f2;
 };
 
 template <typename T>
@@ -51,8 +55,12 @@ struct GridOps {
   static int zpass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
                    const UpdateArgs<T>* u, cudaStream_t st);
   // forward z FFT of mu + update + z inverse FFT (bulk kx); plane tiles store mu_hat only
+  // (bulk_only: kx in [1, Nx/2) only; the planes then take zfwd_planes + zpass_planes)
   static int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
-                    const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st);
+                    const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only,
+                    cudaStream_t st);
+  // forward z FFT of the kx = 0 and kx = Nx/2 planes of mu into mu_hat
+  static int zfwd_planes(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, const cpx<T>* tw, cudaStream_t st);
   // plane-fused x r2c + y fft (returns -3 when the plane path does not apply)
   static int xy_fwd(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* twx, const cpx<T>* twy,
                     const FHArgs& fh, cudaStream_t st);

@@ -45,13 +45,13 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 k_zfused256(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __restrict__ out0,
             cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny,
-            UpdateArgs<T> u, int store_mu) {
+            UpdateArgs<T> u, int store_mu, int kx0) {
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* bufA = reinterpret_cast<cpx<T>*>(smraw);  // N x W
   cpx<T>* bufB = bufA + N * W;                        // N x W (phi_hat staging, then second ifft)
   const int c = threadIdx.x & 15;
   const int j = threadIdx.x >> 4;
-  const int kx = blockIdx.y;
+  const int kx = (int)blockIdx.y + kx0;
   const int ky = blockIdx.x * W + c;
   const bool plane = (kx == 0 || kx == u.Nxh - 1);
   const bool live = ky < Ny;
@@ -121,12 +121,14 @@ k_zfused256(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>*
 
 template <typename T>
 int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
-           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, cudaStream_t st) {
+           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only, cudaStream_t st) {
   const size_t sm = (size_t)2 * N * W * sizeof(cpx<T>);
   auto k = k_zfused256<T>;
   if (set_smem(k, sm)) return -1;
-  dim3 grid((g.ny + W - 1) / W, g.nxh);
-  k<<<grid, 256, sm, st>>>(muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu);
+  const int kx0 = bulk_only ? 1 : 0;
+  if (g.nxh - 2 * kx0 <= 0) return 0;
+  dim3 grid((g.ny + W - 1) / W, g.nxh - 2 * kx0);
+  k<<<grid, 256, sm, st>>>(muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
   return 0;
 }
 

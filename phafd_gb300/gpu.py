@@ -17,7 +17,8 @@ GRIDATOM = {"none": 0, "gaussian": 1, "LJish": 2, "LJish/linear": 3}
 NOISE = {"off": 0, "reference": 1, "philox": 2}
 ZGHOST = {"rank1": 0, "periodic": 1}
 SCHEDULE = {"reference": 0, "resident": 1}
-ERRORS = {-1: "invalid", -2: "cuda", -3: "nan", -4: "overflow", -5: "constraint", -6: "unsupported", -7: "nomem"}
+ERRORS = {-1: "invalid", -2: "cuda", -3: "nan", -4: "overflow", -5: "constraint", -6: "unsupported", -7: "nomem",
+          -8: "timeout"}
 
 # every symbol declared in include/phafd_gpu.h
 EXPORTS = [
@@ -35,6 +36,8 @@ EXPORTS = [
     "phafd_half_list_size", "phafd_half_list", "phafd_grid_list_size", "phafd_grid_list",
     "phafd_stage_gradient", "phafd_stage_borders_and_build", "phafd_stage_pairs",
     "phafd_gradphi_noalloc",
+    "phafd_compute_complex", "phafd_structure_factor",
+    "phafd_set_linear_substeps", "phafd_grid_device", "phafd_deposit_density", "phafd_grid_add_device",
 ]
 
 
@@ -47,7 +50,8 @@ class SemiParams(C.Structure):
 class Counters(C.Structure):
     _fields_ = [("num_less_zero", C.c_longlong), ("num_great_zero", C.c_longlong),
                 ("neighbor_calls", C.c_longlong), ("timestep", C.c_longlong),
-                ("status", C.c_longlong), ("nan_step", C.c_longlong), ("kernels_per_step", C.c_longlong)]
+                ("status", C.c_longlong), ("nan_step", C.c_longlong), ("kernels_per_step", C.c_longlong),
+                ("kernels_per_rebuild", C.c_longlong)]
 
 
 class PhafdError(RuntimeError):
@@ -110,6 +114,12 @@ def load(path=None):
         "phafd_stage_gradient": [vp],
         "phafd_stage_borders_and_build": [vp],
         "phafd_stage_pairs": [vp],
+        "phafd_compute_complex": [vp, C.c_int, C.c_int, dp],
+        "phafd_structure_factor": [vp, C.c_int, dp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")],
+        "phafd_set_linear_substeps": [vp, C.c_int, C.c_double],
+        "phafd_grid_device": [vp, C.c_int, C.POINTER(vp)],
+        "phafd_deposit_density": [vp, vp],
+        "phafd_grid_add_device": [vp, vp, C.c_double],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -191,6 +201,36 @@ class PhafdGPU:
             out = np.zeros(self.shape, np.float64)
             self._call("phafd_grid_get", FIELD[field], out.reshape(-1))
         return out
+
+    # ---- spectra and the learned macro step
+    COMPLEX = {"real": 0, "imag": 1, "modulus": 2, "norm": 3}
+
+    def compute_complex(self, field, quant):
+        """compute complex ft_phi|ft_chempot real|imag|modulus|norm, layout [ky][kz][kx]."""
+        nz, ny, nx = self.shape
+        out = np.zeros((ny, nz, nx // 2 + 1), np.float64)
+        self._call("phafd_compute_complex", FIELD[field], self.COMPLEX[quant], out.reshape(-1))
+        return out
+
+    def structure_factor(self, nbins):
+        sk = np.zeros(nbins, np.float64)
+        cnt = np.zeros(nbins, np.int64)
+        self._call("phafd_structure_factor", nbins, sk, cnt)
+        return sk, cnt
+
+    def set_linear_substeps(self, nsub, f2=0.0):
+        self._call("phafd_set_linear_substeps", int(nsub), float(f2))
+
+    def grid_device(self, field="phi"):
+        p = C.c_void_p()
+        self._call("phafd_grid_device", FIELD[field], C.byref(p))
+        return p.value
+
+    def deposit_density(self, rho_ptr):
+        self._call("phafd_deposit_density", C.c_void_p(rho_ptr))
+
+    def grid_add_device(self, src_ptr, scale=1.0):
+        self._call("phafd_grid_add_device", C.c_void_p(src_ptr), float(scale))
 
     def atoms_create(self, tags, mol, types, x):
         self.n = len(tags)
