@@ -178,6 +178,10 @@ int phafd_structure_factor(phafd_ctx* ctx, int nbins, double* sk, long long* cou
  * phafd_grid_add_device adds scale * src (device, context precision) to phi
  * and re-derives the spectrum and gradient the next step starts from. */
 int phafd_set_linear_substeps(phafd_ctx* ctx, int nsub, double f2);
+/* copy the dynamic state (fields, spectra, beads, lists, step counters) of
+ * src into dst; both set up with the same grid, beads and schedule on one
+ * device (fix parameters such as noise may differ) */
+int phafd_ctx_copy_state(phafd_ctx* dst, phafd_ctx* src);
 int phafd_grid_device(phafd_ctx* ctx, int field, void** dev);
 int phafd_deposit_density(phafd_ctx* ctx, void* rho);
 int phafd_grid_add_device(phafd_ctx* ctx, const void* src, double scale);

@@ -83,9 +83,11 @@ __global__ void k_axpy(T* __restrict__ y, const T* __restrict__ x, T scale, long
 
 // shell sums of |F|^2 over the half spectrum [kx][kz][ky]; modes with
 // 0 < kx < Nx/2 stand for their mirror too (weight 2)
+// |q| in units of the x-axis dq (ry = dqy/dqx, rz = dqz/dqx): integer
+// wavenumbers of a cubic box give exact squares, so shell edges are exact
 template <typename T>
-__global__ void k_shells(const cpx<T>* __restrict__ F, int Nx, int Ny, int Nz, double dqx, double dqy, double dqz,
-                         double binw, int nbins, double* __restrict__ sum, unsigned long long* __restrict__ cnt) {
+__global__ void k_shells(const cpx<T>* __restrict__ F, int Nx, int Ny, int Nz, double ry, double rz, int nbins,
+                         double* __restrict__ sum, unsigned long long* __restrict__ cnt) {
   extern __shared__ double sh[];
   double* ss = sh;
   unsigned long long* sc = reinterpret_cast<unsigned long long*>(sh + nbins);
@@ -96,8 +98,8 @@ __global__ void k_shells(const cpx<T>* __restrict__ F, int Nx, int Ny, int Nz, d
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < total; m += (long long)gridDim.x * blockDim.x) {
     const int ky = (int)(m % Ny), kz = (int)((m / Ny) % Nz), kx = (int)(m / ((long long)Ny * Nz));
     if (kx == 0 && ky == 0 && kz == 0) continue;
-    const double qx = dqx * kx, qy = dqy * wrap_index(ky, Ny), qz = dqz * wrap_index(kz, Nz);
-    const int b = (int)(sqrt(qx * qx + qy * qy + qz * qz) / binw);
+    const double qx = (double)kx, qy = ry * wrap_index(ky, Ny), qz = rz * wrap_index(kz, Nz);
+    const int b = (int)floor(sqrt(qx * qx + qy * qy + qz * qz) + 1e-9);
     if (b >= nbins) continue;
     const int w = (kx == 0 || 2 * kx == Nx) ? 1 : 2;
     const cpx<T> f = F[m];
@@ -1415,16 +1417,16 @@ int phafd_structure_factor(phafd_ctx* c, int nbins, double* sk, long long* count
   double* dsum = acc.as<double>();
   unsigned long long* dcnt = reinterpret_cast<unsigned long long*>(dsum + nbins);
   FHArgs none{0, 0, c->fh_counters(), 0, nullptr};
-  const double tp = 2.0 * M_PI;
+  const double ry = c->period[0] / c->period[1], rz = c->period[0] / c->period[2];
   const size_t shm = (size_t)nbins * 16;
   if (c->precision == PHAFD_FP64) {
     c->r2c<double>(c->phi.as<double>(), nullptr, c->w1.as<cpx<double>>(), none);
-    k_shells<double><<<1024, 256, shm, c->st>>>(c->w1.as<cpx<double>>(), c->N[0], c->N[1], c->N[2], tp / c->period[0],
-                                                tp / c->period[1], tp / c->period[2], tp / c->period[0], nbins, dsum, dcnt);
+    k_shells<double><<<1024, 256, shm, c->st>>>(c->w1.as<cpx<double>>(), c->N[0], c->N[1], c->N[2], ry, rz, nbins,
+                                                dsum, dcnt);
   } else {
     c->r2c<float>(c->phi.as<float>(), nullptr, c->w1.as<cpx<float>>(), none);
-    k_shells<float><<<1024, 256, shm, c->st>>>(c->w1.as<cpx<float>>(), c->N[0], c->N[1], c->N[2], tp / c->period[0],
-                                               tp / c->period[1], tp / c->period[2], tp / c->period[0], nbins, dsum, dcnt);
+    k_shells<float><<<1024, 256, shm, c->st>>>(c->w1.as<cpx<float>>(), c->N[0], c->N[1], c->N[2], ry, rz, nbins,
+                                               dsum, dcnt);
   }
   CK(cudaGetLastError());
   std::vector<double> hs(nbins);
@@ -1498,6 +1500,39 @@ int phafd_grid_add_device(phafd_ctx* c, const void* src, double scale) {
   }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
+  API_END(c)
+}
+
+int phafd_ctx_copy_state(phafd_ctx* dst, phafd_ctx* src) {
+  if (!dst || !src) return PHAFD_ERR_INVALID;
+  phafd_ctx* c = dst;
+  API_BEGIN(c)
+  if (dst->device != src->device || dst->precision != src->precision || !dst->setup_done || !src->setup_done ||
+      dst->nreal != src->nreal || dst->n != src->n || dst->schedule != src->schedule)
+    throw std::invalid_argument("copy_state: contexts differ in device, precision, grid, beads or schedule");
+  CK(cudaSetDevice(src->device));
+  CK(cudaStreamSynchronize(dst->st));
+  CK(cudaStreamSynchronize(src->st));
+  auto cp = [&](DevBuf& d, const DevBuf& s) {
+    if (d.bytes != s.bytes) throw std::invalid_argument("copy_state: buffer sizes differ");
+    if (s.bytes) CK(cudaMemcpyAsync(d.p, s.p, s.bytes, cudaMemcpyDeviceToDevice, src->st));
+  };
+  for (auto pr : {std::make_pair(&dst->phi, &src->phi), std::make_pair(&dst->gx, &src->gx),
+                  std::make_pair(&dst->gy, &src->gy), std::make_pair(&dst->gz, &src->gz),
+                  std::make_pair(&dst->dep, &src->dep), std::make_pair(&dst->phat[0], &src->phat[0]),
+                  std::make_pair(&dst->phat[1], &src->phat[1]), std::make_pair(&dst->bx, &src->bx),
+                  std::make_pair(&dst->bux, &src->bux), std::make_pair(&dst->bf, &src->bf),
+                  std::make_pair(&dst->bxhold, &src->bxhold), std::make_pair(&dst->bfchain, &src->bfchain),
+                  std::make_pair(&dst->btang, &src->btang), std::make_pair(&dst->bimage, &src->bimage),
+                  std::make_pair(&dst->bin_of, &src->bin_of), std::make_pair(&dst->bin_count, &src->bin_count),
+                  std::make_pair(&dst->bin_start, &src->bin_start), std::make_pair(&dst->sorted, &src->sorted),
+                  std::make_pair(&dst->bin_off, &src->bin_off), std::make_pair(&dst->nbr, &src->nbr),
+                  std::make_pair(&dst->nnbr, &src->nnbr), std::make_pair(&dst->gl, &src->gl),
+                  std::make_pair(&dst->ngl, &src->ngl), std::make_pair(&dst->d_counters, &src->d_counters)})
+    cp(*pr.first, *pr.second);
+  CK(cudaStreamSynchronize(src->st));
+  dst->cur = src->cur;
+  dst->timestep = src->timestep;
   API_END(c)
 }
 

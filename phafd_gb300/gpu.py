@@ -38,6 +38,7 @@ EXPORTS = [
     "phafd_gradphi_noalloc",
     "phafd_compute_complex", "phafd_structure_factor",
     "phafd_set_linear_substeps", "phafd_grid_device", "phafd_deposit_density", "phafd_grid_add_device",
+    "phafd_ctx_copy_state",
 ]
 
 
@@ -120,6 +121,7 @@ def load(path=None):
         "phafd_grid_device": [vp, C.c_int, C.POINTER(vp)],
         "phafd_deposit_density": [vp, vp],
         "phafd_grid_add_device": [vp, vp, C.c_double],
+        "phafd_ctx_copy_state": [vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -231,6 +233,10 @@ class PhafdGPU:
 
     def grid_add_device(self, src_ptr, scale=1.0):
         self._call("phafd_grid_add_device", C.c_void_p(src_ptr), float(scale))
+
+    def copy_state_from(self, other):
+        """this context's dynamic state := other's (same set-up)."""
+        self._call("phafd_ctx_copy_state", other._c)
 
     def atoms_create(self, tags, mol, types, x):
         self.n = len(tags)

@@ -71,15 +71,16 @@ def test_gradients_match_oracle(gpu_lib):
     net.set_params(p)
     net.set_norm(NORM)
     net.zero_grad()
-    loss = net.forward_backward(dev(phi).data_ptr(), dev(rho).data_ptr(), 3.1, dev(tgt).data_ptr())
+    dphi, drho, dtgt = dev(phi), dev(rho), dev(tgt)  # kept alive while the library reads them
+    loss = net.forward_backward(dphi.data_ptr(), drho.data_ptr(), 3.1, dtgt.data_ptr())
     g = net.get_grad()
     lo, go = FNOOracle(p, shape, NORM, bf=True).loss_and_grad(phi, rho, 3.1, tgt)
-    assert abs(loss - lo) < 1e-3 * lo
     gflat = FNOOracle.flat(go)
+    errs = {}
     for name, (o, shp) in F.layout().items():
         n = int(np.prod(shp))
-        e = rel(g[o:o + n], gflat[o:o + n])
-        assert e < 3e-2, (name, e)
+        errs[name] = rel(g[o:o + n], gflat[o:o + n])
+    assert abs(loss - lo) < 1e-3 * lo and max(errs.values()) < 3e-2, (loss, lo, errs)
     net.close()
 
 
