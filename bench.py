@@ -330,6 +330,11 @@ def run_gpu(args):
                        "note": "state uploaded once from host arrays, %d steps each followed by a bead read, phi read at the end; includes set-up" % k}
         e.close()
 
+    # FP32 production path against the FP64 path from the same state and
+    # the same Philox noise: relative S(k) error (max over shells) after 50 steps
+    if rank == 0 and world == 1 and not args.no_e2e:
+        line["fp32_vs_fp64"] = precision_check(cfg, chains, local, 50)
+
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, dt = cpu_baseline_oracle(cfg, chains, 3)
         line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
@@ -340,6 +345,29 @@ def run_gpu(args):
     if torch_dist:
         torch_dist.destroy_process_group()
     return 0
+
+
+def precision_check(cfg, chains, device, steps):
+    import numpy as np
+    from phafd_gb300 import workloads as W
+    from phafd_gb300.gpu import PhafdGPU
+    out = {}
+    res = {}
+    for prec in (32, 64):
+        g = PhafdGPU(precision=prec, device=device, schedule="resident")
+        W.apply(g, cfg, chains=chains)
+        g.setup()
+        g.run(steps)
+        res[prec] = (g.structure_factor(cfg["n"] // 2)[0], g.grid_get("phi"))
+        g.close()
+    s32, p32 = res[32]
+    s64, p64 = res[64]
+    m = s64[1:] > 0
+    out["steps"] = steps
+    out["sk_rel_err_max"] = float(np.max(np.abs(s32[1:][m] - s64[1:][m]) / s64[1:][m]))
+    out["phi_max_abs_err"] = float(np.max(np.abs(p32 - p64)))
+    out["mass_err"] = float(abs(p32.mean() - p64.mean()))
+    return out
 
 
 def run_ensemble(args):
@@ -429,6 +457,20 @@ def run_learned(args):
     torch.cuda.synchronize()
     t_sur = time.perf_counter() - t0
     judged = [{"step": j[0], "sk_err": j[1], "mass_err": j[2], "accepted": bool(j[3])} for j in run.judged]
+    phase_s = dict(run.times)
+    # network inference alone, CUDA events around the call
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    rho = torch.zeros((n_eval,) * 3, device="cuda")
+    corr = torch.empty_like(rho)
+    phi = torch.full_like(rho, 0.4)
+    net.infer(phi.data_ptr(), rho.data_ptr(), 3.0, corr.data_ptr())
+    torch.cuda.synchronize()
+    ev0.record()
+    for _ in range(5):
+        net.infer(phi.data_ptr(), rho.data_ptr(), 3.0, corr.data_ptr())
+    ev1.record()
+    torch.cuda.synchronize()
+    infer_ms = ev0.elapsed_time(ev1) / 5
     run.close()
     net.close()
     v_sur, v_plain = nsub / t_sur, nsub / t_plain
@@ -446,6 +488,7 @@ def run_learned(args):
         "horizon_substeps": horizon, "errors_vs_plain": herr,
         "macro_error_rel": {"train": gain_train, "held_out_128": gain_held, "linear_step_alone": 1.0},
         "judge": judged, "train_loss": hist, "seconds": {"generate": t_gen, "train": t_train},
+        "timed_phase_seconds": phase_s, "network_infer_ms": infer_ms,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -461,6 +504,62 @@ def W_nbeads(cfg):
     return cfg["nchains"] * cfg["chain_len"]
 
 
+def fno_bytes_per_inference(n):
+    """Compulsory HBM bytes of one network inference on an n^3 grid: lift
+    (phi, rho in; v0 and its x-stage partials out), four layers (v in, x-inverse
+    rows in, v out, x-stage partials out for the next layer), the y stages of
+    the spectral branches, the projection and the centring."""
+    N = n ** 3
+    halves = max(1, n // 128)
+    xst = 16 * 32 * 4 * halves / n          # x-stage partials per node
+    rows = 32 * 16 * 2 / n                  # x-inverse input per node
+    lift = 8 + 64 + xst
+    layers = 4 * (64 + rows + 64) + 3 * xst
+    spectral = 4 * (xst + rows)
+    proj = 64 + 4 + 8
+    return N * (lift + layers + spectral + proj)
+
+
+def run_fno_infer(args):
+    """Inference of the spectral neural operator alone (random parameters)."""
+    import numpy as np
+    import torch
+    from phafd_gb300 import build as B
+    B.build()
+    from phafd_gb300.fno import FNO, init_params
+    n = 256 if args.workload == "fno_infer256" else 128
+    net = FNO((n, n, n))
+    net.set_params(init_params(0, out_scale=1.0))
+    net.set_norm(np.array([0.4, 0.02, 0.0, 1.0, 3.0, 0.3, 1e-3, 0.0], np.float32))
+    g = torch.Generator(device="cuda").manual_seed(0)
+    phi = 0.4 + 0.02 * torch.randn((n, n, n), device="cuda", generator=g)
+    rho = torch.relu(torch.randn((n, n, n), device="cuda", generator=g)) * 0.1
+    corr = torch.empty_like(phi)
+    st = torch.cuda.current_stream()
+    for _ in range(max(args.warmup, 3)):
+        net.infer(phi.data_ptr(), rho.data_ptr(), 3.0, corr.data_ptr(), stream=st.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        net.infer(phi.data_ptr(), rho.data_ptr(), 3.0, corr.data_ptr(), stream=st.cuda_stream)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    peak, kind = measured_peak()
+    nbytes = fno_bytes_per_inference(n)
+    line = {"metric": "network inferences/s (spectral neural operator, %d^3)" % n, "value": 1000.0 / ms,
+            "unit": "inferences/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 activations, f32 accumulate", "data": "synthetic",
+            "config": {"workload": args.workload, "grid": [n] * 3, "channels": 32, "layers": 4, "modes": 16},
+            "roofline": {"bound": "hbm", "achieved": nbytes / (ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": nbytes / (ms / 1000.0) / 1e9 / peak, "peak_kind": kind, "bytes": nbytes}}
+    print(json.dumps(line), flush=True)
+    net.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -469,6 +568,8 @@ def main():
         return run_ensemble(args)
     if args.workload in ("learned128", "learned256"):
         return run_learned(args)
+    if args.workload in ("fno_infer128", "fno_infer256"):
+        return run_fno_infer(args)
     return run_gpu(args)
 
 

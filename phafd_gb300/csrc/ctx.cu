@@ -204,6 +204,7 @@ struct phafd_ctx {
   int* d_check_done() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 6); }
   // graph
   cudaGraphExec_t gexec = nullptr;
+  cudaGraphExec_t gexec1[2] = {nullptr, nullptr};  // one step, per spectrum parity (resident)
   bool eager_done = false;
   long long kernels_per_step = 0;
   long long rebuild_kernels = 0;  // kernels of the conditional rebuild body
@@ -220,6 +221,8 @@ struct phafd_ctx {
 
   ~phafd_ctx() {
     if (gexec) cudaGraphExecDestroy(gexec);
+    for (auto ge : gexec1)
+      if (ge) cudaGraphExecDestroy(ge);
     if (uref_h) cudaFreeHost(uref_h);
     for (cudaEvent_t e : {ev_fork, ev_dep, ev_join, ev_pl_fork, ev_pl_join}) if (e) cudaEventDestroy(e);
     if (stc) cudaStreamDestroy(stc);
@@ -233,6 +236,10 @@ struct phafd_ctx {
   void invalidate_graph() {
     if (gexec) cudaGraphExecDestroy(gexec);
     gexec = nullptr;
+    for (auto& ge : gexec1) {
+      if (ge) cudaGraphExecDestroy(ge);
+      ge = nullptr;
+    }
     eager_done = false;
   }
 
@@ -1174,34 +1181,38 @@ static void enqueue_run(phafd_ctx* c, int nsteps) {
       CK(cudaGetLastError());
       if (use_graph) c->eager_done = true;
     } else {
-      if (resident && c->gexec && c->cur != c->graph_cur) {
-        c->step_once();  // bring the spectrum parity back to the captured one
-        CK(cudaGetLastError());
-        c->timestep += 1;
-        resident_spectrum_flip(c);
-        continue;
-      }
-      if (!c->gexec) {
-        // capture the two buffer parities of the resident schedule as one graph of two steps
-        c->graph_cur = c->cur;
-        cudaGraph_t g;
-        CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
-        c->step_once();
-        if (resident) { resident_spectrum_flip(c); c->step_once(); resident_spectrum_flip(c); }
-        CK(cudaStreamEndCapture(c->st, &g));
-        c->kernels_per_step = count_kernels(g) / (resident ? 2 : 1);
-        CK(cudaGraphInstantiate(&c->gexec, g, 0));
-        cudaGraphDestroy(g);
-      }
-      if (resident && s + 1 < nsteps) {
+      // Graphs: two steps (both spectrum parities of the resident schedule)
+      // for runs of two or more, one step per parity for the rest.
+      if (resident && nsteps - s >= 2 && (!c->gexec || c->cur == c->graph_cur)) {
+        if (!c->gexec) {
+          c->graph_cur = c->cur;
+          cudaGraph_t g;
+          CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
+          c->step_once();
+          resident_spectrum_flip(c);
+          c->step_once();
+          resident_spectrum_flip(c);
+          CK(cudaStreamEndCapture(c->st, &g));
+          c->kernels_per_step = count_kernels(g) / 2;
+          CK(cudaGraphInstantiate(&c->gexec, g, 0));
+          cudaGraphDestroy(g);
+        }
         CK(cudaGraphLaunch(c->gexec, c->st));
         ++s;
         c->timestep += 2;
         continue;  // the pair of steps leaves cur unchanged
       }
-      // odd remainder (or reference schedule): one eager step
-      c->step_once();
-      CK(cudaGetLastError());
+      const int par = resident ? c->cur : 0;
+      if (!c->gexec1[par]) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
+        c->step_once();
+        CK(cudaStreamEndCapture(c->st, &g));
+        if (!c->kernels_per_step) c->kernels_per_step = count_kernels(g);
+        CK(cudaGraphInstantiate(&c->gexec1[par], g, 0));
+        cudaGraphDestroy(g);
+      }
+      CK(cudaGraphLaunch(c->gexec1[par], c->st));
     }
     c->timestep += 1;
     if (resident) resident_spectrum_flip(c);

@@ -689,56 +689,65 @@ __global__ void __launch_bounds__(NTH) k_layer_bwd(const bf16* __restrict__ delt
 
 // ------------------------------------------------------------------ y and z stages (FP32)
 // forward DFT along y of the x-stage partials (summed over halves):
-// out[z][ky'][kx][c] = sum_y in(z, y, kx, c) e^{-2 pi i ky y / Ny}
+// out[z][ky'][kx][c] += sum_{y in chunk} in(z, y, kx, c) e^{-2 pi i ky y / Ny}
+// grid (Nz, Ny / YCH); out must be zeroed; the chunk sums meet in atomics.
+constexpr int YCH = 16;
 __global__ void __launch_bounds__(256) k_ydft(const float* __restrict__ in, const float2* __restrict__ ey,
                                               float2* __restrict__ out, Dims d) {
-  extern __shared__ float2 sey[];  // [16][Ny]
-  for (int q = threadIdx.x; q < NK * d.Ny; q += 256) sey[q] = ey[q];
-  __syncthreads();
-  const int z = blockIdx.x;
+  __shared__ float2 sey[NK * YCH];
+  const int z = blockIdx.x, y0 = blockIdx.y * YCH;
+  for (int q = threadIdx.x; q < NK * YCH; q += 256) sey[q] = ey[(q / YCH) * d.Ny + y0 + q % YCH];
   const int kx = threadIdx.x & 7, c = threadIdx.x >> 3;
-  float2 acc[NK];
+  float2 v[YCH];
 #pragma unroll
-  for (int k = 0; k < NK; ++k) acc[k] = make_float2(0.f, 0.f);
-  for (int y = 0; y < d.Ny; ++y) {
-    const size_t row = (size_t)z * d.Ny + y;
-    float2 v = make_float2(0.f, 0.f);
+  for (int yy = 0; yy < YCH; ++yy) {
+    const size_t row = (size_t)z * d.Ny + y0 + yy;
+    float2 a = make_float2(0.f, 0.f);
     for (int h = 0; h < d.H; ++h) {
       const float2 w = *reinterpret_cast<const float2*>(in + ((row * d.H + h) * C + c) * KR + 2 * kx);
-      v.x += w.x;
-      v.y += w.y;
+      a.x += w.x;
+      a.y += w.y;
     }
-#pragma unroll
-    for (int k = 0; k < NK; ++k) {
-      const float2 e = sey[k * d.Ny + y];
-      acc[k].x += v.x * e.x - v.y * e.y;
-      acc[k].y += v.x * e.y + v.y * e.x;
-    }
+    v[yy] = a;
   }
+  __syncthreads();
 #pragma unroll
-  for (int k = 0; k < NK; ++k) out[(((size_t)z * NK + k) * NKX + kx) * C + c] = acc[k];
+  for (int k = 0; k < NK; ++k) {
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int yy = 0; yy < YCH; ++yy) {
+      const float2 e = sey[k * YCH + yy];
+      re += v[yy].x * e.x - v[yy].y * e.y;
+      im += v[yy].x * e.y + v[yy].y * e.x;
+    }
+    float2* o = out + (((size_t)z * NK + k) * NKX + kx) * C + c;
+    atomicAdd(&o->x, re);
+    atomicAdd(&o->y, im);
+  }
 }
 
 // inverse DFT along y: out[row][c][2 kx + ri] = sum_ky' in[z][ky'][kx][c] e^{+2 pi i ky y / Ny}
+// grid (Nz, Ny / YCH)
 __global__ void __launch_bounds__(256) k_yidft(const float2* __restrict__ in, const float2* __restrict__ ey,
                                                bf16* __restrict__ out, Dims d) {
-  extern __shared__ float2 sey[];
-  for (int q = threadIdx.x; q < NK * d.Ny; q += 256) sey[q] = ey[q];
-  __syncthreads();
-  const int z = blockIdx.x;
+  __shared__ float2 sey[NK * YCH];
+  const int z = blockIdx.x, y0 = blockIdx.y * YCH;
+  for (int q = threadIdx.x; q < NK * YCH; q += 256) sey[q] = ey[(q / YCH) * d.Ny + y0 + q % YCH];
   const int kx = threadIdx.x & 7, c = threadIdx.x >> 3;
   float2 a[NK];
 #pragma unroll
   for (int k = 0; k < NK; ++k) a[k] = in[(((size_t)z * NK + k) * NKX + kx) * C + c];
-  for (int y = 0; y < d.Ny; ++y) {
+  __syncthreads();
+#pragma unroll 4
+  for (int yy = 0; yy < YCH; ++yy) {
     float re = 0.f, im = 0.f;
 #pragma unroll
     for (int k = 0; k < NK; ++k) {
-      const float2 e = sey[k * d.Ny + y];  // e^{-i}: use its conjugate
+      const float2 e = sey[k * YCH + yy];  // e^{-i}: use its conjugate
       re += a[k].x * e.x + a[k].y * e.y;
       im += a[k].y * e.x - a[k].x * e.y;
     }
-    const size_t row = (size_t)z * d.Ny + y;
+    const size_t row = (size_t)z * d.Ny + y0 + yy;
     *reinterpret_cast<__nv_bfloat162*>(out + (row * C + c) * KR + 2 * kx) = __floats2bfloat162_rn(re, im);
   }
 }
@@ -1167,10 +1176,15 @@ struct phafd_fno {
 
   // spectral branch of layer l: x-stage partials in vx -> x-inverse input in yx
   void spectral(int l, bool save) {
-    k_ydft<<<d.Nz, 256, smem_ey(), st>>>(vx.as<float>(), ey.as<float2>(), vxy.as<float2>(), d);
+    ydft(vx.as<float>(), vxy.as<float2>());
     k_zmix<<<NK * NKX, 256, smem_z(2), st>>>(vxy.as<float2>(), ez.as<float2>(), R(l),
                                              save ? vhat[l].as<float2>() : nullptr, yxy.as<float2>(), inv_n(), d);
-    k_yidft<<<d.Nz, 256, smem_ey(), st>>>(yxy.as<float2>(), ey.as<float2>(), yx.as<bf16>(), d);
+    k_yidft<<<dim3(d.Nz, d.Ny / YCH), 256, 0, st>>>(yxy.as<float2>(), ey.as<float2>(), yx.as<bf16>(), d);
+  }
+
+  void ydft(const float* in, float2* out) {
+    FCK(cudaMemsetAsync(out, 0, (size_t)d.Nz * NK * NKX * C * sizeof(float2), st));
+    k_ydft<<<dim3(d.Nz, d.Ny / YCH), 256, 0, st>>>(in, ey.as<float2>(), out, d);
   }
 
   LiftIn lift_in(const float* phi, const float* rho, float chi) const {
@@ -1234,11 +1248,11 @@ struct phafd_fno {
     int cur = 0;
     for (int l = 3; l >= 0; --l) {
       // adjoint spectral chain: dYx partials (vx) -> dVx (yx)
-      k_ydft<<<d.Nz, 256, smem_ey(), st>>>(vx.as<float>(), ey.as<float2>(), vxy.as<float2>(), d);
+      ydft(vx.as<float>(), vxy.as<float2>());
       float* gR = grad.as<float>() + layer_off(l) + 1056;
       k_zmix_adj<<<NK * NKX, 256, smem_z(3), st>>>(vxy.as<float2>(), ez.as<float2>(), R(l), vhat[l].as<float2>(), gR,
                                                    yxy.as<float2>(), inv_n(), d);
-      k_yidft<<<d.Nz, 256, smem_ey(), st>>>(yxy.as<float2>(), ey.as<float2>(), yx.as<bf16>(), d);
+      k_yidft<<<dim3(d.Nz, d.Ny / YCH), 256, 0, st>>>(yxy.as<float2>(), ey.as<float2>(), yx.as<bf16>(), d);
       const bf16* dl = delta[cur].as<bf16>();
       bf16* dout = delta[1 - cur].as<bf16>();
       if (l > 0)
@@ -1298,7 +1312,7 @@ int phafd_fno_selftest(int device, int result[2]) {
 int phafd_fno_create(phafd_fno** out, int device, int nx, int ny, int nz, int train) {
   if (!out) return PHAFD_ERR_INVALID;
   *out = nullptr;
-  if (nx < TX || nx % TX || ny < NK || nz < NK || ((long long)nz * ny) % TPC) return PHAFD_ERR_UNSUPPORTED;
+  if (nx < TX || nx % TX || ny < NK || nz < NK || ny % YCH || ((long long)nz * ny) % TPC) return PHAFD_ERR_UNSUPPORTED;
   phafd_fno* f = new phafd_fno();
   f->device = device;
   f->train = train != 0;
@@ -1352,8 +1366,6 @@ int phafd_fno_create(phafd_fno** out, int device, int nx, int ny, int nz, int tr
     smem_attr(k_proj_train, SM_TRAIN);
     smem_attr(k_layer_bwd<true, true, false>, SM_TRAIN);
     smem_attr(k_layer_bwd<false, false, true>, SM_TRAIN);
-    smem_attr(k_ydft, f->smem_ey());
-    smem_attr(k_yidft, f->smem_ey());
     smem_attr(k_zmix, f->smem_z(2));
     smem_attr(k_zmix_adj, f->smem_z(3));
     f->refresh();

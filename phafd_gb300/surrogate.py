@@ -213,12 +213,19 @@ class Runner:
         self.done = 0
         self.judged = []
         self.macro = False
+        self.times = {"judge": 0.0, "density": 0.0, "network": 0.0, "step": 0.0, "add": 0.0, "plain": 0.0}
+
+    def _t(self, key, fn, *a):
+        t0 = time.perf_counter()
+        fn(*a)
+        self.times[key] += time.perf_counter() - t0
 
     def _macro(self, s):
-        s.deposit_density(self.rho.data_ptr())
-        self.net.infer(s.grid_device("phi"), self.rho.data_ptr(), self.cfg["chi"], self.corr.data_ptr())
-        s.run(1)
-        s.grid_add_device(self.corr.data_ptr(), 1.0)
+        self._t("density", s.deposit_density, self.rho.data_ptr())
+        self._t("network", self.net.infer, s.grid_device("phi"), self.rho.data_ptr(), self.cfg["chi"],
+                self.corr.data_ptr())
+        self._t("step", s.run, 1)
+        self._t("add", s.grid_add_device, self.corr.data_ptr(), 1.0)
 
     def judge(self):
         self.jp.copy_state_from(self.main)
@@ -239,7 +246,7 @@ class Runner:
         end = self.done + nsteps
         while self.done < end:
             if self.use_surrogate and self.done % self.judge_every == 0:
-                self.judge()
+                self._t("judge", self.judge)
             if self.use_surrogate and end - self.done >= self.K:
                 if not self.macro:
                     self.main.set_linear_substeps(self.K, self.f2)
@@ -251,7 +258,7 @@ class Runner:
                     self.main.set_linear_substeps(1)
                     self.macro = False
                 k = min(self.K, end - self.done)
-                self.main.run(k)
+                self._t("plain", self.main.run, k)
                 self.done += k
 
     def close(self):
