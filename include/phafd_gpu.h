@@ -168,10 +168,10 @@ int phafd_compute_complex(phafd_ctx* ctx, int field, int quant, double* out);
 int phafd_structure_factor(phafd_ctx* ctx, int nbins, double* sk, long long* counts);
 
 /* ---- learned macro step support (no reference counterpart) ----
- * nsub > 1 makes each step a macro step: the Model-B update of nsub
- * linearised substeps (dmu/dphi = f2 about the mean, the rest of mu frozen at
- * the step's start), beads moved with nsub * dt; nsub = 1 restores the plain
- * step.  phafd_grid_device returns the device address of a real field (FP32
+ * nsub > 1 makes each step a macro step (resident schedule): the Model-B
+ * update of nsub linearised substeps (dmu/dphi = f2 about the mean, the rest
+ * of mu frozen at the step's start) and nsub bead substeps of dt against the
+ * field of the step's start; nsub = 1 restores the plain step.  phafd_grid_device returns the device address of a real field (FP32
  * or FP64 as the context); phafd_deposit_density writes to the device array
  * rho (nx*ny*nz, context precision) the sum over beads of the gridatom shape
  * function (pair_gridatom_*.cpp without epsilon and the phi factor);

@@ -549,7 +549,7 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
         mu_add = expfac;
         expfac = expfac * (T)p.dv;
       }
-      atomicAdd(p.dep + node, mu_add);
+      if (p.dep) atomicAdd(p.dep + node, mu_add);  // null: forces only (substeps of a macro step)
       add(0, -p.gx[node] * expfac);
       add(1, -p.gy[node] * expfac);
       add(2, -p.gz[node] * expfac);
@@ -680,15 +680,18 @@ __global__ void k_chain_force(BeadArgs a) {
   }
 }
 
+// (nsub > 1: substep `sub` of a macro step; its noise is keyed by
+// step * nsub + sub so that every substep draws fresh numbers)
 template <typename T>
-__global__ void k_chain_move(BeadArgs a, int half, double dt) {
+__global__ void k_chain_move(BeadArgs a, int half, double dt, int nsub, int sub) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const int fi = a.sf_fix[i];
   if (fi < 0) return;
   const SemiDev& P = a.sf[fi];
   T xi[3] = {0, 0, 0};
-  if (P.noise == PHAFD_NOISE_PHILOX && P.temp > 0) bead_gauss(P.seed, (uint64_t)(*a.d_step), half, i, xi);
+  const uint64_t key = nsub > 1 ? (uint64_t)(*a.d_step) * (uint64_t)nsub + (uint64_t)sub : (uint64_t)(*a.d_step);
+  if (P.noise == PHAFD_NOISE_PHILOX && P.temp > 0) bead_gauss(P.seed, key, half, i, xi);
   T fc[3], fp[3], t[3];
   for (int d = 0; d < 3; ++d) {
     fc[d] = (T)a.fchain[3 * (size_t)i + d];
@@ -771,12 +774,12 @@ void launch_drag(const BeadArgs& a, double dt, cudaStream_t st) {
 }
 
 template <typename T>
-void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st) {
+void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st, int nsub, int sub) {
   if (a.n == 0 || !a.any_semi) return;
   k_chain_force<T><<<nblk(a.n, 128), 128, 0, st>>>(a);
-  k_chain_move<T><<<nblk(a.n, 128), 128, 0, st>>>(a, half, dt);
+  k_chain_move<T><<<nblk(a.n, 128), 128, 0, st>>>(a, half, dt, nsub, sub);
 }
-template void launch_chain_half<float>(const BeadArgs&, int, double, cudaStream_t);
-template void launch_chain_half<double>(const BeadArgs&, int, double, cudaStream_t);
+template void launch_chain_half<float>(const BeadArgs&, int, double, cudaStream_t, int, int);
+template void launch_chain_half<double>(const BeadArgs&, int, double, cudaStream_t, int, int);
 
 }  // namespace phafd

@@ -71,6 +71,7 @@ template <typename T> void launch_pair(const BeadArgs& a, const PairArgs<T>& p, 
 template <typename T> void launch_dep_zero(const BeadArgs& a, T* dep, cudaStream_t st);
 template <typename T> void launch_density(const BeadArgs& a, const PairArgs<T>& p, T* rho, cudaStream_t st);
 void launch_drag(const BeadArgs& a, double dt, cudaStream_t st);
-template <typename T> void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st);
+template <typename T>
+void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st, int nsub = 1, int sub = 0);
 
 }  // namespace phafd

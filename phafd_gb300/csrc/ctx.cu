@@ -582,13 +582,11 @@ struct phafd_ctx {
       CK(cudaStreamWaitEvent(st2, ev_fork, 0));
     }
     // initial_integrate
-    // (a macro step of nsub substeps moves the beads with nsub * dt)
-    const double bdt = dt * nsub;
-    launch_drag(ba, bdt, bs);
-    launch_chain_half<T>(ba, 0, bdt, bs);
+    launch_drag(ba, dt, bs);
+    launch_chain_half<T>(ba, 0, dt, bs, nsub, 0);
     // final_integrate of the beads (independent of the field update)
-    launch_drag(ba, bdt, bs);
-    launch_chain_half<T>(ba, 1, bdt, bs);
+    launch_drag(ba, dt, bs);
+    launch_chain_half<T>(ba, 1, dt, bs, nsub, 0);
     mark(3);
     if (have_conj) {
       FHArgs fh{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
@@ -602,11 +600,13 @@ struct phafd_ctx {
           chk(GridOps<T>::xr2c(geom, phi.as<T>(), dep.as<T>(), W1, twf[0], fh, st), "x r2c");
           mark(4);
           dep_reset<T>(fork);
+          macro_bead_substeps<T>(bs);
           chk(GridOps<T>::ypass(geom, -1, W1, W1, nullptr, twf[1], st), "y fft");
         } else {
           chk(prc, "xy fwd");
           mark(4);
           dep_reset<T>(fork);
+          macro_bead_substeps<T>(bs);
         }
         mark(5);
         mark(6);
@@ -629,6 +629,10 @@ struct phafd_ctx {
           CK(cudaStreamWaitEvent(st, ev_pl_join, 0));
         }
         mark(7);
+        if (fork && nsub > 1) {  // the bead substeps read phi and grad phi, which the inverse overwrites
+          CK(cudaEventRecord(ev_join, st2));
+          CK(cudaStreamWaitEvent(st, ev_join, 0));
+        }
         if (!use_plane || !yx_fused<T>()) yx_inverse<T>(phi.as<T>(), (T)1, (T)1, true, true);
       } else {
         // post_force + pre_final_integrate: mu = dep + FH(phi), r2c
@@ -647,20 +651,21 @@ struct phafd_ctx {
   // Neighbor::decide + build.  Inside a graph capture the rebuild kernels
   // form the body of a conditional node that the check kernel switches on,
   // so a step without a rebuild runs one kernel here instead of eleven.
-  void neighbor_stage() {
+  void neighbor_stage(cudaStream_t sn = nullptr) {
+    if (!sn) sn = st;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaGraph_t g = nullptr;
-    CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    CK(cudaStreamGetCaptureInfo(sn, &cs, nullptr, &g, nullptr, nullptr, nullptr));
     if (cs != cudaStreamCaptureStatusActive) {
-      launch_neighbor(ba, false, st);
+      launch_neighbor(ba, false, sn);
       return;
     }
     cudaGraphConditionalHandle h;
     CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
-    launch_neighbor_check(ba, h, 1, st);
+    launch_neighbor_check(ba, h, 1, sn);
     const cudaGraphNode_t* deps = nullptr;
     size_t ndeps = 0;
-    CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+    CK(cudaStreamGetCaptureInfo(sn, &cs, nullptr, &g, &deps, nullptr, &ndeps));
     cudaGraphNodeParams p{};
     p.type = cudaGraphNodeTypeConditional;
     p.conditional.handle = h;
@@ -668,13 +673,33 @@ struct phafd_ctx {
     p.conditional.size = 1;
     cudaGraphNode_t node;
     CK(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p));
-    CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    CK(cudaStreamUpdateCaptureDependencies(sn, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
     cudaGraph_t body = p.conditional.phGraph_out[0];
     CK(cudaStreamBeginCaptureToGraph(stc, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     launch_rebuild(ba, stc);
     cudaGraph_t unused = nullptr;
     CK(cudaStreamEndCapture(stc, &unused));
     rebuild_kernels = count_kernels(body);
+  }
+
+  // Substeps 1..nsub-1 of a macro step for the beads: neighbor check, pair
+  // forces against the field of the step's start (no deposit: the field's
+  // linearised update uses the deposit of substep 0), integration with dt.
+  // They follow the deposit reset on the bead stream, so the reset sees the
+  // lists the deposit used.
+  template <typename T>
+  void macro_bead_substeps(cudaStream_t bs) {
+    if (nsub <= 1 || n == 0) return;
+    PairArgs<T> pa = pair_args<T>();
+    pa.dep = nullptr;
+    for (int sub = 1; sub < nsub; ++sub) {
+      neighbor_stage(bs);
+      if (have_lj || ga_style != PHAFD_GRIDATOM_NONE) launch_pair<T>(ba, pa, bs);
+      launch_drag(ba, dt, bs);
+      launch_chain_half<T>(ba, 0, dt, bs, nsub, sub);
+      launch_drag(ba, dt, bs);
+      launch_chain_half<T>(ba, 1, dt, bs, nsub, sub);
+    }
   }
 
   // zero the deposit nodes once the x pass has consumed them: on the bead
@@ -1457,6 +1482,8 @@ int phafd_set_linear_substeps(phafd_ctx* c, int nsub, double f2) {
   if (nsub < 1) throw std::invalid_argument("substeps must be >= 1");
   if (nsub > 1 && c->c_noise == PHAFD_NOISE_REFERENCE)
     throw std::invalid_argument("macro steps draw Philox noise (the reference stream has one draw per substep)");
+  if (nsub > 1 && c->schedule != PHAFD_SCHEDULE_RESIDENT)
+    throw std::invalid_argument("macro steps need the resident schedule");
   c->nsub = nsub;
   c->f2_lin = f2;
   c->invalidate_graph();

@@ -78,14 +78,21 @@ PHAFD_D uint64_t mndesc(uint32_t saddr, uint32_t mno, uint32_t ko, int swap) {
   return swap ? tc::sdesc(saddr, mno, ko) : tc::sdesc(saddr, ko, mno);
 }
 
-// GELU, tanh form, and its derivative
+// GELU, tanh form, and its derivative.  tanh is the hardware approximation
+// (tanh.approx.f32, relative error about 2^-11, below the BF16 resolution of
+// the activations it feeds).
+PHAFD_D float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 PHAFD_D float gelu(float x) {
   const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
-  return 0.5f * x * (1.f + tanhf(u));
+  return 0.5f * x * (1.f + tanh_hw(u));
 }
 PHAFD_D float gelu_d(float x) {
   const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
-  const float t = tanhf(u);
+  const float t = tanh_hw(u);
   return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * 0.7978845608028654f * (1.f + 0.134145f * x * x);
 }
 
@@ -367,12 +374,13 @@ __global__ void __launch_bounds__(NTH) k_lift(LiftIn in, const bf16* __restrict_
     tc::commit(t.bar);
   }
   if (mma_wait(t, 0, st)) {
+#pragma unroll
     for (int i = 0; i < TPC; ++i) {
       float v[32];
       tmem_row32(tmem, 32 * i, v);
 #pragma unroll
       for (int c = 0; c < 32; ++c) v[c] += pb[c];
-      store_row(v0 + (size_t)(t.node0[i] + x) * C, sm + SM_T0, i, x, v);
+      store_row(v0 ? v0 + (size_t)(t.node0[i] + x) * C : nullptr, sm + SM_T0, i, x, v);
     }
     operands_ready();
     if (threadIdx.x == 0) {
@@ -408,6 +416,7 @@ __global__ void __launch_bounds__(NTH) k_layer(const bf16* __restrict__ vin, con
   }
   const int x = threadIdx.x;
   if (mma_wait(t, 0, st)) {
+#pragma unroll
     for (int i = 0; i < TPC; ++i) {
       float v[32];
       tmem_row32(tmem, 32 * i, v);
@@ -433,39 +442,237 @@ __global__ void __launch_bounds__(NTH) k_layer(const bf16* __restrict__ vin, con
   tile_end(t, 128);
 }
 
-// projection, inference: out = q2 . GELU(Q1 v4 + q1b) + q2b; sum(out) in FP64
-__global__ void __launch_bounds__(NTH) k_proj(const bf16* __restrict__ v4, const bf16* __restrict__ Q1b,
-                                               const float* __restrict__ q1b, const float* __restrict__ q2, float q2b,
-                                               float* __restrict__ out, double* __restrict__ sum, Dims d, Status st) {
+// ---- persistent, double-buffered tile kernels (inference)
+// A CTA walks tile groups g = blockIdx.x, blockIdx.x + gridDim.x, ... (grid a
+// multiple of the x-halves, so every group of a CTA has the same half and the
+// half's tables load once).  While group g runs its MMA / epilogue chain, the
+// loads of group g + gridDim.x fly into the other buffer.
+constexpr uint32_t SP_T0 = 0;                    // 2 x 32 KB activation tiles
+constexpr uint32_t SP_BS = 65536;                // 2 x 4 KB spectral B rows
+constexpr uint32_t SP_RAW = SP_BS + 8192;        // 2 x 4 KB phi / rho rows (lift)
+constexpr uint32_t SP_ASP = SP_RAW + 8192;       // G (or F^T) half, 4 KB
+constexpr uint32_t SP_BM = SP_ASP + 4096;        // W, 2 KB
+constexpr uint32_t SP_BM2 = SP_BM + 2048;        // P or Q1, 2 KB
+constexpr uint32_t SP_B2 = SP_BM2 + 2048;        // F half, 4 KB
+constexpr uint32_t SP_BAR = SP_B2 + 4096;
+constexpr uint32_t SP_TOTAL = SP_BAR + 64;       // ~92 KB: 2 CTAs (2 x 256 TMEM columns) per SM
+
+enum { TM_LIFT = 0, TM_FIRST = 1, TM_MID = 2, TM_LAST = 3 };
+
+struct TileArgs {
+  LiftIn in;
+  const bf16* vin;  // input activations (middle and last layers)
+  const bf16 *Pb, *Wb, *Gtab, *yx, *Ftab, *Q1b;
+  const float *pb, *b, *q1b, *q2;
+  bf16* vout;
+  float* vx;
+  float* out;
+  double* sum;
+  long long ngroups;
+};
+
+PHAFD_D void set_group(Tile& t, long long g, const Dims& d) {
+  t.rg = (int)(g / d.H);
+  t.h = (int)(g % d.H);
+#pragma unroll
+  for (int i = 0; i < TPC; ++i) {
+    t.row[i] = (long long)t.rg * TPC + i;
+    t.node0[i] = t.row[i] * d.Nx + (long long)t.h * TX;
+  }
+}
+// phi and rho rows of the 4 tiles (FP32) -> raw [i][0: phi, 1: rho][128]
+PHAFD_D void load_raw(unsigned char* dst, const LiftIn& in, const Tile& t) {
+  for (int q = threadIdx.x; q < TPC * 2 * (TX / 4); q += NTH) {
+    const int i = q / (2 * (TX / 4)), f = (q / (TX / 4)) & 1, c = q % (TX / 4);
+    const float* src = (f ? in.rho : in.phi) + t.node0[i] + 4 * c;
+    cp_async16(dst + ((i * 2 + f) * TX + 4 * c) * 4, src);
+  }
+}
+PHAFD_D void issue_main_at(const Tile& t, uint32_t d0, uint32_t a_off, uint32_t b_off, int ksteps, bool spec,
+                           uint32_t asp_off, uint32_t bs_off) {
+  const uint32_t id = tc::idesc_bf16(128, 32, 0, 0);
+  const uint32_t bsbo = (uint32_t)ksteps * 256;
+  for (int i = 0; i < TPC; ++i) {
+    const uint32_t dd = d0 + 32 * i;
+    for (int s = 0; s < ksteps; ++s)
+      tc::mma(dd, kdesc(t.sbase + a_off + 512 * i + 256 * s, 2048), kdesc(t.sbase + b_off + 256 * s, bsbo), id, s > 0);
+    if (spec) tc::mma(dd, kdesc(t.sbase + asp_off, 256), kdesc(t.sbase + bs_off + 1024 * i, 256), id, 1);
+  }
+}
+PHAFD_D void issue_xdft_at(const Tile& t, uint32_t d0, uint32_t a_off, uint32_t b2_off, int swap) {
+  const uint32_t id = tc::idesc_bf16(128, 16, 1, 0);
+  for (int s = 0; s < TX / 16; ++s)
+    tc::mma(d0, mndesc(t.sbase + a_off + 4096 * s, 128, 2048, swap), kdesc(t.sbase + b2_off + 256 * s, 2048), id,
+            s > 0);
+}
+// all threads: operands written by this CTA visible to the tensor core
+PHAFD_D void smem_ready() {
+  tc::fence_async_smem();
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(NTH) k_tiles(TileArgs a, Dims d, int swap, Status st) {
   extern __shared__ __align__(1024) unsigned char sm[];
   Tile t;
-  tile_begin(t, sm, d, 128);
-  const uint32_t tmem = *t.taddr_slot;
-  load_act(sm + SM_T0, v4, t);
-  load_kmajor(sm + SM_BM, Q1b, 32, 32);
-  cp_async_commit();
-  operands_ready();
+  t.sm = sm;
+  t.sbase = tc::smem_u32(sm);
+  t.bar = reinterpret_cast<uint64_t*>(sm + SP_BAR);
+  t.taddr_slot = reinterpret_cast<uint32_t*>(sm + SP_BAR + 16);
   if (threadIdx.x == 0) {
-    issue_main(t, tmem, SM_T0, SM_BM, 2, false);
-    tc::commit(t.bar);
+    tc::mbar_init(t.bar, 1);
+    tc::fence_mbar_init();
   }
+  if (threadIdx.x < 32) {
+    tc::tmem_alloc(t.taddr_slot, 256);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *t.taddr_slot;
+  const uint32_t XD = 128;  // TMEM column of the x-stage DFT accumulator
   const int x = threadIdx.x;
-  double acc = 0.0;
-  if (mma_wait(t, 0, st)) {
-    for (int i = 0; i < TPC; ++i) {
-      float v[32];
-      tmem_row32(tmem, 32 * i, v);
-      float o = q2b;
-#pragma unroll
-      for (int k = 0; k < 32; ++k) o += q2[k] * gelu(v[k] + q1b[k]);
-      out[t.node0[i] + x] = o;
-      acc += (double)o;
-    }
+  long long g = blockIdx.x;
+  set_group(t, g, d);  // the half h is fixed per CTA
+  // tables and weights, once
+  if (MODE == TM_LIFT || MODE == TM_FIRST) load_kmajor(sm + SP_BM2, a.Pb, 32, 16);
+  if (MODE != TM_LIFT) {
+    load_kmajor(sm + SP_BM, a.Wb, 32, 32);
+    load_aspec(sm + SP_ASP, a.Gtab, t.h);
   }
+  if (MODE == TM_LAST) load_kmajor(sm + SP_BM2, a.Q1b, 32, 32);
+  if (MODE != TM_LAST) load_b2(sm + SP_B2, a.Ftab, d, t.h);
+  // first group
+  if (g < a.ngroups) {
+    if (MODE == TM_LIFT || MODE == TM_FIRST) load_raw(sm + SP_RAW, a.in, t);
+    if (MODE == TM_MID || MODE == TM_LAST) load_act(sm + SP_T0, a.vin, t);
+    if (MODE != TM_LIFT) load_bspec(sm + SP_BS, a.yx, t);
+  }
+  cp_async_commit();
+  uint32_t ph = 0;
+  bool ok = true;
+  double acc = 0.0;
+  for (int it = 0; g < a.ngroups; ++it) {
+    const int b = it & 1;
+    const uint32_t T0 = SP_T0 + 32768u * b, BS = SP_BS + 4096u * b;
+    const long long gn = g + gridDim.x;
+    if (gn < a.ngroups) {  // prefetch the next group into the other buffers
+      Tile tn = t;
+      set_group(tn, gn, d);
+      if (MODE == TM_LIFT || MODE == TM_FIRST) load_raw(sm + SP_RAW + 4096 * (1 - b), a.in, tn);
+      if (MODE == TM_MID || MODE == TM_LAST) load_act(sm + SP_T0 + 32768 * (1 - b), a.vin, tn);
+      if (MODE != TM_LIFT) load_bspec(sm + SP_BS + 4096 * (1 - b), a.yx, tn);
+    }
+    cp_async_commit();
+    cp_async_wait<1>();
+    set_group(t, g, d);
+    if (MODE == TM_LIFT || MODE == TM_FIRST) {
+      __syncthreads();  // raw rows of this group landed for every thread
+      const float* raw = reinterpret_cast<const float*>(sm + SP_RAW + 4096 * b);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
-  tile_end(t, 128);
+      for (int i = 0; i < TPC; ++i) {
+        float v[16];
+        v[0] = (raw[(i * 2) * TX + x] - a.in.n0) / a.in.n1;
+        v[1] = (raw[(i * 2 + 1) * TX + x] - a.in.n2) / a.in.n3;
+        v[2] = a.in.chi_n;
+#pragma unroll
+        for (int k = 3; k < 16; ++k) v[k] = 0.f;
+        store_inputs(sm + T0, i, x, v);
+      }
+    }
+    smem_ready();
+    if (MODE == TM_LIFT || MODE == TM_FIRST) {
+      // v0 = P in + pb
+      if (threadIdx.x == 0) {
+        issue_main_at(t, tmem, T0, SP_BM2, 1, false, 0, 0);
+        tc::commit(t.bar);
+      }
+      ok = ok && mma_wait(t, ph, st);
+      ph ^= 1;
+      if (ok) {
+#pragma unroll
+        for (int i = 0; i < TPC; ++i) {
+          float v[32];
+          tmem_row32(tmem, 32 * i, v);
+#pragma unroll
+          for (int c = 0; c < 32; ++c) v[c] += a.pb[c];
+          store_row(nullptr, sm + T0, i, x, v);
+        }
+      }
+      smem_ready();
+    }
+    if (MODE != TM_LIFT) {
+      // pre = W v + b + G Yx
+      if (ok && threadIdx.x == 0) {
+        issue_main_at(t, tmem, T0, SP_BM, 2, true, SP_ASP, BS);
+        tc::commit(t.bar);
+      }
+      ok = ok && mma_wait(t, ph, st);
+      ph ^= 1;
+      if (ok) {
+#pragma unroll
+        for (int i = 0; i < TPC; ++i) {
+          float v[32];
+          tmem_row32(tmem, 32 * i, v);
+          const size_t o = (size_t)(t.node0[i] + x) * C;
+          if (MODE == TM_LAST) {
+#pragma unroll
+            for (int c = 0; c < 32; ++c) v[c] += a.b[c];
+            store_row(nullptr, sm + T0, i, x, v);
+          } else {
+#pragma unroll
+            for (int c = 0; c < 32; ++c) v[c] = gelu(v[c] + a.b[c]);
+            store_row(a.vout + o, sm + T0, i, x, v);
+          }
+        }
+      }
+      smem_ready();
+    }
+    if (MODE == TM_LAST) {
+      // out = q2 . GELU(Q1 v4 + q1b)
+      if (ok && threadIdx.x == 0) {
+        issue_main_at(t, tmem, T0, SP_BM2, 2, false, 0, 0);
+        tc::commit(t.bar);
+      }
+      ok = ok && mma_wait(t, ph, st);
+      ph ^= 1;
+      if (ok) {
+#pragma unroll
+        for (int i = 0; i < TPC; ++i) {
+          float v[32];
+          tmem_row32(tmem, 32 * i, v);
+          float o = 0.f;
+#pragma unroll
+          for (int k = 0; k < 32; ++k) o += a.q2[k] * gelu(v[k] + a.q1b[k]);
+          a.out[t.node0[i] + x] = o;
+          acc += (double)o;
+        }
+      }
+    } else {
+      // x-stage DFT of the tile's output
+      if (ok && threadIdx.x == 0) {
+        issue_xdft_at(t, tmem + XD, T0, SP_B2, swap);
+        tc::commit(t.bar);
+      }
+      ok = ok && mma_wait(t, ph, st);
+      ph ^= 1;
+      if (ok) store_xdft(a.vx, tmem + XD, t, d);
+    }
+    tc::fence_before();
+    __syncthreads();  // this group's buffers are free for the load two groups on
+    tc::fence_after();
+    g = gn;
+  }
+  cp_async_wait<0>();
+  if (MODE == TM_LAST) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(a.sum, acc);
+  }
+  tile_end(t, 256);
 }
 
 // correction = scale * (out - mean(out))
@@ -512,6 +719,7 @@ __global__ void __launch_bounds__(NTH) k_proj_train(const bf16* __restrict__ v4,
   float dq2b = 0.f;
   bool ok = mma_wait(t, 0, st);
   if (ok) {
+#pragma unroll
     for (int i = 0; i < TPC; ++i) {
       float v[32];
       tmem_row32(tmem, 32 * i, v);
@@ -541,6 +749,7 @@ __global__ void __launch_bounds__(NTH) k_proj_train(const bf16* __restrict__ v4,
   }
   ok = ok && mma_wait(t, 1, st);
   if (ok) {
+#pragma unroll
     for (int i = 0; i < TPC; ++i) {
       float v[32];
       tmem_row32(tmem, 32 * i, v);
@@ -550,6 +759,7 @@ __global__ void __launch_bounds__(NTH) k_proj_train(const bf16* __restrict__ v4,
   // v4 tile no longer needed: delta4 into T0 after the MMAs that read it
   __syncthreads();
   if (ok) {
+#pragma unroll
     for (int i = 0; i < TPC; ++i) {
       float v[32];
       tmem_row32(tmem, 32 * i, v);
@@ -639,6 +849,7 @@ __global__ void __launch_bounds__(NTH) k_layer_bwd(const bf16* __restrict__ delt
 #pragma unroll
   for (int c = 0; c < 32; ++c) dpb[c] = 0.f;
   if (ok) {
+#pragma unroll
     for (int i = 0; i < TPC; ++i) {
       float v[32];
       tmem_row32(tmem, 32 * i, v);
@@ -1112,6 +1323,7 @@ struct phafd_fno {
   Dbuf act[5], pre[3], delta[2];
   Dbuf vx, vxy, yxy, yx, vhat[4], out, sum, loss, errf;
   long long adam_t = 0;
+  int nsm = 1;  // SMs of the device (persistent grids)
 
   size_t smem_ey() const { return (size_t)NK * d.Ny * sizeof(float2); }
   size_t smem_z(int extra) const { return ((size_t)d.Nz * C + (size_t)NK * d.Nz + (size_t)extra * NK * C) * sizeof(float2); }
@@ -1220,6 +1432,69 @@ struct phafd_fno {
     FCK(cudaGetLastError());
   }
 
+  // inference: lift x-stage only, then layer 0 rebuilding v0, layers 1-2,
+  // and the last layer with the projection; out and sum(out) filled
+  // persistent grid: a multiple of the x-halves, at most two CTAs per SM
+  unsigned pgrid() const {
+    const long long n = (long long)ntiles();
+    long long g = 2LL * nsm;
+    g -= g % d.H;
+    if (g < d.H) g = d.H;
+    return (unsigned)(g < n ? g : n);
+  }
+
+  TileArgs targs(const LiftIn& in, int l) const {
+    TileArgs a{};
+    a.in = in;
+    a.Pb = Pb.as<bf16>();
+    a.pb = P(OFF_PB);
+    a.Gtab = G.as<bf16>();
+    a.yx = yx.as<bf16>();
+    a.Ftab = F.as<bf16>();
+    a.Q1b = Q1b.as<bf16>();
+    a.q1b = P(OFF_Q1B);
+    a.q2 = P(OFF_Q2);
+    a.vx = vx.as<float>();
+    a.out = out.as<float>();
+    a.sum = sum.as<double>();
+    a.ngroups = (long long)ntiles();
+    if (l >= 0) {
+      a.Wb = W(l);
+      a.b = P(layer_off(l) + 1024);
+    }
+    return a;
+  }
+
+  void infer_forward(const float* phi, const float* rho, float chi) {
+    const Status s = status();
+    bf16* va = act[0].as<bf16>();
+    bf16* vb = act[1].as<bf16>();
+    const LiftIn in = lift_in(phi, rho, chi);
+    const unsigned pg = pgrid();
+    TileArgs a = targs(in, -1);
+    k_tiles<TM_LIFT><<<pg, NTH, SP_TOTAL, st>>>(a, d, swap, s);
+    spectral(0, false);
+    a = targs(in, 0);
+    a.vout = va;
+    k_tiles<TM_FIRST><<<pg, NTH, SP_TOTAL, st>>>(a, d, swap, s);
+    spectral(1, false);
+    a = targs(in, 1);
+    a.vin = va;
+    a.vout = vb;
+    k_tiles<TM_MID><<<pg, NTH, SP_TOTAL, st>>>(a, d, swap, s);
+    spectral(2, false);
+    a = targs(in, 2);
+    a.vin = vb;
+    a.vout = va;
+    k_tiles<TM_MID><<<pg, NTH, SP_TOTAL, st>>>(a, d, swap, s);
+    spectral(3, false);
+    FCK(cudaMemsetAsync(sum.p, 0, 8, st));
+    a = targs(in, 3);
+    a.vin = va;
+    k_tiles<TM_LAST><<<pg, NTH, SP_TOTAL, st>>>(a, d, swap, s);
+    FCK(cudaGetLastError());
+  }
+
   Grads grads(int l) const {
     float* g = grad.as<float>();
     Grads r;
@@ -1277,9 +1552,12 @@ struct phafd_fno {
 };
 
 namespace {
+// dynamic shared memory of a kernel, and the largest shared-memory carveout
+// so that as many tile CTAs as TMEM allows (512 columns per SM) are resident
 template <typename K>
 void smem_attr(K k, size_t bytes) {
   FCK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  FCK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
 }
 }  // namespace
 
@@ -1325,6 +1603,7 @@ int phafd_fno_create(phafd_fno** out, int device, int nx, int ny, int nz, int tr
       return PHAFD_ERR_UNSUPPORTED;
     }
     f->swap = sw;
+    FCK(cudaDeviceGetAttribute(&f->nsm, cudaDevAttrMultiProcessorCount, device));
     FCK(cudaStreamCreateWithFlags(&f->st, cudaStreamNonBlocking));
     f->params.alloc(NPARAM * 4);
     FCK(cudaMemset(f->params.p, 0, f->params.n));
@@ -1360,9 +1639,11 @@ int phafd_fno_create(phafd_fno** out, int device, int nx, int ny, int nz, int tr
     }
     smem_attr(k_lift, SM_INF);
     smem_attr(k_layer<true, true, true>, SM_INF);
-    smem_attr(k_layer<true, true, false>, SM_INF);
     smem_attr(k_layer<false, false, false>, SM_INF);
-    smem_attr(k_proj, SM_INF);
+    smem_attr(k_tiles<TM_LIFT>, SP_TOTAL);
+    smem_attr(k_tiles<TM_FIRST>, SP_TOTAL);
+    smem_attr(k_tiles<TM_MID>, SP_TOTAL);
+    smem_attr(k_tiles<TM_LAST>, SP_TOTAL);
     smem_attr(k_proj_train, SM_TRAIN);
     smem_attr(k_layer_bwd<true, true, false>, SM_TRAIN);
     smem_attr(k_layer_bwd<false, false, true>, SM_TRAIN);
@@ -1424,11 +1705,7 @@ int phafd_fno_infer(phafd_fno* f, const float* phi, const float* rho, float chi,
     FCK(cudaStreamWaitEvent(f->st, ev, 0));
     cudaEventDestroy(ev);
   }
-  f->forward(phi, rho, chi, false);
-  FCK(cudaMemsetAsync(f->sum.p, 0, 8, f->st));
-  k_proj<<<f->ntiles(), NTH, SM_INF, f->st>>>(f->act[0].as<bf16>(), f->Q1b.as<bf16>(), f->P(OFF_Q1B),
-                                                 f->P(OFF_Q2), 0.f, f->out.as<float>(), f->sum.as<double>(), f->d,
-                                                 f->status());
+  f->infer_forward(phi, rho, chi);
   // q2b cancels in out - mean(out)
   k_center<<<1024, 256, 0, f->st>>>(f->out.as<float>(), f->sum.as<double>(), f->norm[6], corr, f->d.nodes);
   FCK(cudaGetLastError());

@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(N * LB / 16)
 k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict__ out,
        const cpx<T>* __restrict__ tw, int Ny, int Nz, FHArgs fh) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  pdl_enter();
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NT = N * LB / 16, STR = LB + 1;
   cpx<T>* sd = s + (size_t)N * STR;  // deposit rows, same layout (PRO == 1)
@@ -142,6 +143,7 @@ __global__ void __launch_bounds__(N * LB * NOUT / 16)
 k_xc2r(const cpx<T>* __restrict__ in, T* __restrict__ out0, T* __restrict__ out1, T s0, T s1, T dq,
        const cpx<T>* __restrict__ tw, int Ny, int Nz, NanArgs nan) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  pdl_enter();
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = LB * NOUT;
   constexpr int NT = N * NL / 16, STR = NL + 1;
@@ -193,6 +195,7 @@ template <typename T, int N, int LB, int S, int NOUT>
 __global__ void __launch_bounds__(N * LB * NOUT / 16)
 k_ypass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __restrict__ tw, long long nlines) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  pdl_enter();
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = LB * NOUT;
   constexpr int NT = N * NL / 16, STR = NL + 1;
@@ -310,6 +313,7 @@ __global__ void __launch_bounds__(N * LB * NOUT / 16)
 k_zpass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __restrict__ tw, int Ny,
         UpdateArgs<T> u, int planes_only) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  pdl_enter();
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = LB * NOUT;
   constexpr int NT = N * NL / 16, STR = NL + 1;
@@ -359,6 +363,7 @@ k_zfused(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __
          cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny,
          UpdateArgs<T> u, int store_mu, int kx0) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  pdl_enter();
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = 2 * LB;
   constexpr int NT = N * NL / 16, STR = NL + 1;
@@ -422,6 +427,23 @@ k_zfused(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __
 }
 
 // -------------------------------------------------------------------- launchers
+// launch with programmatic stream serialization (the kernel starts with
+// pdl_enter), so consecutive passes overlap launch and drain
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // Opt a kernel into more than 48 KB of dynamic shared memory; done once per
 // kernel so that graph capture never sees the attribute call.
 template <typename Kern>
@@ -451,11 +473,11 @@ struct Axis {
     if (dep) {
       auto k = k_xr2c<T, N, LB, 1>;
       if (set_smem(k, sm)) return -1;
-      k<<<grid, N * LB / 16, sm, st>>>(in, dep, out, tw, g.ny, g.nz, fh);
+      launch_pdl(k, dim3(grid), dim3(N * LB / 16), sm, st, in, dep, out, tw, g.ny, g.nz, fh);
     } else {
       auto k = k_xr2c<T, N, LB, 0>;
       if (set_smem(k, sm)) return -1;
-      k<<<grid, N * LB / 16, sm, st>>>(in, dep, out, tw, g.ny, g.nz, fh);
+      launch_pdl(k, dim3(grid), dim3(N * LB / 16), sm, st, in, dep, out, tw, g.ny, g.nz, fh);
     }
     return 0;
   }
@@ -470,7 +492,7 @@ struct Axis {
       if (mul0) return -1;
       auto k = k_xc2r<T, N, LB, false, 2>;
       if (set_smem(k, sm)) return -1;
-      k<<<grid, N * LB * 2 / 16, sm, st>>>(in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
+      launch_pdl(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
     } else {
       constexpr int LB = NLT;
       const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
@@ -478,11 +500,11 @@ struct Axis {
       if (mul0) {
         auto k = k_xc2r<T, N, LB, true, 1>;
         if (set_smem(k, sm)) return -1;
-        k<<<grid, N * LB / 16, sm, st>>>(in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
+        launch_pdl(k, dim3(grid), dim3(N * LB / 16), sm, st, in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
       } else {
         auto k = k_xc2r<T, N, LB, false, 1>;
         if (set_smem(k, sm)) return -1;
-        k<<<grid, N * LB / 16, sm, st>>>(in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
+        launch_pdl(k, dim3(grid), dim3(N * LB / 16), sm, st, in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
       }
     }
     return 0;
@@ -497,13 +519,13 @@ struct Axis {
       const size_t sm = (size_t)N * (2 * LB + 1) * sizeof(cpx<T>);
       auto k = k_ypass<T, N, LB, S, 2>;
       if (set_smem(k, sm)) return -1;
-      k<<<(unsigned)((nlines + LB - 1) / LB), N * LB * 2 / 16, sm, st>>>(in, out0, out1, dq, tw, nlines);
+      launch_pdl(k, dim3((unsigned)((nlines + LB - 1) / LB)), dim3(N * LB * 2 / 16), sm, st, in, out0, out1, dq, tw, nlines);
     } else {
       constexpr int LB = NLT;
       const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
       auto k = k_ypass<T, N, LB, S, 1>;
       if (set_smem(k, sm)) return -1;
-      k<<<(unsigned)((nlines + LB - 1) / LB), N * LB / 16, sm, st>>>(in, out0, out1, dq, tw, nlines);
+      launch_pdl(k, dim3((unsigned)((nlines + LB - 1) / LB)), dim3(N * LB / 16), sm, st, in, out0, out1, dq, tw, nlines);
     }
     return 0;
   }
@@ -520,14 +542,14 @@ struct Axis {
       dim3 grid((g.ny + LB - 1) / LB, gy);
       auto k = k_zpass<T, N, LB, S, 2, UPD>;
       if (set_smem(k, sm)) return -1;
-      k<<<grid, N * LB * 2 / 16, sm, st>>>(in, out0, out1, dq, tw, g.ny, u, planes_only);
+      launch_pdl(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, in, out0, out1, dq, tw, g.ny, u, planes_only);
     } else {
       constexpr int LB = NLT;
       const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
       dim3 grid((g.ny + LB - 1) / LB, gy);
       auto k = k_zpass<T, N, LB, S, 1, UPD>;
       if (set_smem(k, sm)) return -1;
-      k<<<grid, N * LB / 16, sm, st>>>(in, out0, out1, dq, tw, g.ny, u, planes_only);
+      launch_pdl(k, dim3(grid), dim3(N * LB / 16), sm, st, in, out0, out1, dq, tw, g.ny, u, planes_only);
     }
     return 0;
   }
@@ -542,7 +564,7 @@ struct Axis {
     dim3 grid((g.ny + LB - 1) / LB, g.nxh - 2 * kx0);
     auto k = k_zfused<T, N, LB>;
     if (set_smem(k, sm)) return -1;
-    k<<<grid, N * LB * 2 / 16, sm, st>>>(muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
+    launch_pdl(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
     return 0;
   }
 };

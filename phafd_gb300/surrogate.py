@@ -7,7 +7,7 @@ A macro step advances phi over K substeps of dt:
 L_K is the context's own step in macro mode (phafd_set_linear_substeps): K
 Model-B substeps linearised about the mean concentration with the nonlinear
 part of mu (Flory-Huggins remainder and bead deposit) frozen at t, the noise
-of K substeps, and the beads moved once with K dt.  C is the spectral neural
+of K substeps, and K bead substeps of dt against the field of time t.  C is the spectral neural
 operator of include/phafd_fno.h (zero mean, so the macro step conserves
 mass exactly).  The network learns R = phi_plain(t + K dt) - L_K[phi(t)],
 the part of K plain substeps that the linearised step misses, on states of
