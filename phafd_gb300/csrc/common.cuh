@@ -132,17 +132,6 @@ PHAFD_D void cp_async_real(T* smem, const T* gmem) {
   else cp_async8(smem, gmem);
 }
 
-// Programmatic dependent launch.  A grid kernel launched with
-// cudaLaunchAttributeProgrammaticStreamSerialization may be scheduled while
-// its predecessor on the stream drains; it waits here for the predecessor's
-// completion (and memory) before touching any data, then lets its own
-// successor start launching.  Without a programmatic predecessor the wait
-// returns at once.
-PHAFD_D void pdl_enter() {
-  asm volatile("griddepcontrol.wait;\n" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
-}
-
 // signed wavenumber index, reference convention (fixgrid_conjugate.cpp:80-95):
 // index e of N maps to e if e <= N/2, else e - N
 PHAFD_HD int wrap_index(int e, int N) { return e > N / 2 ? e - N : e; }

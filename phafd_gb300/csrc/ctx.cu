@@ -336,6 +336,16 @@ struct phafd_ctx {
     cpx<T>* E = wE.as<cpx<T>>();
     NanArgs nan{nan_check ? 1 : 0, d_nan(), d_step()};
     NanArgs nonan{0, d_nan(), d_step()};
+    if (grad && phi_out && !profiling) {
+      // one launch per direction for the whole inverse chain
+      int rc = GridOps<T>::yinv2(geom, A, Cc, D, B, E, twi[1], st);
+      if (rc != -3) {
+        chk(rc, "y ifft");
+        chk(GridOps<T>::xc2r3(geom, Cc, phi_out, gx.as<T>(), D, gy.as<T>(), E, gz.as<T>(), sp, sg, twi[0], nan, nonan,
+                              st), "x c2r");
+        return;
+      }
+    }
     chk(GridOps<T>::ypass(geom, +1, A, Cc, grad ? D : nullptr, twi[1], st), "y ifft");
     if (grad) chk(GridOps<T>::ypass(geom, +1, B, E, nullptr, twi[1], st), "y ifft");
     mark(8);

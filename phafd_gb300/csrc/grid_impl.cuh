@@ -56,7 +56,6 @@ __global__ void __launch_bounds__(N * LB / 16)
 k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict__ out,
        const cpx<T>* __restrict__ tw, int Ny, int Nz, FHArgs fh) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NT = N * LB / 16, STR = LB + 1;
   cpx<T>* sd = s + (size_t)N * STR;  // deposit rows, same layout (PRO == 1)
@@ -138,17 +137,15 @@ k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict_
 // -------------------------------------------------------------------- x c2r
 // out0 = c2r(m0 * in) * s0 with m0 = i dqx kx if MUL0 else 1
 // out1 = c2r(i dqx kx * in) * s1          (NOUT == 2)
+// one tile (rows y0 .. y0 + 2 LB of plane z); bx is the tile's index along y
 template <typename T, int N, int LB, bool MUL0, int NOUT>
-__global__ void __launch_bounds__(N * LB * NOUT / 16)
-k_xc2r(const cpx<T>* __restrict__ in, T* __restrict__ out0, T* __restrict__ out1, T s0, T s1, T dq,
-       const cpx<T>* __restrict__ tw, int Ny, int Nz, NanArgs nan) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
+PHAFD_D void xc2r_tile(int bx, int z, const cpx<T>* __restrict__ in, T* __restrict__ out0, T* __restrict__ out1,
+                       T s0, T s1, T dq, const cpx<T>* __restrict__ tw, int Ny, int Nz, const NanArgs& nan,
+                       unsigned char* smraw) {
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = LB * NOUT;
   constexpr int NT = N * NL / 16, STR = NL + 1;
-  const int z = blockIdx.y;
-  const int y0 = blockIdx.x * 2 * LB;
+  const int y0 = bx * 2 * LB;
   TILE_LOOP(idx, LB * (N / 2 + 1), NT) {
     const int l = idx % LB, k = idx / LB;
     const int y = y0 + 2 * l;
@@ -189,17 +186,41 @@ k_xc2r(const cpx<T>* __restrict__ in, T* __restrict__ out0, T* __restrict__ out1
   }
 }
 
+template <typename T, int N, int LB, bool MUL0, int NOUT>
+__global__ void __launch_bounds__(N * LB * NOUT / 16)
+k_xc2r(const cpx<T>* __restrict__ in, T* __restrict__ out0, T* __restrict__ out1, T s0, T s1, T dq,
+       const cpx<T>* __restrict__ tw, int Ny, int Nz, NanArgs nan) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  xc2r_tile<T, N, LB, MUL0, NOUT>(blockIdx.x, blockIdx.y, in, out0, out1, s0, s1, dq, tw, Ny, Nz, nan, smraw);
+}
+
+// the three x c2r of the inverse chain in one launch: C -> (phi, dphi/dx)
+// with 2 LB2 rows per tile, D -> dphi/dy and E -> dphi/dz with 2 LB1 rows
+// per tile (LB1 = 2 LB2: same threads and shared memory per tile)
+template <typename T, int N, int LB2>
+__global__ void __launch_bounds__(N * LB2 * 2 / 16)
+k_xc2r3(const cpx<T>* __restrict__ C, T* __restrict__ phi, T* __restrict__ gx, const cpx<T>* __restrict__ D,
+        T* __restrict__ gy, const cpx<T>* __restrict__ E, T* __restrict__ gz, T sp, T sg, T dq,
+        const cpx<T>* __restrict__ tw, int Ny, int Nz, NanArgs nan, NanArgs nonan, int nb0, int nb1) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int bx = blockIdx.x, z = blockIdx.y;
+  if (bx < nb0)
+    xc2r_tile<T, N, LB2, false, 2>(bx, z, C, phi, gx, sp, sg, dq, tw, Ny, Nz, nan, smraw);
+  else if (bx < nb0 + nb1)
+    xc2r_tile<T, N, 2 * LB2, false, 1>(bx - nb0, z, D, gy, nullptr, sg, sg, dq, tw, Ny, Nz, nonan, smraw);
+  else
+    xc2r_tile<T, N, 2 * LB2, false, 1>(bx - nb0 - nb1, z, E, gz, nullptr, sg, sg, dq, tw, Ny, Nz, nonan, smraw);
+}
+
 // -------------------------------------------------------------------- y pass
 // lines contiguous: in[line * N + e]; out0 = FFT_S(in), out1 = FFT_S(i dq m(e) in)
 template <typename T, int N, int LB, int S, int NOUT>
-__global__ void __launch_bounds__(N * LB * NOUT / 16)
-k_ypass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __restrict__ tw, long long nlines) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
+PHAFD_D void ypass_tile(long long bx, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq,
+                        const cpx<T>* __restrict__ tw, long long nlines, unsigned char* smraw) {
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = LB * NOUT;
   constexpr int NT = N * NL / 16, STR = NL + 1;
-  const long long line0 = (long long)blockIdx.x * LB;
+  const long long line0 = bx * LB;
   TILE_LOOP(idx, LB * N, NT) {
     const int l = idx / N, e = idx % N;
     cpx<T> v = mk<T>(0, 0);
@@ -216,6 +237,25 @@ k_ypass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
       if constexpr (NOUT == 2) out1[(line0 + l) * N + e] = s[e * STR + LB + l];
     }
   }
+}
+
+template <typename T, int N, int LB, int S, int NOUT>
+__global__ void __launch_bounds__(N * LB * NOUT / 16)
+k_ypass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __restrict__ tw, long long nlines) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  ypass_tile<T, N, LB, S, NOUT>(blockIdx.x, in, out0, out1, dq, tw, nlines, smraw);
+}
+
+// the two inverse y passes of the inverse chain in one launch: A -> (C, D = i qy)
+// with LB2 lines per tile, B -> E with 2 LB2 lines per tile
+template <typename T, int N, int LB2>
+__global__ void __launch_bounds__(N * LB2 * 2 / 16)
+k_ypass_inv2(const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E, T dq,
+             const cpx<T>* __restrict__ tw, long long nlines, long long nb0) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const long long bx = blockIdx.x;
+  if (bx < nb0) ypass_tile<T, N, LB2, +1, 2>(bx, A, C, D, dq, tw, nlines, smraw);
+  else ypass_tile<T, N, 2 * LB2, +1, 1>(bx - nb0, B, E, nullptr, dq, tw, nlines, smraw);
 }
 
 // -------------------------------------------------------------------- update
@@ -313,7 +353,6 @@ __global__ void __launch_bounds__(N * LB * NOUT / 16)
 k_zpass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __restrict__ tw, int Ny,
         UpdateArgs<T> u, int planes_only) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = LB * NOUT;
   constexpr int NT = N * NL / 16, STR = NL + 1;
@@ -363,7 +402,6 @@ k_zfused(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __
          cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny,
          UpdateArgs<T> u, int store_mu, int kx0) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = 2 * LB;
   constexpr int NT = N * NL / 16, STR = NL + 1;
@@ -427,21 +465,11 @@ k_zfused(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __
 }
 
 // -------------------------------------------------------------------- launchers
-// launch with programmatic stream serialization (the kernel starts with
-// pdl_enter), so consecutive passes overlap launch and drain
+// kernel launch (programmatic dependent launch between the passes was
+// measured 9% slower per step on GB300 and is not used)
 template <typename... KArgs, typename... Args>
-static void launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k, args...);
+static void launch_grid(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+  k<<<grid, block, smem, st>>>(args...);
 }
 
 // Opt a kernel into more than 48 KB of dynamic shared memory; done once per
@@ -473,11 +501,11 @@ struct Axis {
     if (dep) {
       auto k = k_xr2c<T, N, LB, 1>;
       if (set_smem(k, sm)) return -1;
-      launch_pdl(k, dim3(grid), dim3(N * LB / 16), sm, st, in, dep, out, tw, g.ny, g.nz, fh);
+      launch_grid(k, dim3(grid), dim3(N * LB / 16), sm, st, in, dep, out, tw, g.ny, g.nz, fh);
     } else {
       auto k = k_xr2c<T, N, LB, 0>;
       if (set_smem(k, sm)) return -1;
-      launch_pdl(k, dim3(grid), dim3(N * LB / 16), sm, st, in, dep, out, tw, g.ny, g.nz, fh);
+      launch_grid(k, dim3(grid), dim3(N * LB / 16), sm, st, in, dep, out, tw, g.ny, g.nz, fh);
     }
     return 0;
   }
@@ -492,7 +520,7 @@ struct Axis {
       if (mul0) return -1;
       auto k = k_xc2r<T, N, LB, false, 2>;
       if (set_smem(k, sm)) return -1;
-      launch_pdl(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
+      launch_grid(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
     } else {
       constexpr int LB = NLT;
       const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
@@ -500,11 +528,11 @@ struct Axis {
       if (mul0) {
         auto k = k_xc2r<T, N, LB, true, 1>;
         if (set_smem(k, sm)) return -1;
-        launch_pdl(k, dim3(grid), dim3(N * LB / 16), sm, st, in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
+        launch_grid(k, dim3(grid), dim3(N * LB / 16), sm, st, in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
       } else {
         auto k = k_xc2r<T, N, LB, false, 1>;
         if (set_smem(k, sm)) return -1;
-        launch_pdl(k, dim3(grid), dim3(N * LB / 16), sm, st, in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
+        launch_grid(k, dim3(grid), dim3(N * LB / 16), sm, st, in, out0, out1, s0, s1, dq, tw, g.ny, g.nz, nan);
       }
     }
     return 0;
@@ -519,14 +547,41 @@ struct Axis {
       const size_t sm = (size_t)N * (2 * LB + 1) * sizeof(cpx<T>);
       auto k = k_ypass<T, N, LB, S, 2>;
       if (set_smem(k, sm)) return -1;
-      launch_pdl(k, dim3((unsigned)((nlines + LB - 1) / LB)), dim3(N * LB * 2 / 16), sm, st, in, out0, out1, dq, tw, nlines);
+      launch_grid(k, dim3((unsigned)((nlines + LB - 1) / LB)), dim3(N * LB * 2 / 16), sm, st, in, out0, out1, dq, tw, nlines);
     } else {
       constexpr int LB = NLT;
       const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
       auto k = k_ypass<T, N, LB, S, 1>;
       if (set_smem(k, sm)) return -1;
-      launch_pdl(k, dim3((unsigned)((nlines + LB - 1) / LB)), dim3(N * LB / 16), sm, st, in, out0, out1, dq, tw, nlines);
+      launch_grid(k, dim3((unsigned)((nlines + LB - 1) / LB)), dim3(N * LB / 16), sm, st, in, out0, out1, dq, tw, nlines);
     }
+    return 0;
+  }
+
+  static int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E, T* gz,
+                   T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, cudaStream_t st) {
+    constexpr int LB2 = NLT / 2 >= 1 ? NLT / 2 : 1;
+    if (2 * LB2 != NLT) return -3;
+    const size_t sm = (size_t)N * (2 * LB2 + 1) * sizeof(cpx<T>);
+    const int nb0 = (g.ny + 2 * LB2 - 1) / (2 * LB2), nb1 = (g.ny + 4 * LB2 - 1) / (4 * LB2);
+    auto k = k_xc2r3<T, N, LB2>;
+    if (set_smem(k, sm)) return -1;
+    launch_grid(k, dim3(nb0 + 2 * nb1, g.nz), dim3(N * LB2 * 2 / 16), sm, st, C, phi, gx, D, gy, E, gz, sp, sg,
+                (T)g.kq[0], tw, g.ny, g.nz, nan, nonan, nb0, nb1);
+    return 0;
+  }
+
+  static int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E,
+                   const cpx<T>* tw, cudaStream_t st) {
+    constexpr int LB2 = NLT / 2 >= 1 ? NLT / 2 : 1;
+    if (2 * LB2 != NLT) return -3;
+    const long long nlines = (long long)g.nxh * g.nz;
+    const size_t sm = (size_t)N * (2 * LB2 + 1) * sizeof(cpx<T>);
+    const long long nb0 = (nlines + LB2 - 1) / LB2, nb1 = (nlines + 2 * LB2 - 1) / (2 * LB2);
+    auto k = k_ypass_inv2<T, N, LB2>;
+    if (set_smem(k, sm)) return -1;
+    launch_grid(k, dim3((unsigned)(nb0 + nb1)), dim3(N * LB2 * 2 / 16), sm, st, A, C, D, B, E, (T)g.kq[1], tw,
+                nlines, nb0);
     return 0;
   }
 
@@ -542,14 +597,14 @@ struct Axis {
       dim3 grid((g.ny + LB - 1) / LB, gy);
       auto k = k_zpass<T, N, LB, S, 2, UPD>;
       if (set_smem(k, sm)) return -1;
-      launch_pdl(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, in, out0, out1, dq, tw, g.ny, u, planes_only);
+      launch_grid(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, in, out0, out1, dq, tw, g.ny, u, planes_only);
     } else {
       constexpr int LB = NLT;
       const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
       dim3 grid((g.ny + LB - 1) / LB, gy);
       auto k = k_zpass<T, N, LB, S, 1, UPD>;
       if (set_smem(k, sm)) return -1;
-      launch_pdl(k, dim3(grid), dim3(N * LB / 16), sm, st, in, out0, out1, dq, tw, g.ny, u, planes_only);
+      launch_grid(k, dim3(grid), dim3(N * LB / 16), sm, st, in, out0, out1, dq, tw, g.ny, u, planes_only);
     }
     return 0;
   }
@@ -564,7 +619,7 @@ struct Axis {
     dim3 grid((g.ny + LB - 1) / LB, g.nxh - 2 * kx0);
     auto k = k_zfused<T, N, LB>;
     if (set_smem(k, sm)) return -1;
-    launch_pdl(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
+    launch_grid(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
     return 0;
   }
 };
@@ -587,6 +642,29 @@ int GridOps<T>::xc2r(const Geom& g, const cpx<T>* in, T* out0, T s0, bool mul0, 
                      const NanArgs& nan, cudaStream_t st) {
   switch (g.nx) {
 #define CASE(n) case n: return Axis<T, n>::xc2r(g, in, out0, s0, mul0, out1, s1, tw, nan, st);
+    PHAFD_FOR_SIZES(CASE)
+#undef CASE
+  }
+  return -2;
+}
+
+template <typename T>
+int GridOps<T>::xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E,
+                      T* gz, T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan,
+                      cudaStream_t st) {
+  switch (g.nx) {
+#define CASE(n) case n: return Axis<T, n>::xc2r3(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, st);
+    PHAFD_FOR_SIZES(CASE)
+#undef CASE
+  }
+  return -2;
+}
+
+template <typename T>
+int GridOps<T>::yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E,
+                      const cpx<T>* tw, cudaStream_t st) {
+  switch (g.ny) {
+#define CASE(n) case n: return Axis<T, n>::yinv2(g, A, C, D, B, E, tw, st);
     PHAFD_FOR_SIZES(CASE)
 #undef CASE
   }

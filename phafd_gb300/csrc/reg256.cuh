@@ -47,7 +47,6 @@ k_zfused256(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>*
             cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny,
             UpdateArgs<T> u, int store_mu, int kx0) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
   cpx<T>* bufA = reinterpret_cast<cpx<T>*>(smraw);  // N x W
   cpx<T>* bufB = bufA + N * W;                        // N x W (phi_hat staging, then second ifft)
   const int c = threadIdx.x & 15;
@@ -129,7 +128,7 @@ int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T
   const int kx0 = bulk_only ? 1 : 0;
   if (g.nxh - 2 * kx0 <= 0) return 0;
   dim3 grid((g.ny + W - 1) / W, g.nxh - 2 * kx0);
-  launch_pdl(k, grid, dim3(256), sm, st, muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
+  launch_grid(k, grid, dim3(256), sm, st, muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
   return 0;
 }
 
