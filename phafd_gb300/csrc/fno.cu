@@ -47,6 +47,7 @@ constexpr int NMODE = NK * NK * NKX;
 constexpr int TX = 128;    // nodes of a tile along x
 constexpr int TPC = 4;     // tiles (rows) per CTA
 constexpr int NTH = 128;   // threads per tile CTA
+constexpr int NTP = 256;   // threads of the inference tile CTAs (two warps per TMEM lane quarter)
 
 // flat parameter vector
 constexpr size_t OFF_P = 0, OFF_PB = 512;
@@ -175,7 +176,7 @@ PHAFD_D void operands_ready() {
 // ---- loads into shared memory (cp.async, all threads)
 // activation tiles [node][32] -> unified layout at `dst`
 PHAFD_D void load_act(unsigned char* dst, const bf16* act, const Tile& t) {
-  for (int q = threadIdx.x; q < TPC * TX * 4; q += NTH) {
+  for (int q = threadIdx.x; q < TPC * TX * 4; q += blockDim.x) {
     const int i = q >> 9, x = (q >> 2) & (TX - 1), g = q & 3;
     cp_async16(dst + tile_off(i, x, 8 * g), act + (size_t)(t.node0[i] + x) * C + 8 * g);
   }
@@ -183,28 +184,28 @@ PHAFD_D void load_act(unsigned char* dst, const bf16* act, const Tile& t) {
 // K-major matrix of `rows` rows and K columns (row-major [rows][K] in HBM)
 PHAFD_D void load_kmajor(unsigned char* dst, const bf16* src, int rows, int K) {
   const int kc = K / 8;
-  for (int q = threadIdx.x; q < rows * kc; q += NTH) {
+  for (int q = threadIdx.x; q < rows * kc; q += blockDim.x) {
     const int r = q / kc, c = q % kc;
     cp_async16(dst + (r & 7) * 16 + c * 128 + (r >> 3) * (K * 16), src + (size_t)r * K + 8 * c);
   }
 }
 // x-half of a [16][Nx] table as K-major B (N = 16 rows, K = 128 x)
 PHAFD_D void load_b2(unsigned char* dst, const bf16* tab, const Dims& d, int h) {
-  for (int q = threadIdx.x; q < KR * (TX / 8); q += NTH) {
+  for (int q = threadIdx.x; q < KR * (TX / 8); q += blockDim.x) {
     const int r = q / (TX / 8), c = q % (TX / 8);
     cp_async16(dst + (r & 7) * 16 + c * 128 + (r >> 3) * 2048, tab + (size_t)r * d.Nx + h * TX + 8 * c);
   }
 }
 // x-half of a [Nx][16] table as K-major A (M = 128 x, K = 16)
 PHAFD_D void load_aspec(unsigned char* dst, const bf16* tab, int h) {
-  for (int q = threadIdx.x; q < TX * 2; q += NTH) {
+  for (int q = threadIdx.x; q < TX * 2; q += blockDim.x) {
     const int x = q >> 1, c = q & 1;
     cp_async16(dst + (x & 7) * 16 + c * 128 + (x >> 3) * 256, tab + (size_t)(h * TX + x) * KR + 8 * c);
   }
 }
 // per-row spectral B parts [row][32][16] of the 4 tiles
 PHAFD_D void load_bspec(unsigned char* dst, const bf16* rows16, const Tile& t) {
-  for (int q = threadIdx.x; q < TPC * C * 2; q += NTH) {
+  for (int q = threadIdx.x; q < TPC * C * 2; q += blockDim.x) {
     const int i = q >> 6, n = (q >> 1) & 31, c = q & 1;
     cp_async16(dst + i * 1024 + (n & 7) * 16 + c * 128 + (n >> 3) * 256,
                rows16 + ((size_t)t.row[i] * C + n) * KR + 8 * c);
@@ -242,8 +243,9 @@ PHAFD_D void issue_wgrad(const Tile& t, uint32_t tmem, uint32_t col0, uint32_t a
 }
 
 // ---- epilogue pieces
+// a warp reads the TMEM lane quarter (warp % 4)
 PHAFD_D uint32_t lane_addr(uint32_t tmem, uint32_t col) {
-  return tmem + ((uint32_t)(32 * (threadIdx.x >> 5)) << 16) + col;
+  return tmem + ((uint32_t)(32 * ((threadIdx.x >> 5) & 3)) << 16) + col;
 }
 PHAFD_D void tmem_row32(uint32_t tmem, uint32_t col, float* v) {
   tc::tmem_ld16(lane_addr(tmem, col), v);
@@ -284,6 +286,7 @@ PHAFD_D void load_row(const bf16* g, float* v) {
 }
 // lane (i, c): 16 x-stage DFT values of row i, channel c -> [row][half][c][16]
 PHAFD_D void store_xdft(float* out, uint32_t tmem, const Tile& t, const Dims& d) {
+  if (threadIdx.x >= 128) return;  // the 128 TMEM lanes belong to the first four warps
   float v[16];
   tc::tmem_ld16(lane_addr(tmem, 0), v);
   const int i = threadIdx.x >> 5, c = threadIdx.x & 31;
@@ -447,15 +450,23 @@ __global__ void __launch_bounds__(NTH) k_layer(const bf16* __restrict__ vin, con
 // multiple of the x-halves, so every group of a CTA has the same half and the
 // half's tables load once).  While group g runs its MMA / epilogue chain, the
 // loads of group g + gridDim.x fly into the other buffer.
-constexpr uint32_t SP_T0 = 0;                    // 2 x 32 KB activation tiles
-constexpr uint32_t SP_BS = 65536;                // 2 x 4 KB spectral B rows
-constexpr uint32_t SP_RAW = SP_BS + 8192;        // 2 x 4 KB phi / rho rows (lift)
-constexpr uint32_t SP_ASP = SP_RAW + 8192;       // G (or F^T) half, 4 KB
-constexpr uint32_t SP_BM = SP_ASP + 4096;        // W, 2 KB
-constexpr uint32_t SP_BM2 = SP_BM + 2048;        // P or Q1, 2 KB
-constexpr uint32_t SP_B2 = SP_BM2 + 2048;        // F half, 4 KB
-constexpr uint32_t SP_BAR = SP_B2 + 4096;
-constexpr uint32_t SP_TOTAL = SP_BAR + 64;       // ~92 KB: 2 CTAs (2 x 256 TMEM columns) per SM
+// Shared-memory map for NB buffers (NB = 2: persistent and double-buffered,
+// ~92 KB and 256 TMEM columns, two CTAs per SM; NB = 1: one tile group per
+// CTA, ~52 KB and 128 TMEM columns, four CTAs per SM).
+template <int NB>
+struct SP {
+  static constexpr uint32_t T0 = 0;                     // NB x 32 KB activation tiles
+  static constexpr uint32_t BS = 32768u * NB;           // NB x 4 KB spectral B rows
+  static constexpr uint32_t RAW = BS + 4096u * NB;      // NB x 4 KB phi / rho rows (lift)
+  static constexpr uint32_t ASP = RAW + 4096u * NB;     // G half, 4 KB
+  static constexpr uint32_t BM = ASP + 4096;            // W, 2 KB
+  static constexpr uint32_t BM2 = BM + 2048;            // P or Q1, 2 KB
+  static constexpr uint32_t B2 = BM2 + 2048;            // F half, 4 KB
+  static constexpr uint32_t BAR = B2 + 4096;
+  static constexpr uint32_t TOTAL = BAR + 64;
+  static constexpr uint32_t TCOLS = NB == 2 ? 256 : 128;
+  static constexpr uint32_t XD = NB == 2 ? 128 : 0;    // TMEM column of the x-stage DFT
+};
 
 enum { TM_LIFT = 0, TM_FIRST = 1, TM_MID = 2, TM_LAST = 3 };
 
@@ -482,7 +493,7 @@ PHAFD_D void set_group(Tile& t, long long g, const Dims& d) {
 }
 // phi and rho rows of the 4 tiles (FP32) -> raw [i][0: phi, 1: rho][128]
 PHAFD_D void load_raw(unsigned char* dst, const LiftIn& in, const Tile& t) {
-  for (int q = threadIdx.x; q < TPC * 2 * (TX / 4); q += NTH) {
+  for (int q = threadIdx.x; q < TPC * 2 * (TX / 4); q += blockDim.x) {
     const int i = q / (2 * (TX / 4)), f = (q / (TX / 4)) & 1, c = q % (TX / 4);
     const float* src = (f ? in.rho : in.phi) + t.node0[i] + 4 * c;
     cp_async16(dst + ((i * 2 + f) * TX + 4 * c) * 4, src);
@@ -513,67 +524,69 @@ PHAFD_D void smem_ready() {
   tc::fence_after();
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(NTH) k_tiles(TileArgs a, Dims d, int swap, Status st) {
+template <int MODE, int NB>
+__global__ void __launch_bounds__(NTP) k_tiles(TileArgs a, Dims d, int swap, Status st) {
   extern __shared__ __align__(1024) unsigned char sm[];
+  using L = SP<NB>;
   Tile t;
   t.sm = sm;
   t.sbase = tc::smem_u32(sm);
-  t.bar = reinterpret_cast<uint64_t*>(sm + SP_BAR);
-  t.taddr_slot = reinterpret_cast<uint32_t*>(sm + SP_BAR + 16);
+  t.bar = reinterpret_cast<uint64_t*>(sm + L::BAR);
+  t.taddr_slot = reinterpret_cast<uint32_t*>(sm + L::BAR + 16);
   if (threadIdx.x == 0) {
     tc::mbar_init(t.bar, 1);
     tc::fence_mbar_init();
   }
   if (threadIdx.x < 32) {
-    tc::tmem_alloc(t.taddr_slot, 256);
+    tc::tmem_alloc(t.taddr_slot, L::TCOLS);
     tc::tmem_relinquish();
   }
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = *t.taddr_slot;
-  const uint32_t XD = 128;  // TMEM column of the x-stage DFT accumulator
-  const int x = threadIdx.x;
+  const uint32_t XD = L::XD;
+  const int x = threadIdx.x & (TX - 1);
+  const int i0 = 2 * (threadIdx.x >> 7);  // this thread's tiles: i0, i0 + 1
   long long g = blockIdx.x;
   set_group(t, g, d);  // the half h is fixed per CTA
   // tables and weights, once
-  if (MODE == TM_LIFT || MODE == TM_FIRST) load_kmajor(sm + SP_BM2, a.Pb, 32, 16);
+  if (MODE == TM_LIFT || MODE == TM_FIRST) load_kmajor(sm + L::BM2, a.Pb, 32, 16);
   if (MODE != TM_LIFT) {
-    load_kmajor(sm + SP_BM, a.Wb, 32, 32);
-    load_aspec(sm + SP_ASP, a.Gtab, t.h);
+    load_kmajor(sm + L::BM, a.Wb, 32, 32);
+    load_aspec(sm + L::ASP, a.Gtab, t.h);
   }
-  if (MODE == TM_LAST) load_kmajor(sm + SP_BM2, a.Q1b, 32, 32);
-  if (MODE != TM_LAST) load_b2(sm + SP_B2, a.Ftab, d, t.h);
+  if (MODE == TM_LAST) load_kmajor(sm + L::BM2, a.Q1b, 32, 32);
+  if (MODE != TM_LAST) load_b2(sm + L::B2, a.Ftab, d, t.h);
   // first group
   if (g < a.ngroups) {
-    if (MODE == TM_LIFT || MODE == TM_FIRST) load_raw(sm + SP_RAW, a.in, t);
-    if (MODE == TM_MID || MODE == TM_LAST) load_act(sm + SP_T0, a.vin, t);
-    if (MODE != TM_LIFT) load_bspec(sm + SP_BS, a.yx, t);
+    if (MODE == TM_LIFT || MODE == TM_FIRST) load_raw(sm + L::RAW, a.in, t);
+    if (MODE == TM_MID || MODE == TM_LAST) load_act(sm + L::T0, a.vin, t);
+    if (MODE != TM_LIFT) load_bspec(sm + L::BS, a.yx, t);
   }
   cp_async_commit();
   uint32_t ph = 0;
   bool ok = true;
   double acc = 0.0;
   for (int it = 0; g < a.ngroups; ++it) {
-    const int b = it & 1;
-    const uint32_t T0 = SP_T0 + 32768u * b, BS = SP_BS + 4096u * b;
+    const int b = NB == 2 ? (it & 1) : 0;
+    const uint32_t T0 = L::T0 + 32768u * b, BS = L::BS + 4096u * b;
     const long long gn = g + gridDim.x;
-    if (gn < a.ngroups) {  // prefetch the next group into the other buffers
+    if (NB == 2 && gn < a.ngroups) {  // prefetch the next group into the other buffers
       Tile tn = t;
       set_group(tn, gn, d);
-      if (MODE == TM_LIFT || MODE == TM_FIRST) load_raw(sm + SP_RAW + 4096 * (1 - b), a.in, tn);
-      if (MODE == TM_MID || MODE == TM_LAST) load_act(sm + SP_T0 + 32768 * (1 - b), a.vin, tn);
-      if (MODE != TM_LIFT) load_bspec(sm + SP_BS + 4096 * (1 - b), a.yx, tn);
+      if (MODE == TM_LIFT || MODE == TM_FIRST) load_raw(sm + L::RAW + 4096 * (1 - b), a.in, tn);
+      if (MODE == TM_MID || MODE == TM_LAST) load_act(sm + L::T0 + 32768 * (1 - b), a.vin, tn);
+      if (MODE != TM_LIFT) load_bspec(sm + L::BS + 4096 * (1 - b), a.yx, tn);
     }
     cp_async_commit();
     cp_async_wait<1>();
     set_group(t, g, d);
     if (MODE == TM_LIFT || MODE == TM_FIRST) {
       __syncthreads();  // raw rows of this group landed for every thread
-      const float* raw = reinterpret_cast<const float*>(sm + SP_RAW + 4096 * b);
+      const float* raw = reinterpret_cast<const float*>(sm + L::RAW + 4096 * b);
 #pragma unroll
-      for (int i = 0; i < TPC; ++i) {
+      for (int i = i0; i < i0 + 2; ++i) {
         float v[16];
         v[0] = (raw[(i * 2) * TX + x] - a.in.n0) / a.in.n1;
         v[1] = (raw[(i * 2 + 1) * TX + x] - a.in.n2) / a.in.n3;
@@ -587,14 +600,14 @@ __global__ void __launch_bounds__(NTH) k_tiles(TileArgs a, Dims d, int swap, Sta
     if (MODE == TM_LIFT || MODE == TM_FIRST) {
       // v0 = P in + pb
       if (threadIdx.x == 0) {
-        issue_main_at(t, tmem, T0, SP_BM2, 1, false, 0, 0);
+        issue_main_at(t, tmem, T0, L::BM2, 1, false, 0, 0);
         tc::commit(t.bar);
       }
       ok = ok && mma_wait(t, ph, st);
       ph ^= 1;
       if (ok) {
 #pragma unroll
-        for (int i = 0; i < TPC; ++i) {
+        for (int i = i0; i < i0 + 2; ++i) {
           float v[32];
           tmem_row32(tmem, 32 * i, v);
 #pragma unroll
@@ -607,14 +620,14 @@ __global__ void __launch_bounds__(NTH) k_tiles(TileArgs a, Dims d, int swap, Sta
     if (MODE != TM_LIFT) {
       // pre = W v + b + G Yx
       if (ok && threadIdx.x == 0) {
-        issue_main_at(t, tmem, T0, SP_BM, 2, true, SP_ASP, BS);
+        issue_main_at(t, tmem, T0, L::BM, 2, true, L::ASP, BS);
         tc::commit(t.bar);
       }
       ok = ok && mma_wait(t, ph, st);
       ph ^= 1;
       if (ok) {
 #pragma unroll
-        for (int i = 0; i < TPC; ++i) {
+        for (int i = i0; i < i0 + 2; ++i) {
           float v[32];
           tmem_row32(tmem, 32 * i, v);
           const size_t o = (size_t)(t.node0[i] + x) * C;
@@ -634,14 +647,14 @@ __global__ void __launch_bounds__(NTH) k_tiles(TileArgs a, Dims d, int swap, Sta
     if (MODE == TM_LAST) {
       // out = q2 . GELU(Q1 v4 + q1b)
       if (ok && threadIdx.x == 0) {
-        issue_main_at(t, tmem, T0, SP_BM2, 2, false, 0, 0);
+        issue_main_at(t, tmem, T0, L::BM2, 2, false, 0, 0);
         tc::commit(t.bar);
       }
       ok = ok && mma_wait(t, ph, st);
       ph ^= 1;
       if (ok) {
 #pragma unroll
-        for (int i = 0; i < TPC; ++i) {
+        for (int i = i0; i < i0 + 2; ++i) {
           float v[32];
           tmem_row32(tmem, 32 * i, v);
           float o = 0.f;
@@ -654,7 +667,7 @@ __global__ void __launch_bounds__(NTH) k_tiles(TileArgs a, Dims d, int swap, Sta
     } else {
       // x-stage DFT of the tile's output
       if (ok && threadIdx.x == 0) {
-        issue_xdft_at(t, tmem + XD, T0, SP_B2, swap);
+        issue_xdft_at(t, tmem + XD, T0, L::B2, swap);
         tc::commit(t.bar);
       }
       ok = ok && mma_wait(t, ph, st);
@@ -672,7 +685,7 @@ __global__ void __launch_bounds__(NTH) k_tiles(TileArgs a, Dims d, int swap, Sta
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(a.sum, acc);
   }
-  tile_end(t, 256);
+  tile_end(t, L::TCOLS);
 }
 
 // correction = scale * (out - mean(out))
@@ -1434,8 +1447,11 @@ struct phafd_fno {
 
   // inference: lift x-stage only, then layer 0 rebuilding v0, layers 1-2,
   // and the last layer with the projection; out and sum(out) filled
+  static constexpr int TNB = 1;  // tile buffers of the inference kernels (1: one group per CTA)
+
   // persistent grid: a multiple of the x-halves, at most two CTAs per SM
   unsigned pgrid() const {
+    if (TNB == 1) return ntiles();
     const long long n = (long long)ntiles();
     long long g = 2LL * nsm;
     g -= g % d.H;
@@ -1472,26 +1488,26 @@ struct phafd_fno {
     const LiftIn in = lift_in(phi, rho, chi);
     const unsigned pg = pgrid();
     TileArgs a = targs(in, -1);
-    k_tiles<TM_LIFT><<<pg, NTH, SP_TOTAL, st>>>(a, d, swap, s);
+    k_tiles<TM_LIFT, TNB><<<pg, NTP, SP<TNB>::TOTAL, st>>>(a, d, swap, s);
     spectral(0, false);
     a = targs(in, 0);
     a.vout = va;
-    k_tiles<TM_FIRST><<<pg, NTH, SP_TOTAL, st>>>(a, d, swap, s);
+    k_tiles<TM_FIRST, TNB><<<pg, NTP, SP<TNB>::TOTAL, st>>>(a, d, swap, s);
     spectral(1, false);
     a = targs(in, 1);
     a.vin = va;
     a.vout = vb;
-    k_tiles<TM_MID><<<pg, NTH, SP_TOTAL, st>>>(a, d, swap, s);
+    k_tiles<TM_MID, TNB><<<pg, NTP, SP<TNB>::TOTAL, st>>>(a, d, swap, s);
     spectral(2, false);
     a = targs(in, 2);
     a.vin = vb;
     a.vout = va;
-    k_tiles<TM_MID><<<pg, NTH, SP_TOTAL, st>>>(a, d, swap, s);
+    k_tiles<TM_MID, TNB><<<pg, NTP, SP<TNB>::TOTAL, st>>>(a, d, swap, s);
     spectral(3, false);
     FCK(cudaMemsetAsync(sum.p, 0, 8, st));
     a = targs(in, 3);
     a.vin = va;
-    k_tiles<TM_LAST><<<pg, NTH, SP_TOTAL, st>>>(a, d, swap, s);
+    k_tiles<TM_LAST, TNB><<<pg, NTP, SP<TNB>::TOTAL, st>>>(a, d, swap, s);
     FCK(cudaGetLastError());
   }
 
@@ -1640,10 +1656,10 @@ int phafd_fno_create(phafd_fno** out, int device, int nx, int ny, int nz, int tr
     smem_attr(k_lift, SM_INF);
     smem_attr(k_layer<true, true, true>, SM_INF);
     smem_attr(k_layer<false, false, false>, SM_INF);
-    smem_attr(k_tiles<TM_LIFT>, SP_TOTAL);
-    smem_attr(k_tiles<TM_FIRST>, SP_TOTAL);
-    smem_attr(k_tiles<TM_MID>, SP_TOTAL);
-    smem_attr(k_tiles<TM_LAST>, SP_TOTAL);
+    smem_attr(k_tiles<TM_LIFT, phafd_fno::TNB>, SP<phafd_fno::TNB>::TOTAL);
+    smem_attr(k_tiles<TM_FIRST, phafd_fno::TNB>, SP<phafd_fno::TNB>::TOTAL);
+    smem_attr(k_tiles<TM_MID, phafd_fno::TNB>, SP<phafd_fno::TNB>::TOTAL);
+    smem_attr(k_tiles<TM_LAST, phafd_fno::TNB>, SP<phafd_fno::TNB>::TOTAL);
     smem_attr(k_proj_train, SM_TRAIN);
     smem_attr(k_layer_bwd<true, true, false>, SM_TRAIN);
     smem_attr(k_layer_bwd<false, false, true>, SM_TRAIN);
