@@ -612,7 +612,9 @@ struct Axis {
   static int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
                     const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only,
                     cudaStream_t st) {
-    constexpr int LB = NLT / 2 >= 1 ? NLT / 2 : 1;
+    // columns per tile: for N >= 512 a full NLT (64-byte row segments of the
+    // strided z columns instead of 32-byte ones)
+    constexpr int LB = N >= 512 ? NLT : (NLT / 2 >= 1 ? NLT / 2 : 1);
     const size_t sm = (size_t)N * (3 * LB + 1) * sizeof(cpx<T>);
     const int kx0 = bulk_only ? 1 : 0;
     if (g.nxh - 2 * kx0 <= 0) return 0;

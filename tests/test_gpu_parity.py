@@ -222,3 +222,20 @@ def test_fp32_lists_are_tight_supersets(gpu_lib, zghost):
                       (canon_grid(g.grid_list()), canon_grid(o.grid_list()))):
         assert want <= got
         assert len(got - want) <= max(2, len(want) // 1000)
+
+
+@pytest.mark.parametrize("shape", [(512, 16, 16), (16, 16, 512)])
+def test_fp64_field_steps_with_512_point_axes(gpu_lib, shape):
+    """512-point transforms (wider z tiles, x rows) against the oracle."""
+    nz, ny, nx = shape
+    o = Oracle(); g = gpu(64, "resident")
+    for d in (o, g):
+        d.domain([-nx / 2, -ny / 2, -nz / 2], [float(nx), float(ny), float(nz)])
+        d.grid_style(nx, ny, nz)
+        d.grid_populate_constant(0.45, 0.02, 3)
+        d.fix_conjugate_volfrac(11, mobility=1.0, temp=0.01, volFH=1.0, gamma=100.0, noise="philox")
+        d.fix_floryhuggins(temp=1.0, volFH=1.0, chi=3.0)
+        d.set_dt(1e-4)
+        d.setup()
+        d.run(5)
+    assert rel_err(g.grid_get("phi"), o.grid_get("phi")) < 1e-10
