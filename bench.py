@@ -458,6 +458,17 @@ def run_learned(args):
     t_sur = time.perf_counter() - t0
     judged = [{"step": j[0], "sk_err": j[1], "mass_err": j[2], "accepted": bool(j[3])} for j in run.judged]
     phase_s = dict(run.times)
+    run.close()
+    # the same judged run with the linearised macro step alone
+    lin = S.Runner(cfg, chains, None, judge_every=100, sk_bound=SK_BOUND, mass_bound=MASS_BOUND)
+    lin.run(100)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lin.run(nsub)
+    torch.cuda.synchronize()
+    t_lin = time.perf_counter() - t0
+    judged_lin = [{"step": j[0], "sk_err": j[1], "accepted": bool(j[3])} for j in lin.judged]
+    lin.close()
     # network inference alone, CUDA events around the call
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     rho = torch.zeros((n_eval,) * 3, device="cuda")
@@ -471,7 +482,6 @@ def run_learned(args):
     ev1.record()
     torch.cuda.synchronize()
     infer_ms = ev0.elapsed_time(ev1) / 5
-    run.close()
     net.close()
     v_sur, v_plain = nsub / t_sur, nsub / t_plain
     line = {
@@ -485,6 +495,8 @@ def run_learned(args):
                    "train_samples": 2 * args.traj, "epochs": args.epochs,
                    "timing": "host wall clock around run(), synchronised; includes the judge windows"},
         "plain_steps_per_s": v_plain, "speedup_vs_plain": v_sur / v_plain,
+        "linear_macro_steps_per_s": nsub / t_lin, "linear_macro_speedup_vs_plain": (nsub / t_lin) / v_plain,
+        "judge_linear_macro": judged_lin,
         "horizon_substeps": horizon, "errors_vs_plain": herr,
         "macro_error_rel": {"train": gain_train, "held_out_128": gain_held, "linear_step_alone": 1.0},
         "judge": judged, "train_loss": hist, "seconds": {"generate": t_gen, "train": t_train},

@@ -194,7 +194,8 @@ def gain(net, data):
 
 # --------------------------------------------------------------------- runs
 class Runner:
-    """Production run with the learned macro step and its judge."""
+    """Production run with the learned macro step and its judge (net None:
+    the linearised macro step alone, judged the same way)."""
 
     def __init__(self, cfg, chains, net, K=K_SUB, judge_every=100, sk_bound=1e-2, mass_bound=1e-6, nbins=None):
         import torch
@@ -221,6 +222,9 @@ class Runner:
         self.times[key] += time.perf_counter() - t0
 
     def _macro(self, s):
+        if self.net is None:  # the linearised macro step alone (the method without the network)
+            self._t("step", s.run, 1)
+            return
         self._t("density", s.deposit_density, self.rho.data_ptr())
         self._t("network", self.net.infer, s.grid_device("phi"), self.rho.data_ptr(), self.cfg["chi"],
                 self.corr.data_ptr())
