@@ -112,6 +112,13 @@ int phafd_set_zghost(phafd_ctx* ctx, int mode);                      /* CommBric
 int phafd_set_schedule(phafd_ctx* ctx, int schedule);
 int phafd_set_keep_chempot(phafd_ctx* ctx, int keep);               /* also store mu = deposit + FH (grid->chempot) each step */
 int phafd_set_plane_fusion(phafd_ctx* ctx, int on);                 /* x and y passes fused per z-plane in thread-block clusters (Nx == Ny) */
+/* on (default): single-substep resident steps store grad phi only at grid
+ * nodes within (gridatom cutoff + skin) of the beads' positions at the last
+ * neighbor rebuild -- the only nodes the pair forces read while no bead has
+ * moved more than skin since; a step after which some bead has moved further
+ * stores it everywhere.  Reads of the gradient fields (phafd_grid_get,
+ * phafd_grid_device) first recompute them everywhere from the current phi. */
+int phafd_set_gradient_mask(phafd_ctx* ctx, int on);
 
 /* ---- beads (atom_style / atom_populate, atom.cpp:26-110,219-252) ---- */
 int phafd_atoms_create(phafd_ctx* ctx, int n, const int* tags, const int* mol, const int* types, const double* x);

@@ -735,6 +735,64 @@ void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st) {
   launch_rebuild(a, st);
 }
 
+// Node mask of the gradient.  The pair kernel reads grad phi only at nodes
+// within the coupling cutoff of a bead's current position.  At each rebuild
+// the mask marks every node within cutoff + skin of the bead positions of
+// that rebuild (xhold); before the inverse transform of a step the guard
+// checks that no bead has moved more than skin since, which keeps every
+// node the next pair evaluation reads inside the mask.  The inverse x pass
+// then stores the three gradient components at masked nodes only, unless
+// the guard fired (then everywhere, until the next rebuild clears it).
+__global__ void k_gmask_clear(BeadArgs a) {
+  if (!*a.flag) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *a.gmask_off = 0;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < a.gmask_words;
+       k += (long long)gridDim.x * blockDim.x)
+    a.gmask[k] = 0u;
+}
+__global__ void k_gmask_build(BeadArgs a) {
+  if (!*a.flag) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  int lo[3], hi[3];
+  double u[3];
+  for (int d = 0; d < 3; ++d) {
+    u[d] = (a.x[3 * i + d] - a.boxlo[d]) / a.dx[d];
+    lo[d] = (int)floor(u[d] - a.gmask_r / a.dx[d]);
+    hi[d] = (int)ceil(u[d] + a.gmask_r / a.dx[d]);
+  }
+  const double r2 = a.gmask_r * a.gmask_r;
+  for (int kz = lo[2]; kz <= hi[2]; ++kz) {
+    const double dz = (kz - u[2]) * a.dx[2];
+    const int wz = ((kz % a.N[2]) + a.N[2]) % a.N[2];
+    for (int ky = lo[1]; ky <= hi[1]; ++ky) {
+      const double dy = (ky - u[1]) * a.dx[1];
+      const int wy = ((ky % a.N[1]) + a.N[1]) % a.N[1];
+      for (int kx = lo[0]; kx <= hi[0]; ++kx) {
+        const double dxx = (kx - u[0]) * a.dx[0];
+        if (dxx * dxx + dy * dy + dz * dz > r2) continue;
+        const int wx = ((kx % a.N[0]) + a.N[0]) % a.N[0];
+        const long long node = ((long long)wz * a.N[1] + wy) * a.N[0] + wx;
+        atomicOr(a.gmask + (node >> 5), 1u << (node & 31));
+      }
+    }
+  }
+}
+
+__global__ void k_gmask_guard(BeadArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double d0 = a.x[3 * i] - a.xhold[3 * i];
+  const double d1 = a.x[3 * i + 1] - a.xhold[3 * i + 1];
+  const double d2 = a.x[3 * i + 2] - a.xhold[3 * i + 2];
+  if (d0 * d0 + d1 * d1 + d2 * d2 > a.gmask_guardsq) *a.gmask_off = 1;
+}
+
+void launch_gmask_guard(const BeadArgs& a, cudaStream_t st) {
+  if (a.n == 0 || !a.gmask) return;
+  k_gmask_guard<<<nblk(a.n, 256), 256, 0, st>>>(a);
+}
+
 void launch_rebuild(const BeadArgs& a, cudaStream_t st) {
   if (a.n == 0) return;
   const int T = 256;
@@ -749,6 +807,10 @@ void launch_rebuild(const BeadArgs& a, cudaStream_t st) {
   k_bin_sort<<<nblk(a.nbins, T) > 4096 ? 4096 : nblk(a.nbins, T), T, 0, st>>>(a);
   if (a.fp32_lists) k_build_fp32<<<nblk(a.n, 128), 128, 0, st>>>(a);
   else k_build<<<nblk(a.n, 128), 128, 0, st>>>(a);
+  if (a.gmask) {
+    k_gmask_clear<<<1024, 256, 0, st>>>(a);
+    k_gmask_build<<<nblk(a.n, 128), 128, 0, st>>>(a);
+  }
   k_build_done<<<1, 1, 0, st>>>(a);
 }
 

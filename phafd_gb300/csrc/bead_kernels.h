@@ -21,6 +21,11 @@ struct BeadArgs {
   double boxlo[3], boxhi[3], period[3];
   double triggersq, cutneigh, cutneighsq;
   int* flag;            // rebuild requested (device)
+  uint32_t* gmask;      // bit per grid node within gmask_r of a bead's position at the last rebuild (null: none)
+  long long gmask_words;
+  double gmask_r;       // radius of the mask: coupling cutoff + skin (+ a round-off margin)
+  double gmask_guardsq; // squared displacement since the last rebuild up to which the mask covers every read
+  int* gmask_off;       // set: the mask does not cover the current positions (cleared by a rebuild)
   int* check_done;      // blocks of k_check finished (last one sets the graph condition)
   int* status;          // sticky ST_* bits
   long long* ncalls;    // Neighbor::ncalls
@@ -67,6 +72,8 @@ void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st);
 // setting a graph conditional to the rebuild flag) and the rebuild kernels
 void launch_neighbor_check(const BeadArgs& a, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
 void launch_rebuild(const BeadArgs& a, cudaStream_t st);
+// sets *gmask_off when a bead moved more than sqrt(gmask_guardsq) since the last rebuild
+void launch_gmask_guard(const BeadArgs& a, cudaStream_t st);
 template <typename T> void launch_pair(const BeadArgs& a, const PairArgs<T>& p, cudaStream_t st);
 template <typename T> void launch_dep_zero(const BeadArgs& a, T* dep, cudaStream_t st);
 template <typename T> void launch_density(const BeadArgs& a, const PairArgs<T>& p, T* rho, cudaStream_t st);

@@ -153,6 +153,8 @@ struct phafd_ctx {
   bool keep_chempot = false;
   bool chempot_from_mu = false;
   bool use_plane = false;  // plane-fused x/y passes where they apply (phafd_set_plane_fusion)
+  bool use_gmask = true;   // gradient stored near beads only during steps (phafd_set_gradient_mask)
+  bool grad_partial = false;  // gx, gy, gz hold values at masked nodes only
   int nsub = 1;            // substeps of one step (phafd_set_linear_substeps)
   double f2_lin = 0.0;     // dmu/dphi of the linearisation
   int graph_cur = 0;
@@ -169,6 +171,7 @@ struct phafd_ctx {
   DevBuf bin_of, bin_count, bin_cursor, bin_start, sorted, scan_tmp, bin_off;
   DevBuf nbr, nnbr, gl, ngl;
   DevBuf dragc, sf_fix, sf_start, sf_len, sf_par;
+  DevBuf gmask;  // one bit per grid node (beads with a grid coupling)
   BeadArgs ba{};
   // pairs
   bool have_lj = false;
@@ -194,7 +197,7 @@ struct phafd_ctx {
   bool setup_done = false;
   // device counters
   DevBuf d_counters;  // [0..1] FH counters (ull), [2] step, [3] nan_step, [4] ncalls, [5] flag|status,
-                      // [6] blocks of the neighbor check done
+                      // [6] blocks of the neighbor check done | gradient mask off
   unsigned long long* fh_counters() const { return d_counters.as<unsigned long long>(); }
   long long* d_step() const { return d_counters.as<long long>() + 2; }
   long long* d_nan() const { return d_counters.as<long long>() + 3; }
@@ -202,6 +205,7 @@ struct phafd_ctx {
   int* d_flag() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 5); }
   int* d_status() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 5) + 1; }
   int* d_check_done() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 6); }
+  int* d_gmask_off() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 6) + 1; }
   // graph
   cudaGraphExec_t gexec = nullptr;
   cudaGraphExec_t gexec1[2] = {nullptr, nullptr};  // one step, per spectrum parity (resident)
@@ -327,7 +331,7 @@ struct phafd_ctx {
 
   // y inverse and x c2r of A (and B): phi (scale sp, optional) and grad (scale sg)
   template <typename T>
-  void yx_inverse(T* phi_out, T sp, T sg, bool grad, bool nan_check) {
+  void yx_inverse(T* phi_out, T sp, T sg, bool grad, bool nan_check, bool masked = false) {
     const cpx<T>* twi[3] = {tw[0][1].as<cpx<T>>(), tw[1][1].as<cpx<T>>(), tw[2][1].as<cpx<T>>()};
     cpx<T>* A = wA.as<cpx<T>>();
     cpx<T>* B = wB.as<cpx<T>>();
@@ -342,7 +346,7 @@ struct phafd_ctx {
       if (rc != -3) {
         chk(rc, "y ifft");
         chk(GridOps<T>::xc2r3(geom, Cc, phi_out, gx.as<T>(), D, gy.as<T>(), E, gz.as<T>(), sp, sg, twi[0], nan, nonan,
-                              st), "x c2r");
+                              masked ? gmask.as<uint32_t>() : nullptr, d_gmask_off(), st), "x c2r");
         return;
       }
     }
@@ -421,6 +425,31 @@ struct phafd_ctx {
     a.sf_fix = sf_fix.as<int>(); a.sf_start = sf_start.as<int>(); a.sf_len = sf_len.as<int>();
     a.sf = sf_par.as<SemiDev>();
     a.any_semi = !semis.empty();
+    a.gmask = gmask.p ? gmask.as<uint32_t>() : nullptr;
+    a.gmask_words = ((long long)nreal + 31) / 32;
+    a.gmask_r = ga_maxcut + skin + 1e-3 * std::min(a.dx[0], std::min(a.dx[1], a.dx[2]));
+    a.gmask_guardsq = skin * skin;
+    a.gmask_off = d_gmask_off();
+  }
+
+  // steps store grad phi at masked nodes only (single-substep resident steps
+  // with a grid coupling; the x pass is the merged inverse launch)
+  bool gmask_steps() const {
+    return use_gmask && gmask.p && nsub == 1 && schedule == PHAFD_SCHEDULE_RESIDENT && have_conj && !profiling &&
+           !use_plane && n > 0;
+  }
+
+  // full gradient fields again after masked steps
+  void full_gradient() {
+    if (!grad_partial) return;
+    if (precision == PHAFD_FP64)
+      inverse_chain<double>(phat[cur].as<cpx<double>>(), nullptr, nullptr, 0.0, 1.0 / (double)nreal, true, false);
+    else
+      inverse_chain<float>(phat[cur].as<cpx<float>>(), nullptr, nullptr, 0.0f, (float)(1.0 / (double)nreal), true,
+                           false);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    grad_partial = false;
   }
 
   void setup_neighbor_structs() {
@@ -465,6 +494,12 @@ struct phafd_ctx {
     ba.maxg = maxg;
     if (ga_style != PHAFD_GRIDATOM_NONE) gl.alloc((size_t)std::max(n, 1) * maxg * 4);
     ngl.alloc(std::max(n, 1) * 4);
+    if (ga_style != PHAFD_GRIDATOM_NONE && gridset) {
+      gmask.alloc(((nreal + 31) / 32) * 4);
+      gmask.zero(st);
+      const int off = 1;  // until the first rebuild has built it
+      CK(cudaMemcpyAsync(d_gmask_off(), &off, sizeof(int), cudaMemcpyHostToDevice, st));
+    }
     nnbr.zero(st);
     ngl.zero(st);
   }
@@ -597,6 +632,11 @@ struct phafd_ctx {
     // final_integrate of the beads (independent of the field update)
     launch_drag(ba, dt, bs);
     launch_chain_half<T>(ba, 1, dt, bs, nsub, 0);
+    const bool masked = resident && gmask_steps();
+    if (masked) {
+      launch_gmask_guard(ba, bs);
+      grad_partial = true;
+    }
     mark(3);
     if (have_conj) {
       FHArgs fh{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
@@ -639,11 +679,13 @@ struct phafd_ctx {
           CK(cudaStreamWaitEvent(st, ev_pl_join, 0));
         }
         mark(7);
-        if (fork && nsub > 1) {  // the bead substeps read phi and grad phi, which the inverse overwrites
+        // the bead substeps read phi and grad phi, which the inverse
+        // overwrites; the masked inverse reads the guard's verdict
+        if (fork && (nsub > 1 || masked)) {
           CK(cudaEventRecord(ev_join, st2));
           CK(cudaStreamWaitEvent(st, ev_join, 0));
         }
-        if (!use_plane || !yx_fused<T>()) yx_inverse<T>(phi.as<T>(), (T)1, (T)1, true, true);
+        if (!use_plane || !yx_fused<T>()) yx_inverse<T>(phi.as<T>(), (T)1, (T)1, true, true, masked);
       } else {
         // post_force + pre_final_integrate: mu = dep + FH(phi), r2c
         r2c<T>(phi.as<T>(), dep.as<T>(), muhat.as<cpx<T>>(), fh);
@@ -868,6 +910,13 @@ int phafd_set_plane_fusion(phafd_ctx* c, int on) {
   API_END(c)
 }
 
+int phafd_set_gradient_mask(phafd_ctx* c, int on) {
+  API_BEGIN(c)
+  c->use_gmask = on != 0;
+  c->invalidate_graph();
+  API_END(c)
+}
+
 int phafd_set_keep_chempot(phafd_ctx* c, int keep) {
   API_BEGIN(c)
   c->keep_chempot = keep != 0;
@@ -925,6 +974,7 @@ int phafd_grid_set(phafd_ctx* c, int field, const double* host) {
   DevBuf* b = field == PHAFD_FIELD_PHI ? &c->phi : field == PHAFD_FIELD_GRADX ? &c->gx
             : field == PHAFD_FIELD_GRADY ? &c->gy : field == PHAFD_FIELD_GRADZ ? &c->gz : nullptr;
   if (!b) throw std::invalid_argument("field cannot be set");
+  if (field != PHAFD_FIELD_PHI) c->full_gradient();  // the other two components stay complete
   if (c->precision == PHAFD_FP64) copy_real_to_dev<double>(c, *b, host);
   else copy_real_to_dev<float>(c, *b, host);
   if (field == PHAFD_FIELD_PHI) c->populated = true;
@@ -949,6 +999,7 @@ int phafd_grid_get(phafd_ctx* c, int field, double* host) {
                     : field == PHAFD_FIELD_GRADY ? &c->gy : field == PHAFD_FIELD_GRADZ ? &c->gz
                     : field == PHAFD_FIELD_CHEMPOT ? (c->chempot_from_mu ? &c->mu : &c->dep) : nullptr;
     if (!b) throw std::invalid_argument("bad field");
+    if (field == PHAFD_FIELD_GRADX || field == PHAFD_FIELD_GRADY || field == PHAFD_FIELD_GRADZ) c->full_gradient();
     if (f64) copy_real_to_host<double>(c, *b, host);
     else copy_real_to_host<float>(c, *b, host);
   }
@@ -1164,6 +1215,7 @@ int phafd_setup(phafd_ctx* c) {
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
   c->invalidate_graph();
+  c->grad_partial = false;
   c->setup_done = true;
   int rc = check_status(c);
   if (rc) return rc;
@@ -1507,6 +1559,7 @@ int phafd_grid_device(phafd_ctx* c, int field, void** dev) {
                   : field == PHAFD_FIELD_GRADY ? &c->gy : field == PHAFD_FIELD_GRADZ ? &c->gz
                   : field == PHAFD_FIELD_CHEMPOT ? &c->dep : nullptr;
   if (!b) throw std::invalid_argument("bad field");
+  if (field == PHAFD_FIELD_GRADX || field == PHAFD_FIELD_GRADY || field == PHAFD_FIELD_GRADZ) c->full_gradient();
   *dev = b->p;
   API_END(c)
 }
@@ -1548,6 +1601,7 @@ int phafd_grid_add_device(phafd_ctx* c, const void* src, double scale) {
   }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
+  if (resident) c->grad_partial = false;
   API_END(c)
 }
 
@@ -1576,10 +1630,12 @@ int phafd_ctx_copy_state(phafd_ctx* dst, phafd_ctx* src) {
                   std::make_pair(&dst->bin_start, &src->bin_start), std::make_pair(&dst->sorted, &src->sorted),
                   std::make_pair(&dst->bin_off, &src->bin_off), std::make_pair(&dst->nbr, &src->nbr),
                   std::make_pair(&dst->nnbr, &src->nnbr), std::make_pair(&dst->gl, &src->gl),
-                  std::make_pair(&dst->ngl, &src->ngl), std::make_pair(&dst->d_counters, &src->d_counters)})
+                  std::make_pair(&dst->ngl, &src->ngl), std::make_pair(&dst->d_counters, &src->d_counters),
+                  std::make_pair(&dst->gmask, &src->gmask)})
     cp(*pr.first, *pr.second);
   CK(cudaStreamSynchronize(src->st));
   dst->cur = src->cur;
+  dst->grad_partial = src->grad_partial;
   dst->timestep = src->timestep;
   API_END(c)
 }

@@ -137,11 +137,12 @@ k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict_
 // -------------------------------------------------------------------- x c2r
 // out0 = c2r(m0 * in) * s0 with m0 = i dqx kx if MUL0 else 1
 // out1 = c2r(i dqx kx * in) * s1          (NOUT == 2)
-// one tile (rows y0 .. y0 + 2 LB of plane z); bx is the tile's index along y
+// one tile (rows y0 .. y0 + 2 LB of plane z); bx is the tile's index along y;
+// mask0 / mask1: node bitsets limiting the stores of output 0 / 1 (null: all)
 template <typename T, int N, int LB, bool MUL0, int NOUT>
 PHAFD_D void xc2r_tile(int bx, int z, const cpx<T>* __restrict__ in, T* __restrict__ out0, T* __restrict__ out1,
                        T s0, T s1, T dq, const cpx<T>* __restrict__ tw, int Ny, int Nz, const NanArgs& nan,
-                       unsigned char* smraw) {
+                       unsigned char* smraw, const uint32_t* mask0 = nullptr, const uint32_t* mask1 = nullptr) {
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = LB * NOUT;
   constexpr int NT = N * NL / 16, STR = NL + 1;
@@ -176,7 +177,9 @@ PHAFD_D void xc2r_tile(int bx, int z, const cpx<T>* __restrict__ in, T* __restri
         const int y = y0 + 2 * l + h;
         if (y < Ny) {
           const T val = (h == 0 ? v.x : v.y) * sc;
-          out[((size_t)z * Ny + y) * N + x] = val;
+          const size_t node = ((size_t)z * Ny + y) * N + x;
+          const uint32_t* mk = q == 0 ? mask0 : mask1;
+          if (!mk || ((mk[node >> 5] >> (node & 31)) & 1u)) out[node] = val;
           if (q == 0 && nan.check && z == 0 && y == 0 && x == 0 && isnan(val))
             atomicCAS(reinterpret_cast<unsigned long long*>(nan.nan_step), (unsigned long long)-1LL,
                       (unsigned long long)(*nan.d_step));
@@ -201,15 +204,18 @@ template <typename T, int N, int LB2>
 __global__ void __launch_bounds__(N * LB2 * 2 / 16)
 k_xc2r3(const cpx<T>* __restrict__ C, T* __restrict__ phi, T* __restrict__ gx, const cpx<T>* __restrict__ D,
         T* __restrict__ gy, const cpx<T>* __restrict__ E, T* __restrict__ gz, T sp, T sg, T dq,
-        const cpx<T>* __restrict__ tw, int Ny, int Nz, NanArgs nan, NanArgs nonan, int nb0, int nb1) {
+        const cpx<T>* __restrict__ tw, int Ny, int Nz, NanArgs nan, NanArgs nonan, int nb0, int nb1,
+        const uint32_t* __restrict__ mask, const int* __restrict__ mask_off) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int bx = blockIdx.x, z = blockIdx.y;
+  const uint32_t* gmask = mask && !*mask_off ? mask : nullptr;
   if (bx < nb0)
-    xc2r_tile<T, N, LB2, false, 2>(bx, z, C, phi, gx, sp, sg, dq, tw, Ny, Nz, nan, smraw);
+    xc2r_tile<T, N, LB2, false, 2>(bx, z, C, phi, gx, sp, sg, dq, tw, Ny, Nz, nan, smraw, nullptr, gmask);
   else if (bx < nb0 + nb1)
-    xc2r_tile<T, N, 2 * LB2, false, 1>(bx - nb0, z, D, gy, nullptr, sg, sg, dq, tw, Ny, Nz, nonan, smraw);
+    xc2r_tile<T, N, 2 * LB2, false, 1>(bx - nb0, z, D, gy, nullptr, sg, sg, dq, tw, Ny, Nz, nonan, smraw, gmask);
   else
-    xc2r_tile<T, N, 2 * LB2, false, 1>(bx - nb0 - nb1, z, E, gz, nullptr, sg, sg, dq, tw, Ny, Nz, nonan, smraw);
+    xc2r_tile<T, N, 2 * LB2, false, 1>(bx - nb0 - nb1, z, E, gz, nullptr, sg, sg, dq, tw, Ny, Nz, nonan, smraw,
+                                       gmask);
 }
 
 // -------------------------------------------------------------------- y pass
@@ -559,7 +565,8 @@ struct Axis {
   }
 
   static int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E, T* gz,
-                   T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, cudaStream_t st) {
+                   T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
+                   const int* gmask_off, cudaStream_t st) {
     constexpr int LB2 = NLT / 2 >= 1 ? NLT / 2 : 1;
     if (2 * LB2 != NLT) return -3;
     const size_t sm = (size_t)N * (2 * LB2 + 1) * sizeof(cpx<T>);
@@ -567,7 +574,7 @@ struct Axis {
     auto k = k_xc2r3<T, N, LB2>;
     if (set_smem(k, sm)) return -1;
     launch_grid(k, dim3(nb0 + 2 * nb1, g.nz), dim3(N * LB2 * 2 / 16), sm, st, C, phi, gx, D, gy, E, gz, sp, sg,
-                (T)g.kq[0], tw, g.ny, g.nz, nan, nonan, nb0, nb1);
+                (T)g.kq[0], tw, g.ny, g.nz, nan, nonan, nb0, nb1, gmask, gmask_off);
     return 0;
   }
 
@@ -653,9 +660,10 @@ int GridOps<T>::xc2r(const Geom& g, const cpx<T>* in, T* out0, T s0, bool mul0, 
 template <typename T>
 int GridOps<T>::xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E,
                       T* gz, T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan,
-                      cudaStream_t st) {
+                      const uint32_t* gmask, const int* gmask_off, cudaStream_t st) {
   switch (g.nx) {
-#define CASE(n) case n: return Axis<T, n>::xc2r3(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, st);
+#define CASE(n) \
+  case n: return Axis<T, n>::xc2r3(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
     PHAFD_FOR_SIZES(CASE)
 #undef CASE
   }

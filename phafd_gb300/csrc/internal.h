@@ -55,8 +55,11 @@ struct GridOps {
   // the inverse chain's three x c2r (phi + dphi/dx from C, dphi/dy from D,
   // dphi/dz from E) and two inverse y passes (A -> C, D; B -> E) as one
   // launch each (-3: not available for this length)
+  // (gmask: node bitset; unless gmask is null or *gmask_off is set, the three
+  // gradients are stored at set bits only)
   static int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E, T* gz,
-                   T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, cudaStream_t st);
+                   T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
+                   const int* gmask_off, cudaStream_t st);
   static int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E,
                    const cpx<T>* tw, cudaStream_t st);
   static int zpass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,

@@ -25,6 +25,7 @@ EXPORTS = [
     "phafd_ctx_create", "phafd_ctx_destroy", "phafd_last_error", "phafd_build_info",
     "phafd_domain", "phafd_grid_style", "phafd_grid_populate_constant", "phafd_grid_set", "phafd_grid_get",
     "phafd_set_zghost", "phafd_set_schedule", "phafd_set_keep_chempot", "phafd_set_plane_fusion",
+    "phafd_set_gradient_mask",
     "phafd_atoms_create", "phafd_atoms_get",
     "phafd_pair_gridatom", "phafd_pair_gridatom_coeff", "phafd_pair_lj_cut",
     "phafd_neighbor",
@@ -83,6 +84,7 @@ def load(path=None):
         "phafd_set_schedule": [vp, C.c_int],
         "phafd_set_keep_chempot": [vp, C.c_int],
         "phafd_set_plane_fusion": [vp, C.c_int],
+        "phafd_set_gradient_mask": [vp, C.c_int],
         "phafd_domain": [vp, dp, dp],
         "phafd_grid_style": [vp, C.c_int, C.c_int, C.c_int],
         "phafd_grid_populate_constant": [vp, C.c_double, C.c_double, C.c_int],
@@ -180,6 +182,10 @@ class PhafdGPU:
 
     def set_plane_fusion(self, on=True):
         self._call("phafd_set_plane_fusion", int(on))
+
+    def set_gradient_mask(self, on=True):
+        """Store grad phi only near the beads during steps (the default)."""
+        self._call("phafd_set_gradient_mask", int(on))
 
     def domain(self, boxlo, period):
         self._call("phafd_domain", np.asarray(boxlo, np.float64), np.asarray(period, np.float64))
