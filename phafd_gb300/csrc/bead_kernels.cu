@@ -737,8 +737,8 @@ void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st) {
 
 // Node mask of the gradient.  The pair kernel reads grad phi only at nodes
 // within the coupling cutoff of a bead's current position.  At each rebuild
-// the mask marks every node within cutoff + skin of the bead positions of
-// that rebuild (xhold); before the inverse transform of a step the guard
+// the mask marks every 32-byte sector (gmask_g nodes along x) holding a node
+// within cutoff + skin of the bead positions of that rebuild (xhold); before the inverse transform of a step the guard
 // checks that no bead has moved more than skin since, which keeps every
 // node the next pair evaluation reads inside the mask.  The inverse x pass
 // then stores the three gradient components at masked nodes only, unless
@@ -772,8 +772,8 @@ __global__ void k_gmask_build(BeadArgs a) {
         const double dxx = (kx - u[0]) * a.dx[0];
         if (dxx * dxx + dy * dy + dz * dz > r2) continue;
         const int wx = ((kx % a.N[0]) + a.N[0]) % a.N[0];
-        const long long node = ((long long)wz * a.N[1] + wy) * a.N[0] + wx;
-        atomicOr(a.gmask + (node >> 5), 1u << (node & 31));
+        const long long sec = (((long long)wz * a.N[1] + wy) * a.N[0] + wx) / a.gmask_g;
+        atomicOr(a.gmask + (sec >> 5), 1u << (sec & 31));
       }
     }
   }

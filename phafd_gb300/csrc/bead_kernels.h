@@ -21,8 +21,10 @@ struct BeadArgs {
   double boxlo[3], boxhi[3], period[3];
   double triggersq, cutneigh, cutneighsq;
   int* flag;            // rebuild requested (device)
-  uint32_t* gmask;      // bit per grid node within gmask_r of a bead's position at the last rebuild (null: none)
+  uint32_t* gmask;      // bit per 32-byte sector of a grid field (gmask_g nodes) holding a node within gmask_r
+                        // of a bead's position at the last rebuild (null: none)
   long long gmask_words;
+  int gmask_g;
   double gmask_r;       // radius of the mask: coupling cutoff + skin (+ a round-off margin)
   double gmask_guardsq; // squared displacement since the last rebuild up to which the mask covers every read
   int* gmask_off;       // set: the mask does not cover the current positions (cleared by a rebuild)

@@ -171,7 +171,7 @@ struct phafd_ctx {
   DevBuf bin_of, bin_count, bin_cursor, bin_start, sorted, scan_tmp, bin_off;
   DevBuf nbr, nnbr, gl, ngl;
   DevBuf dragc, sf_fix, sf_start, sf_len, sf_par;
-  DevBuf gmask;  // one bit per grid node (beads with a grid coupling)
+  DevBuf gmask;  // one bit per 32-byte sector of a real field (beads with a grid coupling)
   BeadArgs ba{};
   // pairs
   bool have_lj = false;
@@ -426,7 +426,8 @@ struct phafd_ctx {
     a.sf = sf_par.as<SemiDev>();
     a.any_semi = !semis.empty();
     a.gmask = gmask.p ? gmask.as<uint32_t>() : nullptr;
-    a.gmask_words = ((long long)nreal + 31) / 32;
+    a.gmask_g = 32 / (int)rsz();
+    a.gmask_words = ((long long)nreal / a.gmask_g + 32) / 32;
     a.gmask_r = ga_maxcut + skin + 1e-3 * std::min(a.dx[0], std::min(a.dx[1], a.dx[2]));
     a.gmask_guardsq = skin * skin;
     a.gmask_off = d_gmask_off();
@@ -495,7 +496,7 @@ struct phafd_ctx {
     if (ga_style != PHAFD_GRIDATOM_NONE) gl.alloc((size_t)std::max(n, 1) * maxg * 4);
     ngl.alloc(std::max(n, 1) * 4);
     if (ga_style != PHAFD_GRIDATOM_NONE && gridset) {
-      gmask.alloc(((nreal + 31) / 32) * 4);
+      gmask.alloc(((nreal / (32 / rsz()) + 32) / 32) * 4);
       gmask.zero(st);
       const int off = 1;  // until the first rebuild has built it
       CK(cudaMemcpyAsync(d_gmask_off(), &off, sizeof(int), cudaMemcpyHostToDevice, st));

@@ -58,56 +58,48 @@ k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict_
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NT = N * LB / 16, STR = LB + 1;
-  cpx<T>* sd = s + (size_t)N * STR;  // deposit rows, same layout (PRO == 1)
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * LB;
-  unsigned long long nless = 0, ngreat = 0;
   // rows 2l and 2l+1 of the tile land as the real and imaginary parts of line l
-  TILE_LOOP(idx, LB * N, NT) {
-    const int l = idx / N, x = idx % N;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int y = y0 + 2 * l + h;
-      T* dst = reinterpret_cast<T*>(&s[x * STR + l]) + h;
-      T* dstd = reinterpret_cast<T*>(&sd[x * STR + l]) + h;
-      if (y < Ny) {
-        const size_t o = ((size_t)z * Ny + y) * N + x;
-        cp_async_real(dst, in0 + o);
-        if constexpr (PRO == 1) cp_async_real(dstd, dep + o);
-      } else {
-        *dst = (T)0;
-        if constexpr (PRO == 1) *dstd = (T)0;
-      }
-    }
-  }
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  if constexpr (PRO == 1) {
+  if constexpr (PRO == 0) {
     TILE_LOOP(idx, LB * N, NT) {
       const int l = idx / N, x = idx % N;
-      T* v = reinterpret_cast<T*>(&s[x * STR + l]);
-      const T* dd = reinterpret_cast<const T*>(&sd[x * STR + l]);
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int y = y0 + 2 * l + h;
+        T* dst = reinterpret_cast<T*>(&s[x * STR + l]) + h;
+        if (y < Ny) cp_async_real(dst, in0 + ((size_t)z * Ny + y) * N + x);
+        else *dst = (T)0;
+      }
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+  } else {
+    // mu = deposit + FH(phi) on the way in (registers), one shared tile
+    unsigned long long nless = 0, ngreat = 0;
+    TILE_LOOP(idx, LB * N, NT) {
+      const int l = idx / N, x = idx % N;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int y = y0 + 2 * l + h;
+        T p = (T)0;
         if (y < Ny) {
-          T p = v[h];
+          const size_t o = ((size_t)z * Ny + y) * N + x;
+          p = in0[o];
+          const T dd = dep[o];
           if (fh.enabled) {
             // fixgrid_floryhuggins.cpp:72-82
             if (p <= (T)0) { p = -p; nless++; }
             else if (p >= (T)1) { p = (T)1 - (p - (T)1); ngreat++; }
-            p = dd[h] + (T)fh.tv * (fh_log_ratio(p) + (T)fh.chi * ((T)1 - (T)2 * p));
+            p = dd + (T)fh.tv * (fh_log_ratio(p) + (T)fh.chi * ((T)1 - (T)2 * p));
           } else {
-            p = dd[h];
+            p = dd;
           }
-          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[((size_t)z * Ny + y) * N + x] = p;
-          v[h] = p;
+          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[o] = p;
         }
+        reinterpret_cast<T*>(&s[x * STR + l])[h] = p;
       }
     }
-  }
-  if constexpr (PRO == 1) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       nless += __shfl_down_sync(0xffffffffu, nless, off);
@@ -129,6 +121,12 @@ k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict_
     const cpx<T> b = mk<T>((T)0.5 * d.y, (T)-0.5 * d.x);
     const int y = y0 + 2 * l;
     const size_t o = ((size_t)k * Nz + z) * Ny + y;
+    if constexpr (sizeof(T) == 4) {
+      if (y + 1 < Ny && (Ny & 1) == 0) {  // o even: a 16-byte aligned pair
+        *reinterpret_cast<float4*>(&out[o]) = make_float4(a.x, a.y, b.x, b.y);
+        continue;
+      }
+    }
     if (y < Ny) out[o] = a;
     if (y + 1 < Ny) out[o + 1] = b;
   }
@@ -138,7 +136,13 @@ k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict_
 // out0 = c2r(m0 * in) * s0 with m0 = i dqx kx if MUL0 else 1
 // out1 = c2r(i dqx kx * in) * s1          (NOUT == 2)
 // one tile (rows y0 .. y0 + 2 LB of plane z); bx is the tile's index along y;
-// mask0 / mask1: node bitsets limiting the stores of output 0 / 1 (null: all)
+// mask0 / mask1 limit the stores of output 0 / 1 (null: all) to the 32-byte
+// sectors whose bit is set: bit g covers nodes [g G, g G + G), G = 32 / sizeof(T),
+// so a store never fills part of a sector.  The tile's mask words are staged
+// in shared memory behind the FFT lines (xc2r_mask_words of them).
+template <typename T, int N, int LB>
+constexpr int xc2r_mask_words() { return (2 * LB * N) / ((32 / (int)sizeof(T)) * 32) + 2; }
+
 template <typename T, int N, int LB, bool MUL0, int NOUT>
 PHAFD_D void xc2r_tile(int bx, int z, const cpx<T>* __restrict__ in, T* __restrict__ out0, T* __restrict__ out1,
                        T s0, T s1, T dq, const cpx<T>* __restrict__ tw, int Ny, int Nz, const NanArgs& nan,
@@ -146,7 +150,17 @@ PHAFD_D void xc2r_tile(int bx, int z, const cpx<T>* __restrict__ in, T* __restri
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = LB * NOUT;
   constexpr int NT = N * NL / 16, STR = NL + 1;
+  constexpr int G = 32 / (int)sizeof(T);
   const int y0 = bx * 2 * LB;
+  uint32_t* mw = reinterpret_cast<uint32_t*>(s + (size_t)N * STR);
+  const size_t row0 = ((size_t)z * Ny + y0) * N;
+  const size_t w0 = (row0 / G) >> 5;
+  if (mask0 || mask1) {
+    const int rows = Ny - y0 < 2 * LB ? Ny - y0 : 2 * LB;
+    const int nw = (int)((((row0 + (size_t)rows * N - 1) / G) >> 5) - w0 + 1);
+    const uint32_t* m = mask0 ? mask0 : mask1;
+    for (int i = threadIdx.x; i < nw; i += NT) mw[i] = m[w0 + i];
+  }
   TILE_LOOP(idx, LB * (N / 2 + 1), NT) {
     const int l = idx % LB, k = idx / LB;
     const int y = y0 + 2 * l;
@@ -178,8 +192,8 @@ PHAFD_D void xc2r_tile(int bx, int z, const cpx<T>* __restrict__ in, T* __restri
         if (y < Ny) {
           const T val = (h == 0 ? v.x : v.y) * sc;
           const size_t node = ((size_t)z * Ny + y) * N + x;
-          const uint32_t* mk = q == 0 ? mask0 : mask1;
-          if (!mk || ((mk[node >> 5] >> (node & 31)) & 1u)) out[node] = val;
+          const size_t sec = node / G;
+          if (!(q == 0 ? mask0 : mask1) || ((mw[(sec >> 5) - w0] >> (sec & 31)) & 1u)) out[node] = val;
           if (q == 0 && nan.check && z == 0 && y == 0 && x == 0 && isnan(val))
             atomicCAS(reinterpret_cast<unsigned long long*>(nan.nan_step), (unsigned long long)-1LL,
                       (unsigned long long)(*nan.d_step));
@@ -502,7 +516,7 @@ struct Axis {
   static int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
                   cudaStream_t st) {
     constexpr int LB = NLT;
-    const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>) * (dep ? 2 : 1);
+    const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
     dim3 grid((g.ny + 2 * LB - 1) / (2 * LB), g.nz);
     if (dep) {
       auto k = k_xr2c<T, N, LB, 1>;
@@ -569,7 +583,7 @@ struct Axis {
                    const int* gmask_off, cudaStream_t st) {
     constexpr int LB2 = NLT / 2 >= 1 ? NLT / 2 : 1;
     if (2 * LB2 != NLT) return -3;
-    const size_t sm = (size_t)N * (2 * LB2 + 1) * sizeof(cpx<T>);
+    const size_t sm = (size_t)N * (2 * LB2 + 1) * sizeof(cpx<T>) + 4 * (size_t)xc2r_mask_words<T, N, 2 * LB2>();
     const int nb0 = (g.ny + 2 * LB2 - 1) / (2 * LB2), nb1 = (g.ny + 4 * LB2 - 1) / (4 * LB2);
     auto k = k_xc2r3<T, N, LB2>;
     if (set_smem(k, sm)) return -1;
@@ -670,9 +684,21 @@ int GridOps<T>::xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T
   return -2;
 }
 
+namespace r256 {
+template <typename T>
+int ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw, cudaStream_t st);
+template <typename T>
+int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E, const cpx<T>* tw,
+          cudaStream_t st);
+template <typename T>
+int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
+           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only, cudaStream_t st);
+}
+
 template <typename T>
 int GridOps<T>::yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E,
                       const cpx<T>* tw, cudaStream_t st) {
+  if (g.ny == 256) return r256::yinv2<T>(g, A, C, D, B, E, tw, st);
   switch (g.ny) {
 #define CASE(n) case n: return Axis<T, n>::yinv2(g, A, C, D, B, E, tw, st);
     PHAFD_FOR_SIZES(CASE)
@@ -684,6 +710,7 @@ int GridOps<T>::yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, cons
 template <typename T>
 int GridOps<T>::ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
                       cudaStream_t st) {
+  if (g.ny == 256) return r256::ypass<T>(g, sign, in, out0, out1, tw, st);
   switch (g.ny) {
 #define CASE(n)                                                                   \
   case n:                                                                         \
@@ -695,11 +722,6 @@ int GridOps<T>::ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, c
   return -2;
 }
 
-namespace r256 {
-template <typename T>
-int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
-           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only, cudaStream_t st);
-}
 
 template <typename T>
 int GridOps<T>::zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,

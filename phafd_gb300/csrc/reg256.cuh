@@ -41,8 +41,9 @@ PHAFD_D void get16(const cpx<T>* buf, cpx<T>* v, int j, int c) {
 
 // z fft of mu + Model-B update + z ifft of phi_hat' and i qz phi_hat', for
 // Nz = 256.  Same contract as k_zfused (grid_impl.cuh).
+// FP32: at most 80 registers so three CTAs (24 warps) share an SM
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
 k_zfused256(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __restrict__ out0,
             cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny,
             UpdateArgs<T> u, int store_mu, int kx0) {
@@ -117,6 +118,124 @@ k_zfused256(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>*
       out1[col + (size_t)(j + 16 * r) * Ny] = d[r];
     }
   }
+}
+
+// Row passes (y): lines contiguous, in[line * 256 + e].  The 16 butterflies
+// of a line are 16 consecutive lanes (a warp = two lines), so every load and
+// store of a warp touches two contiguous 16-element segments, and the
+// exchange between the two radix-16 stages stays inside the warp
+// (__syncwarp, no CTA barrier).  Exchange buffer of a line: element e at
+// e + e / 16 (stride 17 between the butterflies' writes: conflict-free).
+constexpr int RS = N + N / 16;
+
+template <typename T>
+PHAFD_D void rput16(cpx<T>* rb, const cpx<T>* v, int j) {
+#pragma unroll
+  for (int r = 0; r < 16; ++r) rb[17 * j + r] = v[r];  // element 16 j + r
+}
+template <typename T>
+PHAFD_D void rget16(const cpx<T>* rb, cpx<T>* v, int j) {
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r] = rb[j + 17 * r];  // element j + 16 r
+}
+
+// v[r] = element j + 16 r of the line in, of its transform (sign S) out
+template <typename T, int S>
+PHAFD_D void row256(cpx<T>* v, cpx<T>* rb, int j, const cpx<T>* __restrict__ tw) {
+  fft::dft16<S>(v);
+  rput16(rb, v, j);
+  __syncwarp();
+  rget16(rb, v, j);
+  twiddle16<T, S>(v, j, tw);
+  fft::dft16<S>(v);
+}
+
+// 16 lines from line 16 bx: out0 = FFT_S(in), out1 = FFT_S(i dq m(e) in)
+// (NOUT == 2, which reads `in` again after storing out0: not in place)
+template <typename T, int S, int NOUT>
+PHAFD_D void yrow_tile(long long bx, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq,
+                       const cpx<T>* __restrict__ tw, long long nlines, unsigned char* smraw) {
+  const int j = threadIdx.x & 15, c = threadIdx.x >> 4;
+  cpx<T>* rb = reinterpret_cast<cpx<T>*>(smraw) + c * RS;
+  const long long line = bx * W + c;
+  const bool live = line < nlines;
+  const cpx<T>* src = in + (live ? line : 0) * N;
+  cpx<T> v[16];
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r] = live ? src[j + 16 * r] : mk<T>(0, 0);
+  row256<T, S>(v, rb, j, tw);
+  if (live) {
+#pragma unroll
+    for (int r = 0; r < 16; ++r) out0[line * N + j + 16 * r] = v[r];
+  }
+  if constexpr (NOUT == 2) {
+    __syncwarp();  // the exchange buffer is read before it is rewritten
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int e = j + 16 * r;
+      v[r] = live ? deriv(src[e], dq, wrap_index(e, N)) : mk<T>(0, 0);
+    }
+    row256<T, S>(v, rb, j, tw);
+    if (live) {
+#pragma unroll
+      for (int r = 0; r < 16; ++r) out1[line * N + j + 16 * r] = v[r];
+    }
+  }
+}
+
+template <typename T, int S, int NOUT>
+__global__ void __launch_bounds__(256)
+k_yrow256(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __restrict__ tw, long long nlines) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  yrow_tile<T, S, NOUT>(blockIdx.x, in, out0, out1, dq, tw, nlines, smraw);
+}
+
+// the two inverse y passes of the inverse chain: A -> (C, D = i qy) in CTAs
+// [0, nb), B -> E in [nb, 2 nb)
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_yinv2row256(const cpx<T>* __restrict__ A, cpx<T>* __restrict__ C, cpx<T>* __restrict__ D,
+              const cpx<T>* __restrict__ B, cpx<T>* __restrict__ E, T dq, const cpx<T>* __restrict__ tw,
+              long long nlines, long long nb) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const long long bx = blockIdx.x;
+  if (bx < nb) yrow_tile<T, +1, 2>(bx, A, C, D, dq, tw, nlines, smraw);
+  else yrow_tile<T, +1, 1>(bx - nb, B, E, nullptr, dq, tw, nlines, smraw);
+}
+
+template <typename T>
+int ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
+          cudaStream_t st) {
+  const long long nlines = (long long)g.nxh * g.nz;
+  const size_t sm = (size_t)W * RS * sizeof(cpx<T>);
+  const unsigned nb = (unsigned)((nlines + W - 1) / W);
+  const T dq = (T)g.kq[1];
+  if (out1 && (in == out0 || in == out1)) return -1;
+#define YROW(S, NO)                                                                                  \
+  {                                                                                                  \
+    auto k = k_yrow256<T, S, NO>;                                                                    \
+    if (set_smem(k, sm)) return -1;                                                                  \
+    launch_grid(k, dim3(nb), dim3(256), sm, st, in, out0, out1, dq, tw, nlines);                     \
+    return 0;                                                                                        \
+  }
+  if (sign < 0) {
+    if (out1) YROW(-1, 2) else YROW(-1, 1)
+  } else {
+    if (out1) YROW(+1, 2) else YROW(+1, 1)
+  }
+#undef YROW
+}
+
+template <typename T>
+int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E, const cpx<T>* tw,
+          cudaStream_t st) {
+  const long long nlines = (long long)g.nxh * g.nz;
+  const size_t sm = (size_t)W * RS * sizeof(cpx<T>);
+  const long long nb = (nlines + W - 1) / W;
+  auto k = k_yinv2row256<T>;
+  if (set_smem(k, sm)) return -1;
+  launch_grid(k, dim3((unsigned)(2 * nb)), dim3(256), sm, st, A, C, D, B, E, (T)g.kq[1], tw, nlines, nb);
+  return 0;
 }
 
 template <typename T>
