@@ -754,26 +754,31 @@ __global__ void k_gmask_build(BeadArgs a) {
   if (!*a.flag) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  int lo[3], hi[3];
   double u[3];
-  for (int d = 0; d < 3; ++d) {
-    u[d] = (a.x[3 * i + d] - a.boxlo[d]) / a.dx[d];
-    lo[d] = (int)floor(u[d] - a.gmask_r / a.dx[d]);
-    hi[d] = (int)ceil(u[d] + a.gmask_r / a.dx[d]);
-  }
+  for (int d = 0; d < 3; ++d) u[d] = (a.x[3 * i + d] - a.boxlo[d]) / a.dx[d];
   const double r2 = a.gmask_r * a.gmask_r;
-  for (int kz = lo[2]; kz <= hi[2]; ++kz) {
+  const int zlo = (int)floor(u[2] - a.gmask_r / a.dx[2]), zhi = (int)ceil(u[2] + a.gmask_r / a.dx[2]);
+  const int ylo = (int)floor(u[1] - a.gmask_r / a.dx[1]), yhi = (int)ceil(u[1] + a.gmask_r / a.dx[1]);
+  // per grid row inside the sphere: its x range, then one bit per sector
+  for (int kz = zlo; kz <= zhi; ++kz) {
     const double dz = (kz - u[2]) * a.dx[2];
     const int wz = ((kz % a.N[2]) + a.N[2]) % a.N[2];
-    for (int ky = lo[1]; ky <= hi[1]; ++ky) {
+    for (int ky = ylo; ky <= yhi; ++ky) {
       const double dy = (ky - u[1]) * a.dx[1];
+      const double rem = r2 - dy * dy - dz * dz;
+      if (rem < 0.0) continue;
+      const double h = sqrt(rem) / a.dx[0];
+      const int xlo = (int)ceil(u[0] - h), xhi = (int)floor(u[0] + h);
       const int wy = ((ky % a.N[1]) + a.N[1]) % a.N[1];
-      for (int kx = lo[0]; kx <= hi[0]; ++kx) {
-        const double dxx = (kx - u[0]) * a.dx[0];
-        if (dxx * dxx + dy * dy + dz * dz > r2) continue;
-        const int wx = ((kx % a.N[0]) + a.N[0]) % a.N[0];
-        const long long sec = (((long long)wz * a.N[1] + wy) * a.N[0] + wx) / a.gmask_g;
+      const long long row = ((long long)wz * a.N[1] + wy) * a.N[0];
+      for (int x = xlo; x <= xhi;) {
+        const int wx = ((x % a.N[0]) + a.N[0]) % a.N[0];
+        const long long node = row + wx;
+        const long long sec = node / a.gmask_g;
         atomicOr(a.gmask + (sec >> 5), 1u << (sec & 31));
+        // next node of this row in another sector
+        const int left = a.gmask_g - (int)(node % a.gmask_g);
+        x += left < a.N[0] - wx ? left : a.N[0] - wx;
       }
     }
   }

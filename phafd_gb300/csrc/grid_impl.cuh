@@ -58,48 +58,56 @@ k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict_
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NT = N * LB / 16, STR = LB + 1;
+  cpx<T>* sd = s + (size_t)N * STR;  // deposit rows, same layout (PRO == 1)
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * LB;
+  unsigned long long nless = 0, ngreat = 0;
   // rows 2l and 2l+1 of the tile land as the real and imaginary parts of line l
-  if constexpr (PRO == 0) {
-    TILE_LOOP(idx, LB * N, NT) {
-      const int l = idx / N, x = idx % N;
+  TILE_LOOP(idx, LB * N, NT) {
+    const int l = idx / N, x = idx % N;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int y = y0 + 2 * l + h;
-        T* dst = reinterpret_cast<T*>(&s[x * STR + l]) + h;
-        if (y < Ny) cp_async_real(dst, in0 + ((size_t)z * Ny + y) * N + x);
-        else *dst = (T)0;
+    for (int h = 0; h < 2; ++h) {
+      const int y = y0 + 2 * l + h;
+      T* dst = reinterpret_cast<T*>(&s[x * STR + l]) + h;
+      T* dstd = reinterpret_cast<T*>(&sd[x * STR + l]) + h;
+      if (y < Ny) {
+        const size_t o = ((size_t)z * Ny + y) * N + x;
+        cp_async_real(dst, in0 + o);
+        if constexpr (PRO == 1) cp_async_real(dstd, dep + o);
+      } else {
+        *dst = (T)0;
+        if constexpr (PRO == 1) *dstd = (T)0;
       }
     }
-    cp_async_commit();
-    cp_async_wait<0>();
-  } else {
-    // mu = deposit + FH(phi) on the way in (registers), one shared tile
-    unsigned long long nless = 0, ngreat = 0;
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  if constexpr (PRO == 1) {
     TILE_LOOP(idx, LB * N, NT) {
       const int l = idx / N, x = idx % N;
+      T* v = reinterpret_cast<T*>(&s[x * STR + l]);
+      const T* dd = reinterpret_cast<const T*>(&sd[x * STR + l]);
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int y = y0 + 2 * l + h;
-        T p = (T)0;
         if (y < Ny) {
-          const size_t o = ((size_t)z * Ny + y) * N + x;
-          p = in0[o];
-          const T dd = dep[o];
+          T p = v[h];
           if (fh.enabled) {
             // fixgrid_floryhuggins.cpp:72-82
             if (p <= (T)0) { p = -p; nless++; }
             else if (p >= (T)1) { p = (T)1 - (p - (T)1); ngreat++; }
-            p = dd + (T)fh.tv * (fh_log_ratio(p) + (T)fh.chi * ((T)1 - (T)2 * p));
+            p = dd[h] + (T)fh.tv * (fh_log_ratio(p) + (T)fh.chi * ((T)1 - (T)2 * p));
           } else {
-            p = dd;
+            p = dd[h];
           }
-          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[o] = p;
+          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[((size_t)z * Ny + y) * N + x] = p;
+          v[h] = p;
         }
-        reinterpret_cast<T*>(&s[x * STR + l])[h] = p;
       }
     }
+  }
+  if constexpr (PRO == 1) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       nless += __shfl_down_sync(0xffffffffu, nless, off);
@@ -516,7 +524,7 @@ struct Axis {
   static int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
                   cudaStream_t st) {
     constexpr int LB = NLT;
-    const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>);
+    const size_t sm = (size_t)N * (LB + 1) * sizeof(cpx<T>) * (dep ? 2 : 1);
     dim3 grid((g.ny + 2 * LB - 1) / (2 * LB), g.nz);
     if (dep) {
       auto k = k_xr2c<T, N, LB, 1>;
@@ -649,9 +657,28 @@ struct Axis {
 
 #define PHAFD_FOR_SIZES(M) M(16) M(32) M(64) M(96) M(128) M(160) M(256) M(512)
 
+namespace r256 {
+template <typename T>
+int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
+         cudaStream_t st);
+template <typename T>
+int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E, T* gz, T sp,
+          T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
+          const int* gmask_off, cudaStream_t st);
+template <typename T>
+int ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw, cudaStream_t st);
+template <typename T>
+int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E, const cpx<T>* tw,
+          cudaStream_t st);
+template <typename T>
+int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
+           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only, cudaStream_t st);
+}
+
 template <typename T>
 int GridOps<T>::xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
                      cudaStream_t st) {
+  if (g.nx == 256) return r256::xr2c<T>(g, in, dep, out, tw, fh, st);
   switch (g.nx) {
 #define CASE(n) case n: return Axis<T, n>::xr2c(g, in, dep, out, tw, fh, st);
     PHAFD_FOR_SIZES(CASE)
@@ -671,10 +698,12 @@ int GridOps<T>::xc2r(const Geom& g, const cpx<T>* in, T* out0, T s0, bool mul0, 
   return -2;
 }
 
+
 template <typename T>
 int GridOps<T>::xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E,
                       T* gz, T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan,
                       const uint32_t* gmask, const int* gmask_off, cudaStream_t st) {
+  if (g.nx == 256) return r256::xc2r3<T>(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
   switch (g.nx) {
 #define CASE(n) \
   case n: return Axis<T, n>::xc2r3(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
@@ -684,16 +713,6 @@ int GridOps<T>::xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T
   return -2;
 }
 
-namespace r256 {
-template <typename T>
-int ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw, cudaStream_t st);
-template <typename T>
-int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E, const cpx<T>* tw,
-          cudaStream_t st);
-template <typename T>
-int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
-           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only, cudaStream_t st);
-}
 
 template <typename T>
 int GridOps<T>::yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E,

@@ -203,6 +203,232 @@ k_yinv2row256(const cpx<T>* __restrict__ A, cpx<T>* __restrict__ C, cpx<T>* __re
   else yrow_tile<T, +1, 1>(bx - nb, B, E, nullptr, dq, tw, nlines, smraw);
 }
 
+// x c2r of 256-point rows.  A CTA takes 16 complex lines: LP = 16 / NOUT row
+// pairs (rows y0 .. y0 + 2 LP of plane z) times NOUT outputs (output 1 of
+// the spectrum times i dq kx).  Line c = q LP + l packs rows 2l (real part)
+// and 2l + 1 (imaginary part) of output q.  The half spectrum is read with
+// the lanes over y (two rows' values, 16 contiguous bytes per lane) and
+// written Hermitian-completed into the line buffers (element e at
+// e + e / 16, lines RX apart, RX odd: conflict-free in both directions);
+// each line's 16 lanes then run the 256-point inverse in registers and store
+// their rows directly, 16 consecutive nodes per lane group.  Stores of an
+// output with a mask go only to the 32-byte sectors whose bit is set.
+constexpr int RX = N + N / 16 + 1;
+
+template <typename T, int NOUT>
+PHAFD_D void xc2r_tile256(int bx, int z, const cpx<T>* __restrict__ in, T* __restrict__ out0,
+                          T* __restrict__ out1, T s0, T s1, T dq, const cpx<T>* __restrict__ tw, int Ny, int Nz,
+                          const NanArgs& nan, const uint32_t* mask0, const uint32_t* mask1, unsigned char* smraw) {
+  constexpr int LP = W / NOUT;
+  constexpr int G = 32 / (int)sizeof(T);  // nodes per 32-byte sector
+  cpx<T>* zs = reinterpret_cast<cpx<T>*>(smraw);
+  const int y0 = bx * 2 * LP;
+  TILE_LOOP(idx, (N / 2 + 1) * LP, 256) {  // unrolled: every load of a thread in flight at once
+    const int l = idx % LP, k = idx / LP;
+    const int y = y0 + 2 * l;
+    const size_t o = ((size_t)k * Nz + z) * Ny + y;
+    cpx<T> A = mk<T>(0, 0), B = mk<T>(0, 0);
+    if (y < Ny) A = in[o];
+    if (y + 1 < Ny) B = in[o + 1];
+#pragma unroll
+    for (int q = 0; q < NOUT; ++q) {
+      cpx<T> a = A, b = B;
+      if (q == 1) { a = deriv(a, dq, k); b = deriv(b, dq, k); }
+      if (k == 0 || k == N / 2) { a.y = (T)0; b.y = (T)0; }
+      cpx<T>* line = zs + (q * LP + l) * RX;
+      line[k + (k >> 4)] = mk<T>(a.x - b.y, a.y + b.x);
+      if (k > 0 && k < N / 2) line[(N - k) + ((N - k) >> 4)] = mk<T>(a.x + b.y, b.x - a.y);
+    }
+  }
+  __syncthreads();
+  const int j = threadIdx.x & 15, c = threadIdx.x >> 4;
+  const int q = c / LP, l = c % LP;
+  cpx<T>* rb = zs + c * RX;
+  cpx<T> v[16];
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r] = rb[j + 17 * r];  // element j + 16 r
+  __syncwarp();
+  row256<T, +1>(v, rb, j, tw);
+  T* out = q == 0 ? out0 : out1;
+  const T sc = q == 0 ? s0 : s1;
+  const uint32_t* msk = q == 0 ? mask0 : mask1;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int y = y0 + 2 * l + h;
+    if (y >= Ny) continue;
+    const size_t row = ((size_t)z * Ny + y) * N;
+    // the row's sectors are N / G consecutive bits starting at a word boundary
+    uint32_t m0 = ~0u, m1 = ~0u;
+    if (msk) {
+      m0 = msk[(row / G) >> 5];
+      if constexpr (N / G > 32) m1 = msk[((row / G) >> 5) + 1];
+    }
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int x = j + 16 * r;
+      const T val = (h == 0 ? v[r].x : v[r].y) * sc;
+      const int sec = x / G;
+      const uint32_t bit = sec < 32 ? (m0 >> sec) & 1u : (m1 >> (sec & 31)) & 1u;
+      if (bit) out[row + x] = val;
+      if (q == 0 && nan.check && z == 0 && y == 0 && x == 0 && isnan(val))
+        atomicCAS(reinterpret_cast<unsigned long long*>(nan.nan_step), (unsigned long long)-1LL,
+                  (unsigned long long)(*nan.d_step));
+    }
+  }
+}
+
+// x r2c of 256-point rows, optionally fused with mu = deposit + FH(phi)
+// (PRO == 1).  A CTA takes rows y0 .. y0 + 32 of plane z: 16-byte
+// asynchronous copies of the rows (phi, and the deposit) to shared memory,
+// then line c (rows 2c, 2c + 1 as real and imaginary parts) is formed by its
+// 16 lanes, transformed in registers and written back to its line buffer;
+// the Hermitian split of every line's spectrum goes out with the lanes over
+// y, two rows' modes (16 contiguous bytes) per lane.
+template <typename T, int PRO>
+__global__ void __launch_bounds__(256)
+k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict__ out,
+          const cpx<T>* __restrict__ tw, int Ny, int Nz, FHArgs fh) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int ROWS = 2 * W;
+  T* sphi = reinterpret_cast<T*>(smraw);  // [ROWS][N]
+  T* sdep = sphi + ROWS * N;              // [ROWS][N] (PRO == 1)
+  const int z = blockIdx.y;
+  const int y0 = blockIdx.x * ROWS;
+  constexpr int PER = 16 / (int)sizeof(T);  // reals per 16-byte copy
+  for (int i = threadIdx.x; i < ROWS * N / PER; i += 256) {
+    const int row = i / (N / PER), x = (i % (N / PER)) * PER;
+    const int y = y0 + row;
+    if (y < Ny) {
+      const size_t o = ((size_t)z * Ny + y) * N + x;
+      cp_async16(sphi + row * N + x, in0 + o);
+      if constexpr (PRO == 1) cp_async16(sdep + row * N + x, dep + o);
+    }
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  const int j = threadIdx.x & 15, c = threadIdx.x >> 4;
+  cpx<T> v[16];
+  unsigned long long nless = 0, ngreat = 0;
+#pragma unroll
+  for (int r = 0; r < 16; ++r) {
+    const int x = j + 16 * r;
+    T pr[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int row = 2 * c + h;
+      T p = (T)0;
+      if (y0 + row < Ny) {
+        p = sphi[row * N + x];
+        if constexpr (PRO == 1) {
+          const T dd = sdep[row * N + x];
+          if (fh.enabled) {
+            // fixgrid_floryhuggins.cpp:72-82
+            if (p <= (T)0) { p = -p; nless++; }
+            else if (p >= (T)1) { p = (T)1 - (p - (T)1); ngreat++; }
+            p = dd + (T)fh.tv * (fh_log_ratio(p) + (T)fh.chi * ((T)1 - (T)2 * p));
+          } else {
+            p = dd;
+          }
+          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[((size_t)z * Ny + y0 + row) * N + x] = p;
+        }
+      }
+      pr[h] = p;
+    }
+    v[r] = mk<T>(pr[0], pr[1]);
+  }
+  if constexpr (PRO == 1) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      nless += __shfl_down_sync(0xffffffffu, nless, off);
+      ngreat += __shfl_down_sync(0xffffffffu, ngreat, off);
+    }
+    if ((threadIdx.x & 31) == 0 && (nless | ngreat)) {
+      if (nless) atomicAdd(fh.counters + 0, nless);
+      if (ngreat) atomicAdd(fh.counters + 1, ngreat);
+    }
+  }
+  __syncthreads();  // the row tiles are read: their memory becomes the line buffers
+  cpx<T>* zs = reinterpret_cast<cpx<T>*>(smraw);
+  cpx<T>* rb = zs + c * RX;
+  row256<T, -1>(v, rb, j, tw);
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 16; ++r) rb[j + 17 * r] = v[r];  // mode j + 16 r
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < (N / 2 + 1) * W; idx += 256) {
+    const int l = idx % W, k = idx / W;
+    const cpx<T>* line = zs + l * RX;
+    const int km = (N - k) % N;
+    const cpx<T> zk = line[k + (k >> 4)];
+    const cpx<T> zm = conjg(line[km + (km >> 4)]);
+    const cpx<T> a = scale(zk + zm, (T)0.5);
+    const cpx<T> d = zk - zm;
+    const cpx<T> b = mk<T>((T)0.5 * d.y, (T)-0.5 * d.x);
+    const int y = y0 + 2 * l;
+    const size_t o = ((size_t)k * Nz + z) * Ny + y;
+    if constexpr (sizeof(T) == 4) {
+      if (y + 1 < Ny && (Ny & 1) == 0) {  // o even: a 16-byte aligned pair
+        *reinterpret_cast<float4*>(&out[o]) = make_float4(a.x, a.y, b.x, b.y);
+        continue;
+      }
+    }
+    if (y < Ny) out[o] = a;
+    if (y + 1 < Ny) out[o + 1] = b;
+  }
+}
+
+template <typename T>
+int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
+         cudaStream_t st) {
+  const size_t tiles = (size_t)2 * W * N * sizeof(T) * (dep ? 2 : 1);
+  const size_t lines = (size_t)W * RX * sizeof(cpx<T>);
+  const size_t sm = tiles > lines ? tiles : lines;
+  dim3 grid((g.ny + 2 * W - 1) / (2 * W), g.nz);
+  if (dep) {
+    auto k = k_xr2c256<T, 1>;
+    if (set_smem(k, sm)) return -1;
+    launch_grid(k, grid, dim3(256), sm, st, in, dep, out, tw, g.ny, g.nz, fh);
+  } else {
+    auto k = k_xr2c256<T, 0>;
+    if (set_smem(k, sm)) return -1;
+    launch_grid(k, grid, dim3(256), sm, st, in, dep, out, tw, g.ny, g.nz, fh);
+  }
+  return 0;
+}
+
+// the inverse chain's three x c2r in one launch: C -> (phi, dphi/dx) in CTAs
+// [0, nb0), D -> dphi/dy in [nb0, nb0 + nb1), E -> dphi/dz after
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_xc2r3_256(const cpx<T>* __restrict__ C, T* __restrict__ phi, T* __restrict__ gx, const cpx<T>* __restrict__ D,
+            T* __restrict__ gy, const cpx<T>* __restrict__ E, T* __restrict__ gz, T sp, T sg, T dq,
+            const cpx<T>* __restrict__ tw, int Ny, int Nz, NanArgs nan, NanArgs nonan, int nb0, int nb1,
+            const uint32_t* __restrict__ mask, const int* __restrict__ mask_off) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int bx = blockIdx.x, z = blockIdx.y;
+  const uint32_t* gm = mask && !*mask_off ? mask : nullptr;
+  if (bx < nb0)
+    xc2r_tile256<T, 2>(bx, z, C, phi, gx, sp, sg, dq, tw, Ny, Nz, nan, nullptr, gm, smraw);
+  else if (bx < nb0 + nb1)
+    xc2r_tile256<T, 1>(bx - nb0, z, D, gy, nullptr, sg, sg, dq, tw, Ny, Nz, nonan, gm, nullptr, smraw);
+  else
+    xc2r_tile256<T, 1>(bx - nb0 - nb1, z, E, gz, nullptr, sg, sg, dq, tw, Ny, Nz, nonan, gm, nullptr, smraw);
+}
+
+template <typename T>
+int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E, T* gz, T sp,
+          T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
+          const int* gmask_off, cudaStream_t st) {
+  const size_t sm = (size_t)W * RX * sizeof(cpx<T>);
+  const int nb0 = (g.ny + W - 1) / W, nb1 = (g.ny + 2 * W - 1) / (2 * W);
+  auto k = k_xc2r3_256<T>;
+  if (set_smem(k, sm)) return -1;
+  launch_grid(k, dim3(nb0 + 2 * nb1, g.nz), dim3(256), sm, st, C, phi, gx, D, gy, E, gz, sp, sg, (T)g.kq[0], tw,
+              g.ny, g.nz, nan, nonan, nb0, nb1, gmask, gmask_off);
+  return 0;
+}
+
 template <typename T>
 int ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
           cudaStream_t st) {
