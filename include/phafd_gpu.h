@@ -190,6 +190,8 @@ int phafd_set_linear_substeps(phafd_ctx* ctx, int nsub, double f2);
  * device (fix parameters such as noise may differ) */
 int phafd_ctx_copy_state(phafd_ctx* dst, phafd_ctx* src);
 int phafd_grid_device(phafd_ctx* ctx, int field, void** dev);
+/* copy a real field into the device array dst (nx*ny*nz, context precision) */
+int phafd_grid_copy_device(phafd_ctx* ctx, int field, void* dst);
 int phafd_deposit_density(phafd_ctx* ctx, void* rho);
 int phafd_grid_add_device(phafd_ctx* ctx, const void* src, double scale);
 

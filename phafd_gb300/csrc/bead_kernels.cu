@@ -339,74 +339,109 @@ __global__ void k_build(BeadArgs a) {
 // (grid list); the cutoff carries a 1e-5 relative margin, so the lists are
 // supersets of the exact ones (the extra pairs lie beyond every interaction
 // cutoff, which the pair kernel tests again each step).
+// exclusive prefix sum over the L lanes of a group, and the group total
+template <int L>
+PHAFD_D int group_scan(int v, int lane, int& total) {
+  int inc = v;
+#pragma unroll
+  for (int d = 1; d < L; d <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, d, L);
+    if (lane >= d) inc += t;
+  }
+  total = __shfl_sync(0xffffffffu, inc, L - 1, L);
+  return inc - v;
+}
+
+// L lanes per bead (L = 8 while the beads alone would leave most of the GPU
+// idle, else 1): lane l takes stencil bins l, l + L, ... and grid rows l,
+// l + L, ... of the bead; with L > 1 each list is written in (lane, bin or
+// row, member) order after a count pass and a prefix sum over the lanes, so
+// the lists do not depend on timing.
+template <int L>
 __global__ void k_build_fp32(BeadArgs a) {
   if (!*a.flag) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gt / L, lane = gt % L;
+  const bool live = i < a.n;  // dead lanes still take part in the group shuffles
+  const int ii = live ? i : 0;
   const float cut2 = (float)(a.cutneighsq * (1.0 + 1e-5));
   if (a.nbr) {
-    const int b = a.bin_of[i];
+    const int b = a.bin_of[ii];
     const int bx = b % a.nb[0], by = (b / a.nb[0]) % a.nb[1], bz = b / (a.nb[0] * a.nb[1]);
-    const float4 oi = a.bin_off[i];
+    const float4 oi = a.bin_off[ii];
     const float bs[3] = {(float)(a.period[0] / a.nb[0]), (float)(a.period[1] / a.nb[1]), (float)(a.period[2] / a.nb[2])};
-    int cnt = 0;
-    for (int dz = -1; dz <= 1; ++dz) {
-      int cz = bz + dz, sz = 0;
-      if (cz < 0) { cz += a.nb[2]; sz = -1; } else if (cz >= a.nb[2]) { cz -= a.nb[2]; sz = 1; }
-      if (sz != 0 && !a.zperiodic) continue;
-      for (int dy = -1; dy <= 1; ++dy) {
+    // visit(write): count (write == false) or store the entries of this lane's bins
+    auto visit = [&](bool write, int base) {
+      int cnt = 0;
+      for (int st = lane; st < 27 && live; st += L) {
+        const int dx = st % 3 - 1, dy = (st / 3) % 3 - 1, dz = st / 9 - 1;
+        int cz = bz + dz, sz = 0;
+        if (cz < 0) { cz += a.nb[2]; sz = -1; } else if (cz >= a.nb[2]) { cz -= a.nb[2]; sz = 1; }
+        if (sz != 0 && !a.zperiodic) continue;
         int cy = by + dy, sy = 0;
         if (cy < 0) { cy += a.nb[1]; sy = -1; } else if (cy >= a.nb[1]) { cy -= a.nb[1]; sy = 1; }
-        for (int dx = -1; dx <= 1; ++dx) {
-          int cx = bx + dx, sx = 0;
-          if (cx < 0) { cx += a.nb[0]; sx = -1; } else if (cx >= a.nb[0]) { cx -= a.nb[0]; sx = 1; }
-          const int nbn = (cz * a.nb[1] + cy) * a.nb[0] + cx;
-          const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
-          // x_i - (x_j + s L) = (b_i - b_j' ) bs + off_i - off_j, with b_j' = c + s nb
-          const float ex = (float)(bx - (cx + sx * a.nb[0])) * bs[0] + oi.x;
-          const float ey = (float)(by - (cy + sy * a.nb[1])) * bs[1] + oi.y;
-          const float ez = (float)(bz - (cz + sz * a.nb[2])) * bs[2] + oi.z;
-          for (int p = a.bin_start[nbn]; p < a.bin_start[nbn + 1]; ++p) {
-            const int j = a.sorted[p];
-            if (j == i && code == 13) continue;
-            const float4 oj = a.bin_off[j];
-            const float d0 = ex - oj.x, d1 = ey - oj.y, d2 = ez - oj.z;
-            if (d0 * d0 + d1 * d1 + d2 * d2 <= cut2) {
-              if (cnt < a.maxnb) a.nbr[(size_t)i * a.maxnb + cnt] = (j << 5) | code;
-              ++cnt;
-            }
+        int cx = bx + dx, sx = 0;
+        if (cx < 0) { cx += a.nb[0]; sx = -1; } else if (cx >= a.nb[0]) { cx -= a.nb[0]; sx = 1; }
+        const int nbn = (cz * a.nb[1] + cy) * a.nb[0] + cx;
+        const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
+        // x_i - (x_j + s L) = (b_i - b_j') bs + off_i - off_j, with b_j' = c + s nb
+        const float ex = (float)(bx - (cx + sx * a.nb[0])) * bs[0] + oi.x;
+        const float ey = (float)(by - (cy + sy * a.nb[1])) * bs[1] + oi.y;
+        const float ez = (float)(bz - (cz + sz * a.nb[2])) * bs[2] + oi.z;
+        const int p1 = a.bin_start[nbn + 1];
+        for (int p = a.bin_start[nbn]; p < p1; ++p) {
+          const int j = a.sorted[p];
+          if (j == i && code == 13) continue;
+          const float4 oj = a.bin_off[j];
+          const float d0 = ex - oj.x, d1 = ey - oj.y, d2 = ez - oj.z;
+          if (d0 * d0 + d1 * d1 + d2 * d2 <= cut2) {
+            if (write && base + cnt < a.maxnb) a.nbr[(size_t)i * a.maxnb + base + cnt] = (j << 5) | code;
+            ++cnt;
           }
         }
       }
+      return cnt;
+    };
+    int total;
+    if constexpr (L == 1) {
+      total = visit(true, 0);
+    } else {
+      const int mine = visit(false, 0);
+      const int off = group_scan<L>(mine, lane, total);
+      visit(true, off);
     }
-    if (cnt > a.maxnb) { atomicOr(a.status, ST_OVERFLOW); cnt = a.maxnb; }
-    a.nnbr[i] = cnt;
+    if (live && lane == 0) {
+      if (total > a.maxnb) { atomicOr(a.status, ST_OVERFLOW); total = a.maxnb; }
+      a.nnbr[i] = total;
+    }
   }
-  const double xi[3] = {a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2]};
+  const double xi[3] = {a.x[3 * ii], a.x[3 * ii + 1], a.x[3 * ii + 2]};
   if (a.gl) {
     int gi[3];
     float gf[3], dxf[3];
     for (int d = 0; d < 3; ++d) {
-      const double ud = (xi[d] - a.boxlo[d]) / a.dx[d];
+      const double ud = (xi[d] - a.boxlo[d]) * a.invdx[d];
       const double fl = floor(ud);
       gi[d] = (int)fl;
       gf[d] = (float)(ud - fl);
       dxf[d] = (float)a.dx[d];
     }
     const float cut = (float)a.cutneigh * 1.00001f;
-    int cnt = 0;
     const int rz = (int)ceilf(cut / dxf[2]) + 1;
-    for (int oz = -rz; oz <= rz; ++oz) {
-      const int kz = gi[2] + oz;
-      int wz = kz, sz = 0;
-      if (wz < 0) { wz += a.N[2]; sz = 1; } else if (wz >= a.N[2]) { wz -= a.N[2]; sz = -1; }
-      if (wz < 0 || wz >= a.N[2]) continue;
-      if (sz != 0 && !a.zperiodic) continue;
-      const float dz = ((float)oz - gf[2]) * dxf[2];
-      const float remz = cut2 - dz * dz;
-      if (remz < 0.f) continue;
-      const int ry = (int)ceilf(sqrtf(remz) / dxf[1]) + 1;
-      for (int oy = -ry; oy <= ry; ++oy) {
+    const int ry = (int)ceilf(cut / dxf[1]) + 1;
+    const int nrow = (2 * rz + 1) * (2 * ry + 1);
+    auto visit = [&](bool write, int base) {
+      int cnt = 0;
+      for (int row = lane; row < nrow && live; row += L) {
+        const int oz = row / (2 * ry + 1) - rz, oy = row % (2 * ry + 1) - ry;
+        const int kz = gi[2] + oz;
+        int wz = kz, sz = 0;
+        if (wz < 0) { wz += a.N[2]; sz = 1; } else if (wz >= a.N[2]) { wz -= a.N[2]; sz = -1; }
+        if (wz < 0 || wz >= a.N[2]) continue;
+        if (sz != 0 && !a.zperiodic) continue;
+        const float dz = ((float)oz - gf[2]) * dxf[2];
+        const float remz = cut2 - dz * dz;
+        if (remz < 0.f) continue;
         const int ky = gi[1] + oy;
         int wy = ky, sy = 0;
         if (wy < 0) { wy += a.N[1]; sy = 1; } else if (wy >= a.N[1]) { wy -= a.N[1]; sy = -1; }
@@ -422,20 +457,35 @@ __global__ void k_build_fp32(BeadArgs a) {
           if (wx < 0 || wx >= a.N[0]) continue;
           const float dxx = ((float)ox - gf[0]) * dxf[0];
           if (dxx * dxx + dy * dy + dz * dz <= cut2) {
-            const uint32_t node = (uint32_t)(((long long)wz * a.N[1] + wy) * a.N[0] + wx);
-            const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
-            if (cnt < a.maxg) a.gl[(size_t)i * a.maxg + cnt] = (node << 5) | (uint32_t)code;
+            if (write && base + cnt < a.maxg) {
+              const uint32_t node = (uint32_t)(((long long)wz * a.N[1] + wy) * a.N[0] + wx);
+              const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
+              a.gl[(size_t)i * a.maxg + base + cnt] = (node << 5) | (uint32_t)code;
+            }
             ++cnt;
           }
         }
       }
+      return cnt;
+    };
+    int total;
+    if constexpr (L == 1) {
+      total = visit(true, 0);
+    } else {
+      const int mine = visit(false, 0);
+      const int off = group_scan<L>(mine, lane, total);
+      visit(true, off);
     }
-    if (cnt > a.maxg) { atomicOr(a.status, ST_OVERFLOW); cnt = a.maxg; }
-    a.ngl[i] = cnt;
+    if (live && lane == 0) {
+      if (total > a.maxg) { atomicOr(a.status, ST_OVERFLOW); total = a.maxg; }
+      a.ngl[i] = total;
+    }
   }
-  a.xhold[3 * i] = xi[0];
-  a.xhold[3 * i + 1] = xi[1];
-  a.xhold[3 * i + 2] = xi[2];
+  if (live && lane == 0) {
+    a.xhold[3 * i] = xi[0];
+    a.xhold[3 * i + 1] = xi[1];
+    a.xhold[3 * i + 2] = xi[2];
+  }
 }
 
 __global__ void k_build_done(BeadArgs a) {
@@ -499,12 +549,13 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
     const int cnt = a.ngl[i];
     const int t = a.type[i];
     const T cutsq = (T)p.ga_cutsq[t], eps = (T)p.ga_eps[t], phit = (T)p.ga_phi[t];
-    // bead position in grid units: integer part + fraction (FP32 path)
+    // bead position in grid units: integer part + fraction (FP32 path; GB300's
+    // FP64 rate makes a divide per axis and thread cost more than the rest)
     int gi[3];
     T gf[3], dxf[3];
     const double xi[3] = {xi0, xi1, xi2};
     for (int d = 0; d < 3; ++d) {
-      const double ud = (xi[d] - a.boxlo[d]) / a.dx[d];
+      const double ud = (xi[d] - a.boxlo[d]) * a.invdx[d];
       const double fl = floor(ud);
       gi[d] = (int)fl;
       gf[d] = (T)(ud - fl);
@@ -810,7 +861,14 @@ void launch_rebuild(const BeadArgs& a, cudaStream_t st) {
   k_scan_add<<<nblocks, 1024, 0, st>>>(a);
   k_bin_fill<<<nblk(a.n, T), T, 0, st>>>(a);
   k_bin_sort<<<nblk(a.nbins, T) > 4096 ? 4096 : nblk(a.nbins, T), T, 0, st>>>(a);
-  if (a.fp32_lists) k_build_fp32<<<nblk(a.n, 128), 128, 0, st>>>(a);
+  if (a.fp32_lists) {
+    // 8-lane groups while 8 n threads stay within one wave (2048 per SM)
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if ((long long)a.n * 8 <= (long long)nsm * 2048) k_build_fp32<8><<<nblk((long long)a.n * 8, 128), 128, 0, st>>>(a);
+    else k_build_fp32<1><<<nblk(a.n, 128), 128, 0, st>>>(a);
+  }
   else k_build<<<nblk(a.n, 128), 128, 0, st>>>(a);
   if (a.gmask) {
     k_gmask_clear<<<1024, 256, 0, st>>>(a);

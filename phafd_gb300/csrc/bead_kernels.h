@@ -19,6 +19,7 @@ struct BeadArgs {
   double *x, *ux, *f, *xhold, *fchain, *tang;
   int *image, *type;
   double boxlo[3], boxhi[3], period[3];
+  double invdx[3];      // 1 / grid spacing (FP32 pair path: one FP64 multiply instead of a divide)
   double triggersq, cutneigh, cutneighsq;
   int* flag;            // rebuild requested (device)
   uint32_t* gmask;      // bit per 32-byte sector of a grid field (gmask_g nodes) holding a node within gmask_r

@@ -340,13 +340,15 @@ struct phafd_ctx {
     cpx<T>* E = wE.as<cpx<T>>();
     NanArgs nan{nan_check ? 1 : 0, d_nan(), d_step()};
     NanArgs nonan{0, d_nan(), d_step()};
-    if (grad && phi_out && !profiling) {
+    if (grad && phi_out) {
       // one launch per direction for the whole inverse chain
       int rc = GridOps<T>::yinv2(geom, A, Cc, D, B, E, twi[1], st);
       if (rc != -3) {
         chk(rc, "y ifft");
+        mark(8);
         chk(GridOps<T>::xc2r3(geom, Cc, phi_out, gx.as<T>(), D, gy.as<T>(), E, gz.as<T>(), sp, sg, twi[0], nan, nonan,
                               masked ? gmask.as<uint32_t>() : nullptr, d_gmask_off(), st), "x c2r");
+        mark(9);
         return;
       }
     }
@@ -405,6 +407,7 @@ struct phafd_ctx {
       a.boxlo[d] = boxlo[d]; a.boxhi[d] = boxhi[d]; a.period[d] = period[d];
       a.N[d] = N[d];
       a.dx[d] = gridset ? period[d] / N[d] : 1.0;
+      a.invdx[d] = 1.0 / a.dx[d];
     }
     a.triggersq = 0.25 * skin * skin;
     a.cutneigh = cutneigh;
@@ -861,10 +864,15 @@ int phafd_ctx_create(phafd_ctx** out, int device, int precision) {
   c->precision = precision;
   try {
     CK(cudaSetDevice(device));
-    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&c->st3, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&c->stc, cudaStreamNonBlocking));
+    // highest priority: a step's chain of small bead kernels is scheduled
+    // ahead of concurrent bulk work on other streams (the network inference
+    // that overlaps a macro step)
+    int plo = 0, phi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&plo, &phi));
+    CK(cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, phi));
+    CK(cudaStreamCreateWithPriority(&c->st2, cudaStreamNonBlocking, phi));
+    CK(cudaStreamCreateWithPriority(&c->st3, cudaStreamNonBlocking, phi));
+    CK(cudaStreamCreateWithPriority(&c->stc, cudaStreamNonBlocking, phi));
     for (cudaEvent_t* e : {&c->ev_fork, &c->ev_dep, &c->ev_join, &c->ev_pl_fork, &c->ev_pl_join})
       CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     c->d_counters.alloc(7 * sizeof(long long));
@@ -1562,6 +1570,20 @@ int phafd_grid_device(phafd_ctx* c, int field, void** dev) {
   if (!b) throw std::invalid_argument("bad field");
   if (field == PHAFD_FIELD_GRADX || field == PHAFD_FIELD_GRADY || field == PHAFD_FIELD_GRADZ) c->full_gradient();
   *dev = b->p;
+  API_END(c)
+}
+
+int phafd_grid_copy_device(phafd_ctx* c, int field, void* dst) {
+  API_BEGIN(c)
+  if (!c->gridset || !dst) throw std::invalid_argument("grid not created");
+  if (field == PHAFD_FIELD_GRADX || field == PHAFD_FIELD_GRADY || field == PHAFD_FIELD_GRADZ) c->full_gradient();
+  const DevBuf* b = field == PHAFD_FIELD_PHI ? &c->phi : field == PHAFD_FIELD_GRADX ? &c->gx
+                  : field == PHAFD_FIELD_GRADY ? &c->gy : field == PHAFD_FIELD_GRADZ ? &c->gz
+                  : field == PHAFD_FIELD_CHEMPOT ? &c->dep : nullptr;
+  if (!b) throw std::invalid_argument("bad field");
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(dst, b->p, c->nreal * c->rsz(), cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
   API_END(c)
 }
 

@@ -354,6 +354,57 @@ PHAFD_D void store_inputs(unsigned char* tile, int i, int x, const float* v) {
   *reinterpret_cast<uint4*>(tile + tile_off(i, x, 8)) = q[1];
 }
 
+// x-stage DFT of v0 = P in + pb for inference.  v0 is affine in the inputs
+// (phi_n, rho_n, chi_n), so its partial DFT over an x-half is
+//   vx[c][k] = P[c][0] Phi[k] + P[c][1] Rho[k] + (P[c][2] chi_n + pb[c]) O[k]
+// with Phi, Rho the partial DFTs of the two input fields and O[k] the sum of
+// the table row k over the half: two 128-point DFTs per row instead of a
+// 32-channel pass.  One warp per (row, half): lane (f, k) sums field f
+// against table row k (table staged transposed, conflict-free), then lane c
+// writes its 16 values of channel c.
+constexpr int LXW = 8;  // warps (rows) per CTA
+__global__ void __launch_bounds__(LXW * 32) k_lift_xdft(LiftIn in, const bf16* __restrict__ Pb,
+                                                       const float* __restrict__ pb, const bf16* __restrict__ Ftab,
+                                                       const float* __restrict__ osum, float* __restrict__ vx,
+                                                       Dims d) {
+  __shared__ float ft[TX][KR + 1];     // table of this half, [x][k]
+  __shared__ float fld[LXW][2][TX];    // phi_n, rho_n of each warp's row
+  const int h = blockIdx.x % d.H;
+  const long long row = (long long)(blockIdx.x / d.H) * LXW + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int q = threadIdx.x; q < KR * TX; q += LXW * 32) {
+    const int k = q / TX, x = q % TX;
+    ft[x][k] = __bfloat162float(Ftab[(size_t)k * d.Nx + h * TX + x]);
+  }
+  const bool live = row < d.rows;
+  if (live) {
+    const size_t base = (size_t)row * d.Nx + (size_t)h * TX;
+    for (int x = lane; x < TX; x += 32) {
+      fld[w][0][x] = (in.phi[base + x] - in.n0) / in.n1;
+      fld[w][1][x] = (in.rho[base + x] - in.n2) / in.n3;
+    }
+  }
+  __syncthreads();
+  if (!live) return;
+  const int f = lane >> 4, k = lane & 15;
+  float acc = 0.f;
+#pragma unroll 8
+  for (int x = 0; x < TX; ++x) acc += fld[w][f][x] * ft[x][k];
+  const int c = lane;
+  const float p0 = __bfloat162float(Pb[c * 16 + 0]), p1 = __bfloat162float(Pb[c * 16 + 1]);
+  const float cst = __bfloat162float(Pb[c * 16 + 2]) * in.chi_n + pb[c];
+  float v[KR];
+#pragma unroll
+  for (int kk = 0; kk < KR; ++kk) {
+    const float phik = __shfl_sync(0xffffffffu, acc, kk);
+    const float rhok = __shfl_sync(0xffffffffu, acc, 16 + kk);
+    v[kk] = p0 * phik + p1 * rhok + cst * osum[h * KR + kk];
+  }
+  float4* o = reinterpret_cast<float4*>(vx + (((size_t)row * d.H + h) * C + c) * KR);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+}
+
 // v0 = P in + pb; x-stage DFT of v0
 __global__ void __launch_bounds__(NTH) k_lift(LiftIn in, const bf16* __restrict__ Pb, const float* __restrict__ pb,
                                                const bf16* __restrict__ Ftab, bf16* __restrict__ v0,
@@ -914,39 +965,48 @@ __global__ void __launch_bounds__(NTH) k_layer_bwd(const bf16* __restrict__ delt
 // ------------------------------------------------------------------ y and z stages (FP32)
 // forward DFT along y of the x-stage partials (summed over halves):
 // out[z][ky'][kx][c] += sum_{y in chunk} in(z, y, kx, c) e^{-2 pi i ky y / Ny}
-// grid (Nz, Ny / YCH); out must be zeroed; the chunk sums meet in atomics.
+// grid (Nz, Ny / ych), ych = min(Ny, 64) rows per CTA walked 16 at a time;
+// out must be zeroed; the chunk sums meet in atomics (Ny / ych per output).
 constexpr int YCH = 16;
+constexpr int YCHMAX = 64;
 __global__ void __launch_bounds__(256) k_ydft(const float* __restrict__ in, const float2* __restrict__ ey,
-                                              float2* __restrict__ out, Dims d) {
-  __shared__ float2 sey[NK * YCH];
-  const int z = blockIdx.x, y0 = blockIdx.y * YCH;
-  for (int q = threadIdx.x; q < NK * YCH; q += 256) sey[q] = ey[(q / YCH) * d.Ny + y0 + q % YCH];
-  const int kx = threadIdx.x & 7, c = threadIdx.x >> 3;
-  float2 v[YCH];
-#pragma unroll
-  for (int yy = 0; yy < YCH; ++yy) {
-    const size_t row = (size_t)z * d.Ny + y0 + yy;
-    float2 a = make_float2(0.f, 0.f);
-    for (int h = 0; h < d.H; ++h) {
-      const float2 w = *reinterpret_cast<const float2*>(in + ((row * d.H + h) * C + c) * KR + 2 * kx);
-      a.x += w.x;
-      a.y += w.y;
-    }
-    v[yy] = a;
-  }
+                                              float2* __restrict__ out, Dims d, int ych) {
+  __shared__ float2 sey[NK * YCHMAX];
+  const int z = blockIdx.x, y0 = blockIdx.y * ych;
+  for (int q = threadIdx.x; q < NK * ych; q += 256) sey[q] = ey[(q / ych) * d.Ny + y0 + q % ych];
   __syncthreads();
+  const int kx = threadIdx.x & 7, c = threadIdx.x >> 3;
+  float2 acc[NK];
 #pragma unroll
-  for (int k = 0; k < NK; ++k) {
-    float re = 0.f, im = 0.f;
+  for (int k = 0; k < NK; ++k) acc[k] = make_float2(0.f, 0.f);
+  for (int s0 = 0; s0 < ych; s0 += YCH) {
+    float2 v[YCH];
 #pragma unroll
     for (int yy = 0; yy < YCH; ++yy) {
-      const float2 e = sey[k * YCH + yy];
-      re += v[yy].x * e.x - v[yy].y * e.y;
-      im += v[yy].x * e.y + v[yy].y * e.x;
+      const size_t row = (size_t)z * d.Ny + y0 + s0 + yy;
+      float2 a = make_float2(0.f, 0.f);
+      for (int h = 0; h < d.H; ++h) {
+        const float2 w = *reinterpret_cast<const float2*>(in + ((row * d.H + h) * C + c) * KR + 2 * kx);
+        a.x += w.x;
+        a.y += w.y;
+      }
+      v[yy] = a;
     }
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+#pragma unroll
+      for (int yy = 0; yy < YCH; ++yy) {
+        const float2 e = sey[k * ych + s0 + yy];
+        acc[k].x += v[yy].x * e.x - v[yy].y * e.y;
+        acc[k].y += v[yy].x * e.y + v[yy].y * e.x;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
     float2* o = out + (((size_t)z * NK + k) * NKX + kx) * C + c;
-    atomicAdd(&o->x, re);
-    atomicAdd(&o->y, im);
+    atomicAdd(&o->x, acc[k].x);
+    atomicAdd(&o->y, acc[k].y);
   }
 }
 
@@ -1332,7 +1392,7 @@ struct phafd_fno {
   cudaStream_t st = nullptr;
   Dbuf params, grad, adam_m, adam_v;
   Dbuf Pb, Wb, Wtb, Rb, Q1b, Q1tb;
-  Dbuf F, Gt, G, Ft, ey, ez;
+  Dbuf F, Gt, G, Ft, ey, ez, osum;
   Dbuf act[5], pre[3], delta[2];
   Dbuf vx, vxy, yxy, yx, vhat[4], out, sum, loss, errf;
   long long adam_t = 0;
@@ -1358,6 +1418,21 @@ struct phafd_fno {
         gt[(2 * kx) * Nx + x] = bf16_bits((float)(w * c));
         gt[(2 * kx + 1) * Nx + x] = bf16_bits((float)(-w * s));
       }
+    // row sums of the (BF16) x-stage table over each x-half
+    std::vector<float> os((size_t)d.H * KR, 0.f);
+    for (int h = 0; h < d.H; ++h)
+      for (int k = 0; k < KR; ++k) {
+        double sacc = 0.0;
+        for (int x = 0; x < TX; ++x) {
+          const uint32_t u = (uint32_t)f[(size_t)k * Nx + h * TX + x] << 16;
+          float fv;
+          std::memcpy(&fv, &u, 4);
+          sacc += fv;
+        }
+        os[(size_t)h * KR + k] = (float)sacc;
+      }
+    osum.alloc(os.size() * 4);
+    FCK(cudaMemcpy(osum.p, os.data(), os.size() * 4, cudaMemcpyHostToDevice));
     F.alloc(f.size() * 2);
     Gt.alloc(gt.size() * 2);
     G.alloc(g.size() * 2);
@@ -1409,7 +1484,9 @@ struct phafd_fno {
 
   void ydft(const float* in, float2* out) {
     FCK(cudaMemsetAsync(out, 0, (size_t)d.Nz * NK * NKX * C * sizeof(float2), st));
-    k_ydft<<<dim3(d.Nz, d.Ny / YCH), 256, 0, st>>>(in, ey.as<float2>(), out, d);
+    int ych = YCHMAX;  // a multiple of 16 dividing Ny (Ny % 16 == 0 at create)
+    while (d.Ny % ych) ych -= YCH;
+    k_ydft<<<dim3(d.Nz, d.Ny / ych), 256, 0, st>>>(in, ey.as<float2>(), out, d, ych);
   }
 
   LiftIn lift_in(const float* phi, const float* rho, float chi) const {
@@ -1488,7 +1565,9 @@ struct phafd_fno {
     const LiftIn in = lift_in(phi, rho, chi);
     const unsigned pg = pgrid();
     TileArgs a = targs(in, -1);
-    k_tiles<TM_LIFT, TNB><<<pg, NTP, SP<TNB>::TOTAL, st>>>(a, d, swap, s);
+    const unsigned lg = (unsigned)(((d.rows + LXW - 1) / LXW) * d.H);
+    k_lift_xdft<<<lg, LXW * 32, 0, st>>>(in, Pb.as<bf16>(), P(OFF_PB), F.as<bf16>(), osum.as<float>(),
+                                          vx.as<float>(), d);
     spectral(0, false);
     a = targs(in, 0);
     a.vout = va;

@@ -38,8 +38,8 @@ EXPORTS = [
     "phafd_stage_gradient", "phafd_stage_borders_and_build", "phafd_stage_pairs",
     "phafd_gradphi_noalloc",
     "phafd_compute_complex", "phafd_structure_factor",
-    "phafd_set_linear_substeps", "phafd_grid_device", "phafd_deposit_density", "phafd_grid_add_device",
-    "phafd_ctx_copy_state",
+    "phafd_set_linear_substeps", "phafd_grid_device", "phafd_grid_copy_device", "phafd_deposit_density",
+    "phafd_grid_add_device", "phafd_ctx_copy_state",
 ]
 
 
@@ -121,6 +121,7 @@ def load(path=None):
         "phafd_structure_factor": [vp, C.c_int, dp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")],
         "phafd_set_linear_substeps": [vp, C.c_int, C.c_double],
         "phafd_grid_device": [vp, C.c_int, C.POINTER(vp)],
+        "phafd_grid_copy_device": [vp, C.c_int, vp],
         "phafd_deposit_density": [vp, vp],
         "phafd_grid_add_device": [vp, vp, C.c_double],
         "phafd_ctx_copy_state": [vp, vp],
@@ -233,6 +234,10 @@ class PhafdGPU:
         p = C.c_void_p()
         self._call("phafd_grid_device", FIELD[field], C.byref(p))
         return p.value
+
+    def grid_copy_device(self, field, dst_ptr):
+        """Copy a real field into the device array at dst_ptr (waits for it)."""
+        self._call("phafd_grid_copy_device", FIELD[field], C.c_void_p(dst_ptr))
 
     def deposit_density(self, rho_ptr):
         self._call("phafd_deposit_density", C.c_void_p(rho_ptr))

@@ -210,6 +210,9 @@ class Runner:
         self.nbins = nbins or cfg["n"] // 2
         self.rho = torch.empty(self.main.shape, device="cuda")
         self.corr = torch.empty(self.main.shape, device="cuda")
+        self.phi0 = torch.empty(self.main.shape, device="cuda")  # phi(t) for the network
+        self.nstream = torch.cuda.Stream()
+        self.corr_ready = False  # the judge's correction, valid for the main state it was copied from
         self.use_surrogate = True
         self.done = 0
         self.judged = []
@@ -221,21 +224,31 @@ class Runner:
         fn(*a)
         self.times[key] += time.perf_counter() - t0
 
-    def _macro(self, s):
+    def _macro(self, s, reuse=False):
+        """One macro step of context s.  The network reads phi(t) and rho(t)
+        only, so it runs on its own stream while the context takes the step
+        (beads and the linearised field update); its correction is added
+        after both.  reuse: the correction of the same state is in corr."""
         if self.net is None:  # the linearised macro step alone (the method without the network)
             self._t("step", s.run, 1)
             return
-        self._t("density", s.deposit_density, self.rho.data_ptr())
-        self._t("network", self.net.infer, s.grid_device("phi"), self.rho.data_ptr(), self.cfg["chi"],
-                self.corr.data_ptr())
-        self._t("step", s.run, 1)
+        if not reuse:
+            self._t("density", s.deposit_density, self.rho.data_ptr())
+            self._t("density", s.grid_copy_device, "phi", self.phi0.data_ptr())
+            self._t("network", self.net.infer, self.phi0.data_ptr(), self.rho.data_ptr(), self.cfg["chi"],
+                    self.corr.data_ptr(), self.nstream.cuda_stream)
+        self._t("step", s.run_async, 1)
+        self._t("step", s.synchronize)
+        self._t("network", self.nstream.synchronize)
         self._t("add", s.grid_add_device, self.corr.data_ptr(), 1.0)
 
     def judge(self):
         self.jp.copy_state_from(self.main)
         self.js.copy_state_from(self.main)
-        self.jp.run(self.K)
+        self.jp.run_async(self.K)  # the plain rerun overlaps the macro step of js
         self._macro(self.js)
+        self.jp.synchronize()
+        self.corr_ready = self.net is not None  # the main state is the one js started from
         sp, _ = self.jp.structure_factor(self.nbins)
         ss, _ = self.js.structure_factor(self.nbins)
         err = rel_sk_error(ss, sp)
@@ -255,13 +268,15 @@ class Runner:
                 if not self.macro:
                     self.main.set_linear_substeps(self.K, self.f2)
                     self.macro = True
-                self._macro(self.main)
+                self._macro(self.main, reuse=self.corr_ready)
+                self.corr_ready = False
                 self.done += self.K
             else:
                 if self.macro:
                     self.main.set_linear_substeps(1)
                     self.macro = False
                 k = min(self.K, end - self.done)
+                self.corr_ready = False
                 self._t("plain", self.main.run, k)
                 self.done += k
 
