@@ -363,33 +363,40 @@ PHAFD_D void store_inputs(unsigned char* tile, int i, int x, const float* v) {
 // against table row k (table staged transposed, conflict-free), then lane c
 // writes its 16 values of channel c.
 constexpr int LXW = 8;  // warps (rows) per CTA
+constexpr int FTS = TX + 4;  // padded row of the staged table: float4 reads of 8 lanes hit distinct banks
 __global__ void __launch_bounds__(LXW * 32) k_lift_xdft(LiftIn in, const bf16* __restrict__ Pb,
                                                        const float* __restrict__ pb, const bf16* __restrict__ Ftab,
                                                        const float* __restrict__ osum, float* __restrict__ vx,
                                                        Dims d) {
-  __shared__ float ft[TX][KR + 1];     // table of this half, [x][k]
-  __shared__ float fld[LXW][2][TX];    // phi_n, rho_n of each warp's row
+  __shared__ __align__(16) float ft[KR][FTS];      // table of this half, [k][x]
+  __shared__ __align__(16) float fld[LXW][2][TX];  // phi_n, rho_n of each warp's row
   const int h = blockIdx.x % d.H;
   const long long row = (long long)(blockIdx.x / d.H) * LXW + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int q = threadIdx.x; q < KR * TX; q += LXW * 32) {
     const int k = q / TX, x = q % TX;
-    ft[x][k] = __bfloat162float(Ftab[(size_t)k * d.Nx + h * TX + x]);
+    ft[k][x] = __bfloat162float(Ftab[(size_t)k * d.Nx + h * TX + x]);
   }
   const bool live = row < d.rows;
   if (live) {
     const size_t base = (size_t)row * d.Nx + (size_t)h * TX;
-    for (int x = lane; x < TX; x += 32) {
-      fld[w][0][x] = (in.phi[base + x] - in.n0) / in.n1;
-      fld[w][1][x] = (in.rho[base + x] - in.n2) / in.n3;
-    }
+    const float4 p = *reinterpret_cast<const float4*>(in.phi + base + 4 * lane);
+    const float4 r = *reinterpret_cast<const float4*>(in.rho + base + 4 * lane);
+    *reinterpret_cast<float4*>(&fld[w][0][4 * lane]) =
+        make_float4((p.x - in.n0) / in.n1, (p.y - in.n0) / in.n1, (p.z - in.n0) / in.n1, (p.w - in.n0) / in.n1);
+    *reinterpret_cast<float4*>(&fld[w][1][4 * lane]) =
+        make_float4((r.x - in.n2) / in.n3, (r.y - in.n2) / in.n3, (r.z - in.n2) / in.n3, (r.w - in.n2) / in.n3);
   }
   __syncthreads();
   if (!live) return;
   const int f = lane >> 4, k = lane & 15;
   float acc = 0.f;
 #pragma unroll 8
-  for (int x = 0; x < TX; ++x) acc += fld[w][f][x] * ft[x][k];
+  for (int x = 0; x < TX; x += 4) {
+    const float4 a = *reinterpret_cast<const float4*>(&fld[w][f][x]);
+    const float4 b = *reinterpret_cast<const float4*>(&ft[k][x]);
+    acc += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+  }
   const int c = lane;
   const float p0 = __bfloat162float(Pb[c * 16 + 0]), p1 = __bfloat162float(Pb[c * 16 + 1]);
   const float cst = __bfloat162float(Pb[c * 16 + 2]) * in.chi_n + pb[c];
@@ -514,7 +521,8 @@ struct SP {
   static constexpr uint32_t BM2 = BM + 2048;            // P or Q1, 2 KB
   static constexpr uint32_t B2 = BM2 + 2048;            // F half, 4 KB
   static constexpr uint32_t BAR = B2 + 4096;
-  static constexpr uint32_t TOTAL = BAR + 64;
+  static constexpr uint32_t VEC = BAR + 64;             // epilogue vectors: bias, q1b, q2 (3 x 32 floats)
+  static constexpr uint32_t TOTAL = VEC + 384;
   static constexpr uint32_t TCOLS = NB == 2 ? 256 : 128;
   static constexpr uint32_t XD = NB == 2 ? 128 : 0;    // TMEM column of the x-stage DFT
 };
@@ -609,6 +617,18 @@ __global__ void __launch_bounds__(NTP) k_tiles(TileArgs a, Dims d, int swap, Sta
   }
   if (MODE == TM_LAST) load_kmajor(sm + L::BM2, a.Q1b, 32, 32);
   if (MODE != TM_LAST) load_b2(sm + L::B2, a.Ftab, d, t.h);
+  // the epilogue's per-channel vectors, read by every thread from shared memory
+  float* vec = reinterpret_cast<float*>(sm + L::VEC);
+  if (threadIdx.x < 32) {
+    const int c = threadIdx.x;
+    vec[c] = (MODE == TM_LIFT || MODE == TM_FIRST) ? a.pb[c] : 0.f;
+    if (MODE != TM_LIFT) vec[32 + c] = a.b[c];
+    if (MODE == TM_LAST) {
+      vec[32 + c] = a.b[c];
+      vec[64 + c] = a.q1b[c];
+      vec[c] = a.q2[c];
+    }
+  }
   // first group
   if (g < a.ngroups) {
     if (MODE == TM_LIFT || MODE == TM_FIRST) load_raw(sm + L::RAW, a.in, t);
@@ -662,7 +682,7 @@ __global__ void __launch_bounds__(NTP) k_tiles(TileArgs a, Dims d, int swap, Sta
           float v[32];
           tmem_row32(tmem, 32 * i, v);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) v[c] += a.pb[c];
+          for (int c = 0; c < 32; ++c) v[c] += vec[c];
           store_row(nullptr, sm + T0, i, x, v);
         }
       }
@@ -684,11 +704,11 @@ __global__ void __launch_bounds__(NTP) k_tiles(TileArgs a, Dims d, int swap, Sta
           const size_t o = (size_t)(t.node0[i] + x) * C;
           if (MODE == TM_LAST) {
 #pragma unroll
-            for (int c = 0; c < 32; ++c) v[c] += a.b[c];
+            for (int c = 0; c < 32; ++c) v[c] += vec[32 + c];
             store_row(nullptr, sm + T0, i, x, v);
           } else {
 #pragma unroll
-            for (int c = 0; c < 32; ++c) v[c] = gelu(v[c] + a.b[c]);
+            for (int c = 0; c < 32; ++c) v[c] = gelu(v[c] + vec[32 + c]);
             store_row(a.vout + o, sm + T0, i, x, v);
           }
         }
@@ -710,7 +730,7 @@ __global__ void __launch_bounds__(NTP) k_tiles(TileArgs a, Dims d, int swap, Sta
           tmem_row32(tmem, 32 * i, v);
           float o = 0.f;
 #pragma unroll
-          for (int k = 0; k < 32; ++k) o += a.q2[k] * gelu(v[k] + a.q1b[k]);
+          for (int k = 0; k < 32; ++k) o += vec[k] * gelu(v[k] + vec[64 + k]);
           a.out[t.node0[i] + x] = o;
           acc += (double)o;
         }
@@ -965,48 +985,39 @@ __global__ void __launch_bounds__(NTH) k_layer_bwd(const bf16* __restrict__ delt
 // ------------------------------------------------------------------ y and z stages (FP32)
 // forward DFT along y of the x-stage partials (summed over halves):
 // out[z][ky'][kx][c] += sum_{y in chunk} in(z, y, kx, c) e^{-2 pi i ky y / Ny}
-// grid (Nz, Ny / ych), ych = min(Ny, 64) rows per CTA walked 16 at a time;
-// out must be zeroed; the chunk sums meet in atomics (Ny / ych per output).
+// grid (Nz, Ny / YCH); out must be zeroed; the chunk sums meet in atomics.
 constexpr int YCH = 16;
-constexpr int YCHMAX = 64;
 __global__ void __launch_bounds__(256) k_ydft(const float* __restrict__ in, const float2* __restrict__ ey,
-                                              float2* __restrict__ out, Dims d, int ych) {
-  __shared__ float2 sey[NK * YCHMAX];
-  const int z = blockIdx.x, y0 = blockIdx.y * ych;
-  for (int q = threadIdx.x; q < NK * ych; q += 256) sey[q] = ey[(q / ych) * d.Ny + y0 + q % ych];
-  __syncthreads();
+                                              float2* __restrict__ out, Dims d) {
+  __shared__ float2 sey[NK * YCH];
+  const int z = blockIdx.x, y0 = blockIdx.y * YCH;
+  for (int q = threadIdx.x; q < NK * YCH; q += 256) sey[q] = ey[(q / YCH) * d.Ny + y0 + q % YCH];
   const int kx = threadIdx.x & 7, c = threadIdx.x >> 3;
-  float2 acc[NK];
+  float2 v[YCH];
 #pragma unroll
-  for (int k = 0; k < NK; ++k) acc[k] = make_float2(0.f, 0.f);
-  for (int s0 = 0; s0 < ych; s0 += YCH) {
-    float2 v[YCH];
-#pragma unroll
-    for (int yy = 0; yy < YCH; ++yy) {
-      const size_t row = (size_t)z * d.Ny + y0 + s0 + yy;
-      float2 a = make_float2(0.f, 0.f);
-      for (int h = 0; h < d.H; ++h) {
-        const float2 w = *reinterpret_cast<const float2*>(in + ((row * d.H + h) * C + c) * KR + 2 * kx);
-        a.x += w.x;
-        a.y += w.y;
-      }
-      v[yy] = a;
+  for (int yy = 0; yy < YCH; ++yy) {
+    const size_t row = (size_t)z * d.Ny + y0 + yy;
+    float2 a = make_float2(0.f, 0.f);
+    for (int h = 0; h < d.H; ++h) {
+      const float2 w = *reinterpret_cast<const float2*>(in + ((row * d.H + h) * C + c) * KR + 2 * kx);
+      a.x += w.x;
+      a.y += w.y;
     }
-#pragma unroll
-    for (int k = 0; k < NK; ++k) {
-#pragma unroll
-      for (int yy = 0; yy < YCH; ++yy) {
-        const float2 e = sey[k * ych + s0 + yy];
-        acc[k].x += v[yy].x * e.x - v[yy].y * e.y;
-        acc[k].y += v[yy].x * e.y + v[yy].y * e.x;
-      }
-    }
+    v[yy] = a;
   }
+  __syncthreads();
 #pragma unroll
   for (int k = 0; k < NK; ++k) {
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int yy = 0; yy < YCH; ++yy) {
+      const float2 e = sey[k * YCH + yy];
+      re += v[yy].x * e.x - v[yy].y * e.y;
+      im += v[yy].x * e.y + v[yy].y * e.x;
+    }
     float2* o = out + (((size_t)z * NK + k) * NKX + kx) * C + c;
-    atomicAdd(&o->x, acc[k].x);
-    atomicAdd(&o->y, acc[k].y);
+    atomicAdd(&o->x, re);
+    atomicAdd(&o->y, im);
   }
 }
 
@@ -1484,9 +1495,7 @@ struct phafd_fno {
 
   void ydft(const float* in, float2* out) {
     FCK(cudaMemsetAsync(out, 0, (size_t)d.Nz * NK * NKX * C * sizeof(float2), st));
-    int ych = YCHMAX;  // a multiple of 16 dividing Ny (Ny % 16 == 0 at create)
-    while (d.Ny % ych) ych -= YCH;
-    k_ydft<<<dim3(d.Nz, d.Ny / ych), 256, 0, st>>>(in, ey.as<float2>(), out, d, ych);
+    k_ydft<<<dim3(d.Nz, d.Ny / YCH), 256, 0, st>>>(in, ey.as<float2>(), out, d);
   }
 
   LiftIn lift_in(const float* phi, const float* rho, float chi) const {
