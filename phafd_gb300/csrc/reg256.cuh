@@ -41,12 +41,17 @@ PHAFD_D void get16(const cpx<T>* buf, cpx<T>* v, int j, int c) {
 
 // z fft of mu + Model-B update + z ifft of phi_hat' and i qz phi_hat', for
 // Nz = 256.  Same contract as k_zfused (grid_impl.cuh).
-// FP32: at most 80 registers so three CTAs (24 warps) share an SM
-template <typename T>
+// FP32: at most 80 registers so three CTAs (24 warps) share an SM.
+// NOISE and MACRO fix the noise mode and whether the update is a macro step
+// (nsub > 1) at compile time, so the update inlined for the 16 modes of a
+// thread carries no branches or code for the other cases.
+template <typename T, int NOISE, bool MACRO>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
 k_zfused256(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __restrict__ out0,
             cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny,
             UpdateArgs<T> u, int store_mu, int kx0) {
+  u.noise = NOISE;
+  if (!MACRO) u.nsub = 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* bufA = reinterpret_cast<cpx<T>*>(smraw);  // N x W
   cpx<T>* bufB = bufA + N * W;                        // N x W (phi_hat staging, then second ifft)
@@ -478,17 +483,30 @@ int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B,
   return 0;
 }
 
-template <typename T>
-int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
-           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only, cudaStream_t st) {
+template <typename T, int NOISE, bool MACRO>
+int zfused_launch(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
+                  const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int kx0, cudaStream_t st) {
   const size_t sm = (size_t)2 * N * W * sizeof(cpx<T>);
-  auto k = k_zfused256<T>;
+  auto k = k_zfused256<T, NOISE, MACRO>;
   if (set_smem(k, sm)) return -1;
-  const int kx0 = bulk_only ? 1 : 0;
-  if (g.nxh - 2 * kx0 <= 0) return 0;
   dim3 grid((g.ny + W - 1) / W, g.nxh - 2 * kx0);
   launch_grid(k, grid, dim3(256), sm, st, muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
   return 0;
+}
+
+template <typename T>
+int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
+           const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only, cudaStream_t st) {
+  const int kx0 = bulk_only ? 1 : 0;
+  if (g.nxh - 2 * kx0 <= 0) return 0;
+  const bool macro = u.nsub > 1;
+#define ZF(NZ, M) zfused_launch<T, NZ, M>(g, muin, muhat, out0, out1, twf, twi, u, store_mu, kx0, st)
+  switch (u.noise) {
+    case PHAFD_NOISE_OFF: return macro ? ZF(PHAFD_NOISE_OFF, true) : ZF(PHAFD_NOISE_OFF, false);
+    case PHAFD_NOISE_REFERENCE: return macro ? ZF(PHAFD_NOISE_REFERENCE, true) : ZF(PHAFD_NOISE_REFERENCE, false);
+    default: return macro ? ZF(PHAFD_NOISE_PHILOX, true) : ZF(PHAFD_NOISE_PHILOX, false);
+  }
+#undef ZF
 }
 
 }  // namespace r256
