@@ -1,6 +1,6 @@
 // Grid-side kernels of the particle-field step, templated on the arithmetic
-// type T (float or double).  Included once per type by grid_f32.cu and
-// grid_f64.cu.
+// type T (float or double).  The grid_{f32,f64}_{x,y,z}.cu translation units
+// instantiate the GridOps members of one type and one axis family each.
 //
 // Layouts (all in HBM, resident for the whole run)
 //   real field   R[z][y][x]                       x fastest
@@ -424,11 +424,15 @@ k_zpass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
 // tiles, only store mu_hat; k_zpass<planes_only> finishes them.  With
 // kx0 = 1 the grid covers the bulk planes only and the Hermitian planes are
 // transformed by k_zpass<planes_only> on a parallel branch.
-template <typename T, int N, int LB>
+// NOISE and MACRO fix the noise mode and the macro-step flag at compile time
+// (no branches or code for the other cases in the update).
+template <typename T, int N, int LB, int NOISE, bool MACRO>
 __global__ void __launch_bounds__(N * LB * 2 / 16)
 k_zfused(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __restrict__ out0,
          cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny,
          UpdateArgs<T> u, int store_mu, int kx0) {
+  u.noise = NOISE;
+  if (!MACRO) u.nsub = 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* s = reinterpret_cast<cpx<T>*>(smraw);
   constexpr int NL = 2 * LB;
@@ -648,9 +652,23 @@ struct Axis {
     const int kx0 = bulk_only ? 1 : 0;
     if (g.nxh - 2 * kx0 <= 0) return 0;
     dim3 grid((g.ny + LB - 1) / LB, g.nxh - 2 * kx0);
-    auto k = k_zfused<T, N, LB>;
+    const bool macro = u.nsub > 1;
+#define ZF(NZ, M) zfused_go<LB, NZ, M>(grid, sm, muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0, st)
+    switch (u.noise) {
+      case PHAFD_NOISE_OFF: return macro ? ZF(PHAFD_NOISE_OFF, true) : ZF(PHAFD_NOISE_OFF, false);
+      case PHAFD_NOISE_REFERENCE: return macro ? ZF(PHAFD_NOISE_REFERENCE, true) : ZF(PHAFD_NOISE_REFERENCE, false);
+      default: return macro ? ZF(PHAFD_NOISE_PHILOX, true) : ZF(PHAFD_NOISE_PHILOX, false);
+    }
+#undef ZF
+  }
+  template <int LB, int NOISE, bool MACRO>
+  static int zfused_go(dim3 grid, size_t sm, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, T dq,
+                       const cpx<T>* twf, const cpx<T>* twi, int ny, const UpdateArgs<T>& u, int store_mu, int kx0,
+                       cudaStream_t st) {
+    auto k = k_zfused<T, N, LB, NOISE, MACRO>;
     if (set_smem(k, sm)) return -1;
-    launch_grid(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
+    launch_grid(k, dim3(grid), dim3(N * LB * 2 / 16), sm, st, muin, muhat, out0, out1, dq, twf, twi, ny, u, store_mu,
+                kx0);
     return 0;
   }
 };

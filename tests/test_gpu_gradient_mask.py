@@ -12,21 +12,21 @@ from tests.helpers import rel_err
 pytestmark = pytest.mark.gpu
 
 
-def _run(precision, masked, skin, steps, chains=None):
+def _run(precision, masked, skin, steps, chains=None, zghost="periodic"):
     cfg = dict(W.CONFIGS["32cube_64beads"])
     cfg.update(field_noise="philox", bead_temp=1.0, dt=5e-4, skin=skin)
     g = PhafdGPU(precision=precision, schedule="resident")
-    ch = W.apply(g, cfg, chains=chains)
+    ch = W.apply(g, cfg, chains=chains, zghost=zghost)
     g.set_gradient_mask(masked)
     g.setup()
     g.run(steps)
     return g, ch
 
 
-@pytest.mark.parametrize("skin", [0.3, 0.02])
-def test_masked_steps_match_full_stores_fp64(gpu_lib, skin):
-    a, ch = _run(64, True, skin, 60)
-    b, _ = _run(64, False, skin, 60, chains=ch)
+@pytest.mark.parametrize("skin,zghost", [(0.3, "periodic"), (0.02, "periodic"), (0.3, "rank1")])
+def test_masked_steps_match_full_stores_fp64(gpu_lib, skin, zghost):
+    a, ch = _run(64, True, skin, 60, zghost=zghost)
+    b, _ = _run(64, False, skin, 60, chains=ch, zghost=zghost)
     # FP64 deposit atomics reorder sums: round-off differences only; a node
     # missing from the mask would feed the forces a gradient one or more
     # steps old, a difference many orders above this bound
