@@ -154,10 +154,16 @@ PHAFD_D void tile_end(Tile& t, uint32_t ncols) {
 
 // wait for the MMAs committed as phase `ph`; on timeout flag the error.
 // Every thread of the CTA calls it; the result is made uniform so that the
-// barriers behind a failed wait are skipped by all threads alike.
+// barriers behind a failed wait are skipped by all threads alike.  Thread 0
+// polls the MMA barrier; the others wait at the CTA barrier that follows,
+// which costs them no issue slots (the tcgen05 fence after it orders their
+// TMEM reads after the MMAs thread 0 saw complete).
 PHAFD_D bool mma_wait(Tile& t, uint32_t ph, const Status& s) {
-  const bool mine = tc::mbar_wait(t.bar, ph);
-  if (!mine) atomicExch(s.err, 1);
+  bool mine = true;
+  if (threadIdx.x == 0) {
+    mine = tc::mbar_wait(t.bar, ph);
+    if (!mine) atomicExch(s.err, 1);
+  }
   const bool ok = __syncthreads_and(mine) != 0;
   tc::fence_after();
   return ok;
@@ -270,6 +276,15 @@ PHAFD_D void store_row(bf16* g, unsigned char* tile, int i, int x, const float* 
     for (int k = 0; k < 4; ++k) *reinterpret_cast<uint4*>(tile + tile_off(i, x, 8 * k)) = q[k];
   }
 }
+// the activation tile (unified layout) -> HBM [node][32], 16 contiguous
+// bytes per lane (the epilogue writes the tile; this copies it out coalesced)
+PHAFD_D void store_tile(bf16* act, const unsigned char* tile, const Tile& t) {
+  for (int q = threadIdx.x; q < TPC * TX * 4; q += blockDim.x) {
+    const int i = q >> 9, x = (q >> 2) & (TX - 1), g = q & 3;
+    *reinterpret_cast<uint4*>(act + (size_t)(t.node0[i] + x) * C + 8 * g) =
+        *reinterpret_cast<const uint4*>(tile + tile_off(i, x, 8 * g));
+  }
+}
 PHAFD_D void load_row(const bf16* g, float* v) {
   const uint4* gp = reinterpret_cast<const uint4*>(g);
 #pragma unroll
@@ -359,57 +374,68 @@ PHAFD_D void store_inputs(unsigned char* tile, int i, int x, const float* v) {
 //   vx[c][k] = P[c][0] Phi[k] + P[c][1] Rho[k] + (P[c][2] chi_n + pb[c]) O[k]
 // with Phi, Rho the partial DFTs of the two input fields and O[k] the sum of
 // the table row k over the half: two 128-point DFTs per row instead of a
-// 32-channel pass.  One warp per (row, half): lane (f, k) sums field f
-// against table row k (table staged transposed, conflict-free), then lane c
-// writes its 16 values of channel c.
-constexpr int LXW = 8;  // warps (rows) per CTA
+// 32-channel pass.  A CTA stages the table of one x-half in shared memory
+// and its warps take LXR rows each: lane (f, k) sums field f against table
+// row k (float4 reads, conflict-free), then lane c writes its 16 values of
+// channel c.
+constexpr int LXW = 8;   // warps per CTA
+constexpr int LXR = 4;   // rows per warp (the staged table serves LXW * LXR rows)
 constexpr int FTS = TX + 4;  // padded row of the staged table: float4 reads of 8 lanes hit distinct banks
 __global__ void __launch_bounds__(LXW * 32) k_lift_xdft(LiftIn in, const bf16* __restrict__ Pb,
                                                        const float* __restrict__ pb, const bf16* __restrict__ Ftab,
                                                        const float* __restrict__ osum, float* __restrict__ vx,
                                                        Dims d) {
   __shared__ __align__(16) float ft[KR][FTS];      // table of this half, [k][x]
-  __shared__ __align__(16) float fld[LXW][2][TX];  // phi_n, rho_n of each warp's row
+  __shared__ __align__(16) float fld[LXW][2][TX];  // phi_n, rho_n of a warp's current row
   const int h = blockIdx.x % d.H;
-  const long long row = (long long)(blockIdx.x / d.H) * LXW + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int q = threadIdx.x; q < KR * TX; q += LXW * 32) {
-    const int k = q / TX, x = q % TX;
-    ft[k][x] = __bfloat162float(Ftab[(size_t)k * d.Nx + h * TX + x]);
+  // 8 BF16 of the table per 16-byte load
+  for (int q = threadIdx.x; q < KR * TX / 8; q += LXW * 32) {
+    const int k = q / (TX / 8), x = (q % (TX / 8)) * 8;
+    const uint4 raw = *reinterpret_cast<const uint4*>(Ftab + (size_t)k * d.Nx + h * TX + x);
+    const __nv_bfloat162* b2 = reinterpret_cast<const __nv_bfloat162*>(&raw);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float2 f = __bfloat1622float2(b2[e]);
+      ft[k][x + 2 * e] = f.x;
+      ft[k][x + 2 * e + 1] = f.y;
+    }
   }
-  const bool live = row < d.rows;
-  if (live) {
+  __syncthreads();
+  const int c = lane;
+  const float p0 = __bfloat162float(Pb[c * 16 + 0]), p1 = __bfloat162float(Pb[c * 16 + 1]);
+  const float cst = __bfloat162float(Pb[c * 16 + 2]) * in.chi_n + pb[c];
+  const int f = lane >> 4, k = lane & 15;
+  for (int rr = 0; rr < LXR; ++rr) {
+    const long long row = ((long long)(blockIdx.x / d.H) * LXR + rr) * LXW + w;
+    if (row >= d.rows) break;  // warp-uniform
     const size_t base = (size_t)row * d.Nx + (size_t)h * TX;
     const float4 p = *reinterpret_cast<const float4*>(in.phi + base + 4 * lane);
     const float4 r = *reinterpret_cast<const float4*>(in.rho + base + 4 * lane);
+    __syncwarp();  // the previous row's values are read
     *reinterpret_cast<float4*>(&fld[w][0][4 * lane]) =
         make_float4((p.x - in.n0) / in.n1, (p.y - in.n0) / in.n1, (p.z - in.n0) / in.n1, (p.w - in.n0) / in.n1);
     *reinterpret_cast<float4*>(&fld[w][1][4 * lane]) =
         make_float4((r.x - in.n2) / in.n3, (r.y - in.n2) / in.n3, (r.z - in.n2) / in.n3, (r.w - in.n2) / in.n3);
-  }
-  __syncthreads();
-  if (!live) return;
-  const int f = lane >> 4, k = lane & 15;
-  float acc = 0.f;
+    __syncwarp();
+    float acc = 0.f;
 #pragma unroll 8
-  for (int x = 0; x < TX; x += 4) {
-    const float4 a = *reinterpret_cast<const float4*>(&fld[w][f][x]);
-    const float4 b = *reinterpret_cast<const float4*>(&ft[k][x]);
-    acc += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
-  }
-  const int c = lane;
-  const float p0 = __bfloat162float(Pb[c * 16 + 0]), p1 = __bfloat162float(Pb[c * 16 + 1]);
-  const float cst = __bfloat162float(Pb[c * 16 + 2]) * in.chi_n + pb[c];
-  float v[KR];
+    for (int x = 0; x < TX; x += 4) {
+      const float4 a = *reinterpret_cast<const float4*>(&fld[w][f][x]);
+      const float4 b = *reinterpret_cast<const float4*>(&ft[k][x]);
+      acc += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+    }
+    float v[KR];
 #pragma unroll
-  for (int kk = 0; kk < KR; ++kk) {
-    const float phik = __shfl_sync(0xffffffffu, acc, kk);
-    const float rhok = __shfl_sync(0xffffffffu, acc, 16 + kk);
-    v[kk] = p0 * phik + p1 * rhok + cst * osum[h * KR + kk];
-  }
-  float4* o = reinterpret_cast<float4*>(vx + (((size_t)row * d.H + h) * C + c) * KR);
+    for (int kk = 0; kk < KR; ++kk) {
+      const float phik = __shfl_sync(0xffffffffu, acc, kk);
+      const float rhok = __shfl_sync(0xffffffffu, acc, 16 + kk);
+      v[kk] = p0 * phik + p1 * rhok + cst * osum[h * KR + kk];
+    }
+    float4* o = reinterpret_cast<float4*>(vx + (((size_t)row * d.H + h) * C + c) * KR);
 #pragma unroll
-  for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+  }
 }
 
 // v0 = P in + pb; x-stage DFT of v0
@@ -701,7 +727,6 @@ __global__ void __launch_bounds__(NTP) k_tiles(TileArgs a, Dims d, int swap, Sta
         for (int i = i0; i < i0 + 2; ++i) {
           float v[32];
           tmem_row32(tmem, 32 * i, v);
-          const size_t o = (size_t)(t.node0[i] + x) * C;
           if (MODE == TM_LAST) {
 #pragma unroll
             for (int c = 0; c < 32; ++c) v[c] += vec[32 + c];
@@ -709,7 +734,7 @@ __global__ void __launch_bounds__(NTP) k_tiles(TileArgs a, Dims d, int swap, Sta
           } else {
 #pragma unroll
             for (int c = 0; c < 32; ++c) v[c] = gelu(v[c] + vec[32 + c]);
-            store_row(a.vout + o, sm + T0, i, x, v);
+            store_row(nullptr, sm + T0, i, x, v);  // HBM copy below, coalesced
           }
         }
       }
@@ -736,11 +761,12 @@ __global__ void __launch_bounds__(NTP) k_tiles(TileArgs a, Dims d, int swap, Sta
         }
       }
     } else {
-      // x-stage DFT of the tile's output
+      // x-stage DFT of the tile's output; the tile goes to HBM meanwhile
       if (ok && threadIdx.x == 0) {
         issue_xdft_at(t, tmem + XD, T0, L::B2, swap);
         tc::commit(t.bar);
       }
+      if (MODE != TM_LIFT && ok) store_tile(a.vout, sm + T0, t);
       ok = ok && mma_wait(t, ph, st);
       ph ^= 1;
       if (ok) store_xdft(a.vx, tmem + XD, t, d);
@@ -986,9 +1012,13 @@ __global__ void __launch_bounds__(NTH) k_layer_bwd(const bf16* __restrict__ delt
 // forward DFT along y of the x-stage partials (summed over halves):
 // out[z][ky'][kx][c] += sum_{y in chunk} in(z, y, kx, c) e^{-2 pi i ky y / Ny}
 // grid (Nz, Ny / YCH); out must be zeroed; the chunk sums meet in atomics.
+// HC: the number of x-halves when known at compile time (0: d.H), so the
+// 16 x HC loads of a thread are all in flight at once.
 constexpr int YCH = 16;
+template <int HC>
 __global__ void __launch_bounds__(256) k_ydft(const float* __restrict__ in, const float2* __restrict__ ey,
                                               float2* __restrict__ out, Dims d) {
+  const int H = HC > 0 ? HC : d.H;
   __shared__ float2 sey[NK * YCH];
   const int z = blockIdx.x, y0 = blockIdx.y * YCH;
   for (int q = threadIdx.x; q < NK * YCH; q += 256) sey[q] = ey[(q / YCH) * d.Ny + y0 + q % YCH];
@@ -998,8 +1028,9 @@ __global__ void __launch_bounds__(256) k_ydft(const float* __restrict__ in, cons
   for (int yy = 0; yy < YCH; ++yy) {
     const size_t row = (size_t)z * d.Ny + y0 + yy;
     float2 a = make_float2(0.f, 0.f);
-    for (int h = 0; h < d.H; ++h) {
-      const float2 w = *reinterpret_cast<const float2*>(in + ((row * d.H + h) * C + c) * KR + 2 * kx);
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      const float2 w = *reinterpret_cast<const float2*>(in + ((row * H + h) * C + c) * KR + 2 * kx);
       a.x += w.x;
       a.y += w.y;
     }
@@ -1495,7 +1526,11 @@ struct phafd_fno {
 
   void ydft(const float* in, float2* out) {
     FCK(cudaMemsetAsync(out, 0, (size_t)d.Nz * NK * NKX * C * sizeof(float2), st));
-    k_ydft<<<dim3(d.Nz, d.Ny / YCH), 256, 0, st>>>(in, ey.as<float2>(), out, d);
+    const dim3 grid(d.Nz, d.Ny / YCH);
+    if (d.H == 1) k_ydft<1><<<grid, 256, 0, st>>>(in, ey.as<float2>(), out, d);
+    else if (d.H == 2) k_ydft<2><<<grid, 256, 0, st>>>(in, ey.as<float2>(), out, d);
+    else if (d.H == 4) k_ydft<4><<<grid, 256, 0, st>>>(in, ey.as<float2>(), out, d);
+    else k_ydft<0><<<grid, 256, 0, st>>>(in, ey.as<float2>(), out, d);
   }
 
   LiftIn lift_in(const float* phi, const float* rho, float chi) const {
@@ -1574,7 +1609,7 @@ struct phafd_fno {
     const LiftIn in = lift_in(phi, rho, chi);
     const unsigned pg = pgrid();
     TileArgs a = targs(in, -1);
-    const unsigned lg = (unsigned)(((d.rows + LXW - 1) / LXW) * d.H);
+    const unsigned lg = (unsigned)(((d.rows + LXW * LXR - 1) / (LXW * LXR)) * d.H);
     k_lift_xdft<<<lg, LXW * 32, 0, st>>>(in, Pb.as<bf16>(), P(OFF_PB), F.as<bf16>(), osum.as<float>(),
                                           vx.as<float>(), d);
     spectral(0, false);
