@@ -112,7 +112,7 @@ int phafd_set_zghost(phafd_ctx* ctx, int mode);                      /* CommBric
 int phafd_set_schedule(phafd_ctx* ctx, int schedule);
 int phafd_set_keep_chempot(phafd_ctx* ctx, int keep);               /* also store mu = deposit + FH (grid->chempot) each step */
 int phafd_set_plane_fusion(phafd_ctx* ctx, int on);                 /* x and y passes fused per z-plane in thread-block clusters (Nx == Ny) */
-/* on (default): single-substep resident steps store grad phi only at grid
+/* on (off by default): single-substep resident steps store grad phi only at grid
  * nodes within (gridatom cutoff + skin) of the beads' positions at the last
  * neighbor rebuild -- the only nodes the pair forces read while no bead has
  * moved more than skin since; a step after which some bead has moved further
@@ -173,6 +173,12 @@ int phafd_compute_complex(phafd_ctx* ctx, int field, int quant, double* out);
  * q != 0, every mode of the full spectrum counted once (the half spectrum
  * with its mirror modes).  counts[b] = modes in shell b (may be NULL). */
 int phafd_structure_factor(phafd_ctx* ctx, int nbins, double* sk, long long* counts);
+/* compute grid/cluster phi THRESHOLD gt|lt (compute_grid_clusters.cpp:66-229) on the
+ * current phi of the one periodic domain: labels (host, nx*ny*nz int, [z][y][x]) =
+ * the smallest z + (y*nx + x)*ny over the node's 6-connected periodic component of
+ * phi > threshold (greater = 1) or phi < threshold (greater = 0), -1 elsewhere;
+ * nclusters (optional) = the number of components.  Either pointer may be null. */
+int phafd_compute_grid_clusters(phafd_ctx* ctx, double threshold, int greater, int* labels, int* nclusters);
 
 /* ---- learned macro step support (no reference counterpart) ----
  * nsub > 1 makes each step a macro step (resident schedule): the Model-B

@@ -58,6 +58,8 @@ def lib():
             "oracle_set_timestep": [vp, C.c_longlong],
             "oracle_setup": [vp],
             "oracle_run": [vp, C.c_int],
+            "oracle_compute_grid_clusters": [vp, C.c_double, C.c_int,
+                                             np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")],
             "oracle_stage_gradient": [vp],
             "oracle_stage_borders_and_build": [vp],
             "oracle_stage_pairs": [vp],
@@ -225,6 +227,15 @@ class Oracle:
 
     def run(self, nsteps):
         self._call("oracle_run", nsteps)
+
+    def compute_grid_clusters(self, threshold, condition="gt"):
+        """Labels of compute grid/cluster (compute_grid_clusters.cpp:66-229):
+        int32 [z][y][x], -1 outside the clusters."""
+        if condition not in ("lt", "gt"):
+            raise ValueError("Must specify lt or gt for compute grid cluster.")
+        out = np.zeros(self.shape, np.int32)
+        self._call("oracle_compute_grid_clusters", float(threshold), int(condition == "gt"), out)
+        return out
 
     # ---- stage hooks and inspection
     def stage_gradient(self):

@@ -1436,6 +1436,46 @@ int oracle_stage_times(oracle_ctx* c, double* out7) {
 }
 
 // standalone transforms (for FFT unit tests against numpy.fft)
+// compute grid/cluster (compute_grid_clusters.cpp:66-229) on one periodic
+// domain: label = z + (y Nx + x) Ny where phi < or > threshold, else -1
+// (compute_grid_clusters.cpp:72-94); then sweeps over the nodes in (z, y, x)
+// order that set a node and each labelled nearest neighbour (z, y, x wrapped;
+// the reference's LEFTS/RIGHTS planes are the wrapped z neighbours of a
+// one-rank domain) to the smaller of the two labels, until a sweep changes
+// nothing (compute_grid_clusters.cpp:103-196).
+static void grid_clusters_impl(oracle_ctx* c, double threshold, int greater, int* labels) {
+  const int Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
+  auto L = [&](int i, int j, int k) -> int& { return labels[((size_t)i * Ny + j) * Nx + k]; };
+  for (int i = 0; i < Nz; i++)
+    for (int j = 0; j < Ny; j++)
+      for (int k = 0; k < Nx; k++) {
+        const double v = c->PHI(i, j, k);
+        const bool in = greater ? v > threshold : v < threshold;
+        L(i, j, k) = in ? i + (j * Nx + k) * Ny : -1;
+      }
+  bool done = false;
+  while (!done) {
+    done = true;
+    for (int i = 0; i < Nz; i++)
+      for (int j = 0; j < Ny; j++)
+        for (int k = 0; k < Nx; k++) {
+          if (L(i, j, k) == -1) continue;
+          const int nb[6][3] = {{(i + Nz - 1) % Nz, j, k}, {(i + 1) % Nz, j, k}, {i, (j + Ny - 1) % Ny, k},
+                                {i, (j + 1) % Ny, k},       {i, j, (k + Nx - 1) % Nx}, {i, j, (k + 1) % Nx}};
+          for (auto& q : nb) {
+            int& o = L(q[0], q[1], q[2]);
+            if (o == -1 || o == L(i, j, k)) continue;
+            L(i, j, k) = o = std::min(L(i, j, k), o);
+            done = false;
+          }
+        }
+  }
+}
+
+int oracle_compute_grid_clusters(oracle_ctx* c, double threshold, int greater, int* labels) {
+  GUARD(c, { grid_clusters_impl(c, threshold, greater, labels); })
+}
+
 int oracle_fft_r2c(int nx, int ny, int nz, const double* in, double* out_cplx) {
   try {
     FFT3 f(nx, ny, nz);

@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libphafd_gpu.so")
 EXE = os.path.join(OUT, "phafd_gpu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
-CU_SOURCES = ["ctx.cu", "bead_kernels.cu", "noalloc.cu", "fno.cu",
+CU_SOURCES = ["ctx.cu", "bead_kernels.cu", "noalloc.cu", "fno.cu", "clusters.cu",
               "grid_f32_x.cu", "grid_f32_y.cu", "grid_f32_z.cu", "grid_f32_zf.cu",
               "grid_f64_x.cu", "grid_f64_y.cu", "grid_f64_z.cu", "grid_f64_zf.cu"]
 

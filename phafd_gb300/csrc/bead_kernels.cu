@@ -41,8 +41,9 @@ __device__ __forceinline__ int bin_coord(double x, double lo, double inv, int nb
 // neighbor.cpp:79-97
 // With use_cond the last block to finish (threadfence pattern) copies the
 // flag into the graph conditional that gates the rebuild body.
-__global__ void k_check(BeadArgs a, cudaGraphConditionalHandle h, int use_cond) {
+__global__ void k_check(BeadArgs a, cudaGraphConditionalHandle h, int use_cond, long long* step_inc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (step_inc && i == 0) *step_inc += 1;
   if (i < a.n) {
     const double d0 = a.x[3 * i] - a.xhold[3 * i];
     const double d1 = a.x[3 * i + 1] - a.xhold[3 * i + 1];
@@ -509,6 +510,19 @@ __global__ void k_step_begin(long long* d_step) { *d_step += 1; }
 // per-entry arithmetic is (small integer - fraction) * dx in FP32.
 constexpr int PAIR_TPB = 4;
 
+// grid coordinates of a node index (shifts and masks for power-of-two grids)
+PHAFD_D void node_coords(const BeadArgs& a, uint32_t node, int g3[3]) {
+  if (a.lgN[0] >= 0) {
+    g3[0] = (int)(node & (uint32_t)(a.N[0] - 1));
+    g3[1] = (int)((node >> a.lgN[0]) & (uint32_t)(a.N[1] - 1));
+    g3[2] = (int)(node >> (a.lgN[0] + a.lgN[1]));
+  } else {
+    g3[0] = (int)(node % (uint32_t)a.N[0]);
+    g3[1] = (int)((node / (uint32_t)a.N[0]) % (uint32_t)a.N[1]);
+    g3[2] = (int)(node / ((uint32_t)a.N[0] * (uint32_t)a.N[1]));
+  }
+}
+
 template <typename T>
 __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -565,8 +579,8 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
       const uint32_t e = a.gl[(size_t)i * a.maxg + k];
       const uint32_t node = e >> 5;
       const int code = (int)(e & 31u);
-      const int g3[3] = {(int)(node % (uint32_t)a.N[0]), (int)((node / (uint32_t)a.N[0]) % (uint32_t)a.N[1]),
-                         (int)(node / ((uint32_t)a.N[0] * (uint32_t)a.N[1]))};
+      int g3[3];
+      node_coords(a, node, g3);
       T dd[3];
       if constexpr (sizeof(T) == 8) {
         // node coordinate k*dx + boxlo without contraction (npair_grid_bin.cpp:76-88)
@@ -635,8 +649,8 @@ __global__ void k_density(BeadArgs a, PairArgs<T> p, T* rho) {
     const uint32_t e = a.gl[(size_t)i * a.maxg + k];
     const uint32_t node = e >> 5;
     const int code = (int)(e & 31u);
-    const int g3[3] = {(int)(node % (uint32_t)a.N[0]), (int)((node / (uint32_t)a.N[0]) % (uint32_t)a.N[1]),
-                       (int)(node / ((uint32_t)a.N[0] * (uint32_t)a.N[1]))};
+    int g3[3];
+    node_coords(a, node, g3);
     T dd[3];
     for (int d = 0; d < 3; ++d) dd[d] = (T)((double)g3[d] * a.dx[d] + a.boxlo[d] - (xi[d] + img_shift(code, d, a)));
     T rsq = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
@@ -774,15 +788,16 @@ static inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) 
 
 void launch_step_begin(long long* d_step, cudaStream_t st) { k_step_begin<<<1, 1, 0, st>>>(d_step); }
 
-void launch_neighbor_check(const BeadArgs& a, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
+void launch_neighbor_check(const BeadArgs& a, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st,
+                           long long* step_inc) {
   if (a.n == 0) return;
-  k_check<<<nblk(a.n, 256), 256, 0, st>>>(a, h, use_cond);
+  k_check<<<nblk(a.n, 256), 256, 0, st>>>(a, h, use_cond, step_inc);
 }
 
-void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st) {
+void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st, long long* step_inc) {
   if (a.n == 0) return;
   if (force) cudaMemsetAsync(a.flag, 0xff, sizeof(int), st);
-  else launch_neighbor_check(a, 0, 0, st);
+  else launch_neighbor_check(a, 0, 0, st, step_inc);
   launch_rebuild(a, st);
 }
 

@@ -20,6 +20,7 @@ struct BeadArgs {
   int *image, *type;
   double boxlo[3], boxhi[3], period[3];
   double invdx[3];      // 1 / grid spacing (FP32 pair path: one FP64 multiply instead of a divide)
+  int lgN[3];           // log2 N[d] when every N[d] is a power of two, else -1 (node index decode)
   double triggersq, cutneigh, cutneighsq;
   int* flag;            // rebuild requested (device)
   uint32_t* gmask;      // bit per 32-byte sector of a grid field (gmask_g nodes) holding a node within gmask_r
@@ -70,10 +71,13 @@ struct PairArgs {
 };
 
 void launch_step_begin(long long* d_step, cudaStream_t st);
-void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st);
+// step_inc (optional): counter the check kernel increments (the step counter,
+// saving a launch of its own)
+void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st, long long* step_inc = nullptr);
 // the two halves of launch_neighbor: the displacement check (optionally
 // setting a graph conditional to the rebuild flag) and the rebuild kernels
-void launch_neighbor_check(const BeadArgs& a, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
+void launch_neighbor_check(const BeadArgs& a, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st,
+                           long long* step_inc = nullptr);
 void launch_rebuild(const BeadArgs& a, cudaStream_t st);
 // sets *gmask_off when a bead moved more than sqrt(gmask_guardsq) since the last rebuild
 void launch_gmask_guard(const BeadArgs& a, cudaStream_t st);

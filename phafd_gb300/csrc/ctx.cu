@@ -153,7 +153,7 @@ struct phafd_ctx {
   bool keep_chempot = false;
   bool chempot_from_mu = false;
   bool use_plane = false;  // plane-fused x/y passes where they apply (phafd_set_plane_fusion)
-  bool use_gmask = true;   // gradient stored near beads only during steps (phafd_set_gradient_mask)
+  bool use_gmask = false;  // gradient stored near beads only during steps (phafd_set_gradient_mask)
   bool grad_partial = false;  // gx, gy, gz hold values at masked nodes only
   int nsub = 1;            // substeps of one step (phafd_set_linear_substeps)
   double f2_lin = 0.0;     // dmu/dphi of the linearisation
@@ -409,6 +409,13 @@ struct phafd_ctx {
       a.dx[d] = gridset ? period[d] / N[d] : 1.0;
       a.invdx[d] = 1.0 / a.dx[d];
     }
+    bool pow2 = true;
+    for (int d = 0; d < 3; ++d) pow2 = pow2 && N[d] > 0 && (N[d] & (N[d] - 1)) == 0;
+    for (int d = 0; d < 3; ++d) {
+      int lg = 0;
+      while (pow2 && (1 << lg) < N[d]) ++lg;
+      a.lgN[d] = pow2 ? lg : -1;
+    }
     a.triggersq = 0.25 * skin * skin;
     a.cutneigh = cutneigh;
     a.cutneighsq = cutneigh * cutneigh;
@@ -428,7 +435,7 @@ struct phafd_ctx {
     a.sf_fix = sf_fix.as<int>(); a.sf_start = sf_start.as<int>(); a.sf_len = sf_len.as<int>();
     a.sf = sf_par.as<SemiDev>();
     a.any_semi = !semis.empty();
-    a.gmask = gmask.p ? gmask.as<uint32_t>() : nullptr;
+    a.gmask = use_gmask && gmask.p ? gmask.as<uint32_t>() : nullptr;
     a.gmask_g = 32 / (int)rsz();
     a.gmask_words = ((long long)nreal / a.gmask_g + 32) / 32;
     a.gmask_r = ga_maxcut + skin + 1e-3 * std::min(a.dx[0], std::min(a.dx[1], a.dx[2]));
@@ -454,6 +461,17 @@ struct phafd_ctx {
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     grad_partial = false;
+  }
+
+  // the gradient node mask; marked stale until the next rebuild builds it
+  void alloc_gmask() {
+    if (ga_style == PHAFD_GRIDATOM_NONE || !gridset || n == 0) return;
+    if (!gmask.p) {
+      gmask.alloc(((nreal / (32 / rsz()) + 32) / 32) * 4);
+      gmask.zero(st);
+    }
+    const int off = 1;
+    CK(cudaMemcpyAsync(d_gmask_off(), &off, sizeof(int), cudaMemcpyHostToDevice, st));
   }
 
   void setup_neighbor_structs() {
@@ -498,12 +516,7 @@ struct phafd_ctx {
     ba.maxg = maxg;
     if (ga_style != PHAFD_GRIDATOM_NONE) gl.alloc((size_t)std::max(n, 1) * maxg * 4);
     ngl.alloc(std::max(n, 1) * 4);
-    if (ga_style != PHAFD_GRIDATOM_NONE && gridset) {
-      gmask.alloc(((nreal / (32 / rsz()) + 32) / 32) * 4);
-      gmask.zero(st);
-      const int off = 1;  // until the first rebuild has built it
-      CK(cudaMemcpyAsync(d_gmask_off(), &off, sizeof(int), cudaMemcpyHostToDevice, st));
-    }
+    if (use_gmask) alloc_gmask();
     nnbr.zero(st);
     ngl.zero(st);
   }
@@ -609,14 +622,16 @@ struct phafd_ctx {
   template <typename T>
   void enqueue_step() {
     mark(-1);
-    launch_step_begin(d_step(), st);
     const bool resident = schedule == PHAFD_SCHEDULE_RESIDENT && have_conj;
+    // the neighbor check increments the step counter when it runs first
+    const bool fold_step = resident && n > 0;
+    if (!fold_step) launch_step_begin(d_step(), st);
     // fixgrid_gradphi.cpp:45: "once" tests timestep == firststep after the
     // increment, which never holds inside a run: only "every" recomputes
     if (!resident && (have_conj || (have_gradphi && !gradphi_once))) gradient_from_phi<T>();
     mark(0);
     // neighbor
-    if (n > 0) neighbor_stage();
+    if (n > 0) neighbor_stage(nullptr, fold_step ? d_step() : nullptr);
     mark(1);
     // pairs (computed once: the reference's second pass reproduces the first, integrate.cpp:140-146)
     PairArgs<T> pa = pair_args<T>();
@@ -707,18 +722,18 @@ struct phafd_ctx {
   // Neighbor::decide + build.  Inside a graph capture the rebuild kernels
   // form the body of a conditional node that the check kernel switches on,
   // so a step without a rebuild runs one kernel here instead of eleven.
-  void neighbor_stage(cudaStream_t sn = nullptr) {
+  void neighbor_stage(cudaStream_t sn = nullptr, long long* step_inc = nullptr) {
     if (!sn) sn = st;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaGraph_t g = nullptr;
     CK(cudaStreamGetCaptureInfo(sn, &cs, nullptr, &g, nullptr, nullptr, nullptr));
     if (cs != cudaStreamCaptureStatusActive) {
-      launch_neighbor(ba, false, sn);
+      launch_neighbor(ba, false, sn, step_inc);
       return;
     }
     cudaGraphConditionalHandle h;
     CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
-    launch_neighbor_check(ba, h, 1, sn);
+    launch_neighbor_check(ba, h, 1, sn, step_inc);
     const cudaGraphNode_t* deps = nullptr;
     size_t ndeps = 0;
     CK(cudaStreamGetCaptureInfo(sn, &cs, nullptr, &g, &deps, nullptr, &ndeps));
@@ -921,7 +936,14 @@ int phafd_set_plane_fusion(phafd_ctx* c, int on) {
 
 int phafd_set_gradient_mask(phafd_ctx* c, int on) {
   API_BEGIN(c)
+  const bool was = c->use_gmask;
   c->use_gmask = on != 0;
+  if (c->use_gmask && !was && c->setup_done) {
+    CK(cudaSetDevice(c->device));
+    c->alloc_gmask();  // stale until the next neighbor rebuild: full stores meanwhile
+    CK(cudaStreamSynchronize(c->st));
+  }
+  if (c->setup_done) c->fill_bead_args();
   c->invalidate_graph();
   API_END(c)
 }
@@ -1587,6 +1609,28 @@ int phafd_grid_copy_device(phafd_ctx* c, int field, void* dst) {
   API_END(c)
 }
 
+int phafd_compute_grid_clusters(phafd_ctx* c, double threshold, int greater, int* labels, int* nclusters) {
+  API_BEGIN(c)
+  if (!c->gridset) throw std::invalid_argument("grid not created");
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->st));
+  DevBuf lab;
+  lab.alloc(c->nreal * sizeof(int));
+  const int rc = c->precision == PHAFD_FP64
+                     ? grid_clusters<double>(c->phi.as<double>(), c->N[0], c->N[1], c->N[2], threshold, greater,
+                                             lab.as<int>(), nclusters, c->st)
+                     : grid_clusters<float>(c->phi.as<float>(), c->N[0], c->N[1], c->N[2], threshold, greater,
+                                            lab.as<int>(), nclusters, c->st);
+  if (rc == -8) {
+    c->err = "compute grid/cluster: an iteration limit was reached";
+    return PHAFD_ERR_TIMEOUT;
+  }
+  if (rc == -7) throw std::bad_alloc();
+  if (rc != 0) throw CudaError("compute grid/cluster failed");
+  if (labels) CK(cudaMemcpy(labels, lab.p, c->nreal * sizeof(int), cudaMemcpyDeviceToHost));
+  API_END(c)
+}
+
 int phafd_deposit_density(phafd_ctx* c, void* rho) {
   API_BEGIN(c)
   if (!c->gridset || !rho) throw std::invalid_argument("grid not created");
@@ -1653,9 +1697,19 @@ int phafd_ctx_copy_state(phafd_ctx* dst, phafd_ctx* src) {
                   std::make_pair(&dst->bin_start, &src->bin_start), std::make_pair(&dst->sorted, &src->sorted),
                   std::make_pair(&dst->bin_off, &src->bin_off), std::make_pair(&dst->nbr, &src->nbr),
                   std::make_pair(&dst->nnbr, &src->nnbr), std::make_pair(&dst->gl, &src->gl),
-                  std::make_pair(&dst->ngl, &src->ngl), std::make_pair(&dst->d_counters, &src->d_counters),
-                  std::make_pair(&dst->gmask, &src->gmask)})
+                  std::make_pair(&dst->ngl, &src->ngl), std::make_pair(&dst->d_counters, &src->d_counters)})
     cp(*pr.first, *pr.second);
+  // the gradient node mask travels with the counters (its stale flag) only
+  // when both contexts keep one; otherwise dst's mask is stale until its
+  // next rebuild
+  if (dst->gmask.p) {
+    if (src->gmask.p && src->use_gmask && dst->gmask.bytes == src->gmask.bytes) {
+      cp(dst->gmask, src->gmask);
+    } else {
+      const int off = 1;
+      CK(cudaMemcpyAsync(dst->d_gmask_off(), &off, sizeof(int), cudaMemcpyHostToDevice, src->st));
+    }
+  }
   CK(cudaStreamSynchronize(src->st));
   dst->cur = src->cur;
   dst->grad_partial = src->grad_partial;

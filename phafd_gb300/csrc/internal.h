@@ -44,6 +44,13 @@ struct UpdateArgs {
   T f2;
 };
 
+// compute grid/cluster: labels (device, nx*ny*nz) of the periodic
+// 6-connected components of phi > threshold (greater) or < threshold, each
+// the smallest z + (y Nx + x) Ny of its component, -1 elsewhere (clusters.cu)
+template <typename F>
+int grid_clusters(const F* phi, int nx, int ny, int nz, double threshold, int greater, int* labels, int* nclusters,
+                  cudaStream_t st);
+
 template <typename T>
 struct GridOps {
   static int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,

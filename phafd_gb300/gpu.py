@@ -37,7 +37,7 @@ EXPORTS = [
     "phafd_half_list_size", "phafd_half_list", "phafd_grid_list_size", "phafd_grid_list",
     "phafd_stage_gradient", "phafd_stage_borders_and_build", "phafd_stage_pairs",
     "phafd_gradphi_noalloc",
-    "phafd_compute_complex", "phafd_structure_factor",
+    "phafd_compute_complex", "phafd_structure_factor", "phafd_compute_grid_clusters",
     "phafd_set_linear_substeps", "phafd_grid_device", "phafd_grid_copy_device", "phafd_deposit_density",
     "phafd_grid_add_device", "phafd_ctx_copy_state",
 ]
@@ -119,6 +119,7 @@ def load(path=None):
         "phafd_stage_pairs": [vp],
         "phafd_compute_complex": [vp, C.c_int, C.c_int, dp],
         "phafd_structure_factor": [vp, C.c_int, dp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")],
+        "phafd_compute_grid_clusters": [vp, C.c_double, C.c_int, C.c_void_p, C.POINTER(C.c_int)],
         "phafd_set_linear_substeps": [vp, C.c_int, C.c_double],
         "phafd_grid_device": [vp, C.c_int, C.POINTER(vp)],
         "phafd_grid_copy_device": [vp, C.c_int, vp],
@@ -220,6 +221,17 @@ class PhafdGPU:
         out = np.zeros((ny, nz, nx // 2 + 1), np.float64)
         self._call("phafd_compute_complex", FIELD[field], self.COMPLEX[quant], out.reshape(-1))
         return out
+
+    def compute_grid_clusters(self, threshold, condition="gt"):
+        """compute grid/cluster phi threshold gt|lt: (labels int32 [z][y][x],
+        -1 outside the clusters; number of clusters)."""
+        if condition not in ("lt", "gt"):
+            raise ValueError("Must specify lt or gt for compute grid cluster.")
+        out = np.zeros(self.shape, np.int32)
+        ncl = C.c_int(0)
+        self._call("phafd_compute_grid_clusters", float(threshold), int(condition == "gt"),
+                   out.ctypes.data_as(C.c_void_p), C.byref(ncl))
+        return out, ncl.value
 
     def structure_factor(self, nbins):
         sk = np.zeros(nbins, np.float64)

@@ -53,3 +53,16 @@ def test_gradient_read_after_masked_steps_is_complete(gpu_lib):
     a.run(5)
     b.run(5)
     assert rel_err(a.grid_get("phi"), b.grid_get("phi")) < 1e-12
+
+
+def test_mask_switched_on_during_a_run(gpu_lib):
+    """Switched on after set-up the mask starts stale (full stores) until the
+    next neighbor rebuild builds it; the trajectory is unchanged."""
+    a, ch = _run(64, False, 0.3, 10)
+    b, _ = _run(64, False, 0.3, 10, chains=ch)
+    a.set_gradient_mask(True)
+    a.run(50)
+    b.run(50)
+    assert rel_err(a.grid_get("phi"), b.grid_get("phi")) < 1e-12
+    xa, xb = a.atoms_get()[0], b.atoms_get()[0]
+    assert np.abs(xa - xb).max() < 1e-12 * np.abs(xb).max()
