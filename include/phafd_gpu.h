@@ -147,7 +147,17 @@ int phafd_set_dt(phafd_ctx* ctx, double dt);                      /* "dt" comman
 int phafd_set_timestep(phafd_ctx* ctx, long long step);           /* "timestep" command */
 int phafd_setup(phafd_ctx* ctx);                                  /* Integrate::setup, integrate.cpp:33-88 */
 int phafd_run(phafd_ctx* ctx, int nsteps);                        /* Integrate::run, integrate.cpp:90-219 */
-int phafd_run_async(phafd_ctx* ctx, int nsteps);                  /* enqueue the steps and return; phafd_synchronize
+int phafd_run_async(phafd_ctx* ctx, int nsteps);
+/* Integrate::run_until_touching (integrate.cpp:221-415): after every step the
+ * distance between the first and the last bead (stored positions) is compared
+ * with touch_point on the device.  Events: kinds[k] = 0 "cyclisation occured at
+ * step steps[k]", 1 "cyclisation interval ended at step steps[k]" (already less
+ * delay_step).  Without continue_running the run ends after the first touching
+ * step (delay_step is then 0, input.cpp:293); steps_done = the steps taken;
+ * nevents may exceed max_events (only the first max_events are stored). */
+int phafd_run_until_touching(phafd_ctx* ctx, long long nsteps, double touch_point, int continue_running,
+                             int delay_step, long long* steps_done, int max_events, long long* event_steps,
+                             int* event_kinds, int* nevents);                  /* enqueue the steps and return; phafd_synchronize
                                                                      waits and reports device status (replicas overlap) */
 int phafd_counters_get(phafd_ctx* ctx, phafd_counters* out);      /* Integrate::finalise counters, integrate.cpp:418-443 */
 int phafd_synchronize(phafd_ctx* ctx);

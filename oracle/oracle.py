@@ -60,6 +60,11 @@ def lib():
             "oracle_run": [vp, C.c_int],
             "oracle_compute_grid_clusters": [vp, C.c_double, C.c_int,
                                              np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")],
+            "oracle_run_until_touching": [vp, C.c_longlong, C.c_double, C.c_int, C.c_int,
+                                          C.POINTER(C.c_longlong), C.c_int,
+                                          np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS"),
+                                          np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS"),
+                                          C.POINTER(C.c_int)],
             "oracle_stage_gradient": [vp],
             "oracle_stage_borders_and_build": [vp],
             "oracle_stage_pairs": [vp],
@@ -227,6 +232,18 @@ class Oracle:
 
     def run(self, nsteps):
         self._call("oracle_run", nsteps)
+
+    def run_until_touching(self, nsteps, touch_point, continue_running=False, delay_step=0, max_events=1024):
+        """Integrate::run_until_touching (integrate.cpp:221-415): (steps run,
+        [(kind, step)]) with kind 0 = cyclisation at step, 1 = interval ended."""
+        done = C.c_longlong(0)
+        nev = C.c_int(0)
+        steps = np.zeros(max_events, np.int64)
+        kinds = np.zeros(max_events, np.int32)
+        self._call("oracle_run_until_touching", int(nsteps), float(touch_point), int(bool(continue_running)),
+                   int(delay_step), C.byref(done), int(max_events), steps, kinds, C.byref(nev))
+        k = min(nev.value, max_events)
+        return done.value, list(zip(kinds[:k].tolist(), steps[:k].tolist()))
 
     def compute_grid_clusters(self, threshold, condition="gt"):
         """Labels of compute grid/cluster (compute_grid_clusters.cpp:66-229):

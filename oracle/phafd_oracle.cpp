@@ -1351,6 +1351,56 @@ int oracle_run(oracle_ctx* c, int nsteps) {
   })
 }
 
+// Integrate::run_until_touching (integrate.cpp:221-415), one rank: after
+// each step the distance between the first and the last owned bead (stored,
+// wrapped positions) is compared with touch_point; events are (kind, step):
+// kind 0 "cyclisation occured at step", kind 1 "cyclisation interval ended
+// at step" (its step already less delay_step).  Without continue_running
+// the run ends after the first touching step (input.cpp:293 passes delay 0).
+static void run_until_touching_impl(oracle_ctx* c, long long nsteps, double touch_point, int continue_running,
+                                    int delay_step, long long* steps_done, int max_events, long long* ev_step,
+                                    int* ev_kind, int* nevents) {
+  if (!c->setup_done) c->setup();
+  int since = delay_step, breakflag = 0, nev = 0;
+  long long s = 0;
+  auto record = [&](int kind, long long step) {
+    if (nev < max_events) {
+      ev_kind[nev] = kind;
+      ev_step[nev] = step;
+    }
+    ++nev;
+  };
+  for (; s < nsteps; ++s) {
+    c->step();
+    if (c->nan_flag) throw std::runtime_error("NAN encountered in phi.");
+    if (c->semi_fail) throw std::runtime_error("Failed to maintain polymer bond-length constraints.");
+    const int last = c->nowned - 1;
+    const double d0 = c->X(0, last) - c->X(0, 0), d1 = c->X(1, last) - c->X(1, 0), d2 = c->X(2, last) - c->X(2, 0);
+    const double d = std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    if (d < touch_point) {
+      if (since >= delay_step) record(0, c->timestep);
+      since = 0;
+      breakflag = 1;
+    } else {
+      if (breakflag && since == delay_step) record(1, c->timestep - delay_step);
+      since += 1;
+    }
+    if (!continue_running && breakflag) {
+      ++s;
+      break;
+    }
+  }
+  *steps_done = s;
+  *nevents = nev;
+}
+
+int oracle_run_until_touching(oracle_ctx* c, long long nsteps, double touch_point, int continue_running,
+                              int delay_step, long long* steps_done, int max_events, long long* ev_step,
+                              int* ev_kind, int* nevents) {
+  GUARD(c, { run_until_touching_impl(c, nsteps, touch_point, continue_running, delay_step, steps_done, max_events,
+                                     ev_step, ev_kind, nevents); })
+}
+
 // Stage hooks used by unit tests
 int oracle_stage_gradient(oracle_ctx* c) { GUARD(c, { c->gradient(); }) }
 int oracle_stage_borders_and_build(oracle_ctx* c) { GUARD(c, { c->pbc(); c->borders(); c->neighbor_build(); }) }

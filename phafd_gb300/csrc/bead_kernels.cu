@@ -864,6 +864,42 @@ void launch_gmask_guard(const BeadArgs& a, cudaStream_t st) {
   k_gmask_guard<<<nblk(a.n, 256), 256, 0, st>>>(a);
 }
 
+// integrate.cpp:350-370: |x_last - x_first| of the stored (wrapped)
+// positions, operations in the reference's order (no contraction)
+__global__ void k_touch(const double* __restrict__ x, int n, double touch_point, int delay_step,
+                        const long long* __restrict__ d_step, TouchState* s) {
+  const int l = 3 * (n - 1);
+  const double d0 = x[l] - x[0], d1 = x[l + 1] - x[1], d2 = x[l + 2] - x[2];
+  const double d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
+  const long long step = *d_step;
+  if (d < touch_point) {
+    if (s->since >= delay_step) {
+      if (s->nev < s->maxev) {
+        s->ev_kind[s->nev] = 0;
+        s->ev_step[s->nev] = step;
+      }
+      s->nev += 1;
+    }
+    s->since = 0;
+    s->breakflag = 1;
+  } else {
+    if (s->breakflag && s->since == delay_step) {
+      if (s->nev < s->maxev) {
+        s->ev_kind[s->nev] = 1;
+        s->ev_step[s->nev] = step - delay_step;
+      }
+      s->nev += 1;
+    }
+    s->since += 1;
+  }
+}
+
+void launch_touch(const double* x, int n, double touch_point, int delay_step, const long long* d_step,
+                  TouchState* s, cudaStream_t st) {
+  if (n <= 0) return;
+  k_touch<<<1, 1, 0, st>>>(x, n, touch_point, delay_step, d_step, s);
+}
+
 void launch_rebuild(const BeadArgs& a, cudaStream_t st) {
   if (a.n == 0) return;
   const int T = 256;

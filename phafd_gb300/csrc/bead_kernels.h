@@ -79,6 +79,16 @@ void launch_neighbor(const BeadArgs& a, bool force, cudaStream_t st, long long* 
 void launch_neighbor_check(const BeadArgs& a, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st,
                            long long* step_inc = nullptr);
 void launch_rebuild(const BeadArgs& a, cudaStream_t st);
+
+// Integrate::run_until_touching state (integrate.cpp:221-415), on the device
+struct TouchState {
+  int since, breakflag, nev, maxev;
+  long long ev_step[1024];
+  int ev_kind[1024];  // 0: cyclisation at step, 1: cyclisation interval ended at step
+};
+// after a step: distance between the first and the last bead against touch_point
+void launch_touch(const double* x, int n, double touch_point, int delay_step, const long long* d_step,
+                  TouchState* s, cudaStream_t st);
 // sets *gmask_off when a bead moved more than sqrt(gmask_guardsq) since the last rebuild
 void launch_gmask_guard(const BeadArgs& a, cudaStream_t st);
 template <typename T> void launch_pair(const BeadArgs& a, const PairArgs<T>& p, cudaStream_t st);

@@ -39,6 +39,21 @@ __device__ int cl_find(int* p, int v, long long cap, int* err) {
   }
 }
 
+// root of v without writing: in the flatten pass each thread stores only its
+// own node's root, and a halving write from another thread could otherwise
+// put an older ancestor back over it
+__device__ int cl_root(const int* p, int v, long long cap, int* err) {
+  for (long long it = 0;; ++it) {
+    const int pv = p[v];
+    if (pv == v) return v;
+    v = pv;
+    if (it > cap) {
+      atomicExch(err, 1);
+      return v;
+    }
+  }
+}
+
 __device__ void cl_hook(int* p, int a, int b, long long cap, int* err) {
   int ra = cl_find(p, a, cap, err), rb = cl_find(p, b, cap, err);
   for (long long it = 0; ra != rb; ++it) {
@@ -83,7 +98,7 @@ __global__ void k_cl_roots(int* p, int* minid, int nx, int ny, long long n, long
                            int* count) {
   for (long long i = blockIdx.x * (long long)T + threadIdx.x; i < n; i += (long long)gridDim.x * T) {
     if (p[i] < 0) continue;
-    const int r = cl_find(p, (int)i, cap, err);
+    const int r = cl_root(p, (int)i, cap, err);
     p[i] = r;
     if (r == (int)i) atomicAdd(count, 1);
     const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long long)nx * ny));

@@ -21,6 +21,7 @@
 // whole step is captured once into a CUDA graph and replayed.
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <random>
@@ -172,6 +173,11 @@ struct phafd_ctx {
   DevBuf nbr, nnbr, gl, ngl;
   DevBuf dragc, sf_fix, sf_start, sf_len, sf_par;
   DevBuf gmask;  // one bit per 32-byte sector of a real field (beads with a grid coupling)
+  // run_until_touching: a check after every step while set
+  DevBuf touch;
+  bool touch_on = false;
+  double touch_point = 0.0;
+  int touch_delay = 0;
   BeadArgs ba{};
   // pairs
   bool have_lj = false;
@@ -717,6 +723,8 @@ struct phafd_ctx {
       CK(cudaEventRecord(ev_join, st2));
       CK(cudaStreamWaitEvent(st, ev_join, 0));
     }
+    if (touch_on && n > 0)
+      launch_touch(bx.as<double>(), n, touch_point, touch_delay, d_step(), touch.as<TouchState>(), st);
   }
 
   // Neighbor::decide + build.  Inside a graph capture the rebuild kernels
@@ -1266,6 +1274,70 @@ int phafd_run(phafd_ctx* c, int nsteps) {
   CK(cudaStreamSynchronize(c->st));
   if (c->keep_chempot && c->have_conj && nsteps > 0) c->chempot_from_mu = true;
   int rc = check_status(c);
+  if (rc) return rc;
+  API_END(c)
+}
+
+int phafd_run_until_touching(phafd_ctx* c, long long nsteps, double touch_point, int continue_running,
+                             int delay_step, long long* steps_done, int max_events, long long* event_steps,
+                             int* event_kinds, int* nevents) {
+  API_BEGIN(c)
+  CK(cudaSetDevice(c->device));
+  if (c->n < 1) throw std::invalid_argument("run_until_touching needs beads");
+  if (!c->setup_done) {
+    int rc = phafd_setup(c);
+    if (rc) return rc;
+  }
+  if (!continue_running) delay_step = 0;  // input.cpp:293
+  TouchState init{};
+  init.since = delay_step;
+  init.maxev = 1024;
+  c->touch.alloc(sizeof(TouchState));
+  CK(cudaMemcpy(c->touch.p, &init, sizeof(init), cudaMemcpyHostToDevice));
+  c->touch_on = true;
+  c->touch_point = touch_point;
+  c->touch_delay = delay_step;
+  c->invalidate_graph();
+  long long done = 0;
+  int rc = 0;
+  try {
+    if (continue_running) {
+      for (long long left = nsteps; left > 0 && rc == 0;) {
+        const int chunk = (int)std::min<long long>(left, 1 << 20);
+        enqueue_run(c, chunk);
+        CK(cudaStreamSynchronize(c->st));
+        rc = check_status(c);
+        left -= chunk;
+        done += chunk;
+      }
+    } else {
+      // one step at a time: the run ends right after the first touching step
+      for (; done < nsteps && rc == 0;) {
+        enqueue_run(c, 1);
+        int flag = 0;
+        CK(cudaMemcpyAsync(&flag, (char*)c->touch.p + offsetof(TouchState, breakflag), sizeof(int),
+                           cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        rc = check_status(c);
+        ++done;
+        if (flag) break;
+      }
+    }
+  } catch (...) {
+    c->touch_on = false;
+    c->invalidate_graph();
+    throw;
+  }
+  TouchState out{};
+  CK(cudaMemcpy(&out, c->touch.p, sizeof(out), cudaMemcpyDeviceToHost));
+  c->touch_on = false;
+  c->invalidate_graph();
+  if (steps_done) *steps_done = done;
+  if (nevents) *nevents = out.nev;
+  for (int k = 0; k < std::min(out.nev, std::min(max_events, out.maxev)); ++k) {
+    if (event_steps) event_steps[k] = out.ev_step[k];
+    if (event_kinds) event_kinds[k] = out.ev_kind[k];
+  }
   if (rc) return rc;
   API_END(c)
 }

@@ -37,7 +37,7 @@ EXPORTS = [
     "phafd_half_list_size", "phafd_half_list", "phafd_grid_list_size", "phafd_grid_list",
     "phafd_stage_gradient", "phafd_stage_borders_and_build", "phafd_stage_pairs",
     "phafd_gradphi_noalloc",
-    "phafd_compute_complex", "phafd_structure_factor", "phafd_compute_grid_clusters",
+    "phafd_compute_complex", "phafd_structure_factor", "phafd_compute_grid_clusters", "phafd_run_until_touching",
     "phafd_set_linear_substeps", "phafd_grid_device", "phafd_grid_copy_device", "phafd_deposit_density",
     "phafd_grid_add_device", "phafd_ctx_copy_state",
 ]
@@ -120,6 +120,8 @@ def load(path=None):
         "phafd_compute_complex": [vp, C.c_int, C.c_int, dp],
         "phafd_structure_factor": [vp, C.c_int, dp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")],
         "phafd_compute_grid_clusters": [vp, C.c_double, C.c_int, C.c_void_p, C.POINTER(C.c_int)],
+        "phafd_run_until_touching": [vp, C.c_longlong, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_longlong),
+                                     C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)],
         "phafd_set_linear_substeps": [vp, C.c_int, C.c_double],
         "phafd_grid_device": [vp, C.c_int, C.POINTER(vp)],
         "phafd_grid_copy_device": [vp, C.c_int, vp],
@@ -221,6 +223,19 @@ class PhafdGPU:
         out = np.zeros((ny, nz, nx // 2 + 1), np.float64)
         self._call("phafd_compute_complex", FIELD[field], self.COMPLEX[quant], out.reshape(-1))
         return out
+
+    def run_until_touching(self, nsteps, touch_point, continue_running=False, delay_step=0, max_events=1024):
+        """Integrate::run_until_touching: (steps run, [(kind, step)]), kind 0 =
+        cyclisation at step, 1 = cyclisation interval ended at step."""
+        done = C.c_longlong(0)
+        nev = C.c_int(0)
+        steps = np.zeros(max_events, np.int64)
+        kinds = np.zeros(max_events, np.int32)
+        self._call("phafd_run_until_touching", int(nsteps), float(touch_point), int(bool(continue_running)),
+                   int(delay_step), C.byref(done), int(max_events), steps.ctypes.data_as(C.c_void_p),
+                   kinds.ctypes.data_as(C.c_void_p), C.byref(nev))
+        k = min(nev.value, max_events)
+        return done.value, list(zip(kinds[:k].tolist(), steps[:k].tolist()))
 
     def compute_grid_clusters(self, threshold, condition="gt"):
         """compute grid/cluster phi threshold gt|lt: (labels int32 [z][y][x],
