@@ -208,8 +208,19 @@ class Interpreter {
       run(std::stoll(w.at(0)));
     } else if (cmd == "write_field") {
       write_field(w.at(0), w.at(1));
-    } else if (cmd == "run_until_touching") {
-      throw std::runtime_error("run_until_touching is not supported by phafd_gpu");
+    } else if (cmd == "run_until_touching") {  // input.cpp:274-295
+      if (dt_ <= 0.0) throw std::runtime_error("Cannot run simulation without setting dt > 0.");
+      const long long nsteps = std::stoll(w.at(0));
+      if (w.size() < 2) throw std::runtime_error("Must provide a size at which atoms are considered touching.");
+      if (w.size() < 3) throw std::runtime_error("Must say whether to continue simulation after touching occurs.");
+      if (w[2] == "continue") {
+        if (w.size() < 4) throw std::runtime_error("Must say delay to mention new cyclisation events.");
+        run_until_touching(nsteps, num(w[1]), true, (int)num(w[3]));
+      } else if (w[2] == "stop") {
+        run_until_touching(nsteps, num(w[1]), false, 0);
+      } else {
+        throw std::runtime_error("Must say whether to continue simulation after touching occurs.");
+      }
     } else {
       throw std::invalid_argument("Unknown command: " + cmd);
     }
@@ -457,6 +468,39 @@ class Interpreter {
     std::ofstream f(fname, std::ios::binary);
     if (!f) throw std::runtime_error("cannot open " + fname);
     f.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)(buf.size() * sizeof(double)));
+  }
+
+  // integrate.cpp:221-415: the events come back from the device in order and
+  // are printed with the reference's text after the run
+  void run_until_touching(long long nsteps, double touch, bool cont, int delay) {
+    std::cout << "Running simulation of solution." << std::endl;
+    if (dry_) {
+      std::cout << "dry run: " << nsteps << " steps parsed" << std::endl;
+      return;
+    }
+    check(phafd_setup(ctx()));
+    auto t0 = std::chrono::steady_clock::now();
+    const int maxev = 1024;
+    std::vector<long long> steps(maxev);
+    std::vector<int> kinds(maxev);
+    long long done = 0;
+    int nev = 0;
+    check(phafd_run_until_touching(ctx(), nsteps, touch, cont ? 1 : 0, delay, &done, maxev, steps.data(),
+                                   kinds.data(), &nev));
+    auto t1 = std::chrono::steady_clock::now();
+    for (int k = 0; k < std::min(nev, maxev); ++k)
+      std::cout << (kinds[k] == 0 ? "cyclisation occured at step " : "cyclisation interval ended at step ")
+                << steps[k] << std::endl;
+    if (nev > maxev) std::cout << "(" << nev - maxev << " further events not kept)" << std::endl;
+    phafd_counters c{};
+    check(phafd_counters_get(ctx(), &c));
+    std::cout << "number of neighbor calls = " << c.neighbor_calls << std::endl;
+    std::cout << "other flags:" << std::endl;
+    for (auto& f : fh_fixes_)  // Integrate::finalise, integrate.cpp:418-443
+      std::cout << f.first << " had phi < 0 " << c.num_less_zero << " times, and phi > 1 " << c.num_great_zero
+                << "times." << std::endl;
+    std::cout << "Run time = " << std::chrono::duration_cast<std::chrono::microseconds>(t1 - t0).count() / 1e6
+              << "seconds." << std::endl;
   }
 
   void run(long long nsteps) {  // integrate.cpp:90-219

@@ -125,3 +125,32 @@ def test_script_run_matches_binding(exe, tmp_path, gpu_lib):
     # atomics, so two runs agree to FP32 round-off, not bit for bit
     ref = g.grid_get("phi")
     assert np.abs(ref - phi_script).max() < 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("line,msg", [
+    ("run_until_touching 20 1.5 stop", None),
+    ("run_until_touching 20 1.5 continue 5", None),
+    ("run_until_touching 20", "Must provide a size at which atoms are considered touching."),
+    ("run_until_touching 20 1.5", "Must say whether to continue simulation after touching occurs."),
+    ("run_until_touching 20 1.5 continue", "Must say delay to mention new cyclisation events."),
+    ("run_until_touching 20 1.5 maybe", "Must say whether to continue simulation after touching occurs."),
+])
+def test_run_until_touching_syntax(exe, tmp_path, line, msg):
+    """input.cpp:274-295 argument checks (dry run)."""
+    scene(tmp_path, SCRIPT.replace("run 20", line))
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    if msg is None:
+        assert r.returncode == 0, r.stderr
+        assert "dry run: 20 steps parsed" in r.stdout
+    else:
+        assert r.returncode == 1 and msg in r.stderr
+
+
+@pytest.mark.gpu
+def test_script_run_until_touching_stops(exe, tmp_path, gpu_lib):
+    """A touch size beyond the box: the first step touches and the run stops."""
+    scene(tmp_path, SCRIPT.replace("run 20", "run_until_touching 20 1000.0 stop"))
+    r = run(exe, tmp_path, "-sf", "gpu")
+    assert r.returncode == 0, r.stderr
+    assert "cyclisation occured at step 1" in r.stdout
+    assert "number of neighbor calls =" in r.stdout
