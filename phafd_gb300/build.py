@@ -74,8 +74,9 @@ def build(force=False, verbose=False):
         subprocess.check_call([nv] + ARCH + ["-shared", "-o", tmp] + objs)
         os.replace(tmp, LIB)
     host_srcs = [os.path.join(HOST, f) for f in sorted(os.listdir(HOST))] if os.path.isdir(HOST) else []
+    host_hdrs = [f for f in host_srcs if f.endswith(".hpp")]
     host_srcs = [f for f in host_srcs if f.endswith(".cpp")]
-    if host_srcs and (force or _newer(EXE, host_srcs + [LIB] + hdrs)):
+    if host_srcs and (force or _newer(EXE, host_srcs + host_hdrs + [LIB] + hdrs)):
         tmp = EXE + ".tmp%d" % os.getpid()
         subprocess.check_call(["g++", "-O2", "-std=c++17", "-o", tmp] + host_srcs +
                               ["-I" + os.path.join(ROOT, "include"), "-L" + OUT, "-lphafd_gpu",

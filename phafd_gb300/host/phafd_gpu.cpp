@@ -12,8 +12,11 @@
 //   package gpu [precision 32|64] [schedule resident|reference]
 //               [zghost periodic|rank1] [noise philox|reference|off]
 //               [device N] [plane on|off]
-// and one output command for checking a run without the (out of scope) dumps:
+// and one output command for raw fields:
 //   write_field phi|chempot|gradx|grady|gradz FILE   (raw float64, [z][y][x])
+// Dumps (atom, lammpsatom, grid) are written as the reference writes them
+// (vtk_dump.hpp); per-grid attributes are phi, chempot and c_NAME of
+// compute grid/cluster.
 // "-dry-run" parses and checks the script without touching a GPU.
 #include <algorithm>
 #include <chrono>
@@ -31,6 +34,7 @@
 #include <vector>
 
 #include "phafd_gpu.h"
+#include "vtk_dump.hpp"
 
 namespace {
 
@@ -129,6 +133,10 @@ class Interpreter {
   double dt_ = 0.0;
   long long timestep_ = 0;
   std::vector<std::pair<std::string, bool>> fh_fixes_;  // names of grid/floryhuggins fixes
+  std::vector<phafd_dump::Spec> dumps_;
+  struct Cluster { double threshold; bool greater; };
+  std::map<std::string, Cluster> clusters_;  // compute NAME grid/cluster phi THRESHOLD lt|gt
+  std::set<std::string> compute_names_;
 
   void check(int rc) {
     if (rc != PHAFD_OK) throw std::runtime_error(ctx_ ? phafd_last_error(ctx_) : "libphafd_gpu call failed");
@@ -194,9 +202,10 @@ class Interpreter {
       command_group(w);
     } else if (cmd == "fix") {
       command_fix(w);
-    } else if (cmd == "compute" || cmd == "dump") {
-      std::cerr << "WARNING: " << cmd << " " << (w.empty() ? "" : w[0])
-                << " is outside the GPU particle-field step and is ignored." << std::endl;
+    } else if (cmd == "compute") {
+      command_compute(w);
+    } else if (cmd == "dump") {
+      command_dump(w);
     } else if (cmd == "timestep") {
       timestep_ = std::stoll(w.at(0));
       if (!dry_) check(phafd_set_timestep(ctx(), timestep_));
@@ -456,6 +465,107 @@ class Interpreter {
     }
   }
 
+  // Compute::init + ComputeGridClusters::init (compute.cpp:13-27,
+  // compute_grid_clusters.cpp:23-64); other computes only feed dumps of the
+  // reference and are not built here
+  void command_compute(const Words& w) {
+    const std::string name = w.at(0);
+    if (compute_names_.count(name)) throw std::runtime_error("Error: Duplicate of compute " + name + std::string("."));
+    compute_names_.insert(name);
+    const std::string style = w.at(1);
+    if (style == "grid/cluster" || style == "grid/cluster/gpu") {
+      if (w.at(2) != "phi") throw std::runtime_error("Must use phi as array for clustering.");
+      const double thr = num(w.at(3));
+      const std::string cond = w.at(4);
+      if (cond != "lt" && cond != "gt") throw std::runtime_error("Must specify lt or gt for compute grid cluster.");
+      clusters_[name] = Cluster{thr, cond == "gt"};
+    } else {
+      std::cerr << "WARNING: compute " << name << " " << style << " is not built by phafd_gpu and is ignored."
+                << std::endl;
+    }
+  }
+
+  // Dump::init + Dump::setup checks (dump.cpp:28-233)
+  void command_dump(const Words& w) {
+    phafd_dump::Spec d = phafd_dump::parse(w);
+    for (auto& o : dumps_)
+      if (o.name == d.name) throw std::runtime_error("Error: Duplicate of dump " + d.name + std::string("."));
+    if (d.type == "ftgrid") throw std::runtime_error("ftgrid dumps are not built by phafd_gpu");
+    if (d.type == "grid") {
+      if (!gridset_) throw std::runtime_error("phi does not exist, but needed to save dump.");
+      for (auto& a : d.attributes) {
+        if (a.rfind("c_", 0) == 0) {
+          if (!clusters_.count(a.substr(2)))
+            throw std::runtime_error("Cannot write dump, compute ID " + a.substr(2) + std::string("doesn't exist."));
+        } else if (a.rfind("gradphi_", 0) == 0) {
+          // the reference's arrays hold the gradient of the step's starting
+          // phi; the resident state holds the gradient of the current phi
+          throw std::runtime_error("gradphi attributes are not written by phafd_gpu (use write_field)");
+        } else if (a == "chempot") {
+          if (!dry_) check(phafd_set_keep_chempot(ctx(), 1));
+        } else if (a != "phi") {
+          throw std::runtime_error("Dump error: Attribute does not exist.");
+        }
+      }
+    } else {
+      phafd_dump::check_atoms(d);
+    }
+    dumps_.push_back(d);
+  }
+
+  void write_dumps(bool force_all) {
+    bool any = false;
+    for (auto& d : dumps_) any = any || force_all || timestep_ % d.every == 0;
+    if (!any) return;
+    std::cout << "Saving on step " << timestep_ << std::endl;
+    const size_t nr = (size_t)grid_n_[0] * grid_n_[1] * grid_n_[2];
+    std::vector<double> x, ux, f;
+    std::vector<int> img;
+    std::map<std::string, std::vector<double>> fields;
+    for (auto& d : dumps_) {
+      if (!force_all && timestep_ % d.every != 0) continue;
+      phafd_dump::Atoms a;
+      phafd_dump::Grid g;
+      if (d.type == "grid") {
+        g.nx = grid_n_[0]; g.ny = grid_n_[1]; g.nz = grid_n_[2];
+        for (int k = 0; k < 3; ++k) {
+          g.boxlo[k] = boxlo_[k];
+          g.spacing[k] = period_[k] / grid_n_[k];
+        }
+        for (auto& att : d.attributes) {
+          if (!fields.count(att)) {
+            std::vector<double> buf(nr);
+            if (att == "phi") {
+              check(phafd_grid_get(ctx(), PHAFD_FIELD_PHI, buf.data()));
+            } else if (att == "chempot") {
+              check(phafd_grid_get(ctx(), PHAFD_FIELD_CHEMPOT, buf.data()));
+            } else {
+              const Cluster& c = clusters_.at(att.substr(2));
+              std::vector<int> lab(nr);
+              check(phafd_compute_grid_clusters(ctx(), c.threshold, c.greater ? 1 : 0, lab.data(), nullptr));
+              for (size_t k = 0; k < nr; ++k) buf[k] = lab[k];
+            }
+            fields[att] = std::move(buf);
+          }
+          g.fields[att] = fields[att].data();
+        }
+      } else {
+        if (x.empty()) {
+          x.resize(3 * (size_t)natoms_); ux.resize(x.size()); f.resize(x.size()); img.resize(natoms_);
+          check(phafd_atoms_get(ctx(), x.data(), ux.data(), f.data(), img.data()));
+        }
+        a.n = natoms_;
+        a.x = x.data(); a.ux = ux.data(); a.f = f.data(); a.images = img.data();
+        a.tags = tags_.data(); a.mols = mols_.data(); a.types = types_.data();
+        for (int k = 0; k < 3; ++k) {
+          a.boxlo[k] = boxlo_[k];
+          a.boxhi[k] = boxlo_[k] + period_[k];
+        }
+      }
+      phafd_dump::write_step(d, timestep_, dt_, &a, &g);
+    }
+  }
+
   void write_field(const std::string& field, const std::string& fname) {
     const std::map<std::string, int> ids = {{"phi", PHAFD_FIELD_PHI}, {"chempot", PHAFD_FIELD_CHEMPOT},
                                             {"gradx", PHAFD_FIELD_GRADX}, {"grady", PHAFD_FIELD_GRADY},
@@ -473,6 +583,7 @@ class Interpreter {
   // integrate.cpp:221-415: the events come back from the device in order and
   // are printed with the reference's text after the run
   void run_until_touching(long long nsteps, double touch, bool cont, int delay) {
+    if (!dumps_.empty()) throw std::runtime_error("phafd_gpu writes no dumps during run_until_touching");
     std::cout << "Running simulation of solution." << std::endl;
     if (dry_) {
       std::cout << "dry run: " << nsteps << " steps parsed" << std::endl;
@@ -510,10 +621,22 @@ class Interpreter {
       return;
     }
     check(phafd_setup(ctx()));
+    // Integrate::setup (integrate.cpp:47-84): collection headers, then the
+    // dumps of the starting step
+    for (auto& d : dumps_) phafd_dump::collection_header(d);
+    write_dumps(false);
     auto t0 = std::chrono::steady_clock::now();
     const long long chunk = 1000;
-    for (long long s = 0; s < nsteps; s += chunk) check(phafd_run(ctx(), (int)std::min(chunk, nsteps - s)));
+    for (long long s = 0; s < nsteps;) {
+      long long n = std::min(chunk, nsteps - s);
+      for (auto& d : dumps_) n = std::min(n, d.every - timestep_ % d.every);  // stop at the next dump step
+      check(phafd_run(ctx(), (int)n));
+      s += n;
+      timestep_ += n;
+      write_dumps(false);  // integrate.cpp:179-186
+    }
     auto t1 = std::chrono::steady_clock::now();
+    for (auto& d : dumps_) phafd_dump::collection_footer(d);
     phafd_counters c{};
     check(phafd_counters_get(ctx(), &c));
     for (auto& f : fh_fixes_)  // Integrate::finalise, integrate.cpp:418-443

@@ -71,7 +71,7 @@ def test_dry_run_parses_reference_script(exe, tmp_path):
     r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
     assert r.returncode == 0, r.stderr
     assert "dry run: 20 steps parsed" in r.stdout
-    assert "dump realgrid" in r.stderr  # dumps are outside the step: warned, not run
+    assert r.stderr == ""  # the grid dump is a built command now
 
 
 def test_styles_need_the_gpu_suffix(exe, tmp_path):
@@ -127,6 +127,15 @@ def test_script_run_matches_binding(exe, tmp_path, gpu_lib):
     assert np.abs(ref - phi_script).max() < 1e-5 * np.abs(ref).max()
 
 
+NODUMP = SCRIPT.replace("dump realgrid grid out 100 attributes 1 phi\n", "")
+
+
+def test_no_dumps_during_run_until_touching(exe, tmp_path):
+    scene(tmp_path, SCRIPT.replace("run 20", "run_until_touching 20 1.5 stop"))
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    assert r.returncode == 1 and "no dumps during run_until_touching" in r.stderr
+
+
 @pytest.mark.parametrize("line,msg", [
     ("run_until_touching 20 1.5 stop", None),
     ("run_until_touching 20 1.5 continue 5", None),
@@ -137,7 +146,7 @@ def test_script_run_matches_binding(exe, tmp_path, gpu_lib):
 ])
 def test_run_until_touching_syntax(exe, tmp_path, line, msg):
     """input.cpp:274-295 argument checks (dry run)."""
-    scene(tmp_path, SCRIPT.replace("run 20", line))
+    scene(tmp_path, NODUMP.replace("run 20", line))
     r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
     if msg is None:
         assert r.returncode == 0, r.stderr
@@ -149,7 +158,7 @@ def test_run_until_touching_syntax(exe, tmp_path, line, msg):
 @pytest.mark.gpu
 def test_script_run_until_touching_stops(exe, tmp_path, gpu_lib):
     """A touch size beyond the box: the first step touches and the run stops."""
-    scene(tmp_path, SCRIPT.replace("run 20", "run_until_touching 20 1000.0 stop"))
+    scene(tmp_path, NODUMP.replace("run 20", "run_until_touching 20 1000.0 stop"))
     r = run(exe, tmp_path, "-sf", "gpu")
     assert r.returncode == 0, r.stderr
     assert "cyclisation occured at step 1" in r.stdout
