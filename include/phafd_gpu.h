@@ -123,6 +123,12 @@ int phafd_set_gradient_mask(phafd_ctx* ctx, int on);
 /* ---- beads (atom_style / atom_populate, atom.cpp:26-110,219-252) ---- */
 int phafd_atoms_create(phafd_ctx* ctx, int n, const int* tags, const int* mol, const int* types, const double* x);
 int phafd_atoms_get(phafd_ctx* ctx, double* x, double* ux, double* f, int* images);
+/* image flags of every bead, packed as Domain::set_image (x in bits 0-9, y in
+ * 10-19, z from 20, each offset by 512): the "ix" attribute that
+ * atom_populate read_dump restores (read_dump.cpp:239-240); called after
+ * phafd_atoms_create and before phafd_setup, which rebuilds the unwrapped
+ * positions from x and these flags */
+int phafd_atoms_set_images(phafd_ctx* ctx, const int* images);
 
 /* ---- pairs (input.cpp:99-153) ---- */
 int phafd_pair_gridatom(phafd_ctx* ctx, int style, double cut);  /* PairGridAtom*::settings, pair_gridatom_gaussian.cpp:123-142 */

@@ -1085,6 +1085,15 @@ int phafd_atoms_get(phafd_ctx* c, double* x, double* ux, double* f, int* images)
   API_END(c)
 }
 
+int phafd_atoms_set_images(phafd_ctx* c, const int* images) {
+  API_BEGIN(c)
+  if (!images && c->n > 0) throw std::invalid_argument("null images");
+  if (c->setup_done) throw std::runtime_error("image flags are restored before setup");
+  CK(cudaSetDevice(c->device));
+  if (c->n > 0) CK(cudaMemcpy(c->bimage.p, images, (size_t)c->n * 4, cudaMemcpyHostToDevice));
+  API_END(c)
+}
+
 int phafd_pair_gridatom(phafd_ctx* c, int style, double cut) {
   API_BEGIN(c)
   if (c->ntypes <= 0) throw std::runtime_error("Cannot create pair style before atoms are made.");

@@ -26,7 +26,7 @@ EXPORTS = [
     "phafd_domain", "phafd_grid_style", "phafd_grid_populate_constant", "phafd_grid_set", "phafd_grid_get",
     "phafd_set_zghost", "phafd_set_schedule", "phafd_set_keep_chempot", "phafd_set_plane_fusion",
     "phafd_set_gradient_mask",
-    "phafd_atoms_create", "phafd_atoms_get",
+    "phafd_atoms_create", "phafd_atoms_get", "phafd_atoms_set_images",
     "phafd_pair_gridatom", "phafd_pair_gridatom_coeff", "phafd_pair_lj_cut",
     "phafd_neighbor",
     "phafd_fix_conjugate_volfrac", "phafd_fix_floryhuggins", "phafd_fix_gradphi", "phafd_fix_drag",
@@ -92,6 +92,7 @@ def load(path=None):
         "phafd_grid_get": [vp, C.c_int, dp],
         "phafd_atoms_create": [vp, C.c_int, ip, ip, ip, dp],
         "phafd_atoms_get": [vp, dp, dp, dp, ip],
+        "phafd_atoms_set_images": [vp, ip],
         "phafd_pair_gridatom": [vp, C.c_int, C.c_double],
         "phafd_pair_gridatom_coeff": [vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double],
         "phafd_pair_lj_cut": [vp, C.c_double, C.c_double, C.c_double],
@@ -286,6 +287,13 @@ class PhafdGPU:
         x = np.zeros((n, 3)); ux = np.zeros((n, 3)); f = np.zeros((n, 3)); im = np.zeros(n, np.int32)
         self._call("phafd_atoms_get", x.reshape(-1), ux.reshape(-1), f.reshape(-1), im)
         return x[:self.n], ux[:self.n], f[:self.n], im[:self.n]
+
+    def atoms_set_images(self, images):
+        """packed image flags of every bead (restart), before setup."""
+        im = np.ascontiguousarray(images, np.int32)
+        if len(im) != self.n:
+            raise ValueError("one image flag per bead")
+        self._call("phafd_atoms_set_images", np.ascontiguousarray(np.resize(im, max(self.n, 1))))
 
     def pair_gridatom(self, style, cut):
         self._call("phafd_pair_gridatom", GRIDATOM[style], cut)

@@ -34,6 +34,7 @@
 #include <vector>
 
 #include "phafd_gpu.h"
+#include "read_dump.hpp"
 #include "vtk_dump.hpp"
 
 namespace {
@@ -182,17 +183,20 @@ class Interpreter {
       if (!gridset_) throw std::invalid_argument("CAnnot use command grid_populate before grid_style is set.");
       if (w.size() >= 5 && w[0] == "constant" && w[1] == "concentration") {
         if (!dry_) check(phafd_grid_populate_constant(ctx(), num(w[2]), num(w[3]), inum(w[4])));
+      } else if (!w.empty() && w[0] == "read_dump") {
+        grid_read_dump(w);
       } else {
         throw std::runtime_error("grid_populate " + (w.empty() ? std::string() : w[0]) +
-                                 " is not supported by phafd_gpu (constant concentration only)");
+                                 " is not supported by phafd_gpu (constant concentration or read_dump)");
       }
       populated_ = true;
     } else if (cmd == "atom_style") {
       command_atom_style(w);
     } else if (cmd == "atom_populate") {
       if (!atomset_) throw std::invalid_argument("CAnnot use command atom_populate before atom_style is set.");
-      if (w.size() < 2 || w[0] != "read_atoms") throw std::runtime_error("Invalid atom_populate command.");
-      read_atoms(w[1]);
+      if (w.size() >= 2 && w[0] == "read_atoms") read_atoms(w[1]);
+      else if (w.size() >= 2 && w[0] == "read_dump") atom_read_dump(w);
+      else throw std::runtime_error("Invalid atom_populate command.");
     } else if (cmd == "neighbor") {
       if (npairs_ == 0 && ntypes_ > 0) throw std::runtime_error("Must call neighbor after pairs are given.");
       if (!gridset_) throw std::runtime_error("Must call neighbor after subboxes are set (via grid style).");
@@ -317,6 +321,38 @@ class Interpreter {
     ntypes_ = types_.empty() ? 0 : *std::max_element(types_.begin(), types_.end()) + 1;
     groups_["all"] = {{0, natoms_}};
     if (!dry_) check(phafd_atoms_create(ctx(), natoms_, tags_.data(), mols_.data(), types_.data(), xs_.data()));
+    atoms_made_ = true;
+  }
+
+  // grid_populate read_dump FILE attributes N ... (grid.cpp:168-176): phi is
+  // uploaded; chempot and the gradient are rebuilt from phi by every step, so
+  // the arrays read for them only pass the reference's checks
+  void grid_read_dump(const Words& w) {
+    Words v(w);
+    v[0] = "grid";
+    const auto s = phafd_dump::parse_read(v);
+    const auto fields = phafd_dump::read_grid(s, grid_n_[0], grid_n_[1], grid_n_[2]);
+    if (!dry_) check(phafd_grid_set(ctx(), PHAFD_FIELD_PHI, fields.at("phi").data()));
+  }
+
+  // atom_populate read_dump FILE attributes N ... (atom.cpp:125-134)
+  void atom_read_dump(const Words& w) {
+    Words v(w);
+    v[0] = "atom";
+    const auto s = phafd_dump::parse_read(v);
+    const auto r = phafd_dump::read_atoms(s, natoms_, molecule_flag_);
+    tags_ = r.tags;
+    mols_ = molecule_flag_ ? r.mols : std::vector<int>(natoms_, 0);
+    types_ = r.types;
+    xs_ = r.x;
+    std::set<int> ts(tags_.begin(), tags_.end());
+    if (ts.size() != tags_.size()) throw std::runtime_error("duplicate IDs found on processor(s).");
+    ntypes_ = types_.empty() ? 0 : *std::max_element(types_.begin(), types_.end()) + 1;
+    groups_["all"] = {{0, natoms_}};
+    if (!dry_) {
+      check(phafd_atoms_create(ctx(), natoms_, tags_.data(), mols_.data(), types_.data(), xs_.data()));
+      if (phafd_dump::has(s.attributes, "ix")) check(phafd_atoms_set_images(ctx(), r.images.data()));
+    }
     atoms_made_ = true;
   }
 

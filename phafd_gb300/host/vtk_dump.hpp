@@ -164,9 +164,18 @@ inline void atom_attribute(std::ostream& f, const std::string& w, const Atoms& a
   else throw std::runtime_error("Invalid per atom quantity in dump file.");
 }
 
+// the errors dump.cpp:369-409 and :956-977 raise at the first write, raised
+// when the command is read (the LAMMPS style writes the owned beads, :503)
 inline void check_atoms(const Spec& s) {
-  if (s.which_atoms != "owned" && s.which_atoms != "all")
+  if (s.type == "atom" && s.which_atoms != "owned" && s.which_atoms != "all")
     throw std::runtime_error("need atoms to be dumped to be owned, all, local, or ghost");
+  bool hasx = false;
+  for (auto& w : s.attributes) {
+    hasx = hasx || w == "x";
+    if (w != "x" && w != "F" && w != "ux" && w != "ix" && w != "ID" && w != "molID" && w != "type" && w != "label")
+      throw std::runtime_error("Invalid per atom quantity in dump file.");
+  }
+  if (s.type == "atom" && !hasx) throw std::runtime_error("Atom dump must contain positions.");
 }
 
 // write_atom_timestep + write_atom_timestep_pvtp (dump.cpp:343-480); with one

@@ -40,11 +40,11 @@ write_field phi phi.bin
 
 @pytest.fixture(scope="module")
 def exe():
-    if not os.path.exists(EXE):
-        from phafd_gb300 import build as B
-        try:
-            B.build()
-        except Exception as e:  # pragma: no cover
+    from phafd_gb300 import build as B
+    try:
+        B.build()  # incremental: relinks the host program when a source or header changed
+    except Exception as e:  # pragma: no cover
+        if not os.path.exists(EXE):
             pytest.skip("cannot build: %s" % e)
     return EXE
 
@@ -163,3 +163,151 @@ def test_script_run_until_touching_stops(exe, tmp_path, gpu_lib):
     assert r.returncode == 0, r.stderr
     assert "cyclisation occured at step 1" in r.stdout
     assert "number of neighbor calls =" in r.stdout
+
+
+DUMPS = SCRIPT.replace("dump realgrid grid out 100 attributes 1 phi\n",
+                       "compute cl grid/cluster phi 0.5 gt\n"
+                       "dump beads atom/owned vtk/beads 10 attributes 3 x ID type decimalplaces 12 fmt e\n"
+                       "dump fields grid vtk/fields 10 attributes 3 phi chempot c_cl\n"
+                       "dump traj lammpsatom vtk/traj 10 attributes 2 ID x\n")
+
+
+def test_dump_commands_parse(exe, tmp_path):
+    scene(tmp_path, DUMPS)
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    assert r.returncode == 0, r.stderr
+    assert r.stderr == ""
+    for bad, msg in [("attributes 3 phi chempot c_cl", "attributes 3 phi chempot c_nope"),
+                     ("attributes 3 x ID type", "attributes 3 x ID bogus")]:
+        scene(tmp_path, DUMPS.replace(bad, msg))
+        r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+        assert r.returncode == 1
+
+
+@pytest.mark.gpu
+def test_script_dumps_match_fields(exe, tmp_path, gpu_lib):
+    """Atom, grid (phi, chempot, cluster labels) and LAMMPS-style dumps on
+    steps 0, 10 and 20 of a script run: the last grid dump holds the phi the
+    script writes after the run, its labels equal an independent periodic
+    labelling of that phi, and the bead positions agree with a binding run."""
+    from tests.cluster_ref import periodic_min_id_labels
+    chains = scene(tmp_path, DUMPS)
+    (tmp_path / "vtk").mkdir()
+    r = run(exe, tmp_path, "-sf", "gpu")
+    assert r.returncode == 0, r.stderr
+    for t in (0, 10, 20):
+        assert "Saving on step %d" % t in r.stdout
+        for name in ("beads_p0_%d.vtp", "beads_%d.pvtp", "fields_p0_%d.vti", "fields_%d.pvti"):
+            assert (tmp_path / "vtk" / (name % t)).exists(), name % t
+    pvd = (tmp_path / "vtk" / "fields.pvd").read_text()
+    assert pvd.count("<DataSet ") == 3 and pvd.endswith("</Collection>\n</VTKFile>")
+    raw = (tmp_path / "vtk" / "fields_p0_20.vti").read_bytes()
+    at = raw.index(b"\n_") + 2
+    n = 32 ** 3
+    arrays = []
+    for c in range(3):
+        assert int.from_bytes(raw[at:at + 4], "little") == 8 * n
+        arrays.append(np.frombuffer(raw, "<f8", n, at + 4).reshape(32, 32, 32))
+        at += 4 + 8 * n
+    phi = np.fromfile(tmp_path / "phi.bin", dtype=np.float64).reshape(32, 32, 32)
+    assert np.array_equal(arrays[0], phi)
+    assert np.isfinite(arrays[1]).all() and np.abs(arrays[1]).max() > 0
+    want, _ = periodic_min_id_labels(phi, 0.5, True)
+    assert np.array_equal(arrays[2].astype(np.int64), want.astype(np.int64))
+    vtp = (tmp_path / "vtk" / "beads_p0_20.vtp").read_text()
+    body = vtp.split('format="ascii">\n')[1].split("\n</DataArray>")[0]
+    x = np.array(body.split(), dtype=np.float64).reshape(-1, 3)
+    from phafd_gb300.gpu import PhafdGPU
+    cfg = dict(W.CONFIGS["32cube_64beads"], dt=5e-4, field_noise="philox")
+    g = PhafdGPU(precision=32)
+    W.apply(g, cfg, chains=chains)
+    g.set_timestep(0)
+    g.setup()
+    g.run(20)
+    xb = g.atoms_get()[0]
+    assert x.shape == xb.shape
+    assert np.abs(x - xb).max() < 1e-5 * np.abs(xb).max()
+    lmp = (tmp_path / "vtk" / "traj_p0.lmmpstrj").read_text()
+    assert lmp.count("ITEM: TIMESTEP") == 3 and "ITEM: ATOMS ID x y z \n" in lmp
+
+
+def restart_files(tmp_path, attrs_grid=("phi",), attrs_atoms=("x", "ID", "type", "molID", "ix"), nz=32):
+    """A step-10 .vti / .vtp pair in the dump writer's format (restated in
+    tests/test_vtk_dump.py) for the 32^3 grid and 64 beads of SCRIPT."""
+    from tests.test_vtk_dump import expect_vti, expect_vtp
+    cfg = W.CONFIGS["32cube_64beads"]
+    x, tags, mol, types = W.random_walk_chains(cfg["nchains"], cfg["chain_len"], cfg["origin"], cfg["L"],
+                                               cfg["chain_seed"])
+    rng = np.random.default_rng(3)
+    g = dict(nx=32, ny=32, nz=nz, origin=(-16.0,) * 3, spacing=(1.0,) * 3,
+             fields={a: 0.5 + 0.02 * rng.standard_normal(32 * 32 * nz) for a in attrs_grid})
+    (tmp_path / "rs").mkdir(exist_ok=True)
+    (tmp_path / "rs" / "g_p0_10.vti").write_bytes(expect_vti(g, list(attrs_grid)))
+    n = len(tags)
+    img = (512 << 20) | (512 << 10) | 512
+    a = dict(n=n, x=np.asarray(x).reshape(-1), ux=np.asarray(x).reshape(-1), F=np.zeros(3 * n),
+             ints=dict(ID=tags, type=types, molID=mol, ix=np.full(n, img), label=np.zeros(n, int)))
+    (tmp_path / "rs" / "b_p0_10.vtp").write_text(expect_vtp(a, list(attrs_atoms), 16, "e"))
+
+
+RESTART = (SCRIPT.replace("grid_populate constant concentration 0.5 0.02 ${seed1}",
+                          "grid_populate read_dump rs/g_p0_10.vti attributes 1 phi")
+           .replace("atom_populate read_atoms atoms_p%.data",
+                    "atom_populate read_dump rs/b_p%_10.vtp attributes 5 x ID type molID ix")
+           .replace("timestep 0", "timestep 10"))
+
+
+def test_restart_commands_parse(exe, tmp_path):
+    scene(tmp_path, RESTART)
+    restart_files(tmp_path)
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("edit,files,msg", [
+    (("attributes 1 phi", "attributes 1 chempot"), {}, "Read dump needs attribute phi."),
+    (("attributes 1 phi", "attributes 2 phi chempot"), {}, "Not all attributes requested in read_dump command"),
+    (None, {"nz": 31}, "incorrect size phi in file."),
+    (("rs/g_p0_10.vti", "rs/none.vti"), {}, "file not found."),
+    (("attributes 5 x ID type molID ix", "attributes 4 x ID type molID"), {}, "Read dump needs attribute ix."),
+    (("attributes 5 x ID type molID ix", "attributes 6 x ID type molID ix F"), {}, "Only found attributes"),
+    (("attributes 1 phi", "attributes 1 c_cl"), {}, "Cannot read computes from dump"),
+])
+def test_restart_errors(exe, tmp_path, edit, files, msg):
+    """read_dump.cpp error checks, raised by the dry run."""
+    scene(tmp_path, RESTART.replace(*edit) if edit else RESTART)
+    restart_files(tmp_path, **files)
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    assert r.returncode == 1 and msg in r.stderr, r.stderr
+
+
+@pytest.mark.gpu
+def test_restart_continues_the_run(exe, tmp_path, gpu_lib):
+    """Run 20 steps with dumps on step 10; restart a second script from the
+    step-10 files (grid_populate / atom_populate read_dump, timestep 10) and
+    run 10 steps: both end on the same phi and bead positions.  The noise is
+    keyed by (seed, step), so only the summation order of the rebuilt
+    neighbor lists and of the FP64 deposit atomics differs."""
+    dumps = ("package gpu precision 64\n" + SCRIPT).replace(
+        "dump realgrid grid out 100 attributes 1 phi\n",
+        "dump beads atom/owned rs/b 10 attributes 5 x ID type molID ix decimalplaces 16 fmt e\n"
+        "dump fields grid rs/g 10 attributes 1 phi\n")
+    scene(tmp_path, dumps)
+    (tmp_path / "rs").mkdir()
+    r = run(exe, tmp_path, "-sf", "gpu")
+    assert r.returncode == 0, r.stderr
+    phi_a = np.fromfile(tmp_path / "phi.bin", dtype=np.float64)
+    vtp = (tmp_path / "rs" / "b_p0_20.vtp").read_text()
+    xa = np.array(vtp.split('format="ascii">\n')[1].split("\n")[0].split(), np.float64)
+    restart = ("package gpu precision 64\n" + RESTART).replace("dump realgrid grid out 100 attributes 1 phi\n",
+                                                            "dump fin atom/owned rs/c 10 attributes 1 x "
+                                                            "decimalplaces 16 fmt e\n")
+    (tmp_path / "in.phafd").write_text(restart)
+    r = run(exe, tmp_path, "-sf", "gpu")
+    assert r.returncode == 0, r.stderr
+    assert "Saving on step 20" in r.stdout
+    phi_b = np.fromfile(tmp_path / "phi.bin", dtype=np.float64)
+    vtp = (tmp_path / "rs" / "c_p0_20.vtp").read_text()
+    xb = np.array(vtp.split('format="ascii">\n')[1].split("\n")[0].split(), np.float64)
+    assert np.linalg.norm(phi_b - phi_a) < 1e-10 * np.linalg.norm(phi_a)
+    assert np.abs(xb - xa).max() < 1e-10 * np.abs(xa).max()
