@@ -127,7 +127,9 @@ int phafd_atoms_get(phafd_ctx* ctx, double* x, double* ux, double* f, int* image
  * 10-19, z from 20, each offset by 512): the "ix" attribute that
  * atom_populate read_dump restores (read_dump.cpp:239-240); called after
  * phafd_atoms_create and before phafd_setup, which rebuilds the unwrapped
- * positions from x and these flags */
+ * positions from x and these flags.  Setup then skips the initial bond-length
+ * check of the chain fixes (|bond - bondlength| <= 1e-3): the harmonic
+ * chain's bonds stretch during a run, so a restored state need not pass it */
 int phafd_atoms_set_images(phafd_ctx* ctx, const int* images);
 
 /* ---- pairs (input.cpp:99-153) ---- */

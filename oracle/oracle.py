@@ -45,6 +45,7 @@ def lib():
             "oracle_grid_get": [vp, C.c_int, dp],
             "oracle_atoms_create": [vp, C.c_int, ip, ip, ip, dp],
             "oracle_atoms_get": [vp, dp, dp, dp, ip],
+            "oracle_atoms_set_images": [vp, ip],
             "oracle_pair_gridatom": [vp, C.c_int, C.c_double],
             "oracle_pair_gridatom_coeff": [vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double],
             "oracle_pair_lj_cut": [vp, C.c_double, C.c_double, C.c_double],
@@ -182,6 +183,12 @@ class Oracle:
         self.n = len(tags)
         self._call("oracle_atoms_create", self.n, np.asarray(tags, np.int32), np.asarray(mol, np.int32),
                    np.asarray(types, np.int32), np.ascontiguousarray(x, np.float64).reshape(-1))
+
+    def atoms_set_images(self, images):
+        im = np.ascontiguousarray(images, np.int32)
+        if len(im) != self.n:
+            raise ValueError("one image flag per bead")
+        self._call("oracle_atoms_set_images", np.ascontiguousarray(np.resize(im, max(self.n, 1))))
 
     def atoms_get(self):
         x = np.zeros((self.n, 3)); ux = np.zeros((self.n, 3)); f = np.zeros((self.n, 3))

@@ -413,6 +413,7 @@ struct oracle_ctx {
   double dt = 0.0;
   long long timestep = 0, firststep = 0;
   bool setup_done = false;
+  bool images_restored = false;
   int nan_flag = 0;
   int semi_fail = 0;
   // per-stage timing (seconds) for the CPU baseline
@@ -1070,7 +1071,8 @@ struct oracle_ctx {
     }
     std::fill(Fs.begin(), Fs.end(), 0.0);
     reset_dt();
-    for (auto& f : semis)  // fixatom_semiflexible.cpp:114-140
+    for (auto& f : semis)  // fixatom_semiflexible.cpp:114-140; skipped for beads restored from a dump
+      if (!images_restored)
       for (auto& r : f.ranges)
         for (int mu = r.start + 1; mu < r.end; mu++) {
           double d0 = UX(0, mu) - UX(0, mu - 1), d1 = UX(1, mu) - UX(1, mu - 1), d2 = UX(2, mu) - UX(2, mu - 1);
@@ -1231,11 +1233,21 @@ int oracle_atoms_create(oracle_ctx* c, int n, const int* tags, const int* mol, c
     c->moltags.assign(mol ? mol : tags, (mol ? mol : tags) + n);
     c->labels.assign(n, OWNED);
     c->images.assign(n, c->set_image());
+    c->images_restored = false;
     std::set<int> ts(c->tags.begin(), c->tags.end());
     if ((int)ts.size() != n) throw std::runtime_error("duplicate IDs found on processor(s).");
     int tmax = -1;
     for (int t : c->types) tmax = std::max(tmax, t);
     c->ntypes = tmax + 1;
+  })
+}
+
+// the "ix" attribute of atom_populate read_dump (read_dump.cpp:239-240)
+int oracle_atoms_set_images(oracle_ctx* c, const int* images) {
+  GUARD(c, {
+    if (c->setup_done) throw std::runtime_error("image flags are restored before setup");
+    c->images.assign(images, images + c->nowned);
+    c->images_restored = true;
   })
 }
 

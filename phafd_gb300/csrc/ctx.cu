@@ -201,6 +201,7 @@ struct phafd_ctx {
   double dt = 0;
   long long timestep = 0, firststep = 0;
   bool setup_done = false;
+  bool images_restored = false;  // beads restored from a dump: no initial bond check
   // device counters
   DevBuf d_counters;  // [0..1] FH counters (ull), [2] step, [3] nan_step, [4] ncalls, [5] flag|status,
                       // [6] blocks of the neighbor check done | gradient mask off
@@ -1050,6 +1051,7 @@ int phafd_atoms_create(phafd_ctx* c, int n, const int* tags, const int* mol, con
   if (n < 0) throw std::invalid_argument("negative bead count");
   CK(cudaSetDevice(c->device));
   c->n = n;
+  c->images_restored = false;
   c->tags.assign(tags, tags + n);
   c->types.assign(types, types + n);
   c->mol.assign(mol ? mol : tags, (mol ? mol : tags) + n);
@@ -1091,6 +1093,7 @@ int phafd_atoms_set_images(phafd_ctx* c, const int* images) {
   if (c->setup_done) throw std::runtime_error("image flags are restored before setup");
   CK(cudaSetDevice(c->device));
   if (c->n > 0) CK(cudaMemcpy(c->bimage.p, images, (size_t)c->n * 4, cudaMemcpyHostToDevice));
+  c->images_restored = true;
   API_END(c)
 }
 
@@ -1222,9 +1225,17 @@ int phafd_setup(phafd_ctx* c) {
   if (c->have_conj && c->dt <= 0.0) throw std::runtime_error("Cannot run simulation without setting dt > 0.");
   if (c->have_conj && c->geom.nx == 0) throw std::runtime_error("grid not created");
   // FixAtomSemiFlexible::check_bonds, fixatom_semiflexible.cpp:114-140 (on positions as given)
-  if (!c->semis.empty()) {
+  if (!c->semis.empty() && !c->images_restored) {
+    // FixAtomSemiFlexible::check_bonds on the unwrapped positions
+    // (fixatom_semiflexible.cpp:114-140)
     std::vector<double> x(3 * (size_t)c->n);
+    std::vector<int> img(c->n);
     CK(cudaMemcpy(x.data(), c->bx.p, x.size() * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(img.data(), c->bimage.p, img.size() * 4, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < c->n; ++i) {
+      const int box[3] = {(img[i] & 1023) - 512, (img[i] >> 10 & 1023) - 512, (img[i] >> 20) - 512};
+      for (int d = 0; d < 3; ++d) x[3 * i + d] += box[d] * c->period[d];
+    }
     for (auto& f : c->semis)
       for (auto& r : f.first)
         for (int mu = r.start + 1; mu < r.end; ++mu) {

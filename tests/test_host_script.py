@@ -254,7 +254,7 @@ RESTART = (SCRIPT.replace("grid_populate constant concentration 0.5 0.02 ${seed1
                           "grid_populate read_dump rs/g_p0_10.vti attributes 1 phi")
            .replace("atom_populate read_atoms atoms_p%.data",
                     "atom_populate read_dump rs/b_p%_10.vtp attributes 5 x ID type molID ix")
-           .replace("timestep 0", "timestep 10"))
+           .replace("timestep 0", "timestep 10").replace("run 20", "run 10"))
 
 
 def test_restart_commands_parse(exe, tmp_path):
@@ -305,7 +305,7 @@ def test_restart_continues_the_run(exe, tmp_path, gpu_lib):
     (tmp_path / "in.phafd").write_text(restart)
     r = run(exe, tmp_path, "-sf", "gpu")
     assert r.returncode == 0, r.stderr
-    assert "Saving on step 20" in r.stdout
+    assert "Saving on step 20" in r.stdout and "Saving on step 30" not in r.stdout
     phi_b = np.fromfile(tmp_path / "phi.bin", dtype=np.float64)
     vtp = (tmp_path / "rs" / "c_p0_20.vtp").read_text()
     xb = np.array(vtp.split('format="ascii">\n')[1].split("\n")[0].split(), np.float64)
