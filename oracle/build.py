@@ -11,13 +11,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libphafd_oracle.so")
 SRC = os.path.join(HERE, "phafd_oracle.cpp")
-FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
+FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 
 
 def build(force=False):
     os.makedirs(OUT_DIR, exist_ok=True)
     deps = [SRC, os.path.join(HERE, "phafd_oracle.h"),
-            os.path.join(HERE, "..", "include", "phafd_gpu.h")]
+            os.path.join(HERE, "..", "include", "phafd_gpu.h"), os.path.abspath(__file__)]
     if not force and os.path.exists(LIB):
         if os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
             return LIB

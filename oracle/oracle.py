@@ -78,6 +78,7 @@ def lib():
             "oracle_fft_r2c": [C.c_int, C.c_int, C.c_int, dp, dp],
             "oracle_fft_c2r": [C.c_int, C.c_int, C.c_int, dp, dp],
             "oracle_make_unique_seed": [C.c_int],
+            "oracle_set_threads": [C.c_int],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -92,6 +93,20 @@ def lib():
         L.oracle_bead_gauss.restype = None
         _lib = L
     return _lib
+
+
+def set_threads(n):
+    """Host threads of the oracle's grid loops (FFT lines, pointwise passes,
+    the bulk mode update).  Results are bit-identical for any count."""
+    lib().oracle_set_threads(int(n))
+
+
+def host_threads():
+    """The cores this process may run on."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:  # pragma: no cover
+        return os.cpu_count() or 1
 
 
 def fft_r2c(phi):

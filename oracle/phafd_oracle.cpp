@@ -59,6 +59,7 @@
 #include <set>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "phafd_oracle.h"
@@ -100,6 +101,27 @@ struct Philox {
 // 53-bit uniform in [0,1) from two words
 inline double u53(uint32_t a, uint32_t b) {
   return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+// ------------------------------------------------------------------ threads
+// Host threads for the grid loops (oracle_set_threads; 1 by default).  Every
+// split loop writes disjoint elements with the serial loop's arithmetic, and
+// integer counters are summed per thread, so results are bit-identical for
+// any thread count.
+int g_threads = 1;
+
+// f(begin, end, thread) over contiguous chunks of [0, n)
+template <typename F>
+void par_for(long long n, F&& f) {
+  const int T = (int)std::max(1LL, std::min((long long)g_threads, n));
+  if (T == 1) {
+    if (n > 0) f(0LL, n, 0);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 1; t < T; ++t) th.emplace_back([&f, n, t, T] { f(n * t / T, n * (t + 1) / T, t); });
+  f(0LL, n / T, 0);
+  for (auto& x : th) x.join();
 }
 
 // ------------------------------------------------------------------ FFT
@@ -182,78 +204,95 @@ struct FFT3 {
 
   // real [z][y][x] -> complex ref layout [ky][kz][kx]   (fftw r2c, unnormalised)
   void r2c(const double* r, cd* c) {
-    std::vector<cd> z(nx);
     const int nrows = ny * nz;
-    for (int row = 0; row < nrows; row += 2) {
-      const double* a = r + (size_t)row * nx;
-      const double* b = (row + 1 < nrows) ? r + (size_t)(row + 1) * nx : nullptr;
-      for (int x = 0; x < nx; ++x) z[x] = cd(a[x], b ? b[x] : 0.0);
-      px.exec(z.data(), -1);
-      cd* ha = &H[(size_t)row * nxh];
-      cd* hb = b ? &H[(size_t)(row + 1) * nxh] : nullptr;
-      for (int k = 0; k <= nx / 2; ++k) {
-        cd zk = z[k], zm = std::conj(z[(nx - k) % nx]);
-        ha[k] = 0.5 * (zk + zm);
-        if (hb) hb[k] = cd(0.0, -0.5) * (zk - zm);
+    par_for((nrows + 1) / 2, [&](long long b, long long e, int) {
+      Plan1D p(px);
+      std::vector<cd> z(nx);
+      for (int row = 2 * (int)b; row < 2 * (int)e; row += 2) {
+        const double* a = r + (size_t)row * nx;
+        const double* bb = (row + 1 < nrows) ? r + (size_t)(row + 1) * nx : nullptr;
+        for (int x = 0; x < nx; ++x) z[x] = cd(a[x], bb ? bb[x] : 0.0);
+        p.exec(z.data(), -1);
+        cd* ha = &H[(size_t)row * nxh];
+        cd* hb = bb ? &H[(size_t)(row + 1) * nxh] : nullptr;
+        for (int k = 0; k <= nx / 2; ++k) {
+          cd zk = z[k], zm = std::conj(z[(nx - k) % nx]);
+          ha[k] = 0.5 * (zk + zm);
+          if (hb) hb[k] = cd(0.0, -0.5) * (zk - zm);
+        }
       }
-    }
-    for (int zz = 0; zz < nz; ++zz)
-      for (int k = 0; k < nxh; ++k) {
-        for (int y = 0; y < ny; ++y) line[y] = H[((size_t)zz * ny + y) * nxh + k];
-        py.exec(line.data(), -1);
-        for (int y = 0; y < ny; ++y) H[((size_t)zz * ny + y) * nxh + k] = line[y];
-      }
-    for (int y = 0; y < ny; ++y)
-      for (int k = 0; k < nxh; ++k) {
-        for (int zz = 0; zz < nz; ++zz) line[zz] = H[((size_t)zz * ny + y) * nxh + k];
-        pz.exec(line.data(), -1);
-        for (int zz = 0; zz < nz; ++zz) H[((size_t)zz * ny + y) * nxh + k] = line[zz];
-      }
-    for (int ky = 0; ky < ny; ++ky)
-      for (int kz = 0; kz < nz; ++kz)
-        for (int k = 0; k < nxh; ++k)
-          c[((size_t)ky * nz + kz) * nxh + k] = H[((size_t)kz * ny + ky) * nxh + k];
+    });
+    ypass(-1);
+    zpass(-1);
+    par_for(ny, [&](long long b, long long e, int) {
+      for (int ky = (int)b; ky < (int)e; ++ky)
+        for (int kz = 0; kz < nz; ++kz)
+          for (int k = 0; k < nxh; ++k)
+            c[((size_t)ky * nz + kz) * nxh + k] = H[((size_t)kz * ny + ky) * nxh + k];
+    });
+  }
+
+  // the y transforms of every (z, kx) line of H
+  void ypass(int sign) {
+    par_for(nz, [&](long long b, long long e, int) {
+      Plan1D p(py);
+      std::vector<cd> ln(ny);
+      for (int zz = (int)b; zz < (int)e; ++zz)
+        for (int k = 0; k < nxh; ++k) {
+          for (int y = 0; y < ny; ++y) ln[y] = H[((size_t)zz * ny + y) * nxh + k];
+          p.exec(ln.data(), sign);
+          for (int y = 0; y < ny; ++y) H[((size_t)zz * ny + y) * nxh + k] = ln[y];
+        }
+    });
+  }
+  // the z transforms of every (y, kx) line of H
+  void zpass(int sign) {
+    par_for(ny, [&](long long b, long long e, int) {
+      Plan1D p(pz);
+      std::vector<cd> ln(nz);
+      for (int y = (int)b; y < (int)e; ++y)
+        for (int k = 0; k < nxh; ++k) {
+          for (int zz = 0; zz < nz; ++zz) ln[zz] = H[((size_t)zz * ny + y) * nxh + k];
+          p.exec(ln.data(), sign);
+          for (int zz = 0; zz < nz; ++zz) H[((size_t)zz * ny + y) * nxh + k] = ln[zz];
+        }
+    });
   }
 
   // complex ref layout -> real, unnormalised.  Complex inverse along z and y,
   // then a c2r along x that uses only the real parts of the kx=0 and kx=nx/2
   // entries (the semantics of a multi-dimensional FFTW c2r).
   void c2r(const cd* c, double* r) {
-    for (int ky = 0; ky < ny; ++ky)
-      for (int kz = 0; kz < nz; ++kz)
-        for (int k = 0; k < nxh; ++k)
-          H[((size_t)kz * ny + ky) * nxh + k] = c[((size_t)ky * nz + kz) * nxh + k];
-    for (int y = 0; y < ny; ++y)
-      for (int k = 0; k < nxh; ++k) {
-        for (int zz = 0; zz < nz; ++zz) line[zz] = H[((size_t)zz * ny + y) * nxh + k];
-        pz.exec(line.data(), +1);
-        for (int zz = 0; zz < nz; ++zz) H[((size_t)zz * ny + y) * nxh + k] = line[zz];
-      }
-    for (int zz = 0; zz < nz; ++zz)
-      for (int k = 0; k < nxh; ++k) {
-        for (int y = 0; y < ny; ++y) line[y] = H[((size_t)zz * ny + y) * nxh + k];
-        py.exec(line.data(), +1);
-        for (int y = 0; y < ny; ++y) H[((size_t)zz * ny + y) * nxh + k] = line[y];
-      }
-    std::vector<cd> z(nx);
+    par_for(ny, [&](long long b, long long e, int) {
+      for (int ky = (int)b; ky < (int)e; ++ky)
+        for (int kz = 0; kz < nz; ++kz)
+          for (int k = 0; k < nxh; ++k)
+            H[((size_t)kz * ny + ky) * nxh + k] = c[((size_t)ky * nz + kz) * nxh + k];
+    });
+    zpass(+1);
+    ypass(+1);
     const int nrows = ny * nz;
-    for (int row = 0; row < nrows; row += 2) {
-      const cd* ha = &H[(size_t)row * nxh];
-      const cd* hb = (row + 1 < nrows) ? &H[(size_t)(row + 1) * nxh] : nullptr;
-      for (int k = 0; k <= nx / 2; ++k) {
-        cd a = ha[k], b = hb ? hb[k] : cd(0.0, 0.0);
-        if (k == 0 || k == nx / 2) { a = cd(a.real(), 0.0); b = cd(b.real(), 0.0); }
-        z[k] = a + cd(0.0, 1.0) * b;
-        if (k > 0 && k < nx / 2) z[nx - k] = std::conj(a) + cd(0.0, 1.0) * std::conj(b);
+    par_for((nrows + 1) / 2, [&](long long b, long long e, int) {
+      Plan1D p(px);
+      std::vector<cd> z(nx);
+      for (int row = 2 * (int)b; row < 2 * (int)e; row += 2) {
+        const cd* ha = &H[(size_t)row * nxh];
+        const cd* hb = (row + 1 < nrows) ? &H[(size_t)(row + 1) * nxh] : nullptr;
+        for (int k = 0; k <= nx / 2; ++k) {
+          cd a = ha[k], bb = hb ? hb[k] : cd(0.0, 0.0);
+          if (k == 0 || k == nx / 2) { a = cd(a.real(), 0.0); bb = cd(bb.real(), 0.0); }
+          z[k] = a + cd(0.0, 1.0) * bb;
+          if (k > 0 && k < nx / 2) z[nx - k] = std::conj(a) + cd(0.0, 1.0) * std::conj(bb);
+        }
+        p.exec(z.data(), +1);
+        double* ra = r + (size_t)row * nx;
+        double* rb = hb ? r + (size_t)(row + 1) * nx : nullptr;
+        for (int x = 0; x < nx; ++x) {
+          ra[x] = z[x].real();
+          if (rb) rb[x] = z[x].imag();
+        }
       }
-      px.exec(z.data(), +1);
-      double* ra = r + (size_t)row * nx;
-      double* rb = hb ? r + (size_t)(row + 1) * nx : nullptr;
-      for (int x = 0; x < nx; ++x) {
-        ra[x] = z[x].real();
-        if (rb) rb[x] = z[x].imag();
-      }
-    }
+    });
   }
 };
 
@@ -906,34 +945,42 @@ struct oracle_ctx {
     const int nxt = N[0] / 2 + 1;
     const int globalNy = N[2], globalNz = N[1];
     const cd idqx(0, dqx()), idqy(0, dqy()), idqz(0, dqz());
-    for (int i = 0; i < nzt; i++) {
-      double l = (i > globalNz / 2) ? -globalNz + i : i;
-      for (int j = 0; j < nyt; j++) {
-        double m = (j > globalNy / 2) ? -globalNy + j : j;
-        for (int k = 0; k < nxt; k++) {
-          double n = k;
-          size_t idx = ((size_t)i * nyt + j) * nxt + k;
-          ft_grad[0][idx] = ft_phi[idx] * idqx * n;
-          ft_grad[1][idx] = ft_phi[idx] * idqy * m;
-          ft_grad[2][idx] = ft_phi[idx] * idqz * l;
+    par_for(nzt, [&](long long b, long long e, int) {
+      for (int i = (int)b; i < (int)e; i++) {
+        double l = (i > globalNz / 2) ? -globalNz + i : i;
+        for (int j = 0; j < nyt; j++) {
+          double m = (j > globalNy / 2) ? -globalNy + j : j;
+          for (int k = 0; k < nxt; k++) {
+            double n = k;
+            size_t idx = ((size_t)i * nyt + j) * nxt + k;
+            ft_grad[0][idx] = ft_phi[idx] * idqx * n;
+            ft_grad[1][idx] = ft_phi[idx] * idqy * m;
+            ft_grad[2][idx] = ft_phi[idx] * idqz * l;
+          }
         }
       }
-    }
+    });
     // grid.cpp:262-280: the y and z c2r outputs are swapped on purpose
     fft->c2r(ft_grad[0].data(), grad[0].data());
     fft->c2r(ft_grad[1].data(), grad[2].data());
     fft->c2r(ft_grad[2].data(), grad[1].data());
     const double factor = (double)N[0] * N[1] * N[2];
     for (int d = 0; d < 3; ++d)
-      for (auto& v : grad[d]) v /= factor;
+      par_for((long long)grad[d].size(), [&](long long b, long long e, int) {
+        for (long long n = b; n < e; ++n) grad[d][n] /= factor;
+      });
   }
 
   void floryhuggins() {  // fixgrid_floryhuggins.cpp:65-85
-    for (size_t n = 0; n < nreal; ++n) {
-      if (phi[n] <= 0) { phi[n] = -phi[n]; num_less_zero += 1; }
-      else if (phi[n] >= 1) { phi[n] = 1 - (phi[n] - 1); num_great_zero += 1; }
-      chempot[n] += fh_temp / fh_volFH * (std::log(phi[n] / (1 - phi[n])) + fh_chi * (1 - 2 * phi[n]));
-    }
+    std::vector<long long> lt(g_threads, 0), gt(g_threads, 0);
+    par_for((long long)nreal, [&](long long b, long long e, int t) {
+      for (long long n = b; n < e; ++n) {
+        if (phi[n] <= 0) { phi[n] = -phi[n]; lt[t] += 1; }
+        else if (phi[n] >= 1) { phi[n] = 1 - (phi[n] - 1); gt[t] += 1; }
+        chempot[n] += fh_temp / fh_volFH * (std::log(phi[n] / (1 - phi[n])) + fh_chi * (1 - 2 * phi[n]));
+      }
+    });
+    for (int t = 0; t < g_threads; ++t) { num_less_zero += lt[t]; num_great_zero += gt[t]; }
   }
 
   void set_qs() {  // conjugate.cpp:130-161
@@ -1014,9 +1061,15 @@ struct oracle_ctx {
   void conjugate_update() {  // conjugate.cpp:163-247 (nprocs == 1)
     const int localNx = N[0] / 2 + 1, localNz = N[1], localNy = N[2];
     const int globalNz = N[1];
-    for (int nz = 0; nz < localNz; nz++)
-      for (int ny = 0; ny < localNy; ny++)
-        for (int nx = 1; nx < localNx - 1; nx++) complex_update(nz, ny, nx);
+    // the reference generator's draws follow this loop order: split only
+    // for the counter-based and the silent noise
+    auto bulk = [&](long long b, long long e, int) {
+      for (int nz = (int)b; nz < (int)e; nz++)
+        for (int ny = 0; ny < localNy; ny++)
+          for (int nx = 1; nx < localNx - 1; nx++) complex_update(nz, ny, nx);
+    };
+    if (c_noise == PHAFD_NOISE_REFERENCE) bulk(0, localNz, 0);
+    else par_for(localNz, bulk);
     for (int nx = 0; nx < localNx; nx += localNx - 1) { single(nx); line_single(nx); }
     {
       int nx = localNx - 1;
@@ -1133,6 +1186,11 @@ struct oracle_ctx {
   }
 
 extern "C" {
+
+int oracle_set_threads(int n) {
+  g_threads = std::max(1, std::min(n, 256));
+  return 0;
+}
 
 int oracle_ctx_create(oracle_ctx** out) {
   *out = new oracle_ctx();
