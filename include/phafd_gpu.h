@@ -106,6 +106,15 @@ const char* phafd_build_info(void);
 int phafd_domain(phafd_ctx* ctx, const double boxlo[3], const double period[3]); /* Domain::set_box, domain.cpp:30-76 */
 int phafd_grid_style(phafd_ctx* ctx, int nx, int ny, int nz);   /* Grid::create + create_concentration, grid.cpp:88-113,205-286 */
 int phafd_grid_populate_constant(phafd_ctx* ctx, double average, double variance, int seed); /* Grid::noisy_constant, grid.cpp:289-307 */
+/* Grid::flat_interface (grid.cpp:310-337): hi + variance*U(-1/2,1/2) for
+ * x - boxlo < Lx (average - lo)/(hi - lo), lo + variance*U beyond */
+int phafd_grid_populate_flat_interface(phafd_ctx* ctx, double average, double variance, double hi, double lo,
+                                       int seed);
+/* Grid::sphere (grid.cpp:339-425): 0.5 (hi - lo) tanh((radius - r)/width) +
+ * 0.5 (hi + lo) about the origin, lo chosen for the volume average; `width`
+ * is the profile width itself (the script's argument is its square,
+ * grid.cpp:153-162) */
+int phafd_grid_populate_sphere(phafd_ctx* ctx, double radius, double width, double hi, double average);
 int phafd_grid_set(phafd_ctx* ctx, int field, const double* host);   /* upload a real field, [z][y][x]              */
 int phafd_grid_get(phafd_ctx* ctx, int field, double* host);         /* download a real field or a k-space field    */
 int phafd_set_zghost(phafd_ctx* ctx, int mode);                      /* CommBrick::borders z swaps, comm_brick.cpp:283-352 */

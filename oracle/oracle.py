@@ -41,6 +41,8 @@ def lib():
             "oracle_domain": [vp, dp, dp],
             "oracle_grid_style": [vp, C.c_int, C.c_int, C.c_int],
             "oracle_grid_populate_constant": [vp, C.c_double, C.c_double, C.c_int],
+            "oracle_grid_populate_flat_interface": [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int],
+            "oracle_grid_populate_sphere": [vp, C.c_double, C.c_double, C.c_double, C.c_double],
             "oracle_grid_set": [vp, C.c_int, dp],
             "oracle_grid_get": [vp, C.c_int, dp],
             "oracle_atoms_create": [vp, C.c_int, ip, ip, ip, dp],
@@ -180,6 +182,12 @@ class Oracle:
 
     def grid_populate_constant(self, average, variance, seed):
         self._call("oracle_grid_populate_constant", average, variance, seed)
+
+    def grid_populate_flat_interface(self, average, variance, hi, lo, seed):
+        self._call("oracle_grid_populate_flat_interface", average, variance, hi, lo, seed)
+
+    def grid_populate_sphere(self, radius, width, hi, average):
+        self._call("oracle_grid_populate_sphere", radius, width, hi, average)
 
     def grid_set(self, field, arr):
         self._call("oracle_grid_set", FIELD[field], np.ascontiguousarray(arr, np.float64).reshape(-1))

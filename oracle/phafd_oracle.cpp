@@ -1257,6 +1257,79 @@ int oracle_grid_populate_constant(oracle_ctx* c, double average, double variance
   })
 }
 
+// Grid::flat_interface (grid.cpp:310-337, seeded as in Grid::populate
+// :123-134): hi + variance U for x - sublo < L (average - lo)/(hi - lo), lo +
+// variance U beyond, one draw per node in [z][y][x] order
+static void flat_interface_impl(oracle_ctx* c, double average, double variance, double hi, double lo, int seed) {
+  {
+    if (!c->gridset) throw std::invalid_argument("grid_populate before grid_style");
+    std::uniform_real_distribution<double> real_dist(-0.5, 0.5);
+    std::mt19937 gen;
+    gen.seed(oracle_make_unique_seed(seed));
+    const double Lbox = (average - lo) / (hi - lo) * c->period[0];
+    const double Ox = c->sublo[0], dx = c->period[0] / c->N[0];
+    size_t n = 0;
+    for (int i = 0; i < c->N[2]; i++)
+      for (int j = 0; j < c->N[1]; j++)
+        for (int k = 0; k < c->N[0]; k++) {
+          const double x = k * dx + Ox;
+          if (x - Ox < Lbox) c->phi[n++] = hi + variance * real_dist(gen);
+          else c->phi[n++] = lo + variance * real_dist(gen);
+        }
+    c->populated = true;
+  }
+}
+
+int oracle_grid_populate_flat_interface(oracle_ctx* c, double average, double variance, double hi, double lo,
+                                        int seed) {
+  GUARD(c, { flat_interface_impl(c, average, variance, hi, lo, seed); })
+}
+
+// Grid::sphere (grid.cpp:339-425): tanh profile of `radius` and `width`
+// about the origin, the outer value chosen so that the volume average is av
+static void sphere_impl(oracle_ctx* c, double radius, double width, double hi, double av) {
+  {
+    if (!c->gridset) throw std::invalid_argument("grid_populate before grid_style");
+    for (int d = 0; d < 3; d++)
+      if (radius >= c->period[d] / 2.) throw std::runtime_error("Initial spherical configuration has radius > domain.");
+    const double dx = c->period[0] / c->N[0], dy = c->period[1] / c->N[1], dz = c->period[2] / c->N[2];
+    const double Ox = c->sublo[0], Oy = c->sublo[1], Oz = c->sublo[2];
+    auto shape = [&](double r) { return std::tanh((-r + radius) / width); };
+    double integral = 0;
+    for (int i = 0; i < c->N[2]; i++) {
+      const double z = i * dz + Oz;
+      for (int j = 0; j < c->N[1]; j++) {
+        const double y = j * dy + Oy;
+        for (int k = 0; k < c->N[0]; k++) {
+          const double x = k * dx + Ox;
+          integral += shape(std::sqrt(x * x + y * y + z * z));
+        }
+      }
+    }
+    integral *= dx * dy * dz;
+    const double ifrac = integral / (c->period[0] * c->period[1] * c->period[2]);
+    const double lo = (2 * av - hi * (1 + ifrac)) / (1 - ifrac);
+    if (lo < 0) throw std::runtime_error("Average array value is too small for specified radius.");
+    if (lo > hi) throw std::runtime_error("Average array value is too large for specified radius.");
+    size_t n = 0;
+    for (int i = 0; i < c->N[2]; i++) {
+      const double z = i * dz + Oz;
+      for (int j = 0; j < c->N[1]; j++) {
+        const double y = j * dy + Oy;
+        for (int k = 0; k < c->N[0]; k++) {
+          const double x = k * dx + Ox;
+          c->phi[n++] = 0.5 * (hi - lo) * shape(std::sqrt(x * x + y * y + z * z)) + 0.5 * (hi + lo);
+        }
+      }
+    }
+    c->populated = true;
+  }
+}
+
+int oracle_grid_populate_sphere(oracle_ctx* c, double radius, double width, double hi, double av) {
+  GUARD(c, { sphere_impl(c, radius, width, hi, av); })
+}
+
 int oracle_grid_set(oracle_ctx* c, int field, const double* in) {
   GUARD(c, {
     std::vector<double>* dst = nullptr;

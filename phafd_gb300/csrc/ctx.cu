@@ -1008,6 +1008,63 @@ int phafd_grid_populate_constant(phafd_ctx* c, double average, double variance, 
   API_END(c)
 }
 
+static void upload_phi(phafd_ctx* c, const std::vector<double>& h) {
+  if (c->precision == PHAFD_FP64) copy_real_to_dev<double>(c, c->phi, h.data());
+  else copy_real_to_dev<float>(c, c->phi, h.data());
+  c->populated = true;
+}
+
+int phafd_grid_populate_flat_interface(phafd_ctx* c, double average, double variance, double hi, double lo,
+                                       int seed) {
+  API_BEGIN(c)
+  if (!c->gridset) throw std::invalid_argument("CAnnot use command grid_populate before grid_style is set.");
+  std::vector<double> h(c->nreal);
+  std::uniform_real_distribution<double> rd(-0.5, 0.5);
+  std::mt19937 gen;
+  gen.seed(make_unique_seed(seed));  // grid.cpp:123-134, 310-337
+  const double Lbox = (average - lo) / (hi - lo) * c->period[0];
+  const double Ox = c->boxlo[0], dx = c->period[0] / c->N[0];
+  size_t n = 0;
+  for (int i = 0; i < c->N[2]; i++)
+    for (int j = 0; j < c->N[1]; j++)
+      for (int k = 0; k < c->N[0]; k++) {
+        const double x = k * dx + Ox;
+        h[n++] = (x - Ox < Lbox ? hi : lo) + variance * rd(gen);
+      }
+  upload_phi(c, h);
+  API_END(c)
+}
+
+int phafd_grid_populate_sphere(phafd_ctx* c, double radius, double width, double hi, double average) {
+  API_BEGIN(c)
+  if (!c->gridset) throw std::invalid_argument("CAnnot use command grid_populate before grid_style is set.");
+  for (int d = 0; d < 3; d++)  // grid.cpp:339-425
+    if (radius >= c->period[d] / 2.) throw std::runtime_error("Initial spherical configuration has radius > domain.");
+  const double h3[3] = {c->period[0] / c->N[0], c->period[1] / c->N[1], c->period[2] / c->N[2]};
+  std::vector<double> f(c->nreal);  // tanh((radius - r) / width) at every node, [z][y][x]
+  double integral = 0;
+  size_t n = 0;
+  for (int i = 0; i < c->N[2]; i++) {
+    const double z = i * h3[2] + c->boxlo[2];
+    for (int j = 0; j < c->N[1]; j++) {
+      const double y = j * h3[1] + c->boxlo[1];
+      for (int k = 0; k < c->N[0]; k++) {
+        const double x = k * h3[0] + c->boxlo[0];
+        f[n] = std::tanh((-std::sqrt(x * x + y * y + z * z) + radius) / width);
+        integral += f[n++];
+      }
+    }
+  }
+  integral *= h3[0] * h3[1] * h3[2];
+  const double ifrac = integral / (c->period[0] * c->period[1] * c->period[2]);
+  const double lo = (2 * average - hi * (1 + ifrac)) / (1 - ifrac);
+  if (lo < 0) throw std::runtime_error("Average array value is too small for specified radius.");
+  if (lo > hi) throw std::runtime_error("Average array value is too large for specified radius.");
+  for (auto& v : f) v = 0.5 * (hi - lo) * v + 0.5 * (hi + lo);
+  upload_phi(c, f);
+  API_END(c)
+}
+
 int phafd_grid_set(phafd_ctx* c, int field, const double* host) {
   API_BEGIN(c)
   if (!c->gridset) throw std::invalid_argument("grid not created");

@@ -23,7 +23,8 @@ ERRORS = {-1: "invalid", -2: "cuda", -3: "nan", -4: "overflow", -5: "constraint"
 # every symbol declared in include/phafd_gpu.h
 EXPORTS = [
     "phafd_ctx_create", "phafd_ctx_destroy", "phafd_last_error", "phafd_build_info",
-    "phafd_domain", "phafd_grid_style", "phafd_grid_populate_constant", "phafd_grid_set", "phafd_grid_get",
+    "phafd_domain", "phafd_grid_style", "phafd_grid_populate_constant", "phafd_grid_populate_flat_interface",
+    "phafd_grid_populate_sphere", "phafd_grid_set", "phafd_grid_get",
     "phafd_set_zghost", "phafd_set_schedule", "phafd_set_keep_chempot", "phafd_set_plane_fusion",
     "phafd_set_gradient_mask",
     "phafd_atoms_create", "phafd_atoms_get", "phafd_atoms_set_images",
@@ -88,6 +89,8 @@ def load(path=None):
         "phafd_domain": [vp, dp, dp],
         "phafd_grid_style": [vp, C.c_int, C.c_int, C.c_int],
         "phafd_grid_populate_constant": [vp, C.c_double, C.c_double, C.c_int],
+        "phafd_grid_populate_flat_interface": [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int],
+        "phafd_grid_populate_sphere": [vp, C.c_double, C.c_double, C.c_double, C.c_double],
         "phafd_grid_set": [vp, C.c_int, dp],
         "phafd_grid_get": [vp, C.c_int, dp],
         "phafd_atoms_create": [vp, C.c_int, ip, ip, ip, dp],
@@ -201,6 +204,12 @@ class PhafdGPU:
 
     def grid_populate_constant(self, average, variance, seed):
         self._call("phafd_grid_populate_constant", average, variance, seed)
+
+    def grid_populate_flat_interface(self, average, variance, hi, lo, seed):
+        self._call("phafd_grid_populate_flat_interface", average, variance, hi, lo, seed)
+
+    def grid_populate_sphere(self, radius, width, hi, average):
+        self._call("phafd_grid_populate_sphere", radius, width, hi, average)
 
     def grid_set(self, field, arr):
         self._call("phafd_grid_set", FIELD[field], np.ascontiguousarray(arr, np.float64).reshape(-1))

@@ -183,11 +183,17 @@ class Interpreter {
       if (!gridset_) throw std::invalid_argument("CAnnot use command grid_populate before grid_style is set.");
       if (w.size() >= 5 && w[0] == "constant" && w[1] == "concentration") {
         if (!dry_) check(phafd_grid_populate_constant(ctx(), num(w[2]), num(w[3]), inum(w[4])));
+      } else if (w.size() >= 7 && w[0] == "flat_interface" && w[1] == "concentration") {  // grid.cpp:136-151
+        if (!dry_)
+          check(phafd_grid_populate_flat_interface(ctx(), num(w[2]), num(w[3]), num(w[4]), num(w[5]), inum(w[6])));
+      } else if (w.size() >= 6 && w[0] == "sphere" && w[1] == "concentration") {  // grid.cpp:153-166
+        if (!dry_) check(phafd_grid_populate_sphere(ctx(), num(w[2]), std::sqrt(num(w[3])), num(w[4]), num(w[5])));
       } else if (!w.empty() && w[0] == "read_dump") {
         grid_read_dump(w);
       } else {
         throw std::runtime_error("grid_populate " + (w.empty() ? std::string() : w[0]) +
-                                 " is not supported by phafd_gpu (constant concentration or read_dump)");
+                                 " is not supported by phafd_gpu (constant, flat_interface or sphere "
+                                 "concentration, or read_dump)");
       }
       populated_ = true;
     } else if (cmd == "atom_style") {

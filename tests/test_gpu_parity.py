@@ -239,3 +239,23 @@ def test_fp64_field_steps_with_512_point_axes(gpu_lib, shape):
         d.setup()
         d.run(5)
     assert rel_err(g.grid_get("phi"), o.grid_get("phi")) < 1e-10
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("style", ["flat_interface", "sphere"])
+def test_populate_styles_match_oracle(gpu_lib, precision, style):
+    """grid_populate flat_interface / sphere: host-generated phi uploaded to
+    the context equals the oracle's (FP32 contexts hold its rounding)."""
+    o = Oracle(); g = gpu(precision)
+    for d in (o, g):
+        d.domain([-8.0, -5.0, -6.0], [16.0, 10.0, 12.0])
+        d.grid_style(16, 10, 12)
+        if style == "flat_interface":
+            d.grid_populate_flat_interface(0.45, 0.05, 0.8, 0.2, 7)
+        else:
+            d.grid_populate_sphere(3.5, 2.0 ** 0.5, 0.9, 0.3)
+    want = o.grid_get("phi")
+    got = g.grid_get("phi")
+    # the library's host code may contract multiply-adds (the oracle is built
+    # without): a few ulps in FP64; FP32 holds the rounding (half an ulp below 1)
+    assert np.abs(got - want).max() < (1e-14 if precision == 64 else 6e-8)

@@ -317,3 +317,11 @@ def test_restart_continues_the_run(exe, tmp_path, gpu_lib):
     # unwrapped positions: the restart wraps every bead at its setup, the
     # uninterrupted run only at its neighbor rebuilds
     assert np.abs(uxb - uxa).max() < 1e-10 * np.abs(uxa).max()
+
+
+@pytest.mark.parametrize("line", ["grid_populate flat_interface concentration 0.45 0.05 0.8 0.2 ${seed1}",
+                                  "grid_populate sphere concentration 5.0 4.0 0.9 0.5"])
+def test_populate_styles_parse(exe, tmp_path, line):
+    scene(tmp_path, SCRIPT.replace("grid_populate constant concentration 0.5 0.02 ${seed1}", line))
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    assert r.returncode == 0, r.stderr
