@@ -322,8 +322,7 @@ def run_gpu(args):
         xs = chains[0]
         e = PhafdGPU(precision=32, device=local, schedule="resident")
         t0 = time.perf_counter()
-        W.apply(e, cfg, chains=chains)
-        e.grid_set("phi", phi_host)
+        W.apply(e, cfg, chains=chains, phi=phi_host)  # the state from host arrays: phi, then the beads
         e.setup()
         for _ in range(k):
             e.run(1)

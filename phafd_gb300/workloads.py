@@ -123,13 +123,18 @@ def chain_ranges(nchains, length):
     return [(c * length, (c + 1) * length) for c in range(nchains)]
 
 
-def apply(driver, cfg, chains=None, semiflexible=True, drag=None, zghost="periodic"):
-    """Issue the configuration's script commands on `driver`."""
+def apply(driver, cfg, chains=None, semiflexible=True, drag=None, zghost="periodic", phi=None):
+    """Issue the configuration's script commands on `driver`.  `phi` (a real
+    [z][y][x] array) replaces the generated initial field: the state of a
+    run continued from host memory."""
     n, L, lo = cfg["n"], cfg["L"], cfg["origin"]
     driver.set_zghost(zghost)
     driver.domain([lo, lo, lo], [L, L, L])
     driver.grid_style(n, n, n)
-    driver.grid_populate_constant(cfg["phi0"], cfg["amp"], cfg["grid_seed"])
+    if phi is None:
+        driver.grid_populate_constant(cfg["phi0"], cfg["amp"], cfg["grid_seed"])
+    else:
+        driver.grid_set("phi", phi)
     if chains is None:
         chains = random_walk_chains(cfg["nchains"], cfg["chain_len"], lo, L, cfg["chain_seed"], cfg["bond"])
     x, tags, mol, types = chains
