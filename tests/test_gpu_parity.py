@@ -248,8 +248,8 @@ def test_populate_styles_match_oracle(gpu_lib, precision, style):
     the context equals the oracle's (FP32 contexts hold its rounding)."""
     o = Oracle(); g = gpu(precision)
     for d in (o, g):
-        d.domain([-8.0, -5.0, -6.0], [16.0, 10.0, 12.0])
-        d.grid_style(16, 10, 12)
+        d.domain([-8.0, -5.0, -6.0], [16.0, 10.0, 12.0])  # anisotropic spacing
+        d.grid_style(32, 16, 16)
         if style == "flat_interface":
             d.grid_populate_flat_interface(0.45, 0.05, 0.8, 0.2, 7)
         else:
