@@ -162,6 +162,15 @@ int phafd_fix_semiflexible(phafd_ctx* ctx, int nranges, const int* starts, const
 /* ---- integrate (input.cpp:256-273) ---- */
 int phafd_set_dt(phafd_ctx* ctx, double dt);                      /* "dt" command */
 int phafd_set_timestep(phafd_ctx* ctx, long long step);           /* "timestep" command */
+/* State of the host generator behind PHAFD_NOISE_REFERENCE (the reference's
+ * std::mt19937 of conjugate_volfrac.cpp:64, drawn in its order every step),
+ * as text (about 7 KB): saved with a restart, it continues that stream
+ * exactly, which the reference cannot do.  get: *len = bytes needed
+ * (NUL included), buf may be NULL.  set: after
+ * phafd_fix_conjugate_volfrac, which seeds the generator.  The Philox noise
+ * is keyed by (seed, step) and needs no state. */
+int phafd_noise_state_get(phafd_ctx* ctx, char* buf, int cap, int* len);
+int phafd_noise_state_set(phafd_ctx* ctx, const char* state);
 int phafd_setup(phafd_ctx* ctx);                                  /* Integrate::setup, integrate.cpp:33-88 */
 int phafd_run(phafd_ctx* ctx, int nsteps);                        /* Integrate::run, integrate.cpp:90-219 */
 int phafd_run_async(phafd_ctx* ctx, int nsteps);

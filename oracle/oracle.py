@@ -81,6 +81,8 @@ def lib():
             "oracle_fft_c2r": [C.c_int, C.c_int, C.c_int, dp, dp],
             "oracle_make_unique_seed": [C.c_int],
             "oracle_set_threads": [C.c_int],
+            "oracle_noise_state_get": [vp, C.c_char_p, C.c_int, C.POINTER(C.c_int)],
+            "oracle_noise_state_set": [vp, C.c_char_p],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -206,6 +208,17 @@ class Oracle:
         self.n = len(tags)
         self._call("oracle_atoms_create", self.n, np.asarray(tags, np.int32), np.asarray(mol, np.int32),
                    np.asarray(types, np.int32), np.ascontiguousarray(x, np.float64).reshape(-1))
+
+    def noise_state(self):
+        """the reference-noise generator's state (text)"""
+        n = C.c_int(0)
+        self._call("oracle_noise_state_get", None, 0, C.byref(n))
+        buf = C.create_string_buffer(n.value)
+        self._call("oracle_noise_state_get", buf, n.value, C.byref(n))
+        return buf.value.decode()
+
+    def set_noise_state(self, state):
+        self._call("oracle_noise_state_set", state.encode())
 
     def atoms_set_images(self, images):
         im = np.ascontiguousarray(images, np.int32)

@@ -57,6 +57,7 @@
 #include <memory>
 #include <random>
 #include <set>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <thread>
@@ -1328,6 +1329,34 @@ static void sphere_impl(oracle_ctx* c, double radius, double width, double hi, d
 
 int oracle_grid_populate_sphere(oracle_ctx* c, double radius, double width, double hi, double av) {
   GUARD(c, { sphere_impl(c, radius, width, hi, av); })
+}
+
+static void noise_state_get_impl(oracle_ctx* c, char* buf, int cap, int* len) {
+  std::ostringstream os;
+  os << c->c_gen;
+  const std::string st = os.str();
+  if (len) *len = (int)st.size() + 1;
+  if (buf) {
+    if (cap < (int)st.size() + 1) throw std::invalid_argument("noise state buffer too small");
+    std::memcpy(buf, st.c_str(), st.size() + 1);
+  }
+}
+
+// the mt19937 of the reference noise (conjugate_volfrac.cpp:64) as text
+int oracle_noise_state_get(oracle_ctx* c, char* buf, int cap, int* len) {
+  GUARD(c, { noise_state_get_impl(c, buf, cap, len); })
+}
+
+static void noise_state_set_impl(oracle_ctx* c, const char* state) {
+  std::istringstream is(state);
+  std::mt19937 g;
+  is >> g;
+  if (is.fail()) throw std::invalid_argument("malformed noise state");
+  c->c_gen = g;
+}
+
+int oracle_noise_state_set(oracle_ctx* c, const char* state) {
+  GUARD(c, { noise_state_set_impl(c, state); })
 }
 
 int oracle_grid_set(oracle_ctx* c, int field, const double* in) {

@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <cstring>
 #include <random>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -1062,6 +1063,31 @@ int phafd_grid_populate_sphere(phafd_ctx* c, double radius, double width, double
   if (lo > hi) throw std::runtime_error("Average array value is too large for specified radius.");
   for (auto& v : f) v = 0.5 * (hi - lo) * v + 0.5 * (hi + lo);
   upload_phi(c, f);
+  API_END(c)
+}
+
+int phafd_noise_state_get(phafd_ctx* c, char* buf, int cap, int* len) {
+  API_BEGIN(c)
+  std::ostringstream os;
+  os << c->c_gen;  // the 624 words and position of the host generator, as text
+  const std::string st = os.str();
+  if (len) *len = (int)st.size() + 1;
+  if (buf) {
+    if (cap < (int)st.size() + 1) throw std::invalid_argument("noise state buffer too small");
+    std::memcpy(buf, st.c_str(), st.size() + 1);
+  }
+  API_END(c)
+}
+
+int phafd_noise_state_set(phafd_ctx* c, const char* state) {
+  API_BEGIN(c)
+  if (!state) throw std::invalid_argument("null noise state");
+  if (!c->have_conj) throw std::runtime_error("noise state needs fix grid/conjugate/volfrac");
+  std::istringstream is(state);
+  std::mt19937 g;
+  is >> g;
+  if (is.fail()) throw std::invalid_argument("malformed noise state");
+  c->c_gen = g;
   API_END(c)
 }
 

@@ -32,7 +32,7 @@ EXPORTS = [
     "phafd_neighbor",
     "phafd_fix_conjugate_volfrac", "phafd_fix_floryhuggins", "phafd_fix_gradphi", "phafd_fix_drag",
     "phafd_fix_semiflexible",
-    "phafd_set_dt", "phafd_set_timestep", "phafd_setup", "phafd_run", "phafd_run_async", "phafd_counters_get",
+    "phafd_set_dt", "phafd_set_timestep", "phafd_noise_state_get", "phafd_noise_state_set", "phafd_setup", "phafd_run", "phafd_run_async", "phafd_counters_get",
     "phafd_synchronize",
     "phafd_run_timed", "phafd_profile_stages",
     "phafd_half_list_size", "phafd_half_list", "phafd_grid_list_size", "phafd_grid_list",
@@ -107,6 +107,8 @@ def load(path=None):
         "phafd_fix_semiflexible": [vp, C.c_int, ip, ip, C.POINTER(SemiParams)],
         "phafd_set_dt": [vp, C.c_double],
         "phafd_set_timestep": [vp, C.c_longlong],
+        "phafd_noise_state_get": [vp, C.c_char_p, C.c_int, C.POINTER(C.c_int)],
+        "phafd_noise_state_set": [vp, C.c_char_p],
         "phafd_setup": [vp],
         "phafd_run": [vp, C.c_int],
         "phafd_run_async": [vp, C.c_int],
@@ -296,6 +298,17 @@ class PhafdGPU:
         x = np.zeros((n, 3)); ux = np.zeros((n, 3)); f = np.zeros((n, 3)); im = np.zeros(n, np.int32)
         self._call("phafd_atoms_get", x.reshape(-1), ux.reshape(-1), f.reshape(-1), im)
         return x[:self.n], ux[:self.n], f[:self.n], im[:self.n]
+
+    def noise_state(self):
+        """the reference-noise generator's state (text), for a restart"""
+        n = C.c_int(0)
+        self._call("phafd_noise_state_get", None, 0, C.byref(n))
+        buf = C.create_string_buffer(n.value)
+        self._call("phafd_noise_state_get", buf, n.value, C.byref(n))
+        return buf.value.decode()
+
+    def set_noise_state(self, state):
+        self._call("phafd_noise_state_set", state.encode())
 
     def atoms_set_images(self, images):
         """packed image flags of every bead (restart), before setup."""

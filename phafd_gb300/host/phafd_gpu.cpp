@@ -134,6 +134,7 @@ class Interpreter {
   double dt_ = 0.0;
   long long timestep_ = 0;
   std::vector<std::pair<std::string, bool>> fh_fixes_;  // names of grid/floryhuggins fixes
+  bool conj_set_ = false;                                // a grid/conjugate/volfrac fix exists
   std::vector<phafd_dump::Spec> dumps_;
   struct Cluster { double threshold; bool greater; };
   std::map<std::string, Cluster> clusters_;  // compute NAME grid/cluster phi THRESHOLD lt|gt
@@ -227,6 +228,8 @@ class Interpreter {
       run(std::stoll(w.at(0)));
     } else if (cmd == "write_field") {
       write_field(w.at(0), w.at(1));
+    } else if (cmd == "write_noise_state" || cmd == "read_noise_state") {
+      noise_state(cmd == "write_noise_state", w.at(0));
     } else if (cmd == "run_until_touching") {  // input.cpp:274-295
       if (dt_ <= 0.0) throw std::runtime_error("Cannot run simulation without setting dt > 0.");
       const long long nsteps = std::stoll(w.at(0));
@@ -456,6 +459,7 @@ class Interpreter {
         else throw std::runtime_error("Error: invalid conjugate/volfrac command");
       }
       if (!dry_) check(phafd_fix_conjugate_volfrac(ctx(), seed, M, T, v, g, noise_));
+      conj_set_ = true;
     } else if (style == "grid/floryhuggins") {  // fixgrid_floryhuggins.cpp:22-56
       if (!populated_) throw std::runtime_error("Fix requires grid to be populated.");
       double T = 1, v = 1, chi = 1;
@@ -605,6 +609,28 @@ class Interpreter {
         }
       }
       phafd_dump::write_step(d, timestep_, dt_, &a, &g);
+    }
+  }
+
+  // the reference-noise generator's state for a restart (an extension:
+  // the reference keeps no generator state across runs)
+  void noise_state(bool write, const std::string& fname) {
+    if (!conj_set_) throw std::runtime_error("noise state needs fix grid/conjugate/volfrac");
+    if (write) {
+      if (dry_) return;
+      int n = 0;
+      check(phafd_noise_state_get(ctx(), nullptr, 0, &n));
+      std::vector<char> buf(n);
+      check(phafd_noise_state_get(ctx(), buf.data(), n, &n));
+      std::ofstream f(fname);
+      if (!f) throw std::runtime_error("cannot open " + fname);
+      f << buf.data();
+    } else {
+      std::ifstream f(fname);
+      if (!f) throw std::runtime_error("Cannot open file " + fname);
+      std::stringstream ss;
+      ss << f.rdbuf();
+      if (!dry_) check(phafd_noise_state_set(ctx(), ss.str().c_str()));
     }
   }
 

@@ -325,3 +325,17 @@ def test_populate_styles_parse(exe, tmp_path, line):
     scene(tmp_path, SCRIPT.replace("grid_populate constant concentration 0.5 0.02 ${seed1}", line))
     r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
     assert r.returncode == 0, r.stderr
+
+
+def test_noise_state_commands(exe, tmp_path):
+    """write_noise_state / read_noise_state: after the conjugate fix only."""
+    scene(tmp_path, SCRIPT.replace("timestep 0", "read_noise_state ns.txt\ntimestep 0"))
+    (tmp_path / "ns.txt").write_text("5489")
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    assert r.returncode == 0, r.stderr
+    scene(tmp_path, SCRIPT.replace("fix atom/semiflexible", "write_noise_state ns.txt\nfix atom/semiflexible"))
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    assert r.returncode == 1 and "noise state needs fix grid/conjugate/volfrac" in r.stderr
+    scene(tmp_path, SCRIPT.replace("timestep 0", "read_noise_state none.txt\ntimestep 0"))
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    assert r.returncode == 1 and "Cannot open file none.txt" in r.stderr
