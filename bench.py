@@ -376,6 +376,23 @@ def precision_check(cfg, chains, device, steps):
     out["sk_rel_err_max"] = float(np.max(np.abs(s32[1:][m] - s64[1:][m]) / s64[1:][m]))
     out["phi_max_abs_err"] = float(np.max(np.abs(p32 - p64)))
     out["mass_err"] = float(abs(p32.mean() - p64.mean()))
+    # bead forces of one pair evaluation at identical positions (FP32 pair
+    # arithmetic with compensated sums against FP64)
+    try:
+        forces = {}
+        for prec in (32, 64):
+            g = PhafdGPU(precision=prec, device=device, schedule="resident")
+            W.apply(g, cfg, chains=chains)
+            g.setup()  # lists built and the gradient of phi current
+            g.stage_pairs()  # the step's own pair launch, forces assigned
+            forces[prec] = g.atoms_get()[2]
+            g.close()
+        d = forces[32] - forces[64]
+        out["force_rel_err"] = float(np.linalg.norm(d) / np.linalg.norm(forces[64]))
+        out["force_max_abs_err"] = float(np.abs(d).max())
+    except Exception as e:  # the step numbers above stand without it
+        out["force_rel_err"] = None
+        out["force_error"] = str(e)[:200]
     return out
 
 
