@@ -116,7 +116,12 @@ int phafd_grid_populate_flat_interface(phafd_ctx* ctx, double average, double va
  * grid.cpp:153-162) */
 int phafd_grid_populate_sphere(phafd_ctx* ctx, double radius, double width, double hi, double average);
 int phafd_grid_set(phafd_ctx* ctx, int field, const double* host);   /* upload a real field, [z][y][x]              */
-int phafd_grid_get(phafd_ctx* ctx, int field, double* host);         /* download a real field or a k-space field    */
+/* download a real field ([z][y][x]) or a k-space field (complex, the
+ * reference's [ky][kz][kx] layout, unnormalised r2c convention: ft_phi is the
+ * spectrum of the current phi, ft_chempot the r2c of the last step's mu).
+ * chempot and ft_chempot after steps exist only if phafd_set_keep_chempot(ctx,
+ * 1) preceded them: the step reuses mu's buffers, so such a read is refused */
+int phafd_grid_get(phafd_ctx* ctx, int field, double* host);
 int phafd_set_zghost(phafd_ctx* ctx, int mode);                      /* CommBrick::borders z swaps, comm_brick.cpp:283-352 */
 int phafd_set_schedule(phafd_ctx* ctx, int schedule);
 int phafd_set_keep_chempot(phafd_ctx* ctx, int keep);               /* also store mu = deposit + FH (grid->chempot) each step */

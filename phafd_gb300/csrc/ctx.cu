@@ -154,6 +154,14 @@ struct phafd_ctx {
   int schedule = PHAFD_SCHEDULE_RESIDENT;
   bool keep_chempot = false;
   bool chempot_from_mu = false;
+  // what the last step left readable: without keep_chempot the deposit
+  // buffer is reset inside the step (no real mu remains) and the resident z
+  // pass stores only the Hermitian planes of mu's spectrum
+  bool chempot_lost = false, muhat_stale = false;
+  void note_step() {
+    chempot_lost = have_conj && !keep_chempot;
+    muhat_stale = have_conj && !keep_chempot && schedule == PHAFD_SCHEDULE_RESIDENT;
+  }
   bool use_plane = false;  // plane-fused x/y passes where they apply (phafd_set_plane_fusion)
   bool use_gmask = false;  // gradient stored near beads only during steps (phafd_set_gradient_mask)
   bool grad_partial = false;  // gx, gy, gz hold values at masked nodes only
@@ -1108,6 +1116,8 @@ int phafd_grid_get(phafd_ctx* c, int field, double* host) {
   API_BEGIN(c)
   if (!c->gridset) throw std::invalid_argument("grid not created");
   const bool f64 = c->precision == PHAFD_FP64;
+  if ((field == PHAFD_FIELD_CHEMPOT && c->chempot_lost) || (field == PHAFD_FIELD_FT_CHEMPOT && c->muhat_stale))
+    throw std::runtime_error("chempot after a run is kept only when phafd_set_keep_chempot(ctx, 1) precedes the steps");
   if (field == PHAFD_FIELD_FT_PHI || field == PHAFD_FIELD_FT_CHEMPOT) {
     const DevBuf* b;
     double sc = 1.0;
@@ -1493,6 +1503,7 @@ static void enqueue_run(phafd_ctx* c, int nsteps) {
         CK(cudaGraphLaunch(c->gexec, c->st));
         ++s;
         c->timestep += 2;
+        c->note_step();
         continue;  // the pair of steps leaves cur unchanged
       }
       const int par = resident ? c->cur : 0;
@@ -1508,6 +1519,7 @@ static void enqueue_run(phafd_ctx* c, int nsteps) {
       CK(cudaGraphLaunch(c->gexec1[par], c->st));
     }
     c->timestep += 1;
+    c->note_step();
     if (resident) resident_spectrum_flip(c);
   }
   }
@@ -1551,6 +1563,7 @@ int phafd_profile_stages(phafd_ctx* c, int nsteps, double* stage_ms, int nstage)
     c->profiling = true;
     c->step_once();
     c->profiling = false;
+    c->note_step();
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->st));
     for (size_t k = 1; k < c->marks.size(); ++k) {

@@ -87,6 +87,12 @@ class Interpreter {
     std::string line;
     std::vector<std::string> lines;
     while (std::getline(in, line)) lines.push_back(line);
+    // mu survives a step only when kept from the start: a later
+    // `write_field chempot` asks for it before the first run
+    for (auto& l : lines) {
+      const Words w = split_line(l);
+      if (w.size() >= 2 && w[0] == "write_field" && w[1] == "chempot") want_chempot_ = true;
+    }
     for (size_t li = 0; li < lines.size(); ++li) {
       std::string l = lines[li];
       convert_variables(l, vars);
@@ -135,6 +141,7 @@ class Interpreter {
   long long timestep_ = 0;
   std::vector<std::pair<std::string, bool>> fh_fixes_;  // names of grid/floryhuggins fixes
   bool conj_set_ = false;                                // a grid/conjugate/volfrac fix exists
+  bool want_chempot_ = false;                            // the script writes chempot after a run
   std::vector<phafd_dump::Spec> dumps_;
   struct Cluster { double threshold; bool greater; };
   std::map<std::string, Cluster> clusters_;  // compute NAME grid/cluster phi THRESHOLD lt|gt
@@ -152,6 +159,7 @@ class Interpreter {
       check(phafd_set_schedule(ctx_, schedule_));
       check(phafd_set_zghost(ctx_, zghost_));
       check(phafd_set_plane_fusion(ctx_, plane_));
+      if (want_chempot_) check(phafd_set_keep_chempot(ctx_, 1));
     }
     return ctx_;
   }

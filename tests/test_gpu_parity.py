@@ -260,25 +260,3 @@ def test_populate_styles_match_oracle(gpu_lib, precision, style):
     # without): a few ulps in FP64; FP32 holds the rounding (half an ulp below 1)
     assert np.abs(got - want).max() < (1e-14 if precision == 64 else 6e-8)
 
-
-def test_reference_noise_resume_matches_uninterrupted_run(gpu_lib):
-    """FP64, reference noise: a context restored from phi, wrapped positions,
-    image flags, timestep and the host generator's state continues the run."""
-    cfg = dict(W.CONFIGS["32cube_64beads"], field_noise="reference", dt=5e-4)
-    a = gpu(64, "resident")
-    chains = W.apply(a, cfg)
-    a.setup()
-    a.run(10)
-    phi10, state = a.grid_get("phi"), a.noise_state()
-    x10, _, _, im10 = a.atoms_get()
-    a.run(10)
-    b = gpu(64, "resident")
-    W.apply(b, cfg, chains=(x10.copy(),) + tuple(chains[1:]), phi=phi10)
-    b.atoms_set_images(im10.copy())
-    b.set_noise_state(state)
-    b.set_timestep(10)
-    b.setup()
-    b.run(10)
-    pa = a.grid_get("phi")
-    assert rel_err(b.grid_get("phi"), pa) < 1e-10
-    assert np.abs(b.atoms_get()[1] - a.atoms_get()[1]).max() < 1e-10 * np.abs(a.atoms_get()[1]).max()
