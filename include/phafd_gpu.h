@@ -52,6 +52,11 @@ extern "C" {
 #define PHAFD_FIELD_GRADZ 4
 #define PHAFD_FIELD_FT_PHI 5
 #define PHAFD_FIELD_FT_CHEMPOT 6
+/* the spectrum of the last step's starting phi (unnormalised, reference
+ * layout): what the reference's compute complex ft_phi sees at a dump step,
+ * evaluated inside the step before the update (integrate.cpp:157-165).
+ * Resident schedule; zeros before the first step after set-up. */
+#define PHAFD_FIELD_FT_PHI_STEP_START 7
 
 /* ---- gridatom pair styles (input.cpp:107-116) ---- */
 #define PHAFD_GRIDATOM_NONE 0

@@ -157,8 +157,9 @@ struct phafd_ctx {
   // what the last step left readable: without keep_chempot the deposit
   // buffer is reset inside the step (no real mu remains) and the resident z
   // pass stores only the Hermitian planes of mu's spectrum
-  bool chempot_lost = false, muhat_stale = false;
+  bool chempot_lost = false, muhat_stale = false, stepped = false;
   void note_step() {
+    stepped = true;
     chempot_lost = have_conj && !keep_chempot;
     muhat_stale = have_conj && !keep_chempot && schedule == PHAFD_SCHEDULE_RESIDENT;
   }
@@ -1118,7 +1119,17 @@ int phafd_grid_get(phafd_ctx* c, int field, double* host) {
   const bool f64 = c->precision == PHAFD_FP64;
   if ((field == PHAFD_FIELD_CHEMPOT && c->chempot_lost) || (field == PHAFD_FIELD_FT_CHEMPOT && c->muhat_stale))
     throw std::runtime_error("chempot after a run is kept only when phafd_set_keep_chempot(ctx, 1) precedes the steps");
-  if (field == PHAFD_FIELD_FT_PHI || field == PHAFD_FIELD_FT_CHEMPOT) {
+  if (field == PHAFD_FIELD_FT_PHI_STEP_START) {
+    if (c->schedule != PHAFD_SCHEDULE_RESIDENT || !c->have_conj)
+      throw std::invalid_argument("the step-start spectrum is kept by the resident schedule");
+    if (!c->stepped) {
+      std::fill(host, host + 2 * c->ncplx, 0.0);
+    } else if (f64) {  // the ping-pong buffer the last step read
+      copy_spec_to_host<double>(c, c->phat[1 - c->cur], host, 1.0);
+    } else {
+      copy_spec_to_host<float>(c, c->phat[1 - c->cur], host, 1.0);
+    }
+  } else if (field == PHAFD_FIELD_FT_PHI || field == PHAFD_FIELD_FT_CHEMPOT) {
     const DevBuf* b;
     double sc = 1.0;
     if (field == PHAFD_FIELD_FT_CHEMPOT) b = &c->muhat;
@@ -1368,6 +1379,7 @@ int phafd_setup(phafd_ctx* c) {
   CK(cudaStreamSynchronize(c->st));
   c->invalidate_graph();
   c->grad_partial = false;
+  c->stepped = false;
   c->setup_done = true;
   int rc = check_status(c);
   if (rc) return rc;
@@ -1704,7 +1716,7 @@ int phafd_stage_borders_and_build(phafd_ctx* c) {
 int phafd_compute_complex(phafd_ctx* c, int field, int quant, double* out) {
   API_BEGIN(c)
   if (!c->gridset) throw std::invalid_argument("grid not created");
-  if (field != PHAFD_FIELD_FT_PHI && field != PHAFD_FIELD_FT_CHEMPOT)
+  if (field != PHAFD_FIELD_FT_PHI && field != PHAFD_FIELD_FT_CHEMPOT && field != PHAFD_FIELD_FT_PHI_STEP_START)
     throw std::invalid_argument("Invalid array to compute in compute modulus.");
   if (quant < PHAFD_COMPLEX_REAL || quant > PHAFD_COMPLEX_NORM) throw std::invalid_argument("Invalid argument in compute complex.");
   std::vector<double> spec(2 * c->ncplx);

@@ -12,7 +12,8 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libphafd_gpu.so")
 
-FIELD = {"phi": 0, "chempot": 1, "gradx": 2, "grady": 3, "gradz": 4, "ft_phi": 5, "ft_chempot": 6}
+FIELD = {"phi": 0, "chempot": 1, "gradx": 2, "grady": 3, "gradz": 4, "ft_phi": 5, "ft_chempot": 6,
+         "ft_phi_step_start": 7}
 GRIDATOM = {"none": 0, "gaussian": 1, "LJish": 2, "LJish/linear": 3}
 NOISE = {"off": 0, "reference": 1, "philox": 2}
 ZGHOST = {"rank1": 0, "periodic": 1}

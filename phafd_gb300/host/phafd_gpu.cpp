@@ -144,7 +144,12 @@ class Interpreter {
   bool want_chempot_ = false;                            // the script writes chempot after a run
   std::vector<phafd_dump::Spec> dumps_;
   struct Cluster { double threshold; bool greater; };
-  std::map<std::string, Cluster> clusters_;  // compute NAME grid/cluster phi THRESHOLD lt|gt
+  std::map<std::string, Cluster> clusters_;  // compute grid/cluster NAME phi THRESHOLD lt|gt
+  struct Complex {
+    int field, quant;
+  };
+  std::map<std::string, Complex> complexes_;  // compute complex NAME ft_phi|ft_chempot real|imag|modulus|norm
+  std::map<std::string, std::vector<double>> compute_cache_;  // each compute's array as last computed
   std::set<std::string> compute_names_;
 
   void check(int rc) {
@@ -522,19 +527,33 @@ class Interpreter {
   // Compute::init + ComputeGridClusters::init (compute.cpp:13-27,
   // compute_grid_clusters.cpp:23-64); other computes only feed dumps of the
   // reference and are not built here
-  void command_compute(const Words& w) {
-    const std::string name = w.at(0);
+  void command_compute(const Words& w) {  // compute STYLE NAME args (input.cpp:234-254)
+    std::string style = w.at(0);
+    if (style.size() > 4 && style.compare(style.size() - 4, 4, "/gpu") == 0) style.resize(style.size() - 4);
+    if (style != "complex" && style != "pair" && style != "grid/cluster") throw std::runtime_error("Invalid compute.");
+    const std::string name = w.at(1);  // Compute::init, compute.cpp:13-27
     if (compute_names_.count(name)) throw std::runtime_error("Error: Duplicate of compute " + name + std::string("."));
     compute_names_.insert(name);
-    const std::string style = w.at(1);
-    if (style == "grid/cluster" || style == "grid/cluster/gpu") {
+    if (style == "grid/cluster") {  // compute_grid_clusters.cpp:23-64
       if (w.at(2) != "phi") throw std::runtime_error("Must use phi as array for clustering.");
       const double thr = num(w.at(3));
       const std::string cond = w.at(4);
       if (cond != "lt" && cond != "gt") throw std::runtime_error("Must specify lt or gt for compute grid cluster.");
       clusters_[name] = Cluster{thr, cond == "gt"};
+    } else if (style == "complex") {  // compute_complex.cpp:14-41
+      const std::string arr = w.at(2);
+      int field;
+      if (arr == "ft_phi") field = PHAFD_FIELD_FT_PHI_STEP_START;  // what the reference sees inside the step
+      else if (arr == "ft_chempot") field = PHAFD_FIELD_FT_CHEMPOT;
+      else throw std::runtime_error("Invalid array to compute in compute modulus.");
+      const std::string q = w.at(3);
+      const int quant = q == "real" ? PHAFD_COMPLEX_REAL : q == "imag" ? PHAFD_COMPLEX_IMAG
+                      : q == "modulus" ? PHAFD_COMPLEX_MODULUS : q == "norm" ? PHAFD_COMPLEX_NORM : -1;
+      if (quant < 0) throw std::runtime_error("Invalid argument in compute complex.");
+      if (field == PHAFD_FIELD_FT_CHEMPOT && !dry_) check(phafd_set_keep_chempot(ctx(), 1));
+      complexes_[name] = Complex{field, quant};
     } else {
-      std::cerr << "WARNING: compute " << name << " " << style << " is not built by phafd_gpu and is ignored."
+      std::cerr << "WARNING: compute " << style << " " << name << " is not built by phafd_gpu and is ignored."
                 << std::endl;
     }
   }
@@ -544,13 +563,28 @@ class Interpreter {
     phafd_dump::Spec d = phafd_dump::parse(w);
     for (auto& o : dumps_)
       if (o.name == d.name) throw std::runtime_error("Error: Duplicate of dump " + d.name + std::string("."));
-    if (d.type == "ftgrid") throw std::runtime_error("ftgrid dumps are not built by phafd_gpu");
-    if (d.type == "grid") {
+    // process_attribute_name's checks (dump.cpp:870-990), made when the command is read
+    auto compute_attr = [&](const std::string& a, bool ft) {
+      const std::string cid = a.substr(2);
+      if (!compute_names_.count(cid))
+        throw std::runtime_error("Cannot write dump, compute ID " + cid + std::string("doesn't exist."));
+      if (ft ? !complexes_.count(cid) : !clusters_.count(cid))
+        throw std::runtime_error("Cannot write dump, compute ID " + cid +
+                                 std::string(ft ? "is not a per_ftgrid quantity." : "is not a per_grid quantity."));
+    };
+    if (d.type == "ftgrid") {
+      if (!gridset_) throw std::runtime_error("ft_phi does not exist, but needed to save dump.");
+      for (auto& a : d.attributes) {
+        if (a.rfind("c_", 0) == 0) compute_attr(a, true);
+        else if (a.rfind("f_", 0) == 0) throw std::runtime_error("Cannot write dump, fix ID " + a.substr(2) +
+                                                                 std::string("is not a per_ftgrid quantity."));
+        else throw std::runtime_error("Something wrong, should not get here. ");
+      }
+    } else if (d.type == "grid") {
       if (!gridset_) throw std::runtime_error("phi does not exist, but needed to save dump.");
       for (auto& a : d.attributes) {
         if (a.rfind("c_", 0) == 0) {
-          if (!clusters_.count(a.substr(2)))
-            throw std::runtime_error("Cannot write dump, compute ID " + a.substr(2) + std::string("doesn't exist."));
+          compute_attr(a, false);
         } else if (a.rfind("gradphi_", 0) == 0) {
           // the reference's arrays hold the gradient of the step's starting
           // phi; the resident state holds the gradient of the current phi
@@ -567,7 +601,28 @@ class Interpreter {
     dumps_.push_back(d);
   }
 
-  void write_dumps(bool force_all) {
+  // a compute's array at a dump: computed on dump steps inside a run; the
+  // dump a run writes at its start gets the array as the compute last left
+  // it, zeros before any step (integrate.cpp:62-64)
+  const std::vector<double>& compute_array(const std::string& cid, bool start_of_run) {
+    std::vector<double>& a = compute_cache_[cid];
+    const size_t n = complexes_.count(cid) ? ncplx() : (size_t)grid_n_[0] * grid_n_[1] * grid_n_[2];
+    if (a.size() != n) a.assign(n, 0.0);
+    if (start_of_run) return a;
+    if (complexes_.count(cid)) {
+      const Complex& c = complexes_.at(cid);
+      check(phafd_compute_complex(ctx(), c.field, c.quant, a.data()));
+    } else {
+      const Cluster& c = clusters_.at(cid);
+      std::vector<int> lab(n);
+      check(phafd_compute_grid_clusters(ctx(), c.threshold, c.greater ? 1 : 0, lab.data(), nullptr));
+      for (size_t k = 0; k < n; ++k) a[k] = lab[k];
+    }
+    return a;
+  }
+  size_t ncplx() const { return (size_t)(grid_n_[0] / 2 + 1) * grid_n_[1] * grid_n_[2]; }
+
+  void write_dumps(bool force_all, bool start_of_run) {
     bool any = false;
     for (auto& d : dumps_) any = any || force_all || timestep_ % d.every == 0;
     if (!any) return;
@@ -576,29 +631,34 @@ class Interpreter {
     std::vector<double> x, ux, f;
     std::vector<int> img;
     std::map<std::string, std::vector<double>> fields;
+    std::set<std::string> done;  // computes evaluated at this step
     for (auto& d : dumps_) {
       if (!force_all && timestep_ % d.every != 0) continue;
       phafd_dump::Atoms a;
       phafd_dump::Grid g;
-      if (d.type == "grid") {
-        g.nx = grid_n_[0]; g.ny = grid_n_[1]; g.nz = grid_n_[2];
-        for (int k = 0; k < 3; ++k) {
-          g.boxlo[k] = boxlo_[k];
-          g.spacing[k] = period_[k] / grid_n_[k];
+      if (d.type == "grid" || d.type == "ftgrid") {
+        if (d.type == "grid") {
+          g.nx = grid_n_[0]; g.ny = grid_n_[1]; g.nz = grid_n_[2];
+          for (int k = 0; k < 3; ++k) {
+            g.boxlo[k] = boxlo_[k];
+            g.spacing[k] = period_[k] / grid_n_[k];
+          }
+        } else {  // the transposed half spectrum [ky][kz][kx] (grid.cpp:212-225), spacing dq (domain.cpp:206-208)
+          g.nx = grid_n_[0] / 2 + 1; g.ny = grid_n_[2]; g.nz = grid_n_[1];
+          g.spacing[0] = 2 * 3.141592 / period_[0];
+          g.spacing[1] = 2 * 3.141592 / period_[2];
+          g.spacing[2] = 2 * 3.141592 / period_[1];
         }
         for (auto& att : d.attributes) {
+          if (att.rfind("c_", 0) == 0) {
+            const std::string cid = att.substr(2);
+            g.fields[att] = done.count(cid) ? compute_cache_[cid].data() : compute_array(cid, start_of_run).data();
+            done.insert(cid);
+            continue;
+          }
           if (!fields.count(att)) {
             std::vector<double> buf(nr);
-            if (att == "phi") {
-              check(phafd_grid_get(ctx(), PHAFD_FIELD_PHI, buf.data()));
-            } else if (att == "chempot") {
-              check(phafd_grid_get(ctx(), PHAFD_FIELD_CHEMPOT, buf.data()));
-            } else {
-              const Cluster& c = clusters_.at(att.substr(2));
-              std::vector<int> lab(nr);
-              check(phafd_compute_grid_clusters(ctx(), c.threshold, c.greater ? 1 : 0, lab.data(), nullptr));
-              for (size_t k = 0; k < nr; ++k) buf[k] = lab[k];
-            }
+            check(phafd_grid_get(ctx(), att == "phi" ? PHAFD_FIELD_PHI : PHAFD_FIELD_CHEMPOT, buf.data()));
             fields[att] = std::move(buf);
           }
           g.fields[att] = fields[att].data();
@@ -619,6 +679,7 @@ class Interpreter {
       phafd_dump::write_step(d, timestep_, dt_, &a, &g);
     }
   }
+
 
   // the reference-noise generator's state for a restart (an extension:
   // the reference keeps no generator state across runs)
@@ -700,7 +761,7 @@ class Interpreter {
     // Integrate::setup (integrate.cpp:47-84): collection headers, then the
     // dumps of the starting step
     for (auto& d : dumps_) phafd_dump::collection_header(d);
-    write_dumps(false);
+    write_dumps(false, true);
     auto t0 = std::chrono::steady_clock::now();
     const long long chunk = 1000;
     for (long long s = 0; s < nsteps;) {
@@ -709,7 +770,7 @@ class Interpreter {
       check(phafd_run(ctx(), (int)n));
       s += n;
       timestep_ += n;
-      write_dumps(false);  // integrate.cpp:179-186
+      write_dumps(false, false);  // integrate.cpp:179-186
     }
     auto t1 = std::chrono::steady_clock::now();
     for (auto& d : dumps_) phafd_dump::collection_footer(d);

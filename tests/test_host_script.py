@@ -166,7 +166,7 @@ def test_script_run_until_touching_stops(exe, tmp_path, gpu_lib):
 
 
 DUMPS = SCRIPT.replace("dump realgrid grid out 100 attributes 1 phi\n",
-                       "compute cl grid/cluster phi 0.5 gt\n"
+                       "compute grid/cluster cl phi 0.5 gt\n"
                        "dump beads atom/owned vtk/beads 10 attributes 3 x ID type decimalplaces 12 fmt e\n"
                        "dump fields grid vtk/fields 10 attributes 3 phi chempot c_cl\n"
                        "dump traj lammpsatom vtk/traj 10 attributes 2 ID x\n")
@@ -339,3 +339,35 @@ def test_noise_state_commands(exe, tmp_path):
     scene(tmp_path, SCRIPT.replace("timestep 0", "read_noise_state none.txt\ntimestep 0"))
     r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
     assert r.returncode == 1 and "Cannot open file none.txt" in r.stderr
+
+
+FTDUMP = SCRIPT.replace("dump realgrid grid out 100 attributes 1 phi\n",
+                        "compute complex sk ft_phi norm\n"
+                        "compute complex mu ft_chempot real\n"
+                        "compute grid/cluster cl phi 0.5 gt\n"
+                        "dump spec ftgrid ft/spec 10 attributes 2 c_sk c_mu\n"
+                        "dump fields grid ft/fields 10 attributes 2 phi c_cl\n")
+
+
+def test_compute_and_ftgrid_commands_parse(exe, tmp_path):
+    scene(tmp_path, FTDUMP)
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    assert r.returncode == 0, r.stderr
+    assert r.stderr == ""
+
+
+@pytest.mark.parametrize("edit,msg", [
+    (("compute complex sk ft_phi norm", "compute sk complex ft_phi norm"), "Invalid compute."),
+    (("compute complex sk ft_phi norm", "compute complex sk phi norm"), "Invalid array to compute in compute modulus."),
+    (("compute complex sk ft_phi norm", "compute complex sk ft_phi square"), "Invalid argument in compute complex."),
+    (("compute complex mu ft_chempot real", "compute complex sk ft_chempot real"), "Duplicate of compute sk."),
+    (("attributes 2 c_sk c_mu", "attributes 2 c_sk c_cl"), "Cannot write dump, compute ID clis not a per_ftgrid quantity."),
+    (("attributes 2 c_sk c_mu", "attributes 2 c_sk phi"), "Something wrong, should not get here."),
+    (("attributes 2 phi c_cl", "attributes 2 phi c_sk"), "Cannot write dump, compute ID skis not a per_grid quantity."),
+    (("attributes 2 c_sk c_mu", "attributes 2 c_sk c_none"), "Cannot write dump, compute ID nonedoesn't exist."),
+])
+def test_compute_and_ftgrid_errors(exe, tmp_path, edit, msg):
+    """compute.cpp / compute_complex.cpp / dump.cpp:870-990 messages (dry run)."""
+    scene(tmp_path, FTDUMP.replace(*edit))
+    r = run(exe, tmp_path, "-sf", "gpu", "-dry-run")
+    assert r.returncode == 1 and msg in r.stderr, r.stderr

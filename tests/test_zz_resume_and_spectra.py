@@ -81,3 +81,45 @@ def test_chempot_and_spectra_match_oracle(gpu_lib):
         assert rel_err(g.compute_complex("ft_phi", q), w) < 1e-9, q
     mu_spec = o.grid_get("ft_chempot")
     assert rel_err(g.compute_complex("ft_chempot", "norm"), np.abs(mu_spec) ** 2 * prefac ** 2) < 1e-9
+
+
+from tests.test_host_script import FTDUMP, exe, run, scene  # noqa: E402,F401  (exe is a fixture)
+
+
+def _appended(path, narrays):
+    raw = path.read_bytes()
+    head = raw[:raw.index(b'<AppendedData encoding="raw">')].decode()
+    at = raw.index(b'<AppendedData encoding="raw">\n_') + len(b'<AppendedData encoding="raw">\n_')
+    out = []
+    for _ in range(narrays):
+        nbytes = int.from_bytes(raw[at:at + 4], "little")
+        out.append(np.frombuffer(raw, "<f8", nbytes // 8, at + 4))
+        at += 4 + nbytes
+    return head, out
+
+
+def test_script_ftgrid_dump(exe, tmp_path, gpu_lib):
+    """compute complex + ftgrid dump through a script: zeros in the starting
+    dump (the reference's computes have not run yet), then the spectrum of
+    the dump step's starting phi; its k = 0 mode carries the conserved mass
+    of the initial field.  The grid dump's cluster labels match an
+    independent labelling of the same step's phi."""
+    from tests.cluster_ref import periodic_min_id_labels
+    scene(tmp_path, FTDUMP)
+    (tmp_path / "ft").mkdir()
+    r = run(exe, tmp_path, "-sf", "gpu")
+    assert r.returncode == 0, r.stderr
+    head, (sk0, mu0) = _appended(tmp_path / "ft" / "spec_p0_0.vti", 2)
+    assert 'WholeExtent="0 16 0 31 0  31"' in head and 'Origin="0 0 0 "' in head
+    assert 'Spacing="0.19635 0.19635 0.19635 "' in head  # 2 * 3.141592 / 32
+    assert not sk0.any() and not mu0.any()
+    _, (phi0, cl0) = _appended(tmp_path / "ft" / "fields_p0_0.vti", 2)
+    assert not cl0.any()
+    _, (sk, mu) = _appended(tmp_path / "ft" / "spec_p0_10.vti", 2)
+    assert sk.size == 17 * 32 * 32 and np.isfinite(sk).all() and (sk >= 0).all() and np.isfinite(mu).all()
+    mass = phi0.sum()  # dx = dy = dz = 1: prefac 1
+    assert abs(sk[0] - mass ** 2) < 1e-5 * mass ** 2
+    assert np.abs(mu).max() > 0
+    _, (phi10, cl10) = _appended(tmp_path / "ft" / "fields_p0_10.vti", 2)
+    want, _ = periodic_min_id_labels(phi10.reshape(32, 32, 32), 0.5, True)
+    assert np.array_equal(cl10.astype(np.int64), want.ravel().astype(np.int64))
