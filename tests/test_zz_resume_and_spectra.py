@@ -123,3 +123,22 @@ def test_script_ftgrid_dump(exe, tmp_path, gpu_lib):
     _, (phi10, cl10) = _appended(tmp_path / "ft" / "fields_p0_10.vti", 2)
     want, _ = periodic_min_id_labels(phi10.reshape(32, 32, 32), 0.5, True)
     assert np.array_equal(cl10.astype(np.int64), want.ravel().astype(np.int64))
+
+
+def test_step_start_spectrum_is_the_previous_phi(gpu_lib):
+    """PHAFD_FIELD_FT_PHI_STEP_START after 6 steps: the r2c of phi after 5
+    (the oracle's), zeros right after set-up."""
+    cfg = dict(W.CONFIGS["32cube_64beads"], field_noise="philox", bead_temp=1.0, dt=5e-4)
+    o, g = Oracle(), gpu()
+    chains = W.apply(g, cfg)
+    W.apply(o, cfg, chains=chains)
+    g.setup()
+    o.setup()
+    assert not g.grid_get("ft_phi_step_start").any()
+    o.run(5)
+    want = OR.fft_r2c(o.grid_get("phi"))
+    g.run(6)
+    assert rel_err(g.grid_get("ft_phi_step_start"), want) < 1e-9
+    g.run(1)  # a single step (the other graph path)
+    o.run(1)
+    assert rel_err(g.grid_get("ft_phi_step_start"), OR.fft_r2c(o.grid_get("phi"))) < 1e-9
