@@ -142,3 +142,15 @@ def test_step_start_spectrum_is_the_previous_phi(gpu_lib):
     g.run(1)  # a single step (the other graph path)
     o.run(1)
     assert rel_err(g.grid_get("ft_phi_step_start"), OR.fft_r2c(o.grid_get("phi"))) < 1e-9
+
+
+def test_fp64_run_matches_golden_fixture(gpu_lib):
+    """The CUDA FP64 path on the committed oracle fixture's inputs (16^3
+    grid, 12-bead chain, Philox noise, 10 steps): the parity tolerance."""
+    import os
+    from tests.golden.make_golden import step_case
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_cases.npz"))
+    phi, x, ux, f, im = step_case(gpu(64), g["phi0"], (g["x0"], g["tags"], g["mol"], g["types"]))
+    assert rel_err(phi, g["phi"]) < 1e-10
+    assert np.abs(ux - g["ux"]).max() < 1e-10 * np.abs(g["ux"]).max()
+    assert np.array_equal(im, g["images"])
