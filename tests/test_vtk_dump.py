@@ -202,3 +202,14 @@ def test_lammps_dump_matches_reference_format(written):
     assert not (written / "lmp.pvd").exists()
     assert (written / "lmp_p0.lmmpstrj").read_text() == expect_lammps(s, ["ID", "type", "x", "F"], [0, 10], -1,
                                                                        "lf")
+
+
+def test_ftgrid_dump_matches_reference_format(written):
+    """dump ftgrid of a per_ftgrid compute (dump.cpp:681-867 with the ftgrid
+    branch): dimensions of the transposed half spectrum, spacing dq, origin 0."""
+    sk = 1.0 / (np.arange(4 * 5 * 4) + 3)
+    s = dict(nx=4, ny=5, nz=4, origin=(0.0, 0.0, 0.0),
+             spacing=(2 * 3.141592 / 12.0, 2 * 3.141592 / 10.0, 2 * 3.141592 / 8.0), fields={"c_sk": sk})
+    assert (written / "spec.pvd").read_text() == expect_pvd("spec", [5], 1e-3, "vti")
+    assert (written / "spec_p0_5.vti").read_bytes() == expect_vti(s, ["c_sk"])
+    assert (written / "spec_5.pvti").read_text() == expect_pvti(s, ["c_sk"], "spec_p0_5.vti")

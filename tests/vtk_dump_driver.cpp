@@ -36,6 +36,14 @@ int main(int argc, char** argv) {
   g.spacing[0] = 1.0; g.spacing[1] = 1.0; g.spacing[2] = 1.0;
   g.fields["phi"] = phi.data();
   g.fields["chempot"] = mu.data();
+  // an ftgrid file: the half spectrum [ky][kz][kx] of a 6 (x) x 4 (y) x 5 (z)
+  // grid, spacing dq (x, then the z and y periods), origin 0
+  std::vector<double> sk(4 * 5 * 4);
+  for (size_t i = 0; i < sk.size(); ++i) sk[i] = 1.0 / (i + 3);
+  phafd_dump::Grid ft;
+  ft.nx = 4; ft.ny = 5; ft.nz = 4;
+  ft.spacing[0] = 2 * 3.141592 / 12.0; ft.spacing[1] = 2 * 3.141592 / 10.0; ft.spacing[2] = 2 * 3.141592 / 8.0;
+  ft.fields["c_sk"] = sk.data();
   using V = std::vector<std::string>;
   const std::vector<V> specs = {
       {"a1", "atom/owned", dir + "/sub/atoms", "10", "attributes", "8", "x", "ux", "F", "ix", "ID", "molID", "type", "label"},
@@ -52,5 +60,9 @@ int main(int argc, char** argv) {
     phafd_dump::write_step(s, 10, 1e-3, &a, &g);
     phafd_dump::collection_footer(s);
   }
+  const phafd_dump::Spec fs = phafd_dump::parse(V{"s1", "ftgrid", dir + "/spec", "5", "attributes", "1", "c_sk"});
+  phafd_dump::collection_header(fs);
+  phafd_dump::write_step(fs, 5, 1e-3, &a, &ft);
+  phafd_dump::collection_footer(fs);
   return 0;
 }
