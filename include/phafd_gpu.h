@@ -138,6 +138,20 @@ int phafd_set_plane_fusion(phafd_ctx* ctx, int on);                 /* x and y p
  * stores it everywhere.  Reads of the gradient fields (phafd_grid_get,
  * phafd_grid_device) first recompute them everywhere from the current phi. */
 int phafd_set_gradient_mask(phafd_ctx* ctx, int on);
+/* FP32 contexts only (no effect in FP64; both stages on by default): the
+ * stages that work relative to a reference concentration c, the mean of phi
+ * found at set-up.  PHAFD_CENTER_FFT: the transforms of phi carry phi - c
+ * (N c goes back into the k = 0 mode, c back into phi after the inverse), so
+ * their round-off scales with the fluctuations of phi, not with its mean.
+ * PHAFD_CENTER_FH: the Flory-Huggins part of mu is formed as
+ * tv (f(phi) - f(c)) with one log1p; the constant tv f(c) moves only the
+ * k = 0 mode of mu, which the update does not read (a kept chempot and its
+ * spectrum include it).  Takes effect at the next step.  No counterpart in the
+ * reference, which is FP64 throughout; switching stages off gives the FP32
+ * error budget. */
+#define PHAFD_CENTER_FH 1
+#define PHAFD_CENTER_FFT 2
+int phafd_set_fp32_centering(phafd_ctx* ctx, int stages);
 
 /* ---- beads (atom_style / atom_populate, atom.cpp:26-110,219-252) ---- */
 int phafd_atoms_create(phafd_ctx* ctx, int n, const int* tags, const int* mol, const int* types, const double* x);
@@ -268,12 +282,15 @@ int phafd_stage_pairs(phafd_ctx* ctx);             /* Fs = 0, chempot = 0, pair-
  * device).  phi, gradx, grady, gradz are caller-owned device arrays
  * [z][y][x] of FP64; period is a host array of the three box lengths;
  * stream is a cudaStream_t (NULL = default stream).  Same result as
- * phafd_stage_gradient (fixgrid_gradphi.cpp:42-99).  The scratch spectra
- * live in a fixed 6.5 MB device array inside the library, so every axis must
- * be 16, 32 or 64 points (larger: PHAFD_ERR_UNSUPPORTED, nothing done).  All
- * calls share that array: calls that overlap on the GPU race.  The first
- * call on a device looks up the array's device address; make it before any
- * stream capture on that device.  Allocates no device memory. */
+ * phafd_stage_gradient on the same phi and box.  The scratch spectra live in
+ * a fixed 6.5 MB device array inside the library, so every axis must be 16,
+ * 32 or 64 points (larger: PHAFD_ERR_UNSUPPORTED, nothing done).  All calls
+ * share that array (and the library's twiddle tables): calls that overlap on
+ * the GPU race; calls ordered on one stream need no synchronisation.  The
+ * first call on a device looks up the arrays' device addresses and fills the
+ * twiddle tables with a synchronous copy; make it before any stream capture
+ * on that device.  Later calls only enqueue kernels.  Allocates no device
+ * memory. */
 int phafd_gradphi_noalloc(const double* phi, double* gradx, double* grady, double* gradz, int nx, int ny, int nz,
                           const double* period, void* stream);
 

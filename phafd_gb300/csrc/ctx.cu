@@ -83,6 +83,13 @@ __global__ void k_axpy(T* __restrict__ y, const T* __restrict__ x, T scale, long
     y[k] += scale * x[k];
 }
 
+// F[k = 0] += v: the reference concentration's share N c of the k = 0 mode,
+// after an r2c of phi - c
+template <typename T>
+__global__ void k_origin_add(cpx<T>* F, double v) {
+  F[0].x += (T)v;
+}
+
 // shell sums of |F|^2 over the half spectrum [kx][kz][ky]; modes with
 // 0 < kx < Nx/2 stand for their mirror too (weight 2)
 // |q| in units of the x-axis dq (ry = dqy/dqx, rz = dqz/dqx): integer
@@ -166,6 +173,40 @@ struct phafd_ctx {
   bool use_plane = false;  // plane-fused x/y passes where they apply (phafd_set_plane_fusion)
   bool use_gmask = false;  // gradient stored near beads only during steps (phafd_set_gradient_mask)
   bool grad_partial = false;  // gx, gy, gz hold values at masked nodes only
+  // FP32 reference concentration c (0: none), set at set-up from the mean of
+  // phi: FP32 transforms of phi carry phi - c, with N c added to the k = 0
+  // mode of the spectrum in FP64-exact arithmetic (the spectrum keeps its
+  // meaning), and the Flory-Huggins part of mu is taken relative to f(c), so
+  // that round-off scales with the fluctuations, not with the mean
+  double phi_ref = 0.0;
+  // which FP32 stages use c (phafd_set_fp32_centering): PHAFD_CENTER_FH the
+  // Flory-Huggins part, PHAFD_CENTER_FFT the transforms of phi
+  int center_bits = PHAFD_CENTER_FH | PHAFD_CENTER_FFT;
+  bool centered(int bit = PHAFD_CENTER_FH | PHAFD_CENTER_FFT) const {
+    return precision == PHAFD_FP32 && phi_ref > 0.0 && phi_ref < 1.0 && (center_bits & bit);
+  }
+  // the FP32 value of c the kernels use (0 when the stage is not centered)
+  double ref_c(int bit = PHAFD_CENTER_FFT) const { return centered(bit) ? (double)(float)phi_ref : 0.0; }
+  void center(FHArgs& f, int bit) const {
+    if (!centered(bit)) return;
+    const double c = ref_c(bit);
+    f.c = c;
+    f.inv_c = 1.0 / c;
+    f.fconst = f.enabled ? f.tv * (std::log(c / (1.0 - c)) + f.chi * (1.0 - 2.0 * c)) : 0.0;
+    f.centered = 1;
+  }
+  FHArgs plain_fh() const {  // r2c of phi without the Flory-Huggins prologue
+    FHArgs f{0, 0, fh_counters(), 0, nullptr};
+    center(f, PHAFD_CENTER_FFT);
+    return f;
+  }
+  FHArgs step_fh() const {  // mu = deposit + FH(phi), fused into the x r2c of a step
+    FHArgs f{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
+    center(f, PHAFD_CENTER_FH);
+    return f;
+  }
+  // N f(c) tv: what the k = 0 mode of a centered mu spectrum lacks
+  double mu_origin_shift() const { return (double)nreal * step_fh().fconst; }
   int nsub = 1;            // substeps of one step (phafd_set_linear_substeps)
   double f2_lin = 0.0;     // dmu/dphi of the linearisation
   int graph_cur = 0;
@@ -343,19 +384,20 @@ struct phafd_ctx {
     chk(GridOps<T>::ypass(geom, -1, out, out, nullptr, twf[1], st), "y fft");
     mark(5);
     chk(GridOps<T>::zpass(geom, -1, out, out, nullptr, twf[2], nullptr, st), "z fft");
+    if (fh.centered && !depp) k_origin_add<T><<<1, 1, 0, st>>>(out, (double)nreal * fh.c);  // phi - c was transformed
     mark(6);
   }
 
   // y inverse and x c2r of A (and B): phi (scale sp, optional) and grad (scale sg)
   template <typename T>
-  void yx_inverse(T* phi_out, T sp, T sg, bool grad, bool nan_check, bool masked = false) {
+  void yx_inverse(T* phi_out, T sp, T sg, bool grad, bool nan_check, bool masked = false, double phi_off = 0.0) {
     const cpx<T>* twi[3] = {tw[0][1].as<cpx<T>>(), tw[1][1].as<cpx<T>>(), tw[2][1].as<cpx<T>>()};
     cpx<T>* A = wA.as<cpx<T>>();
     cpx<T>* B = wB.as<cpx<T>>();
     cpx<T>* Cc = wC.as<cpx<T>>();
     cpx<T>* D = wD.as<cpx<T>>();
     cpx<T>* E = wE.as<cpx<T>>();
-    NanArgs nan{nan_check ? 1 : 0, d_nan(), d_step()};
+    NanArgs nan{nan_check ? 1 : 0, d_nan(), d_step(), phi_off};
     NanArgs nonan{0, d_nan(), d_step()};
     if (grad && phi_out) {
       // one launch per direction for the whole inverse chain
@@ -389,10 +431,10 @@ struct phafd_ctx {
   // plane-fused y ifft + x c2r of A (phi, dphi/dx; dphi/dy) and B (dphi/dz);
   // false when the plane path does not apply to this grid
   template <typename T>
-  bool yx_fused() {
+  bool yx_fused(double phi_off) {
     const cpx<T>* twy = tw[1][1].as<cpx<T>>();
     const cpx<T>* twx = tw[0][1].as<cpx<T>>();
-    NanArgs nan{1, d_nan(), d_step()};
+    NanArgs nan{1, d_nan(), d_step(), phi_off};
     NanArgs nonan{0, d_nan(), d_step()};
     const int rc = GridOps<T>::yx_inv(geom, wA.as<cpx<T>>(), phi.as<T>(), (T)1, false, gx.as<T>(), (T)1, twy, twx, nan, st);
     if (rc == -3) return false;
@@ -631,8 +673,7 @@ struct phafd_ctx {
   // ------------------------------------------------------------------ step
   template <typename T>
   void gradient_from_phi() {
-    FHArgs none{0, 0, fh_counters(), 0, nullptr};
-    r2c<T>(phi.as<T>(), nullptr, w1.as<cpx<T>>(), none);
+    r2c<T>(phi.as<T>(), nullptr, w1.as<cpx<T>>(), plain_fh());
     inverse_chain<T>(w1.as<cpx<T>>(), nullptr, nullptr, (T)0, (T)(1.0 / (double)nreal), true, false);
   }
 
@@ -675,7 +716,7 @@ struct phafd_ctx {
     }
     mark(3);
     if (have_conj) {
-      FHArgs fh{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
+      const FHArgs fh = step_fh();
       if (resident) {
         // post_force + pre_final_integrate fused into the x r2c, y fft; then
         // z fft + update + z ifft in one pass (planes finished separately)
@@ -699,6 +740,7 @@ struct phafd_ctx {
         // the state stays an unnormalised r2c spectrum: store N * update
         UpdateArgs<T> u = update_args<T>(phat[cur].as<cpx<T>>(), muhat.as<cpx<T>>(), phat[1 - cur].as<cpx<T>>(),
                                          (double)nreal);
+        u.phi_off = (T)ref_c();  // the inverse chain transforms phi' - c; the c2r adds c back
         // the two Hermitian planes (kx = 0, Nx/2) on a parallel branch, the
         // bulk planes on the main stream
         cudaStream_t ps = fork ? st3 : st;
@@ -721,7 +763,7 @@ struct phafd_ctx {
           CK(cudaEventRecord(ev_join, st2));
           CK(cudaStreamWaitEvent(st, ev_join, 0));
         }
-        if (!use_plane || !yx_fused<T>()) yx_inverse<T>(phi.as<T>(), (T)1, (T)1, true, true, masked);
+        if (!use_plane || !yx_fused<T>(ref_c())) yx_inverse<T>(phi.as<T>(), (T)1, (T)1, true, true, masked, ref_c());
       } else {
         // post_force + pre_final_integrate: mu = dep + FH(phi), r2c
         r2c<T>(phi.as<T>(), dep.as<T>(), muhat.as<cpx<T>>(), fh);
@@ -953,6 +995,14 @@ int phafd_set_plane_fusion(phafd_ctx* c, int on) {
   API_END(c)
 }
 
+int phafd_set_fp32_centering(phafd_ctx* c, int stages) {
+  API_BEGIN(c)
+  if (stages & ~(PHAFD_CENTER_FH | PHAFD_CENTER_FFT)) throw std::invalid_argument("unknown centering stage");
+  c->center_bits = stages;
+  c->invalidate_graph();
+  API_END(c)
+}
+
 int phafd_set_gradient_mask(phafd_ctx* c, int on) {
   API_BEGIN(c)
   const bool was = c->use_gmask;
@@ -1138,6 +1188,8 @@ int phafd_grid_get(phafd_ctx* c, int field, double* host) {
     else b = &c->w1;
     if (f64) copy_spec_to_host<double>(c, *b, host, sc);
     else copy_spec_to_host<float>(c, *b, host, sc);
+    // an FP32 context transforms mu - tv f(c) (see FHArgs): restore its k = 0 mode
+    if (field == PHAFD_FIELD_FT_CHEMPOT) host[0] += c->mu_origin_shift();
   } else {
     const DevBuf* b = field == PHAFD_FIELD_PHI ? &c->phi : field == PHAFD_FIELD_GRADX ? &c->gx
                     : field == PHAFD_FIELD_GRADY ? &c->gy : field == PHAFD_FIELD_GRADZ ? &c->gz
@@ -1359,18 +1411,27 @@ int phafd_setup(phafd_ctx* c) {
     launch_neighbor(c->ba, true, c->st);  // Integrate::setup: pbc, borders, build
     c->bf.zero(c->st);
   }
+  // FP32 reference concentration: the mean of phi, from the k = 0 mode of an
+  // uncentered r2c
+  if (c->gridset && c->precision == PHAFD_FP32) {
+    c->phi_ref = 0.0;
+    c->r2c<float>(c->phi.as<float>(), nullptr, c->w1.as<cpx<float>>(), c->plain_fh());
+    float origin[2];
+    CK(cudaMemcpyAsync(origin, c->w1.p, sizeof(origin), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    const double mean = (double)origin[0] / (double)c->nreal;
+    c->phi_ref = std::isfinite(mean) && mean > 0.0 && mean < 1.0 ? mean : 0.0;
+  }
   // field state
   if (c->gridset && (c->have_conj || c->have_gradphi)) {
     if (c->precision == PHAFD_FP64) {
       if (c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj) {
-        FHArgs none{0, 0, c->fh_counters(), 0, nullptr};
-        c->r2c<double>(c->phi.as<double>(), nullptr, c->phat[c->cur].as<cpx<double>>(), none);
+        c->r2c<double>(c->phi.as<double>(), nullptr, c->phat[c->cur].as<cpx<double>>(), c->plain_fh());
         c->inverse_chain<double>(c->phat[c->cur].as<cpx<double>>(), nullptr, nullptr, 0.0, 1.0 / (double)c->nreal, true, false);
       }
     } else {
       if (c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj) {
-        FHArgs none{0, 0, c->fh_counters(), 0, nullptr};
-        c->r2c<float>(c->phi.as<float>(), nullptr, c->phat[c->cur].as<cpx<float>>(), none);
+        c->r2c<float>(c->phi.as<float>(), nullptr, c->phat[c->cur].as<cpx<float>>(), c->plain_fh());
         c->inverse_chain<float>(c->phat[c->cur].as<cpx<float>>(), nullptr, nullptr, 0.0f, (float)(1.0 / (double)c->nreal), true, false);
       }
     }
@@ -1745,7 +1806,7 @@ int phafd_structure_factor(phafd_ctx* c, int nbins, double* sk, long long* count
   acc.zero(c->st);
   double* dsum = acc.as<double>();
   unsigned long long* dcnt = reinterpret_cast<unsigned long long*>(dsum + nbins);
-  FHArgs none{0, 0, c->fh_counters(), 0, nullptr};
+  const FHArgs none = c->plain_fh();  // phi - c in FP32: the k = 0 mode is not binned
   const double ry = c->period[0] / c->period[1], rz = c->period[0] / c->period[2];
   const size_t shm = (size_t)nbins * 16;
   if (c->precision == PHAFD_FP64) {
@@ -1852,7 +1913,7 @@ int phafd_grid_add_device(phafd_ctx* c, const void* src, double scale) {
   if (!c->gridset || !src) throw std::invalid_argument("grid not created");
   CK(cudaSetDevice(c->device));
   const bool resident = c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj && c->setup_done;
-  FHArgs none{0, 0, c->fh_counters(), 0, nullptr};
+  const FHArgs none = c->plain_fh();
   if (c->precision == PHAFD_FP64) {
     k_axpy<double><<<1024, 256, 0, c->st>>>(c->phi.as<double>(), (const double*)src, scale, (long long)c->nreal);
     if (resident) {

@@ -16,8 +16,9 @@
 //   y / z / x : the spectral derivative i*dq*m (fixgrid_conjugate.cpp:80-105)
 //   x-inverse : the 1/N of the gradient and the NaN check of phi(0,0,0)
 #pragma once
+#include <map>
 #include <mutex>
-#include <unordered_map>
+#include <utility>
 
 #include "fft.cuh"
 #include "internal.h"
@@ -30,10 +31,37 @@ namespace phafd {
   _Pragma("unroll") for (int it_##idx = 0; it_##idx < ((TOTAL) + (NT)-1) / (NT); ++it_##idx) \
     if (const int idx = (int)threadIdx.x + it_##idx * (NT); ((TOTAL) % (NT)) == 0 || idx < (TOTAL))
 
-// ln(p / (1 - p)) of fixgrid_floryhuggins.cpp:81: FP64 as written; FP32 as
-// the difference of two hardware logarithms (relative error ~1e-6)
-PHAFD_D double fh_log_ratio(double p) { return log(p / (1.0 - p)); }
-PHAFD_D float fh_log_ratio(float p) { return __logf(p) - __logf(1.0f - p); }
+// Flory-Huggins part of mu at phi = p (fixgrid_floryhuggins.cpp:81-82),
+// tv (ln(p / (1 - p)) + chi (1 - 2 p)).  FP64: the reference's expression.
+// FP32 with a reference concentration c: tv (f(p) - f(c)) written as
+// log1p((p - c) / (c (1 - p))) - 2 chi (p - c), whose rounding is relative to
+// the deviation p - c (the constant tv f(c) only moves the k = 0 mode of mu,
+// which the update multiplies by q^2 = 0).  FP32 without c: the difference of
+// two hardware logarithms.
+PHAFD_D double fh_part(double p, const FHArgs& fh) { return fh.tv * (log(p / (1.0 - p)) + fh.chi * (1.0 - 2.0 * p)); }
+PHAFD_D float fh_part(float p, const FHArgs& fh) {
+  if (fh.centered) {
+    const float d = p - (float)fh.c;
+    return (float)fh.tv * (log1pf(__fdividef(d * (float)fh.inv_c, 1.0f - p)) - 2.0f * (float)fh.chi * d);
+  }
+  return (float)fh.tv * ((__logf(p) - __logf(1.0f - p)) + (float)fh.chi * (1.0f - 2.0f * p));
+}
+
+// mu at one node from phi = p and the bead deposit dd: the reflections of
+// fixgrid_floryhuggins.cpp:72-80 (counted), then deposit + FH part.  Returns
+// the value the r2c transforms; *keep is the materialised chempot.
+template <typename T>
+PHAFD_D T fh_node(T p, T dd, const FHArgs& fh, unsigned long long& nless, unsigned long long& ngreat, T* keep) {
+  if (!fh.enabled) {
+    *keep = dd;
+    return dd;
+  }
+  if (p <= (T)0) { p = -p; nless++; }
+  else if (p >= (T)1) { p = (T)1 - (p - (T)1); ngreat++; }
+  const T m = dd + fh_part(p, fh);
+  *keep = fh.centered ? m + (T)fh.fconst : m;
+  return m;
+}
 
 template <typename T>
 PHAFD_D cpx<T> deriv(cpx<T> a, T dq, int m) {
@@ -92,18 +120,20 @@ k_xr2c(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restrict_
       for (int h = 0; h < 2; ++h) {
         const int y = y0 + 2 * l + h;
         if (y < Ny) {
-          T p = v[h];
-          if (fh.enabled) {
-            // fixgrid_floryhuggins.cpp:72-82
-            if (p <= (T)0) { p = -p; nless++; }
-            else if (p >= (T)1) { p = (T)1 - (p - (T)1); ngreat++; }
-            p = dd[h] + (T)fh.tv * (fh_log_ratio(p) + (T)fh.chi * ((T)1 - (T)2 * p));
-          } else {
-            p = dd[h];
-          }
-          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[((size_t)z * Ny + y) * N + x] = p;
-          v[h] = p;
+          T keep;
+          v[h] = fh_node(v[h], dd[h], fh, nless, ngreat, &keep);
+          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[((size_t)z * Ny + y) * N + x] = keep;
         }
+      }
+    }
+  } else {
+    if (fh.centered) {  // transform phi - c
+      TILE_LOOP(idx, LB * N, NT) {
+        const int l = idx / N, x = idx % N;
+        T* v = reinterpret_cast<T*>(&s[x * STR + l]);
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          if (y0 + 2 * l + h < Ny) v[h] -= (T)fh.c;
       }
     }
   }
@@ -198,7 +228,7 @@ PHAFD_D void xc2r_tile(int bx, int z, const cpx<T>* __restrict__ in, T* __restri
       for (int h = 0; h < 2; ++h) {
         const int y = y0 + 2 * l + h;
         if (y < Ny) {
-          const T val = (h == 0 ? v.x : v.y) * sc;
+          const T val = (h == 0 ? v.x : v.y) * sc + (q == 0 ? (T)nan.offset : (T)0);
           const size_t node = ((size_t)z * Ny + y) * N + x;
           const size_t sec = node / G;
           if (!(q == 0 ? mask0 : mask1) || ((mw[(sec >> 5) - w0] >> (sec & 31)) & 1u)) out[node] = val;
@@ -395,6 +425,7 @@ k_zpass(const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, T dq, const cpx<T>* __rest
       if constexpr (UPD) {
         v = update_mode(u, kx, ky, e, o);
         u.phi_new[o] = scale(v, u.store_scale);
+        if (kx == 0 && ky == 0 && e == 0) v.x -= u.phi_off;
       } else {
         v = in[o];
       }
@@ -505,14 +536,18 @@ static void launch_grid(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
 }
 
 // Opt a kernel into more than 48 KB of dynamic shared memory; done once per
-// kernel so that graph capture never sees the attribute call.
+// (device, kernel) so that graph capture never sees the attribute call.  The
+// attribute belongs to the device that is current when it is set, so a
+// process with contexts on two GPUs sets it on each.
 template <typename Kern>
 static int set_smem(Kern k, size_t bytes) {
   if (bytes <= 48 * 1024) return 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
   static std::mutex mu;
-  static std::unordered_map<const void*, size_t> done;
+  static std::map<std::pair<int, const void*>, size_t> done;
   std::lock_guard<std::mutex> lock(mu);
-  size_t& d = done[reinterpret_cast<const void*>(k)];
+  size_t& d = done[std::make_pair(dev, reinterpret_cast<const void*>(k))];
   if (bytes > d) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return -1;

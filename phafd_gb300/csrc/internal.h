@@ -18,12 +18,19 @@ struct FHArgs {
   unsigned long long* counters;  // [0] phi <= 0 reflections, [1] phi >= 1 reflections
   int enabled;                   // 0: mu = deposit only (no fix grid/floryhuggins)
   void* mu_out;                  // optional: materialised chempot (T*)
+  // FP32 contexts with a reference concentration c (centered != 0): the r2c
+  // of phi transforms phi - c; the Flory-Huggins part of mu is evaluated as
+  // f(p) - f(c) (its rounding then scales with p - c, not with f(p)), and
+  // fconst = tv f(c) is added back only where mu is materialised.
+  double c, inv_c, fconst;
+  int centered;
 };
 
 struct NanArgs {
   int check;
   long long* nan_step;
   const long long* d_step;
+  double offset;  // added to the phi output of a c2r (the reference concentration taken out of its k = 0 mode)
 };
 
 template <typename T>
@@ -42,6 +49,9 @@ struct UpdateArgs {
   // (the base propagator of the learned macro step); f2 = dmu/dphi at the mean
   int nsub;
   T f2;
+  // subtracted from the k = 0 mode in the transform that follows the update
+  // (not in the stored spectrum); the c2r adds it back to phi
+  T phi_off;
 };
 
 // compute grid/cluster: labels (device, nx*ny*nz) of the periodic

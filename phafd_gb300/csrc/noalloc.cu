@@ -14,13 +14,16 @@
 //   * every axis of the grid is 16, 32 or 64 points (at most 64^3 nodes);
 //     larger or other sizes return PHAFD_ERR_UNSUPPORTED and do nothing;
 //   * the scratch array (3 x 33 x 64 x 64 complex doubles, 6.5 MB) and the
-//     twiddle table exist on every GPU that loads the library, until exit;
-//   * every call shares that one array: calls whose work overlaps on the GPU
-//     (different streams, or different host threads on one device) race and
-//     corrupt each other's results.  Order them on one stream;
-//   * the first call on a device resolves the device address of the array
-//     (cudaGetSymbolAddress) with that device current.  Make that first call
-//     before any stream capture on the device.
+//     twiddle tables of the three lengths exist on every GPU that loads the
+//     library, until exit;
+//   * every call shares that one scratch array: calls whose work overlaps on
+//     the GPU (different streams, or different host threads on one device)
+//     race and corrupt each other's results.  Calls ordered on one stream
+//     need no synchronisation between them;
+//   * the first call on a device resolves the device addresses of the arrays
+//     (cudaGetSymbolAddress) with that device current and fills the twiddle
+//     tables with a synchronous copy; later calls only enqueue kernels.  Make
+//     that first call before any stream capture on the device.
 #include <cmath>
 #include <mutex>
 
@@ -34,8 +37,15 @@ constexpr int kMaxDevices = 64;
 
 // three spectra: phi_hat, then the z / y inverse intermediates
 static __device__ __align__(256) cpx<double> g_noalloc_scratch[3 * kNoAllocModes];
-// W_N^m for each axis and direction, N <= kNoAllocMaxN
-static __device__ __align__(256) cpx<double> g_noalloc_twiddle[3 * 2 * kNoAllocMaxN];
+// W_N^m for N = 16, 32, 64, forward then inverse: written once per device
+constexpr int kTwiddleEntries = 2 * (16 + 32 + 64);
+static __device__ __align__(256) cpx<double> g_noalloc_twiddle[kTwiddleEntries];
+
+// offset of the table of length n (16, 32 or 64) and direction dir (0 forward, 1 inverse)
+int twiddle_offset(int n, int dir) {
+  const int base = n == 16 ? 0 : (n == 32 ? 2 * 16 : 2 * (16 + 32));
+  return base + dir * n;
+}
 
 struct DeviceSlot {
   bool ready = false;
@@ -68,36 +78,37 @@ extern "C" int phafd_gradphi_noalloc(const double* phi, double* gradx, double* g
       s.scratch = reinterpret_cast<cpx<double>*>(p);
       if (cudaGetSymbolAddress(&p, g_noalloc_twiddle) != cudaSuccess) return PHAFD_ERR_CUDA;
       s.twiddle = reinterpret_cast<cpx<double>*>(p);
+      // W_N^m = exp(-+ 2 pi i m / N) for every supported length, once
+      double tw[2 * kTwiddleEntries];
+      for (int n : {16, 32, 64})
+        for (int dir = 0; dir < 2; ++dir)
+          for (int m = 0; m < n; ++m) {
+            const long double ang = 2.0L * 3.141592653589793238462643383279502884L * m / n;
+            const int k = 2 * (twiddle_offset(n, dir) + m);
+            tw[k] = (double)std::cos(ang);
+            tw[k + 1] = (dir == 0 ? -1.0 : 1.0) * (double)std::sin(ang);
+          }
+      if (cudaMemcpy(s.twiddle, tw, sizeof(tw), cudaMemcpyHostToDevice) != cudaSuccess) return PHAFD_ERR_CUDA;
       s.ready = true;
     }
     slot = s;
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
 
-  // twiddle tables W_N^m = exp(-+ 2 pi i m / N) for the three axes (host stack, no heap)
-  double tw[3 * 2 * kNoAllocMaxN * 2];
   const int ns[3] = {nx, ny, nz};
-  for (int a = 0; a < 3; ++a)
-    for (int dir = 0; dir < 2; ++dir)
-      for (int m = 0; m < ns[a]; ++m) {
-        const long double ang = 2.0L * 3.141592653589793238462643383279502884L * m / ns[a];
-        const size_t k = ((size_t)(a * 2 + dir) * kNoAllocMaxN + m) * 2;
-        tw[k] = (double)std::cos(ang);
-        tw[k + 1] = (dir == 0 ? -1.0 : 1.0) * (double)std::sin(ang);
-      }
-  if (cudaMemcpyAsync(slot.twiddle, tw, sizeof(tw), cudaMemcpyHostToDevice, st) != cudaSuccess) return PHAFD_ERR_CUDA;
-  auto twp = [&](int axis, int dir) { return slot.twiddle + (size_t)(axis * 2 + dir) * kNoAllocMaxN; };
+  auto twp = [&](int axis, int dir) { return slot.twiddle + twiddle_offset(ns[axis], dir); };
 
   Geom g{};
   g.nx = nx; g.ny = ny; g.nz = nz; g.nxh = nx / 2 + 1;
-  for (int d = 0; d < 3; ++d) g.kq[d] = 2 * 3.141592 / period[d];  // domain.cpp:206-208
+  // dq per axis with the same truncated pi as the context's gradient
+  for (int d = 0; d < 3; ++d) g.kq[d] = 2 * 3.141592 / period[d];
   cpx<double>* S0 = slot.scratch;
   cpx<double>* S1 = slot.scratch + kNoAllocModes;
   cpx<double>* S2 = slot.scratch + 2 * kNoAllocModes;
   const double inv_n = 1.0 / ((double)nx * ny * nz);
   FHArgs none{0.0, 0.0, nullptr, 0, nullptr};
   NanArgs nonan{0, nullptr, nullptr};
-  // phi_hat = r2c(phi) into S0 (fixgrid_gradphi.cpp:48)
+  // phi_hat = r2c(phi) into S0
   if (GridOps<double>::xr2c(g, phi, nullptr, S0, twp(0, 0), none, st)) return PHAFD_ERR_CUDA;
   if (GridOps<double>::ypass(g, -1, S0, S0, nullptr, twp(1, 0), st)) return PHAFD_ERR_CUDA;
   if (GridOps<double>::zpass(g, -1, S0, S0, nullptr, twp(2, 0), nullptr, st)) return PHAFD_ERR_CUDA;
@@ -106,7 +117,7 @@ extern "C" int phafd_gradphi_noalloc(const double* phi, double* gradx, double* g
   // y ifft: S1 -> S1 (plain) and S0 (i qy); S2 -> S2
   if (GridOps<double>::ypass(g, +1, S1, S1, S0, twp(1, 1), st)) return PHAFD_ERR_CUDA;
   if (GridOps<double>::ypass(g, +1, S2, S2, nullptr, twp(1, 1), st)) return PHAFD_ERR_CUDA;
-  // x c2r with the 1/N of fixgrid_gradphi.cpp:91-95
+  // x c2r with the 1/N normalisation
   if (GridOps<double>::xc2r(g, S1, gradx, inv_n, true, nullptr, inv_n, twp(0, 1), nonan, st)) return PHAFD_ERR_CUDA;
   if (GridOps<double>::xc2r(g, S0, grady, inv_n, false, nullptr, inv_n, twp(0, 1), nonan, st)) return PHAFD_ERR_CUDA;
   if (GridOps<double>::xc2r(g, S2, gradz, inv_n, false, nullptr, inv_n, twp(0, 1), nonan, st)) return PHAFD_ERR_CUDA;

@@ -108,7 +108,7 @@ k_yx_inv(const cpx<T>* __restrict__ in, T* __restrict__ out0, T s0, T* __restric
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int y = y0 + 2 * p + h;
-        const T val = (h == 0 ? v.x : v.y) * sc;
+        const T val = (h == 0 ? v.x : v.y) * sc + (j == 0 ? (T)nan.offset : (T)0);
         out[((size_t)z * N + y) * N + x] = val;
         if (j == 0 && nan.check && z == 0 && y == 0 && x == 0 && isnan(val))
           atomicCAS(reinterpret_cast<unsigned long long*>(nan.nan_step), (unsigned long long)-1LL,
@@ -154,14 +154,11 @@ k_xy_fwd(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restric
       const size_t o = ((size_t)z * N + y0 + 2 * p + h) * N + x;
       T q = in0[o];
       if constexpr (PRO == 1) {
-        if (fh.enabled) {
-          if (q <= (T)0) { q = -q; nless++; }
-          else if (q >= (T)1) { q = (T)1 - (q - (T)1); ngreat++; }
-          q = dep[o] + (T)fh.tv * (fh_log_ratio(q) + (T)fh.chi * ((T)1 - (T)2 * q));
-        } else {
-          q = dep[o];
-        }
-        if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[o] = q;
+        T keep;
+        q = fh_node(q, dep[o], fh, nless, ngreat, &keep);
+        if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[o] = keep;
+      } else {
+        if (fh.centered) q -= (T)fh.c;  // transform phi - c
       }
       v[h] = q;
     }
@@ -229,11 +226,14 @@ struct Plane {
   template <typename Kern, typename... Args>
   static int launch(Kern k, size_t sm, int nz, cudaStream_t st, Args... args) {
     if (sm > 227 * 1024) return -3;
+    // the attributes belong to the current device: set once per (device, kernel)
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
     static std::mutex mu;
-    static std::unordered_map<const void*, int> done;
+    static std::map<std::pair<int, const void*>, int> done;
     {
       std::lock_guard<std::mutex> lock(mu);
-      int& d = done[reinterpret_cast<const void*>(k)];
+      int& d = done[std::make_pair(dev, reinterpret_cast<const void*>(k))];
       if (!d) {
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) return -1;
         if (C::CL > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)

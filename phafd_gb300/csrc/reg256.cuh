@@ -282,7 +282,7 @@ PHAFD_D void xc2r_tile256(int bx, int z, const cpx<T>* __restrict__ in, T* __res
 #pragma unroll
     for (int r = 0; r < 16; ++r) {
       const int x = j + 16 * r;
-      const T val = (h == 0 ? v[r].x : v[r].y) * sc;
+      const T val = (h == 0 ? v[r].x : v[r].y) * sc + (q == 0 ? (T)nan.offset : (T)0);
       const int sec = x / G;
       uint32_t bit;
       if constexpr (N / G <= 32) bit = (m0 >> sec) & 1u;
@@ -340,16 +340,11 @@ k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restri
       if (y0 + row < Ny) {
         p = sphi[row * N + x];
         if constexpr (PRO == 1) {
-          const T dd = sdep[row * N + x];
-          if (fh.enabled) {
-            // fixgrid_floryhuggins.cpp:72-82
-            if (p <= (T)0) { p = -p; nless++; }
-            else if (p >= (T)1) { p = (T)1 - (p - (T)1); ngreat++; }
-            p = dd + (T)fh.tv * (fh_log_ratio(p) + (T)fh.chi * ((T)1 - (T)2 * p));
-          } else {
-            p = dd;
-          }
-          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[((size_t)z * Ny + y0 + row) * N + x] = p;
+          T keep;
+          p = fh_node(p, sdep[row * N + x], fh, nless, ngreat, &keep);
+          if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[((size_t)z * Ny + y0 + row) * N + x] = keep;
+        } else {
+          if (fh.centered) p -= (T)fh.c;  // transform phi - c
         }
       }
       pr[h] = p;

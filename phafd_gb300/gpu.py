@@ -27,7 +27,7 @@ EXPORTS = [
     "phafd_domain", "phafd_grid_style", "phafd_grid_populate_constant", "phafd_grid_populate_flat_interface",
     "phafd_grid_populate_sphere", "phafd_grid_set", "phafd_grid_get",
     "phafd_set_zghost", "phafd_set_schedule", "phafd_set_keep_chempot", "phafd_set_plane_fusion",
-    "phafd_set_gradient_mask",
+    "phafd_set_gradient_mask", "phafd_set_fp32_centering",
     "phafd_atoms_create", "phafd_atoms_get", "phafd_atoms_set_images",
     "phafd_pair_gridatom", "phafd_pair_gridatom_coeff", "phafd_pair_lj_cut",
     "phafd_neighbor",
@@ -87,6 +87,7 @@ def load(path=None):
         "phafd_set_keep_chempot": [vp, C.c_int],
         "phafd_set_plane_fusion": [vp, C.c_int],
         "phafd_set_gradient_mask": [vp, C.c_int],
+        "phafd_set_fp32_centering": [vp, C.c_int],
         "phafd_domain": [vp, dp, dp],
         "phafd_grid_style": [vp, C.c_int, C.c_int, C.c_int],
         "phafd_grid_populate_constant": [vp, C.c_double, C.c_double, C.c_int],
@@ -195,8 +196,12 @@ class PhafdGPU:
         self._call("phafd_set_plane_fusion", int(on))
 
     def set_gradient_mask(self, on=True):
-        """Store grad phi only near the beads during steps (the default)."""
+        """Store grad phi only near the beads during steps (off by default)."""
         self._call("phafd_set_gradient_mask", int(on))
+
+    def set_fp32_centering(self, fh=True, fft=True):
+        """FP32 stages taken relative to the mean of phi (both on by default)."""
+        self._call("phafd_set_fp32_centering", (1 if fh else 0) | (2 if fft else 0))
 
     def domain(self, boxlo, period):
         self._call("phafd_domain", np.asarray(boxlo, np.float64), np.asarray(period, np.float64))

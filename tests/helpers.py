@@ -54,3 +54,34 @@ def small_scene(driver, n=32, L=32.0, nbeads=64, seed=7, zghost="periodic", styl
         driver.pair_lj_cut(2 ** (1 / 6), 1.0, 1.0)
     driver.neighbor(skin)
     return x, tags, mol, types
+
+
+def shell_sk(phi, nbins=None):
+    """Shell-averaged structure factor of a real cubic field [z][y][x]: |F(k)|^2
+    of the r2c spectrum summed over integer shells floor(|n|) of the
+    wavenumber index (the k = 0 mode left out; modes with 0 < kx < N/2 count
+    twice, for their mirror), divided by the shell's mode count."""
+    phi = np.asarray(phi, np.float64)
+    n = phi.shape[0]
+    F = np.fft.rfftn(phi)
+    p = np.abs(F) ** 2
+    kz = np.fft.fftfreq(n) * n
+    ky = np.fft.fftfreq(n) * n
+    kx = np.arange(n // 2 + 1, dtype=np.float64)
+    r = np.sqrt(kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2)
+    b = np.floor(r + 1e-9).astype(np.int64)
+    w = np.where((kx == 0) | (kx == n // 2), 1.0, 2.0)[None, None, :] * np.ones_like(p)
+    w[0, 0, 0] = 0.0
+    nb = nbins or n // 2
+    keep = b < nb
+    s = np.bincount(b[keep], (w * p)[keep], minlength=nb)
+    c = np.bincount(b[keep], w[keep], minlength=nb)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return np.where(c > 0, s / np.maximum(c, 1), 0.0)
+
+
+def sk_rel_err(a, b):
+    """max over shells (k >= 1) of |S_a - S_b| / S_b."""
+    sa, sb = shell_sk(a), shell_sk(b)
+    m = sb[1:] > 0
+    return float(np.max(np.abs(sa[1:][m] - sb[1:][m]) / sb[1:][m]))

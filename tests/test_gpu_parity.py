@@ -8,7 +8,7 @@ import pytest
 
 from oracle.oracle import Oracle
 from phafd_gb300 import workloads as W
-from tests.helpers import canon_grid, canon_half, rel_err, small_scene
+from tests.helpers import canon_grid, canon_half, rel_err, sk_rel_err, small_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -105,22 +105,16 @@ def test_fp64_drag_fix_matches_oracle(gpu_lib, zghost):
 
 
 def test_fp32_path_error_against_oracle(gpu_lib):
-    """FP32 production path vs the FP64 oracle: max |dphi| and S(k)."""
+    """FP32 production path vs the FP64 oracle: max |dphi| and the relative
+    shell-averaged S(k) error, within the 1e-5 the FP32 path is held to."""
     o = Oracle(); g = gpu(32, "resident")
     for d in (o, g):
         _full_scene(d, "philox")
         d.setup()
         d.run(30)
     po, pg = o.grid_get("phi"), g.grid_get("phi")
-    assert np.abs(pg - po).max() < 1e-4
-    sk_o = np.abs(np.fft.rfftn(po)) ** 2
-    sk_g = np.abs(np.fft.rfftn(pg)) ** 2
-    k = np.sqrt(sum(np.meshgrid(*(np.fft.fftfreq(32) if i < 2 else np.fft.rfftfreq(32) for i in range(3)),
-                                indexing="ij")[i] ** 2 for i in range(3)))
-    shells = np.minimum((k * 32).astype(int), 16)
-    so = np.bincount(shells.ravel(), sk_o.ravel())[1:]
-    sg = np.bincount(shells.ravel(), sk_g.ravel())[1:]
-    assert np.max(np.abs(sg - so) / so) < 1e-4
+    assert np.abs(pg - po).max() < 1e-5
+    assert sk_rel_err(pg, po) < 1e-5
 
 
 def test_fp32_mass_mode_exact(gpu_lib):

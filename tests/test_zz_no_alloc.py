@@ -6,8 +6,12 @@ outputs as its own device arrays; the library must allocate nothing and use
 its built-in scratch array.  This file runs last so that a failure here comes
 after every other test has run.  It checks the entry point against the
 context-based gradient (phafd_stage_gradient) on two calls in a row, at the
-FP64 transform tolerance of the other tests (1e-12 relative), and that a grid
-beyond the built-in scratch size is refused.
+FP64 transform tolerance of the other tests (1e-12 relative); that two calls
+on different grids enqueued back to back on one stream, with no
+synchronisation between them, both come out right; that repeated calls leave
+the device's free memory unchanged; and that a grid beyond the built-in
+scratch size is refused.  The context gradient it compares with is itself
+held to the FP64 oracle by the parity tests.
 """
 import numpy as np
 import pytest
@@ -32,25 +36,65 @@ def context_gradient(phi, period):
     return out
 
 
+def call(L, t_phi, outs, shape, period, stream):
+    nz, ny, nx = shape
+    return L.phafd_gradphi_noalloc(t_phi.data_ptr(), outs[0].data_ptr(), outs[1].data_ptr(), outs[2].data_ptr(),
+                                   nx, ny, nz, np.asarray(period, np.float64), stream)
+
+
+CASES = [((32, 64, 16), [16 * 0.9, 64 * 1.1, 32 * 0.7]), ((16, 16, 64), [64.0, 16.0, 16.0])]
+
+
 def test_noalloc_gradient_matches_context_gradient_twice(gpu_lib):
     torch = pytest.importorskip("torch")
     from phafd_gb300.gpu import load
     L = load()
     rng = np.random.default_rng(2024)
-    cases = [((32, 64, 16), [16 * 0.9, 64 * 1.1, 32 * 0.7]), ((16, 16, 64), [64.0, 16.0, 16.0])]
-    for shape, period in cases:  # two calls in a row, the second on a different grid
-        nz, ny, nx = shape
+    dev = torch.device("cuda", 0)
+    for shape, period in CASES:  # two calls in a row, the second on a different grid
         phi = 0.4 + 0.1 * rng.standard_normal(shape)
         ref = context_gradient(phi, period)
-        dev = torch.device("cuda", 0)
         t_phi = torch.tensor(phi, dtype=torch.float64, device=dev)
         outs = [torch.full(shape, float("nan"), dtype=torch.float64, device=dev) for _ in range(3)]
         stream = torch.cuda.current_stream(dev).cuda_stream
-        rc = L.phafd_gradphi_noalloc(t_phi.data_ptr(), outs[0].data_ptr(), outs[1].data_ptr(), outs[2].data_ptr(),
-                                     nx, ny, nz, np.asarray(period, np.float64), stream)
+        rc = call(L, t_phi, outs, shape, period, stream)
         torch.cuda.synchronize(dev)
         assert rc == 0
         for got, want in zip(outs, ref):
+            assert rel_err(got.cpu().numpy(), want) < 1e-12
+
+
+def test_noalloc_back_to_back_on_one_stream_allocates_nothing(gpu_lib):
+    """Calls ordered on one stream reuse the shared scratch without a host
+    synchronisation between them; once the first calls have set the device up
+    (and the driver has loaded their kernels), further calls leave the
+    device's free memory where it was."""
+    torch = pytest.importorskip("torch")
+    from phafd_gb300.gpu import load
+    L = load()
+    rng = np.random.default_rng(7)
+    dev = torch.device("cuda", 0)
+    phis = [0.4 + 0.1 * rng.standard_normal(shape) for shape, _ in CASES]
+    refs = [context_gradient(phi, period) for phi, (_, period) in zip(phis, CASES)]
+    t_phis = [torch.tensor(phi, dtype=torch.float64, device=dev) for phi in phis]
+    outs = [[torch.full(shape, float("nan"), dtype=torch.float64, device=dev) for _ in range(3)]
+            for shape, _ in CASES]
+    s = torch.cuda.Stream(device=dev)
+    torch.cuda.synchronize(dev)
+    # first calls: device set-up, and the driver loads each kernel on its
+    # first launch; then measure
+    for k, (shape, period) in enumerate(CASES):
+        assert call(L, t_phis[k], outs[k], shape, period, s.cuda_stream) == 0
+    torch.cuda.synchronize(dev)
+    free0, _ = torch.cuda.mem_get_info(dev)
+    for _ in range(3):
+        for k, (shape, period) in enumerate(CASES):  # no synchronisation between the calls
+            assert call(L, t_phis[k], outs[k], shape, period, s.cuda_stream) == 0
+    torch.cuda.synchronize(dev)
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0
+    for k in range(len(CASES)):
+        for got, want in zip(outs[k], refs[k]):
             assert rel_err(got.cpu().numpy(), want) < 1e-12
 
 
@@ -62,8 +106,7 @@ def test_noalloc_refuses_grids_beyond_its_scratch(gpu_lib):
     shape = (16, 16, 128)
     t = torch.zeros(shape, dtype=torch.float64, device=dev)
     outs = [torch.full(shape, 7.0, dtype=torch.float64, device=dev) for _ in range(3)]
-    rc = L.phafd_gradphi_noalloc(t.data_ptr(), outs[0].data_ptr(), outs[1].data_ptr(), outs[2].data_ptr(),
-                                 128, 16, 16, np.asarray([128.0, 16.0, 16.0]), None)
+    rc = call(L, t, outs, shape, [128.0, 16.0, 16.0], None)
     torch.cuda.synchronize(dev)
     assert rc == PHAFD_ERR_UNSUPPORTED
     assert all(bool((o == 7.0).all()) for o in outs)  # nothing written
