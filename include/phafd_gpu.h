@@ -57,6 +57,14 @@ extern "C" {
  * evaluated inside the step before the update (integrate.cpp:157-165).
  * Resident schedule; zeros before the first step after set-up. */
 #define PHAFD_FIELD_FT_PHI_STEP_START 7
+/* the gradient of the step's starting phi (read only): what the reference's
+ * gradphi arrays hold after a step, since FixGridConjugate::start_of_step
+ * computes them before the update (fixgrid_conjugate.cpp:62-114); the grid
+ * dump's gradphi_x/y/z attributes (dump.cpp:976-981).  Zeros before the
+ * first step, as the reference's arrays start. */
+#define PHAFD_FIELD_GRADX_STEP_START 8
+#define PHAFD_FIELD_GRADY_STEP_START 9
+#define PHAFD_FIELD_GRADZ_STEP_START 10
 
 /* ---- gridatom pair styles (input.cpp:107-116) ---- */
 #define PHAFD_GRIDATOM_NONE 0
@@ -269,6 +277,21 @@ int phafd_half_list_size(phafd_ctx* ctx, long long* n);
 int phafd_half_list(phafd_ctx* ctx, int* out3);
 int phafd_grid_list_size(phafd_ctx* ctx, long long* n);
 int phafd_grid_list(phafd_ctx* ctx, int* out3);
+
+/* ---- compute pair (compute_pair.cpp:43-85) ----
+ * The forces of one pair style on every bead as the reference's compute
+ * evaluates them after a step: bead copies where the step's pair stage left
+ * them, grad phi of the step's starting phi, phi after the step.  style is
+ * PHAFD_PAIR_LJ_CUT or PHAFD_PAIR_GRIDATOM (the context's gridatom style);
+ * out: 3 doubles per bead in phafd_atoms_create order.  The reference's
+ * compute also adds that style's mu deposit to its chempot array once more (a
+ * side effect its chempot dumps show); add_to_chempot != 0 does the same to
+ * the kept chempot (phafd_set_keep_chempot).  Needs phafd_set_pair_snapshot(ctx,
+ * 1) before the steps: each step then keeps the positions of its pair stage. */
+#define PHAFD_PAIR_LJ_CUT 1
+#define PHAFD_PAIR_GRIDATOM 2
+int phafd_set_pair_snapshot(phafd_ctx* ctx, int on);
+int phafd_compute_pair(phafd_ctx* ctx, int style, int add_to_chempot, double* out);
 
 /* ---- stage hooks for unit tests and partial pipelines ---- */
 int phafd_stage_gradient(phafd_ctx* ctx);          /* FixGridConjugate::start_of_step               */

@@ -15,6 +15,7 @@ FIELD = {"phi": 0, "chempot": 1, "gradx": 2, "grady": 3, "gradz": 4, "ft_phi": 5
 GRIDATOM = {"none": 0, "gaussian": 1, "LJish": 2, "LJish/linear": 3}
 NOISE = {"off": 0, "reference": 1, "philox": 2}
 ZGHOST = {"rank1": 0, "periodic": 1}
+PAIR = {"lj/cut": 1, "gridatom": 2}
 
 
 class SemiParams(C.Structure):
@@ -68,6 +69,7 @@ def lib():
                                           np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS"),
                                           np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS"),
                                           C.POINTER(C.c_int)],
+            "oracle_compute_pair": [vp, C.c_int, dp],
             "oracle_stage_gradient": [vp],
             "oracle_stage_borders_and_build": [vp],
             "oracle_stage_pairs": [vp],
@@ -298,6 +300,17 @@ class Oracle:
         return out
 
     # ---- stage hooks and inspection
+    def compute_pair(self, style, add_to_chempot=True):
+        """compute pair (compute_pair.cpp:43-85) after the last step: forces of
+        "lj/cut" or "gridatom" per owned bead, (n, 3); the style's chempot
+        deposit lands in chempot as in the reference (add_to_chempot is the
+        GPU library's switch for the same side effect; the oracle always
+        follows the reference)."""
+        n = self.atoms_get()[0].shape[0]
+        out = np.zeros((n, 3))
+        self._call("oracle_compute_pair", PAIR[style], out)
+        return out
+
     def stage_gradient(self):
         self._call("oracle_stage_gradient")
 

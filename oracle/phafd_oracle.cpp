@@ -1586,6 +1586,29 @@ int oracle_stage_pairs(oracle_ctx* c) {
   })
 }
 
+// ComputePair::end_of_step (compute_pair.cpp:43-85): the forces of one pair
+// style on the owned beads, from the gathered copies as the step's pair stage
+// left them, the gradient arrays of the step's start and phi after the step;
+// the style's chempot deposit goes into chempot as in the reference.  The
+// beads' own forces are kept.
+int oracle_compute_pair(oracle_ctx* c, int style, double* out3) {
+  GUARD(c, {
+    if (style == PHAFD_PAIR_LJ_CUT && !c->have_lj)
+      throw std::invalid_argument("Cannot compute pair style lj/cut, it hasn't been created!");
+    if (style == PHAFD_PAIR_GRIDATOM && c->ga_style == PHAFD_GRIDATOM_NONE)
+      throw std::invalid_argument("Cannot compute pair style gridatom, it hasn't been created!");
+    if (style != PHAFD_PAIR_LJ_CUT && style != PHAFD_PAIR_GRIDATOM) throw std::invalid_argument("unknown pair style");
+    const std::vector<double> keep(c->Fs);
+    std::fill(c->Fs.begin(), c->Fs.end(), 0.0);
+    if (style == PHAFD_PAIR_LJ_CUT) c->pair_lj();
+    else c->pair_gridatom();
+    c->reverse_comm();
+    for (int i = 0; i < c->nowned; ++i)
+      for (int d = 0; d < 3; ++d) out3[3 * i + d] = c->F(d, i);
+    c->Fs = keep;
+  })
+}
+
 // list export: half list as (tag_i, tag_j, shift code) and grid list as (node, tag, shift code)
 // shift code = (sx+1) + 3*(sy+1) + 9*(sz+1) with s in {-1,0,1} periodic images applied to j
 static std::vector<int> owner_map(const oracle_ctx* c) {

@@ -165,8 +165,11 @@ struct phafd_ctx {
   // buffer is reset inside the step (no real mu remains) and the resident z
   // pass stores only the Hermitian planes of mu's spectrum
   bool chempot_lost = false, muhat_stale = false, stepped = false;
+  // compute pair: each step keeps the positions its pair stage used
+  bool pair_snapshot = false, pair_snapped = false;
   void note_step() {
     stepped = true;
+    pair_snapped = pair_snapshot && n > 0;
     chempot_lost = have_conj && !keep_chempot;
     muhat_stale = have_conj && !keep_chempot && schedule == PHAFD_SCHEDULE_RESIDENT;
   }
@@ -224,6 +227,7 @@ struct phafd_ctx {
   DevBuf nbr, nnbr, gl, ngl;
   DevBuf dragc, sf_fix, sf_start, sf_len, sf_par;
   DevBuf gmask;  // one bit per 32-byte sector of a real field (beads with a grid coupling)
+  DevBuf bx_pair, bf_tmp;  // positions of the last pair stage (phafd_set_pair_snapshot); compute pair's forces
   // run_until_touching: a check after every step while set
   DevBuf touch;
   bool touch_on = false;
@@ -522,6 +526,27 @@ struct phafd_ctx {
     grad_partial = false;
   }
 
+  // The gradient of the step's starting phi into gx, gy, gz.  The resident
+  // schedule keeps the gradient of the current phi there: it is rebuilt from
+  // the spectrum the last step read, and true is returned (restore_gradient
+  // puts the current one back).  Other schedules compute it at the step's
+  // start, so the buffers hold it already.
+  bool load_step_start_gradient() {
+    if (schedule != PHAFD_SCHEDULE_RESIDENT || !have_conj) return false;
+    if (precision == PHAFD_FP64)
+      inverse_chain<double>(phat[1 - cur].as<cpx<double>>(), nullptr, nullptr, 0.0, 1.0 / (double)nreal, true, false);
+    else
+      inverse_chain<float>(phat[1 - cur].as<cpx<float>>(), nullptr, nullptr, 0.0f, (float)(1.0 / (double)nreal), true,
+                           false);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    return true;
+  }
+  void restore_gradient() {
+    grad_partial = true;
+    full_gradient();
+  }
+
   // the gradient node mask; marked stale until the next rebuild builds it
   void alloc_gmask() {
     if (ga_style == PHAFD_GRIDATOM_NONE || !gridset || n == 0) return;
@@ -693,6 +718,8 @@ struct phafd_ctx {
     mark(1);
     // pairs (computed once: the reference's second pass reproduces the first, integrate.cpp:140-146)
     PairArgs<T> pa = pair_args<T>();
+    if (n > 0 && pair_snapshot && bx_pair.p)
+      CK(cudaMemcpyAsync(bx_pair.p, bx.p, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     if (n > 0 && (have_lj || ga_style != PHAFD_GRIDATOM_NONE)) launch_pair<T>(ba, pa, st);
     mark(2);
     // Bead integration needs only F: off the profiling path it runs on a
@@ -1017,6 +1044,59 @@ int phafd_set_gradient_mask(phafd_ctx* c, int on) {
   API_END(c)
 }
 
+int phafd_set_pair_snapshot(phafd_ctx* c, int on) {
+  API_BEGIN(c)
+  CK(cudaSetDevice(c->device));
+  c->pair_snapshot = on != 0;
+  c->pair_snapped = false;
+  if (c->pair_snapshot && c->n > 0) c->bx_pair.alloc(3 * (size_t)c->n * sizeof(double));
+  c->invalidate_graph();
+  API_END(c)
+}
+
+// ComputePair::end_of_step (compute_pair.cpp:43-85) after the last step: the
+// style's pair loop over the gathered copies the step's pair stage formed
+// (the reference integrates only the owned beads, so the copies stay there),
+// with the gradient arrays of the step's start and phi after the update
+int phafd_compute_pair(phafd_ctx* c, int style, int add_to_chempot, double* out) {
+  API_BEGIN(c)
+  if (style != PHAFD_PAIR_LJ_CUT && style != PHAFD_PAIR_GRIDATOM) throw std::invalid_argument("unknown pair style");
+  if (style == PHAFD_PAIR_LJ_CUT && !c->have_lj)
+    throw std::invalid_argument("Cannot compute pair style lj/cut, it hasn't been created!");
+  if (style == PHAFD_PAIR_GRIDATOM && c->ga_style == PHAFD_GRIDATOM_NONE)
+    throw std::invalid_argument("Cannot compute pair style gridatom, it hasn't been created!");
+  if (c->n == 0) return PHAFD_OK;
+  if (!c->pair_snapped || !c->bx_pair.p)
+    throw std::runtime_error("compute pair needs steps taken after phafd_set_pair_snapshot(ctx, 1)");
+  CK(cudaSetDevice(c->device));
+  const bool loaded = style == PHAFD_PAIR_GRIDATOM && c->load_step_start_gradient();
+  const size_t bytes = 3 * (size_t)c->n * sizeof(double);
+  if (c->bf_tmp.bytes < bytes) c->bf_tmp.alloc(bytes);
+  c->fill_bead_args();
+  BeadArgs a = c->ba;
+  a.x = c->bx_pair.as<double>();
+  a.f = c->bf_tmp.as<double>();
+  const bool dep = add_to_chempot && style == PHAFD_PAIR_GRIDATOM && c->chempot_from_mu && c->mu.p;
+  if (c->precision == PHAFD_FP64) {
+    PairArgs<double> p = c->pair_args<double>();
+    p.lj = style == PHAFD_PAIR_LJ_CUT;
+    if (style != PHAFD_PAIR_GRIDATOM) p.ga_style = PHAFD_GRIDATOM_NONE;
+    p.dep = dep ? c->mu.as<double>() : nullptr;
+    launch_pair<double>(a, p, c->st);
+  } else {
+    PairArgs<float> p = c->pair_args<float>();
+    p.lj = style == PHAFD_PAIR_LJ_CUT;
+    if (style != PHAFD_PAIR_GRIDATOM) p.ga_style = PHAFD_GRIDATOM_NONE;
+    p.dep = dep ? c->mu.as<float>() : nullptr;
+    launch_pair<float>(a, p, c->st);
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, c->bf_tmp.p, bytes, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (loaded) c->restore_gradient();
+  API_END(c)
+}
+
 int phafd_set_keep_chempot(phafd_ctx* c, int keep) {
   API_BEGIN(c)
   c->keep_chempot = keep != 0;
@@ -1169,7 +1249,17 @@ int phafd_grid_get(phafd_ctx* c, int field, double* host) {
   const bool f64 = c->precision == PHAFD_FP64;
   if ((field == PHAFD_FIELD_CHEMPOT && c->chempot_lost) || (field == PHAFD_FIELD_FT_CHEMPOT && c->muhat_stale))
     throw std::runtime_error("chempot after a run is kept only when phafd_set_keep_chempot(ctx, 1) precedes the steps");
-  if (field == PHAFD_FIELD_FT_PHI_STEP_START) {
+  if (field >= PHAFD_FIELD_GRADX_STEP_START && field <= PHAFD_FIELD_GRADZ_STEP_START) {
+    if (!c->stepped) {
+      std::fill(host, host + c->nreal, 0.0);
+    } else {
+      const bool loaded = c->load_step_start_gradient();
+      const DevBuf& b = field == PHAFD_FIELD_GRADX_STEP_START ? c->gx : field == PHAFD_FIELD_GRADY_STEP_START ? c->gy : c->gz;
+      if (f64) copy_real_to_host<double>(c, b, host);
+      else copy_real_to_host<float>(c, b, host);
+      if (loaded) c->restore_gradient();
+    }
+  } else if (field == PHAFD_FIELD_FT_PHI_STEP_START) {
     if (c->schedule != PHAFD_SCHEDULE_RESIDENT || !c->have_conj)
       throw std::invalid_argument("the step-start spectrum is kept by the resident schedule");
     if (!c->stepped) {
@@ -1400,6 +1490,9 @@ int phafd_setup(phafd_ctx* c) {
             throw std::runtime_error("Adjacent atom displacements do not match the FixAtomSemiFlexible bondlength specified.");
         }
   }
+  if (c->pair_snapshot && c->n > 0 && c->bx_pair.bytes < 3 * (size_t)c->n * sizeof(double))
+    c->bx_pair.alloc(3 * (size_t)c->n * sizeof(double));
+  c->pair_snapped = false;
   if (c->n > 0) {
     if (!c->neigh_set) {  // no lists: bins only serve Domain::pbc on every step
       c->cutneigh = std::min(c->period[0], std::min(c->period[1], c->period[2])) / 3.0;

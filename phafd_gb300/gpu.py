@@ -13,7 +13,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libphafd_gpu.so")
 
 FIELD = {"phi": 0, "chempot": 1, "gradx": 2, "grady": 3, "gradz": 4, "ft_phi": 5, "ft_chempot": 6,
-         "ft_phi_step_start": 7}
+         "ft_phi_step_start": 7, "gradx_step_start": 8, "grady_step_start": 9, "gradz_step_start": 10}
+PAIR = {"lj/cut": 1, "gridatom": 2}
 GRIDATOM = {"none": 0, "gaussian": 1, "LJish": 2, "LJish/linear": 3}
 NOISE = {"off": 0, "reference": 1, "philox": 2}
 ZGHOST = {"rank1": 0, "periodic": 1}
@@ -27,7 +28,7 @@ EXPORTS = [
     "phafd_domain", "phafd_grid_style", "phafd_grid_populate_constant", "phafd_grid_populate_flat_interface",
     "phafd_grid_populate_sphere", "phafd_grid_set", "phafd_grid_get",
     "phafd_set_zghost", "phafd_set_schedule", "phafd_set_keep_chempot", "phafd_set_plane_fusion",
-    "phafd_set_gradient_mask", "phafd_set_fp32_centering",
+    "phafd_set_gradient_mask", "phafd_set_fp32_centering", "phafd_set_pair_snapshot", "phafd_compute_pair",
     "phafd_atoms_create", "phafd_atoms_get", "phafd_atoms_set_images",
     "phafd_pair_gridatom", "phafd_pair_gridatom_coeff", "phafd_pair_lj_cut",
     "phafd_neighbor",
@@ -88,6 +89,8 @@ def load(path=None):
         "phafd_set_plane_fusion": [vp, C.c_int],
         "phafd_set_gradient_mask": [vp, C.c_int],
         "phafd_set_fp32_centering": [vp, C.c_int],
+        "phafd_set_pair_snapshot": [vp, C.c_int],
+        "phafd_compute_pair": [vp, C.c_int, C.c_int, dp],
         "phafd_domain": [vp, dp, dp],
         "phafd_grid_style": [vp, C.c_int, C.c_int, C.c_int],
         "phafd_grid_populate_constant": [vp, C.c_double, C.c_double, C.c_int],
@@ -198,6 +201,17 @@ class PhafdGPU:
     def set_gradient_mask(self, on=True):
         """Store grad phi only near the beads during steps (off by default)."""
         self._call("phafd_set_gradient_mask", int(on))
+
+    def set_pair_snapshot(self, on=True):
+        """Keep each step's pair-stage positions (needed by compute_pair)."""
+        self._call("phafd_set_pair_snapshot", int(on))
+
+    def compute_pair(self, style, add_to_chempot=True):
+        """compute pair after the last step: forces of "lj/cut" or "gridatom"
+        per bead, (n, 3) (compute_pair.cpp:43-85)."""
+        out = np.zeros((max(self.n, 1), 3))
+        self._call("phafd_compute_pair", PAIR[style], int(add_to_chempot), out)
+        return out[:self.n]
 
     def set_fp32_centering(self, fh=True, fft=True):
         """FP32 stages taken relative to the mean of phi (both on by default)."""

@@ -14,9 +14,10 @@
 //               [device N] [plane on|off]
 // and one output command for raw fields:
 //   write_field phi|chempot|gradx|grady|gradz FILE   (raw float64, [z][y][x])
-// Dumps (atom, lammpsatom, grid) are written as the reference writes them
-// (vtk_dump.hpp); per-grid attributes are phi, chempot and c_NAME of
-// compute grid/cluster.
+// Dumps (atom, lammpsatom, grid, ftgrid) are written as the reference writes
+// them (vtk_dump.hpp); per-grid attributes are phi, chempot, gradphi_x/y/z
+// and c_NAME of compute grid/cluster, per-atom attributes include c_NAME of
+// compute pair, per-ftgrid ones c_NAME of compute complex.
 // "-dry-run" parses and checks the script without touching a GPU.
 #include <algorithm>
 #include <chrono>
@@ -149,6 +150,8 @@ class Interpreter {
     int field, quant;
   };
   std::map<std::string, Complex> complexes_;  // compute complex NAME ft_phi|ft_chempot real|imag|modulus|norm
+  std::map<std::string, int> pair_computes_;  // compute pair NAME PAIRSTYLE -> PHAFD_PAIR_*
+  std::set<std::string> pair_names_;          // pair styles created (their reference names)
   std::map<std::string, std::vector<double>> compute_cache_;  // each compute's array as last computed
   std::set<std::string> compute_names_;
 
@@ -385,7 +388,9 @@ class Interpreter {
       last_gridatom_ = style == "gridatom/gaussian" ? PHAFD_GRIDATOM_GAUSSIAN
                      : style == "gridatom/LJish" ? PHAFD_GRIDATOM_LJISH : PHAFD_GRIDATOM_LJISH_LINEAR;
       if (!dry_) check(phafd_pair_gridatom(ctx(), last_gridatom_, num(w.at(1))));
+      pair_names_.insert(style);
     } else if (style == "lj/cut") {
+      pair_names_.insert(style);
       last_gridatom_ = PHAFD_GRIDATOM_NONE;
       if (!dry_) check(phafd_pair_lj_cut(ctx(), num(w.at(1)), num(w.at(2)), num(w.at(3))));
     } else {
@@ -524,9 +529,9 @@ class Interpreter {
     }
   }
 
-  // Compute::init + ComputeGridClusters::init (compute.cpp:13-27,
-  // compute_grid_clusters.cpp:23-64); other computes only feed dumps of the
-  // reference and are not built here
+  // Compute::init + ComputeGridClusters::init / ComputeComplex::init /
+  // ComputePair::init (compute.cpp:13-27, compute_grid_clusters.cpp:23-64,
+  // compute_complex.cpp:14-41, compute_pair.cpp:15-35)
   void command_compute(const Words& w) {  // compute STYLE NAME args (input.cpp:234-254)
     std::string style = w.at(0);
     if (style.size() > 4 && style.compare(style.size() - 4, 4, "/gpu") == 0) style.resize(style.size() - 4);
@@ -552,9 +557,12 @@ class Interpreter {
       if (quant < 0) throw std::runtime_error("Invalid argument in compute complex.");
       if (field == PHAFD_FIELD_FT_CHEMPOT && !dry_) check(phafd_set_keep_chempot(ctx(), 1));
       complexes_[name] = Complex{field, quant};
-    } else {
-      std::cerr << "WARNING: compute " << style << " " << name << " is not built by phafd_gpu and is ignored."
-                << std::endl;
+    } else {  // compute pair NAME PAIRSTYLE (compute_pair.cpp:15-35)
+      const std::string pairname = gpu_style(w.at(2));
+      if (!pair_names_.count(pairname))
+        throw std::invalid_argument("Cannot compute pair style " + pairname + ", it hasn't been created!");
+      pair_computes_[name] = pairname == "lj/cut" ? PHAFD_PAIR_LJ_CUT : PHAFD_PAIR_GRIDATOM;
+      if (!dry_) check(phafd_set_pair_snapshot(ctx(), 1));  // each step keeps its pair-stage positions
     }
   }
 
@@ -585,10 +593,9 @@ class Interpreter {
       for (auto& a : d.attributes) {
         if (a.rfind("c_", 0) == 0) {
           compute_attr(a, false);
-        } else if (a.rfind("gradphi_", 0) == 0) {
-          // the reference's arrays hold the gradient of the step's starting
-          // phi; the resident state holds the gradient of the current phi
-          throw std::runtime_error("gradphi attributes are not written by phafd_gpu (use write_field)");
+        } else if (a == "gradphi_x" || a == "gradphi_y" || a == "gradphi_z") {
+          // the gradient of the step's starting phi, which the reference's
+          // arrays hold at a dump (dump.cpp:976-981)
         } else if (a == "chempot") {
           if (!dry_) check(phafd_set_keep_chempot(ctx(), 1));
         } else if (a != "phi") {
@@ -597,6 +604,14 @@ class Interpreter {
       }
     } else {
       phafd_dump::check_atoms(d);
+      for (auto& a : d.attributes) {  // per-atom computes (dump.cpp:930-950)
+        if (a.rfind("c_", 0) != 0) continue;
+        const std::string cid = a.substr(2);
+        if (!compute_names_.count(cid))
+          throw std::runtime_error("Cannot write dump, compute ID " + cid + std::string("doesn't exist."));
+        if (!pair_computes_.count(cid))
+          throw std::runtime_error("Cannot write dump, compute ID " + cid + std::string("is not a per_atom quantity."));
+      }
     }
     dumps_.push_back(d);
   }
@@ -606,10 +621,15 @@ class Interpreter {
   // it, zeros before any step (integrate.cpp:62-64)
   const std::vector<double>& compute_array(const std::string& cid, bool start_of_run) {
     std::vector<double>& a = compute_cache_[cid];
-    const size_t n = complexes_.count(cid) ? ncplx() : (size_t)grid_n_[0] * grid_n_[1] * grid_n_[2];
+    const size_t n = complexes_.count(cid) ? ncplx()
+                   : pair_computes_.count(cid) ? 3 * (size_t)natoms_ : (size_t)grid_n_[0] * grid_n_[1] * grid_n_[2];
     if (a.size() != n) a.assign(n, 0.0);
     if (start_of_run) return a;
-    if (complexes_.count(cid)) {
+    if (pair_computes_.count(cid)) {
+      // the style's forces after the step; like the reference's compute it
+      // also adds the style's deposit to chempot (compute_pair.cpp:52-68)
+      if (natoms_ > 0) check(phafd_compute_pair(ctx(), pair_computes_.at(cid), 1, a.data()));
+    } else if (complexes_.count(cid)) {
       const Complex& c = complexes_.at(cid);
       check(phafd_compute_complex(ctx(), c.field, c.quant, a.data()));
     } else {
@@ -632,6 +652,12 @@ class Interpreter {
     std::vector<int> img;
     std::map<std::string, std::vector<double>> fields;
     std::set<std::string> done;  // computes evaluated at this step
+    // compute pair runs after every step of the reference, before its dumps
+    // read chempot (integrate.cpp:172-183): evaluate it first
+    for (auto& pc : pair_computes_) {
+      compute_array(pc.first, start_of_run);
+      done.insert(pc.first);
+    }
     for (auto& d : dumps_) {
       if (!force_all && timestep_ % d.every != 0) continue;
       phafd_dump::Atoms a;
@@ -658,7 +684,10 @@ class Interpreter {
           }
           if (!fields.count(att)) {
             std::vector<double> buf(nr);
-            check(phafd_grid_get(ctx(), att == "phi" ? PHAFD_FIELD_PHI : PHAFD_FIELD_CHEMPOT, buf.data()));
+            const int field = att == "phi" ? PHAFD_FIELD_PHI : att == "chempot" ? PHAFD_FIELD_CHEMPOT
+                            : att == "gradphi_x" ? PHAFD_FIELD_GRADX_STEP_START
+                            : att == "gradphi_y" ? PHAFD_FIELD_GRADY_STEP_START : PHAFD_FIELD_GRADZ_STEP_START;
+            check(phafd_grid_get(ctx(), field, buf.data()));
             fields[att] = std::move(buf);
           }
           g.fields[att] = fields[att].data();
@@ -671,6 +700,8 @@ class Interpreter {
         a.n = natoms_;
         a.x = x.data(); a.ux = ux.data(); a.f = f.data(); a.images = img.data();
         a.tags = tags_.data(); a.mols = mols_.data(); a.types = types_.data();
+        for (auto& att : d.attributes)
+          if (att.rfind("c_", 0) == 0) a.computes[att] = compute_cache_[att.substr(2)].data();
         for (int k = 0; k < 3; ++k) {
           a.boxlo[k] = boxlo_[k];
           a.boxhi[k] = boxlo_[k] + period_[k];

@@ -78,6 +78,9 @@ struct Atoms {
   const double *x = nullptr, *ux = nullptr, *f = nullptr;
   const int *images = nullptr, *tags = nullptr, *mols = nullptr, *types = nullptr;
   double boxlo[3] = {0, 0, 0}, boxhi[3] = {0, 0, 0};
+  // per-atom compute arrays by attribute name (c_NAME): 3 components per
+  // bead (compute pair, compute_pair.cpp:9-10)
+  std::map<std::string, const double*> computes;
 };
 
 // real fields [z][y][x] of the one domain, by attribute name (c_NAME for per-grid computes)
@@ -161,6 +164,7 @@ inline void atom_attribute(std::ostream& f, const std::string& w, const Atoms& a
   else if (w == "molID") ascii1(f, w, a.mols, a.n, pv);
   else if (w == "type") ascii1(f, w, a.types, a.n, pv);
   else if (w == "label") ascii1(f, w, nullptr, a.n, pv);  // every bead of the one domain is OWNED (0)
+  else if (a.computes.count(w)) ascii3(f, w, a.computes.at(w), a.n, pv);  // write_ascii_data, 3 components
   else throw std::runtime_error("Invalid per atom quantity in dump file.");
 }
 
@@ -172,7 +176,8 @@ inline void check_atoms(const Spec& s) {
   bool hasx = false;
   for (auto& w : s.attributes) {
     hasx = hasx || w == "x";
-    if (w != "x" && w != "F" && w != "ux" && w != "ix" && w != "ID" && w != "molID" && w != "type" && w != "label")
+    if (w != "x" && w != "F" && w != "ux" && w != "ix" && w != "ID" && w != "molID" && w != "type" && w != "label" &&
+        w.rfind("c_", 0) != 0)
       throw std::runtime_error("Invalid per atom quantity in dump file.");
   }
   if (s.type == "atom" && !hasx) throw std::runtime_error("Atom dump must contain positions.");
@@ -232,6 +237,7 @@ inline void write_lammps(const Spec& s, long long timestep, const Atoms& a) {
     if (w == "x") f << "x y z ";
     else if (w == "F") f << "Fx Fy Fz ";
     else if (w == "ux") f << "ux uy uz ";
+    else if (a.computes.count(w)) f << w << "_0 " << w << "_1 " << w << "_2 ";  // one column per component
     else f << w << " ";
   }
   f << std::endl;
@@ -245,7 +251,10 @@ inline void write_lammps(const Spec& s, long long timestep, const Atoms& a) {
       else if (w == "molID") f << a.mols[p] << " ";
       else if (w == "type") f << a.types[p] << " ";
       else if (w == "label") f << 0 << " ";
-      else throw std::runtime_error("Invalid per atom quantity in dump file.");
+      else if (a.computes.count(w)) {
+        const double* c = a.computes.at(w);
+        f << c[3 * p] << " " << c[3 * p + 1] << " " << c[3 * p + 2] << " ";
+      } else throw std::runtime_error("Invalid per atom quantity in dump file.");
     }
     f << std::endl;
   }

@@ -9,12 +9,16 @@ the final states of the reference's sources in tests/golden/ref_*.npz
   forces within 1e-8 relative; image flags, neighbor builds, reflection
   counts and both lists (as sets) equal;
   resident schedule (which carries the spectrum across steps and keeps the
-  gradient of the current phi): the same except the gradient fields.
+  gradient of the current phi): the same except the gradient fields;
+  both: the step-start gradient fields (what the reference's gradphi dump
+  attributes hold) within 1e-10, and compute pair's per-bead forces and the
+  chempot it leaves within 1e-10.
 """
 import pytest
 
 from tests import ref_scenarios as RS
-from tests.test_ref_pinned import check_state, keeps_plain_chempot, replay
+from tests.helpers import rel_err
+from tests.test_ref_pinned import check_state, replay, replay_computes
 
 pytestmark = pytest.mark.gpu
 
@@ -25,6 +29,13 @@ def test_gpu_matches_the_reference(gpu_lib, name, schedule):
     from phafd_gb300.gpu import PhafdGPU
     g = PhafdGPU(precision=64, schedule=schedule)
     g.set_keep_chempot(True)
+    with_compute = RS.SCENARIOS[name]["compute_pair"]
+    if with_compute:
+        g.set_pair_snapshot(True)
     fx = replay(g, name)
-    check_state(g, fx, 1e-10, 1e-10, grads=schedule == "reference", chempot=keeps_plain_chempot(name))
+    check_state(g, fx, 1e-10, 1e-10, grads=schedule == "reference", chempot=not with_compute)
+    # the gradient the reference's arrays hold after a step, in either schedule
+    for f in ("gradx", "grady", "gradz"):
+        assert rel_err(g.grid_get(f + "_step_start"), fx[f]) < 1e-10, f
+    replay_computes(g, name, fx, 1e-10)
     g.close()

@@ -61,18 +61,25 @@ def check_state(d, fx, field_tol, bead_tol, grads=True, chempot=True):
         assert canon_grid(d.grid_list()) == canon_grid(fx["grid_list"])
 
 
-def keeps_plain_chempot(name):
-    """compute pair re-runs its pair style after the step (compute_pair.cpp:
-    52-68), which adds that style's deposit to the chempot array once more;
-    the step's own mu is compared where no compute pair runs."""
-    return not RS.SCENARIOS[name]["compute_pair"]
+def replay_computes(d, name, fx, tol):
+    """compute pair after the last step (compute_pair.cpp:43-85): the style's
+    per-bead forces, and the chempot array it leaves (the reference's compute
+    re-runs the pair, adding that style's deposit to chempot once more)."""
+    if not RS.SCENARIOS[name]["compute_pair"]:
+        return
+    got = d.compute_pair("gridatom")
+    want = fx["compute_cpair"].reshape(-1, 3)
+    assert rel_err(got, want) < tol
+    assert rel_err(d.grid_get("chempot"), fx["chempot"]) < tol
 
 
 @pytest.mark.parametrize("name", sorted(RS.SCENARIOS))
 def test_oracle_matches_the_reference(name):
     o = Oracle()
     fx = replay(o, name)
-    check_state(o, fx, 1e-12, 1e-12, chempot=keeps_plain_chempot(name))
+    with_compute = RS.SCENARIOS[name]["compute_pair"]
+    check_state(o, fx, 1e-12, 1e-12, chempot=not with_compute)
+    replay_computes(o, name, fx, 1e-12)
 
 
 def test_scenarios_exercise_what_they_claim():
