@@ -43,6 +43,8 @@ def parse():
     p.add_argument("--workload", default=WORKLOAD)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain part of the default line")
+    p.add_argument("--no-fp64", action="store_true", help="skip the FP64 throughput figure")
     p.add_argument("--profile-steps", type=int, default=5)
     p.add_argument("--traj", type=int, default=48, help="training trajectories of the learned workloads")
     p.add_argument("--epochs", type=int, default=6, help="training epochs of the learned workloads")
@@ -72,7 +74,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -108,6 +110,24 @@ class ClockSampler:
                 continue
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu; /proc/cpuinfo as fallback)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
 def measured_peak():
@@ -264,21 +284,28 @@ def run_gpu(args):
     g = PhafdGPU(precision=32, device=local, schedule="resident")
     W.apply(g, cfg, chains=chains)
     g.setup()
+    # clocks are sampled from the warm-up through the timed region and a
+    # continuation of the same steps of at least one second
+    sampler = ClockSampler(local)
+    sampler.start()
     g.run(max(args.warmup, 3))
 
     # stage profile (eager steps with events between stages; not the timed region)
     prof = g.profile_stages(args.profile_steps)
     g.run(2)
 
-    sampler = ClockSampler(local)
     barrier()
     g.synchronize()
-    sampler.start()
     ms = g.run_timed(args.steps)
     g.synchronize()
-    clocks = sampler.stop()
     barrier()
     ms_max = ranks_max(ms)
+    t_soak = time.perf_counter()
+    while time.perf_counter() - t_soak < 1.0:
+        g.run(200)
+        g.synchronize()
+    clocks = sampler.stop()
+    clocks["window"] = "warm-up, timed region and 1 s more of the same steps (50 ms sampling)"
     counters = g.counters()
 
     value = job_throughput(world, args.steps, ms_max)
@@ -292,6 +319,8 @@ def run_gpu(args):
     bstep = W.algorithmic_bytes_per_step(cfg, s)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of this stage in one ncu capture "
+                                  "(profiles/ncu_dram_bytes_256cube.txt), not measured in this run",
                 "algorithmic_bytes_per_launch": sb[dom], "launch_ms": prof[dom]}
     step_roofline = {"bytes_per_step": bstep, "achieved": bstep / (ms_max / args.steps / 1000.0) / 1e9,
                      "peak": peak, "unit": "GB/s"}
@@ -312,70 +341,134 @@ def run_gpu(args):
         "gpu_launches": int(counters.get("kernels_per_step", 0)) * args.steps if counters.get("kernels_per_step") else None,
         "neighbor_calls": counters["neighbor_calls"],
     }
+    phi_host = np.ascontiguousarray(g.grid_get("phi"))
+    g.close()
 
-    # end to end through the public C ABI with host buffers: upload the
-    # state from host memory, then per step one phafd_run(ctx, 1) and a read
-    # of the step's bead result (x, ux, F, images); finally read phi back
+    # the same workload through the FP64 path (the precision the reference computes in)
+    if not args.no_fp64:
+        g64 = PhafdGPU(precision=64, device=local, schedule="resident")
+        W.apply(g64, cfg, chains=chains)
+        g64.setup()
+        g64.run(max(args.warmup, 3))
+        k64 = max(20, min(args.steps, 200))
+        barrier()
+        ms64 = ranks_max(g64.run_timed(k64))
+        line["fp64"] = {"value": job_throughput(world, k64, ms64), "unit": "steps/s", "steps": k64,
+                        "ms_per_step": ms64 / k64,
+                        "step_roofline_frac": W.algorithmic_bytes_per_step(cfg, 8) / (ms64 / k64 / 1000.0) / 1e9 / peak}
+        g64.close()
+
+    # end to end through the public C ABI with host buffers: set-up (context,
+    # upload of the state from host memory, lists, graph) timed apart from the
+    # steady steps, each one phafd_run(ctx, 1) followed by a read of the
+    # step's bead result (x, ux, F, image flags) into host memory
     if not args.no_e2e:
-        k = max(10, min(args.steps, 100))
-        phi_host = np.ascontiguousarray(g.grid_get("phi"))
+        k = max(20, min(args.steps, 200))
         xs = chains[0]
-        e = PhafdGPU(precision=32, device=local, schedule="resident")
+        nb = W.nbeads(cfg)
         t0 = time.perf_counter()
+        e = PhafdGPU(precision=32, device=local, schedule="resident")
         W.apply(e, cfg, chains=chains, phi=phi_host)  # the state from host arrays: phi, then the beads
         e.setup()
+        e.run(1)
+        e.atoms_get()
+        t1 = time.perf_counter()
         for _ in range(k):
             e.run(1)
             e.atoms_get()
         out = e.grid_get("phi")
-        t1 = time.perf_counter()
-        nb = W.nbeads(cfg)
-        h2d = (phi_host.size * 4 + xs.size * 8 + nb * 12) / k
-        d2h = nb * (3 * 8 * 3 + 4) + out.size * 4 / k
-        e2e_v = world * k / ranks_max(t1 - t0)
-        line["e2e"] = {"value": e2e_v, "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
-                       "d2h_bytes_per_step": int(d2h),
-                       "note": "state uploaded once from host arrays, %d steps each followed by a bead read, phi read at the end; includes set-up" % k}
+        t2 = time.perf_counter()
+        steady = world * k / ranks_max(t2 - t1)
+        line["e2e"] = {"value": steady, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                       "d2h_bytes_per_step": int(nb * (3 * 8 * 3 + 4) + out.size * 4 / k),
+                       "setup_s": t1 - t0, "setup_h2d_bytes": int(phi_host.size * 4 + xs.size * 8 + nb * 12),
+                       "value_with_setup": world * (k + 1) / ranks_max(t2 - t0), "steps": k,
+                       "note": "steady state: %d steps, each phafd_run(ctx, 1) then the beads' x, ux, F and image "
+                               "flags read into host memory, phi read after the last; set-up (context, state "
+                               "uploaded from host arrays, first step with list build and graph capture) timed "
+                               "apart as setup_s" % k}
         e.close()
 
-    # FP32 production path against the FP64 path from the same state and
-    # the same Philox noise: relative S(k) error (max over shells) after 50 steps
+    # FP32 production path against the FP64 path and the FP64 oracle from the
+    # same state and the same Philox noise, 50 steps: S(k) error, with the FP32
+    # stages taken relative to the mean of phi switched off one by one
     if rank == 0 and world == 1 and not args.no_e2e:
         line["fp32_vs_fp64"] = precision_check(cfg, chains, local, 50)
+
+    if rank == 0 and world == 1 and not args.no_learned and args.workload == WORKLOAD:
+        try:
+            line["learned"] = learned_vs_plain(args, 256)
+        except Exception as ex:  # the step numbers above stand without it
+            line["learned"] = {"error": str(ex)[:300]}
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, dt, threads = cpu_baseline_oracle(cfg, chains, 3)
         line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                                "cpu_model": cpu_model(), "mpi_ranks": 1,
                                 "sample": "3 steps of %s (FP64 oracle restatement; grid loops on %d threads, bead "
                                           "loops on one) after its set-up" % (args.workload, threads)}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    g.close()
     if torch_dist:
         torch_dist.destroy_process_group()
     return 0
+
+
+def sk_shells(phi):
+    """shell-averaged S(k) of a real cubic field (k = 0 left out)"""
+    from tests.helpers import shell_sk
+    return shell_sk(phi)
 
 
 def precision_check(cfg, chains, device, steps):
     import numpy as np
     from phafd_gb300 import workloads as W
     from phafd_gb300.gpu import PhafdGPU
-    out = {}
-    res = {}
-    for prec in (32, 64):
+
+    def sk_err(a, b):
+        m = b[1:] > 0
+        return float(np.max(np.abs(a[1:][m] - b[1:][m]) / b[1:][m]))
+
+    def run(prec, nsteps, fh=True, fft=True):
         g = PhafdGPU(precision=prec, device=device, schedule="resident")
         W.apply(g, cfg, chains=chains)
+        g.set_fp32_centering(fh=fh, fft=fft)
         g.setup()
-        g.run(steps)
-        res[prec] = (g.structure_factor(cfg["n"] // 2)[0], g.grid_get("phi"))
+        g.run(nsteps)
+        out = g.structure_factor(cfg["n"] // 2)[0], g.grid_get("phi")
         g.close()
-    s32, p32 = res[32]
-    s64, p64 = res[64]
-    m = s64[1:] > 0
-    out["steps"] = steps
-    out["sk_rel_err_max"] = float(np.max(np.abs(s32[1:][m] - s64[1:][m]) / s64[1:][m]))
+        return out
+
+    out = {"steps": steps}
+    s64, p64 = run(64, steps)
+    s32, p32 = run(32, steps)
+    out["sk_rel_err_max"] = sk_err(s32, s64)
     out["phi_max_abs_err"] = float(np.max(np.abs(p32 - p64)))
     out["mass_err"] = float(abs(p32.mean() - p64.mean()))
+    # the FP32 error budget: S(k) error with the stages relative to the mean
+    # of phi switched off one at a time, and the representation floor (the
+    # FP32 rounding of the initial field, no step)
+    budget = {"fh_and_transforms_centered": out["sk_rel_err_max"]}
+    for name, fh, fft in (("transforms_centered_only", False, True), ("fh_centered_only", True, False),
+                          ("none_centered", False, False)):
+        budget[name] = sk_err(run(32, steps, fh, fft)[0], s64)
+    budget["initial_field_rounding"] = sk_err(run(32, 0)[0], run(64, 0)[0])
+    out["budget"] = budget
+    # the FP32 path against the FP64 oracle itself (the reference's CPU algorithm)
+    try:
+        from oracle import oracle as OR
+        from oracle.oracle import Oracle
+        OR.set_threads(OR.host_threads())
+        o = Oracle()
+        W.apply(o, cfg, chains=chains)
+        o.setup()
+        o.run(steps)
+        po = o.grid_get("phi")
+        del o
+        out["sk_rel_err_vs_oracle"] = sk_err(sk_shells(p32), sk_shells(po))
+        out["fp64_gpu_phi_rel_err_vs_oracle"] = float(np.abs(p64 - po).max() / np.abs(po).max())
+    except Exception as ex:
+        out["oracle_error"] = str(ex)[:200]
     # bead forces of one pair evaluation at identical positions (FP32 pair
     # arithmetic with compensated sums against FP64)
     try:
@@ -425,19 +518,16 @@ def run_ensemble(args):
     return 0
 
 
-def run_learned(args):
+def learned_vs_plain(args, n_eval):
     """Learned propagator: train the spectral neural operator on trajectories
     of the plain FP32 integrator at 128^3 (4k-16k beads, chi in [2.5, 3.5],
-    phi0 in [0.35, 0.5]), then on a held-out seed at 128^3 (learned128) or
-    256^3 (learned256) time the plain path and the surrogate path (macro step
-    of K = 20 substeps, judged every 100 substeps) over the same substeps and
-    report their S(k) errors against the plain path."""
+    phi0 in [0.35, 0.5]), then on a held-out seed at n_eval^3 time the plain
+    path and the surrogate path (macro step of K = 20 substeps, judged every
+    100 substeps) over the same substeps and report their S(k) errors against
+    the plain path.  Returns the measurements as a dict."""
     import numpy as np
     import torch
-    from phafd_gb300 import build as B
-    B.build()
     from phafd_gb300 import surrogate as S
-    n_eval = 256 if args.workload == "learned256" else 128
     rng = np.random.default_rng(2024)
     specs = [(128, int(rng.integers(4000, 16001)), rng.uniform(2.5, 3.5), rng.uniform(0.35, 0.5), 5000 + i)
              for i in range(args.traj)]
@@ -510,12 +600,9 @@ def run_learned(args):
     infer_ms = ev0.elapsed_time(ev1) / 5
     net.close()
     v_sur, v_plain = nsub / t_sur, nsub / t_plain
-    line = {
-        "metric": "steps/s, learned macro step vs plain FP32 step", "value": v_sur, "unit": "steps/s",
-        "n_gpus": 1, "steps": nsub, "warmup": max(args.warmup, 3), "ms_per_step": 1000 * t_sur / nsub,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network, f32 field",
-        "data": "synthetic",
-        "config": {"workload": args.workload, "grid": [n_eval] * 3, "beads": W_nbeads(cfg), "K": S.K_SUB,
+    return {
+        "learned_steps_per_s": v_sur, "steps": nsub, "ms_per_step": 1000 * t_sur / nsub,
+        "config": {"grid": [n_eval] * 3, "beads": W_nbeads(cfg), "K": S.K_SUB,
                    "judge_every": 100, "judge_sk_bound": SK_BOUND, "judge_mass_bound": MASS_BOUND,
                    "train_grid": [128] * 3, "train_trajectories": args.traj,
                    "train_samples": 2 * args.traj, "epochs": args.epochs,
@@ -528,6 +615,21 @@ def run_learned(args):
         "judge": judged, "train_loss": hist, "seconds": {"generate": t_gen, "train": t_train},
         "timed_phase_seconds": phase_s, "network_infer_ms": infer_ms,
     }
+
+
+def run_learned(args):
+    """The learned-vs-plain measurement as a line of its own (learned128 /
+    learned256)."""
+    from phafd_gb300 import build as B
+    B.build()
+    n_eval = 256 if args.workload == "learned256" else 128
+    r = learned_vs_plain(args, n_eval)
+    cfg = dict(r.pop("config"), workload=args.workload)
+    line = {"metric": "steps/s, learned macro step vs plain FP32 step", "value": r["learned_steps_per_s"],
+            "unit": "steps/s", "n_gpus": 1, "steps": r["steps"], "warmup": max(args.warmup, 3),
+            "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 network, f32 field", "data": "synthetic", "config": cfg}
+    line.update(r)
     print(json.dumps(line), flush=True)
     return 0
 

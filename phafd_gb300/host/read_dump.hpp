@@ -57,8 +57,46 @@ inline bool has(const std::vector<std::string>& v, const std::string& w) {
   return false;
 }
 
-// ReadDump::process_grid_attributes (read_dump.cpp:90-185): the requested
-// arrays by name, [z][y][x]
+// The arrays of a grid dump (.vti, raw appended data): the XML header is
+// parsed once into a table of DataArray name -> offset into the appended
+// block; each requested array is then read at its offset, as a 4-byte length
+// followed by Nx*Ny*Nz doubles [z][y][x].  The checks and their messages are
+// those of ReadDump::process_grid_attributes (read_dump.cpp:90-185).
+struct VtiTable {
+  std::map<std::string, uint64_t> offset;  // name -> offset after the '_' marker
+  std::streampos data = 0;                 // file position of the first appended byte
+};
+
+// the attribute value NAME="..." of an XML element line, if present
+inline bool xml_attr(const std::string& line, const std::string& name, std::string& value) {
+  const std::string key = name + "=\"";
+  const size_t at = line.find(key);
+  if (at == std::string::npos) return false;
+  const size_t start = at + key.size();
+  const size_t end = line.find('"', start);
+  if (end == std::string::npos) return false;
+  value = line.substr(start, end - start);
+  return true;
+}
+
+inline VtiTable vti_table(std::ifstream& f) {
+  VtiTable t;
+  std::string line;
+  while (std::getline(f, line)) {
+    if (line.rfind("<AppendedData", 0) == 0) {
+      char marker = 0;
+      f.read(&marker, 1);  // the raw block starts after '_'
+      t.data = f.tellg();
+      return t;
+    }
+    std::string name, off;
+    if (line.rfind("<DataArray ", 0) == 0 && xml_attr(line, "Name", name) && xml_attr(line, "offset", off))
+      t.offset[name] = std::stoull(off);
+  }
+  t.data = -1;
+  return t;
+}
+
 inline std::map<std::string, std::vector<double>> read_grid(const ReadSpec& s, int nx, int ny, int nz) {
   std::ifstream f(s.filename, std::ios::in | std::ios::binary);
   if (!f) {
@@ -66,46 +104,24 @@ inline std::map<std::string, std::vector<double>> read_grid(const ReadSpec& s, i
     throw std::runtime_error("file not found.");
   }
   if (!has(s.attributes, "phi")) throw std::runtime_error("Read dump needs attribute phi.");
-  const std::string expstart = "<DataArray Name=";
-  std::vector<std::string> found;
-  size_t ignored = 0;
-  std::string line;
-  while (std::getline(f, line)) {
-    if (line == "<AppendedData encoding=\"raw\">") break;
-    bool hit = false;
-    for (auto& w : s.attributes) {
-      const std::string expected = "<DataArray Name=\"" + w + "\" type=\"Float64\" format=\"appended\" offset=\"";
-      if (line.compare(0, expected.size(), expected) == 0) {
-        found.push_back(w);
-        hit = true;
-        break;
-      }
-    }
-    if (!hit && line.compare(0, expstart.size(), expstart) == 0) {
-      found.push_back("ignore");
-      ++ignored;
-    }
-  }
-  if (found.size() - ignored < s.attributes.size()) {
+  const VtiTable t = vti_table(f);
+  bool all = t.data != std::streampos(-1);
+  for (auto& w : s.attributes) all = all && t.offset.count(w);
+  if (!all) {
     std::string msg = "Not all attributes requested in read_dump command are in " + s.filename +
                       ". List of attributes in file are:";
     for (auto& w : s.attributes) msg += " " + w;
     throw std::runtime_error(msg + ".");
   }
-  char underscore;
-  f.read(&underscore, 1);
-  const uint64_t want = (uint64_t)nx * ny * nz * sizeof(double);  // one rank: no neighbour planes
+  const uint64_t want = (uint64_t)nx * ny * nz * sizeof(double);  // one domain: no neighbour planes
   std::map<std::string, std::vector<double>> out;
-  for (auto& w : found) {
-    uint32_t bytelength = 0;
-    f.read(reinterpret_cast<char*>(&bytelength), sizeof(bytelength));
-    if (w == "ignore") {
-      if (!f || bytelength != want) throw std::runtime_error("incorrect array size in " + s.filename);
-      f.ignore(bytelength);
-      continue;
-    }
+  for (auto& w : s.attributes) {
     if (w != "phi" && w != "chempot" && w != "gradphi_x" && w != "gradphi_y" && w != "gradphi_z")
       throw std::runtime_error("ReadDump error: Attribute does not exist.");
+    f.clear();
+    f.seekg(t.data + (std::streamoff)t.offset.at(w));
+    uint32_t bytelength = 0;
+    f.read(reinterpret_cast<char*>(&bytelength), sizeof(bytelength));
     if (!f || bytelength != want) throw std::runtime_error("incorrect size " + w + " in file.");
     std::vector<double> a((size_t)nx * ny * nz);
     f.read(reinterpret_cast<char*>(a.data()), (std::streamsize)want);
