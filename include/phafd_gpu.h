@@ -146,7 +146,7 @@ int phafd_set_plane_fusion(phafd_ctx* ctx, int on);                 /* x and y p
  * stores it everywhere.  Reads of the gradient fields (phafd_grid_get,
  * phafd_grid_device) first recompute them everywhere from the current phi. */
 int phafd_set_gradient_mask(phafd_ctx* ctx, int on);
-/* FP32 contexts only (no effect in FP64; both stages on by default): the
+/* FP32 contexts only (no effect in FP64; PHAFD_CENTER_FFT by default): the
  * stages that work relative to a reference concentration c, the mean of phi
  * found at set-up.  PHAFD_CENTER_FFT: the transforms of phi carry phi - c
  * (N c goes back into the k = 0 mode, c back into phi after the inverse), so
@@ -154,9 +154,31 @@ int phafd_set_gradient_mask(phafd_ctx* ctx, int on);
  * PHAFD_CENTER_FH: the Flory-Huggins part of mu is formed as
  * tv (f(phi) - f(c)) with one log1p; the constant tv f(c) moves only the
  * k = 0 mode of mu, which the update does not read (a kept chempot and its
- * spectrum include it).  Takes effect at the next step.  No counterpart in the
+ * spectrum include it); it costs a software log1p per node in the x pass
+ * and, measured at 256^3, does not change the S(k) error.  Takes effect at
+ * the next step.  No counterpart in the
  * reference, which is FP64 throughout; switching stages off gives the FP32
  * error budget. */
+/* ---- autotuner (no counterpart in the reference, which leaves its
+ * transforms to FFTW's planner, grid.cpp:236-280) ----
+ * Kernel variants of the step, each parity-tested, which give the same
+ * trajectory up to round-off:
+ *   PHAFD_TUNE_PLANE       the x and y passes fused per z-plane (thread-block
+ *                          clusters exchanging through distributed shared
+ *                          memory; where Nx == Ny and the plane fits)
+ *   PHAFD_TUNE_GENERIC256  the shared-memory tile transforms on 256-point
+ *                          axes in place of the register-resident ones
+ * phafd_set_variants selects a combination (0: the defaults).
+ * phafd_autotune times every applicable combination over `steps` steps (rounded
+ * up to even) of the run itself, after four warm-up steps that capture its
+ * graphs, keeps the
+ * fastest (*best) and writes the milliseconds per step of each combination
+ * to ms[4], indexed by the flags (-1 where a combination does not apply).
+ * The tuning steps advance the run like phafd_run. */
+#define PHAFD_TUNE_PLANE 1
+#define PHAFD_TUNE_GENERIC256 2
+int phafd_set_variants(phafd_ctx* ctx, int flags);
+int phafd_autotune(phafd_ctx* ctx, int steps, int* best, double* ms);
 #define PHAFD_CENTER_FH 1
 #define PHAFD_CENTER_FFT 2
 int phafd_set_fp32_centering(phafd_ctx* ctx, int stages);

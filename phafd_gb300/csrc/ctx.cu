@@ -184,7 +184,9 @@ struct phafd_ctx {
   double phi_ref = 0.0;
   // which FP32 stages use c (phafd_set_fp32_centering): PHAFD_CENTER_FH the
   // Flory-Huggins part, PHAFD_CENTER_FFT the transforms of phi
-  int center_bits = PHAFD_CENTER_FH | PHAFD_CENTER_FFT;
+  // (the transforms by default: measured, centering the Flory-Huggins part
+  // costs the x pass a software log1p per node and leaves S(k) where it was)
+  int center_bits = PHAFD_CENTER_FFT;
   bool centered(int bit = PHAFD_CENTER_FH | PHAFD_CENTER_FFT) const {
     return precision == PHAFD_FP32 && phi_ref > 0.0 && phi_ref < 1.0 && (center_bits & bit);
   }
@@ -1553,6 +1555,66 @@ int phafd_run(phafd_ctx* c, int nsteps) {
   CK(cudaStreamSynchronize(c->st));
   if (c->keep_chempot && c->have_conj && nsteps > 0) c->chempot_from_mu = true;
   int rc = check_status(c);
+  if (rc) return rc;
+  API_END(c)
+}
+
+static void apply_variants(phafd_ctx* c, int flags) {
+  c->use_plane = (flags & PHAFD_TUNE_PLANE) != 0;
+  c->geom.generic256 = (flags & PHAFD_TUNE_GENERIC256) ? 1 : 0;
+  c->invalidate_graph();
+}
+
+int phafd_set_variants(phafd_ctx* c, int flags) {
+  API_BEGIN(c)
+  if (flags & ~(PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256)) throw std::invalid_argument("unknown kernel variant");
+  apply_variants(c, flags);
+  API_END(c)
+}
+
+int phafd_autotune(phafd_ctx* c, int steps, int* best, double* ms) {
+  API_BEGIN(c)
+  if (steps < 1 || !best || !ms) throw std::invalid_argument("autotune: steps >= 1 and output arrays needed");
+  CK(cudaSetDevice(c->device));
+  if (!c->setup_done) {
+    int rc = phafd_setup(c);
+    if (rc) return rc;
+  }
+  const bool has256 = c->N[0] == 256 || c->N[1] == 256 || c->N[2] == 256;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  double best_ms = 1e300;
+  int best_flags = 0;
+  int rc = PHAFD_OK;
+  for (int f = 0; f < 4 && rc == PHAFD_OK; ++f) {
+    ms[f] = -1.0;
+    if ((f & PHAFD_TUNE_GENERIC256) && !has256) continue;
+    if ((f & PHAFD_TUNE_PLANE) && (c->N[0] != c->N[1] || !c->have_conj)) continue;
+    apply_variants(c, f);
+    enqueue_run(c, 4);  // an eager step, then the graphs' captures
+    CK(cudaStreamSynchronize(c->st));
+    rc = check_status(c);
+    if (rc) break;
+    const int timed = steps + (steps & 1);  // whole two-step graphs
+    CK(cudaEventRecord(e0, c->st));
+    enqueue_run(c, timed);
+    CK(cudaEventRecord(e1, c->st));
+    CK(cudaEventSynchronize(e1));
+    rc = check_status(c);
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    ms[f] = (double)t / timed;
+    if (ms[f] < best_ms) {
+      best_ms = ms[f];
+      best_flags = f;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  apply_variants(c, best_flags);
+  *best = best_flags;
+  if (c->keep_chempot && c->have_conj) c->chempot_from_mu = true;
   if (rc) return rc;
   API_END(c)
 }

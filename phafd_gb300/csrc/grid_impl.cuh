@@ -731,7 +731,7 @@ int zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T
 template <typename T>
 int GridOps<T>::xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
                      cudaStream_t st) {
-  if (g.nx == 256) return r256::xr2c<T>(g, in, dep, out, tw, fh, st);
+  if (g.nx == 256 && !g.generic256) return r256::xr2c<T>(g, in, dep, out, tw, fh, st);
   switch (g.nx) {
 #define CASE(n) case n: return Axis<T, n>::xr2c(g, in, dep, out, tw, fh, st);
     PHAFD_FOR_SIZES(CASE)
@@ -756,7 +756,7 @@ template <typename T>
 int GridOps<T>::xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E,
                       T* gz, T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan,
                       const uint32_t* gmask, const int* gmask_off, cudaStream_t st) {
-  if (g.nx == 256) return r256::xc2r3<T>(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
+  if (g.nx == 256 && !g.generic256) return r256::xc2r3<T>(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
   switch (g.nx) {
 #define CASE(n) \
   case n: return Axis<T, n>::xc2r3(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
@@ -770,7 +770,7 @@ int GridOps<T>::xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T
 template <typename T>
 int GridOps<T>::yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E,
                       const cpx<T>* tw, cudaStream_t st) {
-  if (g.ny == 256) return r256::yinv2<T>(g, A, C, D, B, E, tw, st);
+  if (g.ny == 256 && !g.generic256) return r256::yinv2<T>(g, A, C, D, B, E, tw, st);
   switch (g.ny) {
 #define CASE(n) case n: return Axis<T, n>::yinv2(g, A, C, D, B, E, tw, st);
     PHAFD_FOR_SIZES(CASE)
@@ -782,7 +782,7 @@ int GridOps<T>::yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, cons
 template <typename T>
 int GridOps<T>::ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
                       cudaStream_t st) {
-  if (g.ny == 256) return r256::ypass<T>(g, sign, in, out0, out1, tw, st);
+  if (g.ny == 256 && !g.generic256) return r256::ypass<T>(g, sign, in, out0, out1, tw, st);
   switch (g.ny) {
 #define CASE(n)                                                                   \
   case n:                                                                         \
@@ -799,7 +799,7 @@ template <typename T>
 int GridOps<T>::zfused(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1,
                        const cpx<T>* twf, const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int bulk_only,
                        cudaStream_t st) {
-  if (g.nz == 256) return r256::zfused<T>(g, muin, muhat, out0, out1, twf, twi, u, store_mu, bulk_only, st);
+  if (g.nz == 256 && !g.generic256) return r256::zfused<T>(g, muin, muhat, out0, out1, twf, twi, u, store_mu, bulk_only, st);
   switch (g.nz) {
 #define CASE(n) case n: return Axis<T, n>::zfused(g, muin, muhat, out0, out1, twf, twi, u, store_mu, bulk_only, st);
     PHAFD_FOR_SIZES(CASE)

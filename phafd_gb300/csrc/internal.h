@@ -10,6 +10,7 @@ namespace phafd {
 struct Geom {
   int nx, ny, nz, nxh;
   double kq[3];  // 2*3.141592/L per physical axis (domain.cpp:206-208)
+  int generic256;  // 256-point axes take the shared-memory tile transforms, not the register-resident ones
 };
 
 struct FHArgs {

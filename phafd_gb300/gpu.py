@@ -29,6 +29,7 @@ EXPORTS = [
     "phafd_grid_populate_sphere", "phafd_grid_set", "phafd_grid_get",
     "phafd_set_zghost", "phafd_set_schedule", "phafd_set_keep_chempot", "phafd_set_plane_fusion",
     "phafd_set_gradient_mask", "phafd_set_fp32_centering", "phafd_set_pair_snapshot", "phafd_compute_pair",
+    "phafd_set_variants", "phafd_autotune",
     "phafd_atoms_create", "phafd_atoms_get", "phafd_atoms_set_images",
     "phafd_pair_gridatom", "phafd_pair_gridatom_coeff", "phafd_pair_lj_cut",
     "phafd_neighbor",
@@ -90,6 +91,8 @@ def load(path=None):
         "phafd_set_gradient_mask": [vp, C.c_int],
         "phafd_set_fp32_centering": [vp, C.c_int],
         "phafd_set_pair_snapshot": [vp, C.c_int],
+        "phafd_set_variants": [vp, C.c_int],
+        "phafd_autotune": [vp, C.c_int, C.POINTER(C.c_int), dp],
         "phafd_compute_pair": [vp, C.c_int, C.c_int, dp],
         "phafd_domain": [vp, dp, dp],
         "phafd_grid_style": [vp, C.c_int, C.c_int, C.c_int],
@@ -202,6 +205,18 @@ class PhafdGPU:
         """Store grad phi only near the beads during steps (off by default)."""
         self._call("phafd_set_gradient_mask", int(on))
 
+    def set_variants(self, plane=False, generic256=False):
+        """Kernel variants of the step (PHAFD_TUNE_*)."""
+        self._call("phafd_set_variants", (1 if plane else 0) | (2 if generic256 else 0))
+
+    def autotune(self, steps=10):
+        """Time every variant over `steps` steps of the run, keep the fastest:
+        returns (best flags, ms per step by flags, -1 where not applicable)."""
+        best = C.c_int(0)
+        ms = np.zeros(4)
+        self._call("phafd_autotune", steps, C.byref(best), ms)
+        return best.value, ms
+
     def set_pair_snapshot(self, on=True):
         """Keep each step's pair-stage positions (needed by compute_pair)."""
         self._call("phafd_set_pair_snapshot", int(on))
@@ -213,8 +228,8 @@ class PhafdGPU:
         self._call("phafd_compute_pair", PAIR[style], int(add_to_chempot), out)
         return out[:self.n]
 
-    def set_fp32_centering(self, fh=True, fft=True):
-        """FP32 stages taken relative to the mean of phi (both on by default)."""
+    def set_fp32_centering(self, fh=False, fft=True):
+        """FP32 stages taken relative to the mean of phi (the transforms by default)."""
         self._call("phafd_set_fp32_centering", (1 if fh else 0) | (2 if fft else 0))
 
     def domain(self, boxlo, period):

@@ -254,3 +254,48 @@ def test_populate_styles_match_oracle(gpu_lib, precision, style):
     # without): a few ulps in FP64; FP32 holds the rounding (half an ulp below 1)
     assert np.abs(got - want).max() < (1e-14 if precision == 64 else 6e-8)
 
+
+
+@pytest.mark.parametrize("precision,tol", [(64, 1e-10), (32, 2e-5)])
+def test_generic_256_point_plan_matches_oracle(gpu_lib, precision, tol):
+    """The shared-memory tile transforms on 256-point axes (the autotuner's
+    alternative to the register-resident ones) against the oracle."""
+    cfg = dict(W.CONFIGS["32cube_64beads"])
+    cfg.update(n=256, L=256.0, origin=-128.0, nchains=4, chain_len=50, field_noise="philox", bead_temp=1.0,
+               dt=1e-4)
+    o = Oracle(); g = gpu(precision, "resident")
+    g.set_variants(generic256=True)
+    chains = None
+    for d in (o, g):
+        chains = W.apply(d, cfg, chains=chains)
+        d.setup()
+        d.run(3)
+    assert rel_err(g.grid_get("phi"), o.grid_get("phi")) < tol
+    o.stage_gradient()
+    for f in ("gradx", "grady", "gradz"):
+        assert rel_err(g.grid_get(f), o.grid_get(f)) < (tol if precision == 64 else 1e-4), f
+
+
+def test_autotune_steps_are_steps_of_the_run(gpu_lib):
+    """The autotuner times each variant on the run's own steps: afterwards
+    the state equals the oracle's after the same number of steps, and the
+    fastest variant is kept."""
+    cfg = dict(W.CONFIGS["32cube_64beads"])
+    cfg.update(n=64, L=64.0, origin=-32.0, nchains=2, chain_len=40, field_noise="philox", bead_temp=1.0,
+               dt=1e-4)
+    o = Oracle(); g = gpu(64, "resident")
+    chains = None
+    for d in (o, g):
+        chains = W.apply(d, cfg, chains=chains)
+        d.setup()
+    best, ms = g.autotune(steps=2)
+    assert ms[0] > 0 and ms[1] > 0      # separate and plane-fused passes (64 x 64 planes)
+    assert ms[2] < 0 and ms[3] < 0      # no 256-point axis
+    assert best == int(np.argmin(np.where(ms > 0, ms, np.inf)))
+    done = g.counters()["timestep"]
+    assert done == 2 * (4 + 2)
+    o.run(done)
+    g.run(3)
+    o.run(3)
+    assert rel_err(g.grid_get("phi"), o.grid_get("phi")) < 1e-10
+    assert np.abs(g.atoms_get()[0] - o.atoms_get()[0]).max() < 1e-10 * np.abs(o.atoms_get()[0]).max()
