@@ -38,9 +38,13 @@ namespace phafd {
 // the deviation p - c (the constant tv f(c) only moves the k = 0 mode of mu,
 // which the update multiplies by q^2 = 0).  FP32 without c: the difference of
 // two hardware logarithms.
+// (CENTER: the centered FP32 form; a compile-time choice, so the plain
+// kernels carry no code or registers for it)
+template <bool CENTER>
 PHAFD_D double fh_part(double p, const FHArgs& fh) { return fh.tv * (log(p / (1.0 - p)) + fh.chi * (1.0 - 2.0 * p)); }
+template <bool CENTER>
 PHAFD_D float fh_part(float p, const FHArgs& fh) {
-  if (fh.centered) {
+  if constexpr (CENTER) {
     const float d = p - (float)fh.c;
     return (float)fh.tv * (log1pf(__fdividef(d * (float)fh.inv_c, 1.0f - p)) - 2.0f * (float)fh.chi * d);
   }
@@ -50,17 +54,23 @@ PHAFD_D float fh_part(float p, const FHArgs& fh) {
 // mu at one node from phi = p and the bead deposit dd: the reflections of
 // fixgrid_floryhuggins.cpp:72-80 (counted), then deposit + FH part.  Returns
 // the value the r2c transforms; *keep is the materialised chempot.
-template <typename T>
-PHAFD_D T fh_node(T p, T dd, const FHArgs& fh, unsigned long long& nless, unsigned long long& ngreat, T* keep) {
+template <typename T, bool CENTER>
+PHAFD_D T fh_node_t(T p, T dd, const FHArgs& fh, unsigned long long& nless, unsigned long long& ngreat, T* keep) {
   if (!fh.enabled) {
     *keep = dd;
     return dd;
   }
   if (p <= (T)0) { p = -p; nless++; }
   else if (p >= (T)1) { p = (T)1 - (p - (T)1); ngreat++; }
-  const T m = dd + fh_part(p, fh);
-  *keep = fh.centered ? m + (T)fh.fconst : m;
+  const T m = dd + fh_part<CENTER>(p, fh);
+  *keep = CENTER ? m + (T)fh.fconst : m;
   return m;
+}
+// the same with the form chosen at run time (the generic and plane kernels)
+template <typename T>
+PHAFD_D T fh_node(T p, T dd, const FHArgs& fh, unsigned long long& nless, unsigned long long& ngreat, T* keep) {
+  return (sizeof(T) == 4 && fh.centered) ? fh_node_t<T, true>(p, dd, fh, nless, ngreat, keep)
+                                         : fh_node_t<T, false>(p, dd, fh, nless, ngreat, keep);
 }
 
 template <typename T>

@@ -297,7 +297,8 @@ PHAFD_D void xc2r_tile256(int bx, int z, const cpx<T>* __restrict__ in, T* __res
 }
 
 // x r2c of 256-point rows, optionally fused with mu = deposit + FH(phi)
-// (PRO == 1).  A CTA takes rows y0 .. y0 + 32 of plane z: 16-byte
+// (PRO == 1; PRO == 2 with the Flory-Huggins part taken relative to f(c),
+// FP32).  A CTA takes rows y0 .. y0 + 32 of plane z: 16-byte
 // asynchronous copies of the rows (phi, and the deposit) to shared memory,
 // then line c (rows 2c, 2c + 1 as real and imaginary parts) is formed by its
 // 16 lanes, transformed in registers and written back to its line buffer;
@@ -310,7 +311,7 @@ k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restri
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int ROWS = 2 * W;
   T* sphi = reinterpret_cast<T*>(smraw);  // [ROWS][N]
-  T* sdep = sphi + ROWS * N;              // [ROWS][N] (PRO == 1)
+  T* sdep = sphi + ROWS * N;              // [ROWS][N] (PRO >= 1)
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * ROWS;
   constexpr int PER = 16 / (int)sizeof(T);  // reals per 16-byte copy
@@ -320,7 +321,7 @@ k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restri
     if (y < Ny) {
       const size_t o = ((size_t)z * Ny + y) * N + x;
       cp_async16(sphi + row * N + x, in0 + o);
-      if constexpr (PRO == 1) cp_async16(sdep + row * N + x, dep + o);
+      if constexpr (PRO >= 1) cp_async16(sdep + row * N + x, dep + o);
     }
   }
   cp_async_commit();
@@ -339,9 +340,9 @@ k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restri
       T p = (T)0;
       if (y0 + row < Ny) {
         p = sphi[row * N + x];
-        if constexpr (PRO == 1) {
+        if constexpr (PRO >= 1) {  // PRO 2: the Flory-Huggins part relative to f(c)
           T keep;
-          p = fh_node(p, sdep[row * N + x], fh, nless, ngreat, &keep);
+          p = fh_node_t<T, PRO == 2>(p, sdep[row * N + x], fh, nless, ngreat, &keep);
           if (fh.mu_out) reinterpret_cast<T*>(fh.mu_out)[((size_t)z * Ny + y0 + row) * N + x] = keep;
         } else {
           if (fh.centered) p -= (T)fh.c;  // transform phi - c
@@ -351,7 +352,7 @@ k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restri
     }
     v[r] = mk<T>(pr[0], pr[1]);
   }
-  if constexpr (PRO == 1) {
+  if constexpr (PRO >= 1) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       nless += __shfl_down_sync(0xffffffffu, nless, off);
@@ -399,7 +400,11 @@ int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw
   const size_t lines = (size_t)W * RX * sizeof(cpx<T>);
   const size_t sm = tiles > lines ? tiles : lines;
   dim3 grid((g.ny + 2 * W - 1) / (2 * W), g.nz);
-  if (dep) {
+  if (dep && fh.centered && fh.enabled && sizeof(T) == 4) {
+    auto k = k_xr2c256<T, 2>;
+    if (set_smem(k, sm)) return -1;
+    launch_grid(k, grid, dim3(256), sm, st, in, dep, out, tw, g.ny, g.nz, fh);
+  } else if (dep) {
     auto k = k_xr2c256<T, 1>;
     if (set_smem(k, sm)) return -1;
     launch_grid(k, grid, dim3(256), sm, st, in, dep, out, tw, g.ny, g.nz, fh);

@@ -299,3 +299,25 @@ def test_autotune_steps_are_steps_of_the_run(gpu_lib):
     o.run(3)
     assert rel_err(g.grid_get("phi"), o.grid_get("phi")) < 1e-10
     assert np.abs(g.atoms_get()[0] - o.atoms_get()[0]).max() < 1e-10 * np.abs(o.atoms_get()[0]).max()
+
+
+@pytest.mark.parametrize("precision,tol", [(64, 1e-10), (32, 2e-5)])
+def test_512cube_steps_match_oracle(gpu_lib, precision, tol):
+    """The largest single-GPU grid (512^3, box 512) against the oracle: three
+    steps with Philox field and bead noise and four 50-bead chains (the
+    oracle's all-node grid list at this size allows few beads in a test)."""
+    from oracle import oracle as OR
+    cfg = dict(W.CONFIGS["512cube_1Mbeads"])
+    cfg.update(nchains=4, chain_len=50)
+    OR.set_threads(OR.host_threads())
+    o = Oracle(); g = gpu(precision, "resident")
+    chains = None
+    for d in (o, g):
+        chains = W.apply(d, cfg, chains=chains)
+        d.setup()
+        d.run(3)
+    assert rel_err(g.grid_get("phi"), o.grid_get("phi")) < tol
+    xo = o.atoms_get()[0]
+    xg = g.atoms_get()[0]
+    assert np.abs(xg - xo).max() < (1e-10 if precision == 64 else 1e-6) * np.abs(xo).max()
+    assert g.counters()["neighbor_calls"] == o.counters()["neighbor_calls"]
