@@ -291,12 +291,10 @@ def run_gpu(args):
     g.run(max(args.warmup, 3))
     # the project's autotuner picks the kernel variants on the run's own steps
     best, tune_ms = g.autotune(10)
-    def variant_name(f):
-        parts = [("plane-fused x/y" if f & 1 else None), ("generic 256 tiles" if f & 2 else None),
-                 ("prefetching x c2r" if f & 4 else None)]
-        return " + ".join(p for p in parts if p) or "register-resident 256 (default)"
-    autotune = {"best": variant_name(best),
-                "ms_per_step": {variant_name(f): float(tune_ms[f]) for f in range(8) if tune_ms[f] > 0}}
+    names = {0: "register-resident 256 (default)", 1: "plane-fused x/y", 2: "generic 256 tiles",
+             3: "plane-fused x/y + generic 256 tiles"}
+    autotune = {"best": names[best], "ms_per_step": {names[f]: (float(tune_ms[f]) if tune_ms[f] > 0 else None)
+                                                      for f in range(4)}}
 
     # stage profile (eager steps with events between stages; not the timed region)
     prof = g.profile_stages(args.profile_steps)

@@ -1562,14 +1562,12 @@ int phafd_run(phafd_ctx* c, int nsteps) {
 static void apply_variants(phafd_ctx* c, int flags) {
   c->use_plane = (flags & PHAFD_TUNE_PLANE) != 0;
   c->geom.generic256 = (flags & PHAFD_TUNE_GENERIC256) ? 1 : 0;
-  c->geom.xc2r_pipe = (flags & PHAFD_TUNE_XC2R_PIPE) ? 1 : 0;
   c->invalidate_graph();
 }
 
 int phafd_set_variants(phafd_ctx* c, int flags) {
   API_BEGIN(c)
-  if (flags & ~(PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256 | PHAFD_TUNE_XC2R_PIPE))
-    throw std::invalid_argument("unknown kernel variant");
+  if (flags & ~(PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256)) throw std::invalid_argument("unknown kernel variant");
   apply_variants(c, flags);
   API_END(c)
 }
@@ -1589,11 +1587,9 @@ int phafd_autotune(phafd_ctx* c, int steps, int* best, double* ms) {
   double best_ms = 1e300;
   int best_flags = 0;
   int rc = PHAFD_OK;
-  const bool pipe_ok = c->N[0] == 256 && c->precision == PHAFD_FP32;  // the prefetching x c2r's domain
-  for (int f = 0; f < 8 && rc == PHAFD_OK; ++f) {
+  for (int f = 0; f < 4 && rc == PHAFD_OK; ++f) {
     ms[f] = -1.0;
     if ((f & PHAFD_TUNE_GENERIC256) && !has256) continue;
-    if ((f & PHAFD_TUNE_XC2R_PIPE) && (!pipe_ok || (f & PHAFD_TUNE_GENERIC256))) continue;
     if ((f & PHAFD_TUNE_PLANE) && (c->N[0] != c->N[1] || !c->have_conj)) continue;
     apply_variants(c, f);
     enqueue_run(c, 4);  // an eager step, then the graphs' captures

@@ -729,10 +729,6 @@ int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy,
           T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
           const int* gmask_off, cudaStream_t st);
 template <typename T>
-int xc2r3_pipe(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E, T* gz, T sp,
-               T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
-               const int* gmask_off, cudaStream_t st);
-template <typename T>
 int ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw, cudaStream_t st);
 template <typename T>
 int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E, const cpx<T>* tw,
@@ -770,13 +766,7 @@ template <typename T>
 int GridOps<T>::xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E,
                       T* gz, T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan,
                       const uint32_t* gmask, const int* gmask_off, cudaStream_t st) {
-  if (g.nx == 256 && !g.generic256) {
-    if (g.xc2r_pipe) {
-      const int rc = r256::xc2r3_pipe<T>(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
-      if (rc != -3) return rc;
-    }
-    return r256::xc2r3<T>(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
-  }
+  if (g.nx == 256 && !g.generic256) return r256::xc2r3<T>(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
   switch (g.nx) {
 #define CASE(n) \
   case n: return Axis<T, n>::xc2r3(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);

@@ -11,7 +11,6 @@ struct Geom {
   int nx, ny, nz, nxh;
   double kq[3];  // 2*3.141592/L per physical axis (domain.cpp:206-208)
   int generic256;  // 256-point axes take the shared-memory tile transforms, not the register-resident ones
-  int xc2r_pipe;   // the persistent, prefetching form of the merged x c2r (FP32, 256-point rows)
 };
 
 struct FHArgs {

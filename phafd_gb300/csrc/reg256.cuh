@@ -220,29 +220,43 @@ k_yinv2row256(const cpx<T>* __restrict__ A, cpx<T>* __restrict__ C, cpx<T>* __re
 // output with a mask go only to the 32-byte sectors whose bit is set.
 constexpr int RX = N + N / 16 + 1;
 
-// one loaded pair (rows 2l, 2l + 1 at kx = k) into the tile's line buffers,
-// Hermitian-completed, for each of the NOUT outputs
 template <typename T, int NOUT>
-PHAFD_D void xc2r_put256(cpx<T> A, cpx<T> B, int k, int l, T dq, cpx<T>* zs) {
-  constexpr int LP = W / NOUT;
-#pragma unroll
-  for (int q = 0; q < NOUT; ++q) {
-    cpx<T> a = A, b = B;
-    if (q == 1) { a = deriv(a, dq, k); b = deriv(b, dq, k); }
-    if (k == 0 || k == N / 2) { a.y = (T)0; b.y = (T)0; }
-    cpx<T>* line = zs + (q * LP + l) * RX;
-    line[k + (k >> 4)] = mk<T>(a.x - b.y, a.y + b.x);
-    if (k > 0 && k < N / 2) line[(N - k) + ((N - k) >> 4)] = mk<T>(a.x + b.y, b.x - a.y);
-  }
-}
-
-// the tile's lines (complete in zs) inverse-transformed and stored as rows
-template <typename T, int NOUT>
-PHAFD_D void xc2r_out256(int y0, int z, T* __restrict__ out0, T* __restrict__ out1, T s0, T s1,
-                         const cpx<T>* __restrict__ tw, int Ny, const NanArgs& nan, const uint32_t* mask0,
-                         const uint32_t* mask1, cpx<T>* zs) {
+PHAFD_D void xc2r_tile256(int bx, int z, const cpx<T>* __restrict__ in, T* __restrict__ out0,
+                          T* __restrict__ out1, T s0, T s1, T dq, const cpx<T>* __restrict__ tw, int Ny, int Nz,
+                          const NanArgs& nan, const uint32_t* mask0, const uint32_t* mask1, unsigned char* smraw) {
   constexpr int LP = W / NOUT;
   constexpr int G = 32 / (int)sizeof(T);  // nodes per 32-byte sector
+  cpx<T>* zs = reinterpret_cast<cpx<T>*>(smraw);
+  const int y0 = bx * 2 * LP;
+  TILE_LOOP(idx, (N / 2 + 1) * LP, 256) {  // unrolled: every load of a thread in flight at once
+    const int l = idx % LP, k = idx / LP;
+    const int y = y0 + 2 * l;
+    const size_t o = ((size_t)k * Nz + z) * Ny + y;
+    cpx<T> A = mk<T>(0, 0), B = mk<T>(0, 0);
+    if constexpr (sizeof(T) == 4) {
+      if (y + 1 < Ny && (Ny & 1) == 0) {  // o even: one 16-byte load of the pair
+        const float4 ab = *reinterpret_cast<const float4*>(&in[o]);
+        A = mk<T>(ab.x, ab.y);
+        B = mk<T>(ab.z, ab.w);
+      } else {
+        if (y < Ny) A = in[o];
+        if (y + 1 < Ny) B = in[o + 1];
+      }
+    } else {
+      if (y < Ny) A = in[o];
+      if (y + 1 < Ny) B = in[o + 1];
+    }
+#pragma unroll
+    for (int q = 0; q < NOUT; ++q) {
+      cpx<T> a = A, b = B;
+      if (q == 1) { a = deriv(a, dq, k); b = deriv(b, dq, k); }
+      if (k == 0 || k == N / 2) { a.y = (T)0; b.y = (T)0; }
+      cpx<T>* line = zs + (q * LP + l) * RX;
+      line[k + (k >> 4)] = mk<T>(a.x - b.y, a.y + b.x);
+      if (k > 0 && k < N / 2) line[(N - k) + ((N - k) >> 4)] = mk<T>(a.x + b.y, b.x - a.y);
+    }
+  }
+  __syncthreads();
   const int j = threadIdx.x & 15, c = threadIdx.x >> 4;
   const int q = c / LP, l = c % LP;
   cpx<T>* rb = zs + c * RX;
@@ -280,37 +294,6 @@ PHAFD_D void xc2r_out256(int y0, int z, T* __restrict__ out0, T* __restrict__ ou
       atomicCAS(reinterpret_cast<unsigned long long*>(nan.nan_step), (unsigned long long)-1LL,
                 (unsigned long long)(*nan.d_step));
   }
-}
-
-template <typename T, int NOUT>
-PHAFD_D void xc2r_tile256(int bx, int z, const cpx<T>* __restrict__ in, T* __restrict__ out0,
-                          T* __restrict__ out1, T s0, T s1, T dq, const cpx<T>* __restrict__ tw, int Ny, int Nz,
-                          const NanArgs& nan, const uint32_t* mask0, const uint32_t* mask1, unsigned char* smraw) {
-  constexpr int LP = W / NOUT;
-  cpx<T>* zs = reinterpret_cast<cpx<T>*>(smraw);
-  const int y0 = bx * 2 * LP;
-  TILE_LOOP(idx, (N / 2 + 1) * LP, 256) {  // unrolled: every load of a thread in flight at once
-    const int l = idx % LP, k = idx / LP;
-    const int y = y0 + 2 * l;
-    const size_t o = ((size_t)k * Nz + z) * Ny + y;
-    cpx<T> A = mk<T>(0, 0), B = mk<T>(0, 0);
-    if constexpr (sizeof(T) == 4) {
-      if (y + 1 < Ny && (Ny & 1) == 0) {  // o even: one 16-byte load of the pair
-        const float4 ab = *reinterpret_cast<const float4*>(&in[o]);
-        A = mk<T>(ab.x, ab.y);
-        B = mk<T>(ab.z, ab.w);
-      } else {
-        if (y < Ny) A = in[o];
-        if (y + 1 < Ny) B = in[o + 1];
-      }
-    } else {
-      if (y < Ny) A = in[o];
-      if (y + 1 < Ny) B = in[o + 1];
-    }
-    xc2r_put256<T, NOUT>(A, B, k, l, dq, zs);
-  }
-  __syncthreads();
-  xc2r_out256<T, NOUT>(y0, z, out0, out1, s0, s1, tw, Ny, nan, mask0, mask1, zs);
 }
 
 // x r2c of 256-point rows, optionally fused with mu = deposit + FH(phi)
@@ -463,137 +446,6 @@ int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy,
   launch_grid(k, dim3(nb0 + 2 * nb1, g.nz), dim3(256), sm, st, C, phi, gx, D, gy, E, gz, sp, sg, (T)g.kq[0], tw,
               g.ny, g.nz, nan, nonan, nb0, nb1, gmask, gmask_off);
   return 0;
-}
-
-// Persistent form of k_xc2r3_256 for FP32 (the autotuner's
-// PHAFD_TUNE_XC2R_PIPE): each CTA walks the list of tiles (per plane z the
-// C, D and E tiles of k_xc2r3_256) with the grid's stride, and the
-// half-spectrum pairs of its next tile are copied to shared memory
-// asynchronously (cp.async, 16 bytes per pair of rows) while it transforms
-// and stores the current one, so its load latency hides behind its own
-// compute.  Two stage buffers, each large enough for a tile's raw pairs (at
-// most 129 x 16) and, once those are in registers, for its line buffers.
-constexpr int XP_STAGE = W * RX * 8;  // bytes
-static_assert(XP_STAGE >= (N / 2 + 1) * W * 16, "a stage holds the raw pairs of a one-output tile");
-
-struct XTile {
-  int kind, z, bx;  // kind 0: C (phi + dphi/dx), 1: D (dphi/dy), 2: E (dphi/dz)
-};
-PHAFD_D XTile xtile(long long t, int nb0, int nb1) {
-  const int tp = nb0 + 2 * nb1;
-  XTile x;
-  x.z = (int)(t / tp);
-  const int b = (int)(t % tp);
-  if (b < nb0) { x.kind = 0; x.bx = b; }
-  else if (b < nb0 + nb1) { x.kind = 1; x.bx = b - nb0; }
-  else { x.kind = 2; x.bx = b - nb0 - nb1; }
-  return x;
-}
-
-// queue the copies of tile t's raw pairs into `raw` as one commit group
-// (an empty group past the last tile, so every CTA commits one per tile)
-PHAFD_D void xp_issue(long long t, long long ntiles, int nb0, int nb1, const cpx<float>* C, const cpx<float>* D,
-                      const cpx<float>* E, int Ny, int Nz, float4* raw) {
-  if (t < ntiles) {
-    const XTile x = xtile(t, nb0, nb1);
-    const int LP = x.kind == 0 ? W / 2 : W;
-    const cpx<float>* in = x.kind == 0 ? C : x.kind == 1 ? D : E;
-    const int y0 = x.bx * 2 * LP;
-    const int total = (N / 2 + 1) * LP;
-    for (int idx = threadIdx.x; idx < total; idx += 256) {
-      const int l = idx % LP, k = idx / LP;
-      const int y = y0 + 2 * l;
-      if (y + 1 < Ny) cp_async16(&raw[idx], &in[((size_t)k * Nz + x.z) * Ny + y]);
-      else raw[idx] = make_float4(0.f, 0.f, 0.f, 0.f);  // rows past the plane (Ny is even)
-    }
-  }
-  cp_async_commit();
-}
-
-template <int NOUT>
-PHAFD_D void xp_tile(const XTile& x, float4* raw, float* out0, float* out1, float s0, float s1, float dq,
-                     const cpx<float>* __restrict__ tw, int Ny, const NanArgs& nan, const uint32_t* mask0,
-                     const uint32_t* mask1) {
-  constexpr int LP = W / NOUT;
-  constexpr int TOTAL = (N / 2 + 1) * LP, IT = (TOTAL + 255) / 256;
-  float4 r[IT];
-#pragma unroll
-  for (int it = 0; it < IT; ++it) {
-    const int idx = (int)threadIdx.x + 256 * it;
-    if (idx < TOTAL) r[it] = raw[idx];
-  }
-  __syncthreads();  // every raw pair is in registers: the stage becomes the line buffers
-  cpx<float>* zs = reinterpret_cast<cpx<float>*>(raw);
-#pragma unroll
-  for (int it = 0; it < IT; ++it) {
-    const int idx = (int)threadIdx.x + 256 * it;
-    if (idx < TOTAL)
-      xc2r_put256<float, NOUT>(mk<float>(r[it].x, r[it].y), mk<float>(r[it].z, r[it].w), idx / LP, idx % LP, dq, zs);
-  }
-  __syncthreads();
-  xc2r_out256<float, NOUT>(x.bx * 2 * LP, x.z, out0, out1, s0, s1, tw, Ny, nan, mask0, mask1, zs);
-}
-
-// (a template, so that the translation units that include this header do not
-// each define it; instantiated for float only)
-template <typename T>
-__global__ void __launch_bounds__(256, 3)
-k_xc2r3_256p(const cpx<T>* __restrict__ C, T* __restrict__ phi, T* __restrict__ gx, const cpx<T>* __restrict__ D,
-             T* __restrict__ gy, const cpx<T>* __restrict__ E, T* __restrict__ gz, T sp, T sg, T dq,
-             const cpx<T>* __restrict__ tw, int Ny, int Nz, NanArgs nan, NanArgs nonan, int nb0, int nb1,
-             const uint32_t* __restrict__ mask, const int* __restrict__ mask_off, long long ntiles) {
-  static_assert(sizeof(T) == 4, "the prefetching x c2r is FP32 only");
-  extern __shared__ __align__(16) unsigned char smraw[];
-  float4* stage[2] = {reinterpret_cast<float4*>(smraw), reinterpret_cast<float4*>(smraw + XP_STAGE)};
-  const uint32_t* gm = mask && !*mask_off ? mask : nullptr;
-  const long long stride = gridDim.x;
-  long long t = blockIdx.x;
-  xp_issue(t, ntiles, nb0, nb1, C, D, E, Ny, Nz, stage[0]);
-  xp_issue(t + stride, ntiles, nb0, nb1, C, D, E, Ny, Nz, stage[1]);
-  for (int i = 0; t < ntiles; ++i, t += stride) {
-    float4* raw = stage[i & 1];
-    cp_async_wait<1>();  // this tile's group is complete (the next one may still be in flight)
-    __syncthreads();
-    const XTile x = xtile(t, nb0, nb1);
-    if (x.kind == 0) xp_tile<2>(x, raw, phi, gx, sp, sg, dq, tw, Ny, nan, nullptr, gm);
-    else if (x.kind == 1) xp_tile<1>(x, raw, gy, nullptr, sg, sg, dq, tw, Ny, nonan, gm, nullptr);
-    else xp_tile<1>(x, raw, gz, nullptr, sg, sg, dq, tw, Ny, nonan, gm, nullptr);
-    __syncthreads();  // the stage's line buffers are read: refill it
-    xp_issue(t + 2 * stride, ntiles, nb0, nb1, C, D, E, Ny, Nz, raw);
-  }
-  cp_async_wait<0>();
-}
-
-// SM count of the current device, once per device
-inline int sm_count() {
-  static int cache[64] = {0};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-  if (!cache[dev] && cudaDeviceGetAttribute(&cache[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    cache[dev] = 0;
-  return cache[dev];
-}
-
-template <typename T>
-int xc2r3_pipe(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E, T* gz, T sp,
-               T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
-               const int* gmask_off, cudaStream_t st) {
-  if constexpr (sizeof(T) != 4) {
-    return -3;  // FP32 only: FP64 stages would leave one CTA per SM
-  } else {
-    if (g.ny % 2) return -3;
-    const size_t sm = 2 * (size_t)XP_STAGE;
-    const int nb0 = (g.ny + W - 1) / W, nb1 = (g.ny + 2 * W - 1) / (2 * W);
-    const long long ntiles = (long long)(nb0 + 2 * nb1) * g.nz;
-    const int sms = sm_count();
-    if (sms <= 0) return -1;
-    const long long grid = ntiles < 3LL * sms ? ntiles : 3LL * sms;
-    auto k = k_xc2r3_256p<T>;
-    if (set_smem(k, sm)) return -1;
-    launch_grid(k, dim3((unsigned)grid), dim3(256), sm, st, C, phi, gx, D, gy, E, gz, sp, sg, (T)g.kq[0], tw, g.ny,
-                g.nz, nan, nonan, nb0, nb1, gmask, gmask_off, ntiles);
-    return 0;
-  }
 }
 
 template <typename T>
