@@ -292,10 +292,9 @@ def run_gpu(args):
     # the project's autotuner picks the kernel variants on the run's own steps
     best, tune_ms = g.autotune(10)
     names = {0: "register-resident 256 (default)", 1: "plane-fused x/y", 2: "generic 256 tiles",
-             3: "plane-fused x/y + generic 256 tiles", 4: "inverse chain in 64-plane z-chunks",
-             8: "inverse chain in 32-plane z-chunks"}
-    autotune = {"best": names.get(best, str(best)),
-                "ms_per_step": {names.get(f, str(f)): float(tune_ms[f]) for f in range(16) if tune_ms[f] > 0}}
+             3: "plane-fused x/y + generic 256 tiles"}
+    autotune = {"best": names[best], "ms_per_step": {names[f]: (float(tune_ms[f]) if tune_ms[f] > 0 else None)
+                                                      for f in range(4)}}
 
     # stage profile (eager steps with events between stages; not the timed region)
     prof = g.profile_stages(args.profile_steps)

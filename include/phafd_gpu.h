@@ -168,22 +168,15 @@ int phafd_set_gradient_mask(phafd_ctx* ctx, int on);
  *                          memory; where Nx == Ny and the plane fits)
  *   PHAFD_TUNE_GENERIC256  the shared-memory tile transforms on 256-point
  *                          axes in place of the register-resident ones
- *   PHAFD_TUNE_ZCHUNK64/32 (256-point x and y axes) the inverse chain's y and
- *                          x passes alternate over chunks of 64 / 32 z-planes,
- *                          so that each chunk's intermediate spectra are
- *                          still in L2 when the x pass reads them
  * phafd_set_variants selects a combination (0: the defaults).
- * phafd_autotune times the applicable combinations (the plane and 256-point
- * choices crossed, and each z-chunk size alone) over `steps` steps (rounded
+ * phafd_autotune times every applicable combination over `steps` steps (rounded
  * up to even) of the run itself, after four warm-up steps that capture its
  * graphs, keeps the
  * fastest (*best) and writes the milliseconds per step of each combination
- * to ms[16], indexed by the flags (-1 where a combination is not tried).
+ * to ms[4], indexed by the flags (-1 where a combination does not apply).
  * The tuning steps advance the run like phafd_run. */
 #define PHAFD_TUNE_PLANE 1
 #define PHAFD_TUNE_GENERIC256 2
-#define PHAFD_TUNE_ZCHUNK64 4
-#define PHAFD_TUNE_ZCHUNK32 8
 int phafd_set_variants(phafd_ctx* ctx, int flags);
 int phafd_autotune(phafd_ctx* ctx, int steps, int* best, double* ms);
 #define PHAFD_CENTER_FH 1

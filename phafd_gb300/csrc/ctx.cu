@@ -405,25 +405,6 @@ struct phafd_ctx {
     cpx<T>* E = wE.as<cpx<T>>();
     NanArgs nan{nan_check ? 1 : 0, d_nan(), d_step(), phi_off};
     NanArgs nonan{0, d_nan(), d_step()};
-    if (grad && phi_out && geom.zchunk > 0 && geom.nz % geom.zchunk == 0) {
-      // the y and x passes alternate over chunks of z-planes, so that each
-      // chunk's C, D, E are still in L2 when the x pass reads them (the
-      // y_ifft stage mark then covers both passes)
-      bool ok = true;
-      for (int z0 = 0; z0 < geom.nz && ok; z0 += geom.zchunk) {
-        int rc = GridOps<T>::yinv2_z(geom, z0, geom.zchunk, A, Cc, D, B, E, twi[1], st);
-        if (rc == -3) { ok = false; break; }
-        chk(rc, "y ifft");
-        chk(GridOps<T>::xc2r3_z(geom, z0, geom.zchunk, Cc, phi_out, gx.as<T>(), D, gy.as<T>(), E, gz.as<T>(), sp, sg,
-                                twi[0], nan, nonan, masked ? gmask.as<uint32_t>() : nullptr, d_gmask_off(), st),
-            "x c2r");
-      }
-      if (ok) {
-        mark(8);
-        mark(9);
-        return;
-      }
-    }
     if (grad && phi_out) {
       // one launch per direction for the whole inverse chain
       int rc = GridOps<T>::yinv2(geom, A, Cc, D, B, E, twi[1], st);
@@ -1581,14 +1562,12 @@ int phafd_run(phafd_ctx* c, int nsteps) {
 static void apply_variants(phafd_ctx* c, int flags) {
   c->use_plane = (flags & PHAFD_TUNE_PLANE) != 0;
   c->geom.generic256 = (flags & PHAFD_TUNE_GENERIC256) ? 1 : 0;
-  c->geom.zchunk = (flags & PHAFD_TUNE_ZCHUNK32) ? 32 : (flags & PHAFD_TUNE_ZCHUNK64) ? 64 : 0;
   c->invalidate_graph();
 }
 
 int phafd_set_variants(phafd_ctx* c, int flags) {
   API_BEGIN(c)
-  if (flags & ~(PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256 | PHAFD_TUNE_ZCHUNK64 | PHAFD_TUNE_ZCHUNK32))
-    throw std::invalid_argument("unknown kernel variant");
+  if (flags & ~(PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256)) throw std::invalid_argument("unknown kernel variant");
   apply_variants(c, flags);
   API_END(c)
 }
@@ -1608,18 +1587,10 @@ int phafd_autotune(phafd_ctx* c, int steps, int* best, double* ms) {
   double best_ms = 1e300;
   int best_flags = 0;
   int rc = PHAFD_OK;
-  // z-chunks of the inverse chain: register-resident 256-point x and y axes,
-  // separate x/y passes, whole chunks
-  const bool chunk_ok = c->N[0] == 256 && c->N[1] == 256 && c->have_conj;
-  for (int f = 0; f < 16 && rc == PHAFD_OK; ++f) ms[f] = -1.0;
-  const int candidates[] = {0, PHAFD_TUNE_PLANE, PHAFD_TUNE_GENERIC256, PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256,
-                            PHAFD_TUNE_ZCHUNK64, PHAFD_TUNE_ZCHUNK32};
-  for (int f : candidates) {
-    if (rc != PHAFD_OK) break;
+  for (int f = 0; f < 4 && rc == PHAFD_OK; ++f) {
+    ms[f] = -1.0;
     if ((f & PHAFD_TUNE_GENERIC256) && !has256) continue;
     if ((f & PHAFD_TUNE_PLANE) && (c->N[0] != c->N[1] || !c->have_conj)) continue;
-    if ((f & PHAFD_TUNE_ZCHUNK64) && !(chunk_ok && c->N[2] % 64 == 0)) continue;
-    if ((f & PHAFD_TUNE_ZCHUNK32) && !(chunk_ok && c->N[2] % 32 == 0)) continue;
     apply_variants(c, f);
     enqueue_run(c, 4);  // an eager step, then the graphs' captures
     CK(cudaStreamSynchronize(c->st));

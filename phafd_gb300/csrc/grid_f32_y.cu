@@ -11,6 +11,4 @@ template int GridOps<float>::xy_fwd(const Geom&, const float*, const float*, cpx
                                   const FHArgs&, cudaStream_t);
 template int GridOps<float>::yx_inv(const Geom&, const cpx<float>*, float*, float, bool, float*, float, const cpx<float>*,
                                   const cpx<float>*, const NanArgs&, cudaStream_t);
-template int GridOps<float>::yinv2_z(const Geom&, int, int, const cpx<float>*, cpx<float>*, cpx<float>*, const cpx<float>*,
-                                   cpx<float>*, const cpx<float>*, cudaStream_t);
 }

@@ -10,7 +10,4 @@ template int GridOps<double>::xc2r(const Geom&, const cpx<double>*, double*, dou
 template int GridOps<double>::xc2r3(const Geom&, const cpx<double>*, double*, double*, const cpx<double>*, double*, const cpx<double>*, double*,
                                  double, double, const cpx<double>*, const NanArgs&, const NanArgs&, const uint32_t*, const int*,
                                  cudaStream_t);
-template int GridOps<double>::xc2r3_z(const Geom&, int, int, const cpx<double>*, double*, double*, const cpx<double>*, double*,
-                                   const cpx<double>*, double*, double, double, const cpx<double>*, const NanArgs&, const NanArgs&,
-                                   const uint32_t*, const int*, cudaStream_t);
 }

@@ -11,6 +11,4 @@ template int GridOps<double>::xy_fwd(const Geom&, const double*, const double*, 
                                   const FHArgs&, cudaStream_t);
 template int GridOps<double>::yx_inv(const Geom&, const cpx<double>*, double*, double, bool, double*, double, const cpx<double>*,
                                   const cpx<double>*, const NanArgs&, cudaStream_t);
-template int GridOps<double>::yinv2_z(const Geom&, int, int, const cpx<double>*, cpx<double>*, cpx<double>*, const cpx<double>*,
-                                   cpx<double>*, const cpx<double>*, cudaStream_t);
 }

@@ -729,13 +729,6 @@ int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy,
           T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
           const int* gmask_off, cudaStream_t st);
 template <typename T>
-int xc2r3_z(const Geom& g, int z0, int nzc, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E,
-            T* gz, T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
-            const int* gmask_off, cudaStream_t st);
-template <typename T>
-int yinv2_z(const Geom& g, int z0, int nzc, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E,
-            const cpx<T>* tw, cudaStream_t st);
-template <typename T>
 int ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw, cudaStream_t st);
 template <typename T>
 int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E, const cpx<T>* tw,
@@ -794,21 +787,6 @@ int GridOps<T>::yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, cons
 #undef CASE
   }
   return -2;
-}
-
-template <typename T>
-int GridOps<T>::yinv2_z(const Geom& g, int z0, int nzc, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B,
-                        cpx<T>* E, const cpx<T>* tw, cudaStream_t st) {
-  if (g.nx != 256 || g.ny != 256 || g.generic256) return -3;
-  return r256::yinv2_z<T>(g, z0, nzc, A, C, D, B, E, tw, st);
-}
-
-template <typename T>
-int GridOps<T>::xc2r3_z(const Geom& g, int z0, int nzc, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy,
-                        const cpx<T>* E, T* gz, T sp, T sg, const cpx<T>* tw, const NanArgs& nan,
-                        const NanArgs& nonan, const uint32_t* gmask, const int* gmask_off, cudaStream_t st) {
-  if (g.nx != 256 || g.ny != 256 || g.generic256) return -3;
-  return r256::xc2r3_z<T>(g, z0, nzc, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
 }
 
 template <typename T>

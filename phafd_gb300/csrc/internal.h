@@ -11,7 +11,6 @@ struct Geom {
   int nx, ny, nz, nxh;
   double kq[3];  // 2*3.141592/L per physical axis (domain.cpp:206-208)
   int generic256;  // 256-point axes take the shared-memory tile transforms, not the register-resident ones
-  int zchunk;      // > 0: the inverse chain's y and x passes alternate over chunks of this many z-planes
 };
 
 struct FHArgs {
@@ -81,13 +80,6 @@ struct GridOps {
                    const int* gmask_off, cudaStream_t st);
   static int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E,
                    const cpx<T>* tw, cudaStream_t st);
-  // the same two launches over the z-planes [z0, z0 + nzc) only (-3: not
-  // available for these lengths: 256-point x and y axes)
-  static int yinv2_z(const Geom& g, int z0, int nzc, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B,
-                     cpx<T>* E, const cpx<T>* tw, cudaStream_t st);
-  static int xc2r3_z(const Geom& g, int z0, int nzc, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy,
-                     const cpx<T>* E, T* gz, T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan,
-                     const uint32_t* gmask, const int* gmask_off, cudaStream_t st);
   static int zpass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,
                    const UpdateArgs<T>* u, cudaStream_t st);
   // forward z FFT of mu + update + z inverse FFT (bulk kx); plane tiles store mu_hat only

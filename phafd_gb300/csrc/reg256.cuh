@@ -423,9 +423,9 @@ __global__ void __launch_bounds__(256)
 k_xc2r3_256(const cpx<T>* __restrict__ C, T* __restrict__ phi, T* __restrict__ gx, const cpx<T>* __restrict__ D,
             T* __restrict__ gy, const cpx<T>* __restrict__ E, T* __restrict__ gz, T sp, T sg, T dq,
             const cpx<T>* __restrict__ tw, int Ny, int Nz, NanArgs nan, NanArgs nonan, int nb0, int nb1,
-            const uint32_t* __restrict__ mask, const int* __restrict__ mask_off, int z0) {
+            const uint32_t* __restrict__ mask, const int* __restrict__ mask_off) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int bx = blockIdx.x, z = z0 + (int)blockIdx.y;
+  const int bx = blockIdx.x, z = blockIdx.y;
   const uint32_t* gm = mask && !*mask_off ? mask : nullptr;
   if (bx < nb0)
     xc2r_tile256<T, 2>(bx, z, C, phi, gx, sp, sg, dq, tw, Ny, Nz, nan, nullptr, gm, smraw);
@@ -444,22 +444,7 @@ int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy,
   auto k = k_xc2r3_256<T>;
   if (set_smem(k, sm)) return -1;
   launch_grid(k, dim3(nb0 + 2 * nb1, g.nz), dim3(256), sm, st, C, phi, gx, D, gy, E, gz, sp, sg, (T)g.kq[0], tw,
-              g.ny, g.nz, nan, nonan, nb0, nb1, gmask, gmask_off, 0);
-  return 0;
-}
-
-// k_xc2r3_256 over the z-planes [z0, z0 + nzc) only
-template <typename T>
-int xc2r3_z(const Geom& g, int z0, int nzc, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E,
-            T* gz, T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
-            const int* gmask_off, cudaStream_t st) {
-  if (z0 < 0 || nzc < 1 || z0 + nzc > g.nz) return -3;
-  const size_t sm = (size_t)W * RX * sizeof(cpx<T>);
-  const int nb0 = (g.ny + W - 1) / W, nb1 = (g.ny + 2 * W - 1) / (2 * W);
-  auto k = k_xc2r3_256<T>;
-  if (set_smem(k, sm)) return -1;
-  launch_grid(k, dim3(nb0 + 2 * nb1, nzc), dim3(256), sm, st, C, phi, gx, D, gy, E, gz, sp, sg, (T)g.kq[0], tw,
-              g.ny, g.nz, nan, nonan, nb0, nb1, gmask, gmask_off, z0);
+              g.ny, g.nz, nan, nonan, nb0, nb1, gmask, gmask_off);
   return 0;
 }
 
@@ -495,35 +480,6 @@ int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B,
   auto k = k_yinv2row256<T>;
   if (set_smem(k, sm)) return -1;
   launch_grid(k, dim3((unsigned)(2 * nb)), dim3(256), sm, st, A, C, D, B, E, (T)g.kq[1], tw, nlines, nb);
-  return 0;
-}
-
-// k_yinv2row256 over the z-planes [z0, z0 + nzc) only (nzc a multiple of
-// 16, so a tile's 16 lines are consecutive lines kx Nz + z of one kx): the
-// inverse chain in z-chunks, each chunk's C, D, E still in L2 when its x
-// c2r reads them
-template <typename T>
-__global__ void __launch_bounds__(256)
-k_yinv2row256z(const cpx<T>* __restrict__ A, cpx<T>* __restrict__ C, cpx<T>* __restrict__ D,
-               const cpx<T>* __restrict__ B, cpx<T>* __restrict__ E, T dq, const cpx<T>* __restrict__ tw, int Nz,
-               int z0, int nzc, long long nb) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const long long bx = blockIdx.x;
-  const long long lc0 = (bx < nb ? bx : bx - nb) * W;
-  const size_t off = ((size_t)(lc0 / nzc) * Nz + z0 + (size_t)(lc0 % nzc)) * N;
-  if (bx < nb) yrow_tile<T, +1, 2>(0, A + off, C + off, D + off, dq, tw, W, smraw);
-  else yrow_tile<T, +1, 1>(0, B + off, E + off, nullptr, dq, tw, W, smraw);
-}
-
-template <typename T>
-int yinv2_z(const Geom& g, int z0, int nzc, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E,
-            const cpx<T>* tw, cudaStream_t st) {
-  if (nzc % W || z0 < 0 || z0 + nzc > g.nz) return -3;
-  const size_t sm = (size_t)W * RS * sizeof(cpx<T>);
-  const long long nb = (long long)g.nxh * nzc / W;
-  auto k = k_yinv2row256z<T>;
-  if (set_smem(k, sm)) return -1;
-  launch_grid(k, dim3((unsigned)(2 * nb)), dim3(256), sm, st, A, C, D, B, E, (T)g.kq[1], tw, g.nz, z0, nzc, nb);
   return 0;
 }
 
