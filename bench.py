@@ -45,6 +45,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain part of the default line")
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 throughput figure")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the default kernel variants (profiling runs: timings under a profiler mislead the tuner)")
     p.add_argument("--profile-steps", type=int, default=5)
     p.add_argument("--traj", type=int, default=48, help="training trajectories of the learned workloads")
     p.add_argument("--epochs", type=int, default=6, help="training epochs of the learned workloads")
@@ -290,7 +292,7 @@ def run_gpu(args):
     sampler.start()
     g.run(max(args.warmup, 3))
     # the project's autotuner picks the kernel variants on the run's own steps
-    best, tune_ms = g.autotune(10)
+    best, tune_ms = g.autotune(10) if not args.no_autotune else (0, np.zeros(4))
     names = {0: "register-resident 256 (default)", 1: "plane-fused x/y", 2: "generic 256 tiles",
              3: "plane-fused x/y + generic 256 tiles"}
     autotune = {"best": names[best], "ms_per_step": {names[f]: (float(tune_ms[f]) if tune_ms[f] > 0 else None)
