@@ -292,11 +292,11 @@ def run_gpu(args):
     sampler.start()
     g.run(max(args.warmup, 3))
     # the project's autotuner picks the kernel variants on the run's own steps
-    best, tune_ms = g.autotune(10) if not args.no_autotune else (0, np.zeros(4))
-    names = {0: "register-resident 256 (default)", 1: "plane-fused x/y", 2: "generic 256 tiles",
-             3: "plane-fused x/y + generic 256 tiles"}
+    best, tune_ms = g.autotune(10) if not args.no_autotune else (4, np.zeros(8))
+    names = {0: "register-resident 256, x c2r loading its own tiles", 1: "plane-fused x/y", 2: "generic 256 tiles",
+             3: "plane-fused x/y + generic 256 tiles", 4: "register-resident 256, tensor-map fed x c2r (default)"}
     autotune = {"best": names[best], "ms_per_step": {names[f]: (float(tune_ms[f]) if tune_ms[f] > 0 else None)
-                                                      for f in range(4)}}
+                                                      for f in names}}
 
     # stage profile (eager steps with events between stages; not the timed region)
     prof = g.profile_stages(args.profile_steps)

@@ -168,15 +168,22 @@ int phafd_set_gradient_mask(phafd_ctx* ctx, int on);
  *                          memory; where Nx == Ny and the plane fits)
  *   PHAFD_TUNE_GENERIC256  the shared-memory tile transforms on 256-point
  *                          axes in place of the register-resident ones
- * phafd_set_variants selects a combination (0: the defaults).
+ *   PHAFD_TUNE_XC2R_TMA    FP32, Nx = 256, Ny a multiple of 32: the merged
+ *                          x c2r of the inverse chain as a persistent grid fed
+ *                          by tensor-map loads, each CTA's next tile landing
+ *                          while it transforms the current one (in place of
+ *                          the non-persistent grid that loads its own tiles)
+ * phafd_set_variants selects a combination; a new context starts with
+ * PHAFD_TUNE_XC2R_TMA (it has no effect where it does not apply).
  * phafd_autotune times every applicable combination over `steps` steps (rounded
  * up to even) of the run itself, after four warm-up steps that capture its
  * graphs, keeps the
  * fastest (*best) and writes the milliseconds per step of each combination
- * to ms[4], indexed by the flags (-1 where a combination does not apply).
+ * to ms[8], indexed by the flags (-1 where a combination does not apply).
  * The tuning steps advance the run like phafd_run. */
 #define PHAFD_TUNE_PLANE 1
 #define PHAFD_TUNE_GENERIC256 2
+#define PHAFD_TUNE_XC2R_TMA 4
 int phafd_set_variants(phafd_ctx* ctx, int flags);
 int phafd_autotune(phafd_ctx* ctx, int steps, int* best, double* ms);
 #define PHAFD_CENTER_FH 1

@@ -141,4 +141,5 @@ enum : int {
   ST_OVERFLOW = 1,
   ST_CONSTRAINT = 2,
   ST_BINRANGE = 4,
+  ST_TIMEOUT = 8,  // a bounded wait of a grid pass gave up
 };

@@ -412,7 +412,7 @@ struct phafd_ctx {
         chk(rc, "y ifft");
         mark(8);
         chk(GridOps<T>::xc2r3(geom, Cc, phi_out, gx.as<T>(), D, gy.as<T>(), E, gz.as<T>(), sp, sg, twi[0], nan, nonan,
-                              masked ? gmask.as<uint32_t>() : nullptr, d_gmask_off(), st), "x c2r");
+                              masked ? gmask.as<uint32_t>() : nullptr, d_gmask_off(), d_status(), st), "x c2r");
         mark(9);
         return;
       }
@@ -949,6 +949,10 @@ static int check_status(phafd_ctx* c) {
   if (status & ST_CONSTRAINT) {
     c->err = "Failed to maintain polymer bond-length constraints.";
     return PHAFD_ERR_CONSTRAINT;
+  }
+  if (status & ST_TIMEOUT) {
+    c->err = "a grid pass gave up waiting for its tensor-map loads";
+    return PHAFD_ERR_TIMEOUT;
   }
   return PHAFD_OK;
 }
@@ -1562,12 +1566,14 @@ int phafd_run(phafd_ctx* c, int nsteps) {
 static void apply_variants(phafd_ctx* c, int flags) {
   c->use_plane = (flags & PHAFD_TUNE_PLANE) != 0;
   c->geom.generic256 = (flags & PHAFD_TUNE_GENERIC256) ? 1 : 0;
+  c->geom.xc2r_tma = (flags & PHAFD_TUNE_XC2R_TMA) ? 1 : 0;
   c->invalidate_graph();
 }
 
 int phafd_set_variants(phafd_ctx* c, int flags) {
   API_BEGIN(c)
-  if (flags & ~(PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256)) throw std::invalid_argument("unknown kernel variant");
+  if (flags & ~(PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256 | PHAFD_TUNE_XC2R_TMA))
+    throw std::invalid_argument("unknown kernel variant");
   apply_variants(c, flags);
   API_END(c)
 }
@@ -1587,10 +1593,13 @@ int phafd_autotune(phafd_ctx* c, int steps, int* best, double* ms) {
   double best_ms = 1e300;
   int best_flags = 0;
   int rc = PHAFD_OK;
-  for (int f = 0; f < 4 && rc == PHAFD_OK; ++f) {
+  // the tensor-map x c2r replaces the register-resident merged x c2r only
+  const bool tma_ok = c->precision == PHAFD_FP32 && c->N[0] == 256 && c->N[1] % 32 == 0;
+  for (int f = 0; f < 8 && rc == PHAFD_OK; ++f) {
     ms[f] = -1.0;
     if ((f & PHAFD_TUNE_GENERIC256) && !has256) continue;
     if ((f & PHAFD_TUNE_PLANE) && (c->N[0] != c->N[1] || !c->have_conj)) continue;
+    if ((f & PHAFD_TUNE_XC2R_TMA) && (!tma_ok || (f & (PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256)))) continue;
     apply_variants(c, f);
     enqueue_run(c, 4);  // an eager step, then the graphs' captures
     CK(cudaStreamSynchronize(c->st));

@@ -9,5 +9,5 @@ template int GridOps<float>::xc2r(const Geom&, const cpx<float>*, float*, float,
                                 cudaStream_t);
 template int GridOps<float>::xc2r3(const Geom&, const cpx<float>*, float*, float*, const cpx<float>*, float*, const cpx<float>*, float*,
                                  float, float, const cpx<float>*, const NanArgs&, const NanArgs&, const uint32_t*, const int*,
-                                 cudaStream_t);
+                                 int*, cudaStream_t);
 }

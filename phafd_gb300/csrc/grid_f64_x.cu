@@ -9,5 +9,5 @@ template int GridOps<double>::xc2r(const Geom&, const cpx<double>*, double*, dou
                                 cudaStream_t);
 template int GridOps<double>::xc2r3(const Geom&, const cpx<double>*, double*, double*, const cpx<double>*, double*, const cpx<double>*, double*,
                                  double, double, const cpx<double>*, const NanArgs&, const NanArgs&, const uint32_t*, const int*,
-                                 cudaStream_t);
+                                 int*, cudaStream_t);
 }

@@ -727,7 +727,7 @@ int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw
 template <typename T>
 int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E, T* gz, T sp,
           T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
-          const int* gmask_off, cudaStream_t st);
+          const int* gmask_off, int* status, cudaStream_t st);
 template <typename T>
 int ypass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw, cudaStream_t st);
 template <typename T>
@@ -765,8 +765,9 @@ int GridOps<T>::xc2r(const Geom& g, const cpx<T>* in, T* out0, T s0, bool mul0, 
 template <typename T>
 int GridOps<T>::xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E,
                       T* gz, T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan,
-                      const uint32_t* gmask, const int* gmask_off, cudaStream_t st) {
-  if (g.nx == 256 && !g.generic256) return r256::xc2r3<T>(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);
+                      const uint32_t* gmask, const int* gmask_off, int* status, cudaStream_t st) {
+  if (g.nx == 256 && !g.generic256)
+    return r256::xc2r3<T>(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, status, st);
   switch (g.nx) {
 #define CASE(n) \
   case n: return Axis<T, n>::xc2r3(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, nonan, gmask, gmask_off, st);

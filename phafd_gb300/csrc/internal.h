@@ -11,6 +11,7 @@ struct Geom {
   int nx, ny, nz, nxh;
   double kq[3];  // 2*3.141592/L per physical axis (domain.cpp:206-208)
   int generic256;  // 256-point axes take the shared-memory tile transforms, not the register-resident ones
+  int xc2r_tma = 1;  // FP32 merged x c2r on 256-point rows fed by tensor-map loads (persistent grid)
 };
 
 struct FHArgs {
@@ -74,10 +75,11 @@ struct GridOps {
   // dphi/dz from E) and two inverse y passes (A -> C, D; B -> E) as one
   // launch each (-3: not available for this length)
   // (gmask: node bitset; unless gmask is null or *gmask_off is set, the three
-  // gradients are stored at set bits only)
+  // gradients are stored at set bits only; status: device status word that a
+  // pass with bounded waits flags with ST_TIMEOUT)
   static int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E, T* gz,
                    T sp, T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
-                   const int* gmask_off, cudaStream_t st);
+                   const int* gmask_off, int* status, cudaStream_t st);
   static int yinv2(const Geom& g, const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E,
                    const cpx<T>* tw, cudaStream_t st);
   static int zpass(const Geom& g, int sign, const cpx<T>* in, cpx<T>* out0, cpx<T>* out1, const cpx<T>* tw,

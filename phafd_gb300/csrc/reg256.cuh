@@ -15,6 +15,7 @@
 // element-major [e][column], conflict-free for both stage directions.
 #pragma once
 #include "grid_impl.cuh"
+#include "tma.cuh"
 
 namespace phafd {
 namespace r256 {
@@ -220,12 +221,51 @@ k_yinv2row256(const cpx<T>* __restrict__ A, cpx<T>* __restrict__ C, cpx<T>* __re
 // output with a mask go only to the 32-byte sectors whose bit is set.
 constexpr int RX = N + N / 16 + 1;
 
+// x c2r of one line, second part: element j + 16 r of the line's transform
+// v holds nodes x = j + 16 r of rows y0 (real part) and y0 + 1 (imaginary
+// part) of plane z; they are stored scaled by sc.  PHI: the phi output,
+// which also gets nan.offset, runs the step's NaN check and is stored
+// everywhere; otherwise a gradient, stored only to the 32-byte sectors set in
+// msk unless msk is null.
+template <typename T, bool PHI>
+PHAFD_D void xc2r_store256(const cpx<T>* v, int j, int y0, int z, T* __restrict__ out, T sc, int Ny,
+                           const NanArgs& nan, const uint32_t* msk) {
+  constexpr int G = 32 / (int)sizeof(T);  // nodes per 32-byte sector
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int y = y0 + h;
+    if (y >= Ny) continue;
+    const size_t row = ((size_t)z * Ny + y) * N;
+    if (PHI || !msk) {
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        const T val = (h == 0 ? v[r].x : v[r].y) * sc;
+        out[row + j + 16 * r] = PHI ? val + (T)nan.offset : val;
+      }
+    } else {
+      // the row's sectors are N / G consecutive bits starting at a word boundary
+      const uint32_t m0 = msk[(row / G) >> 5];
+      const uint32_t m1 = N / G > 32 ? msk[((row / G) >> 5) + 1] : 0u;
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        const int x = j + 16 * r;
+        const int sec = x / G;
+        const uint32_t bit = sec < 32 ? (m0 >> sec) & 1u : (m1 >> (sec & 31)) & 1u;
+        if (bit) out[row + x] = (h == 0 ? v[r].x : v[r].y) * sc;
+      }
+    }
+    // integrate.cpp:190: the step's NaN check reads phi at node (0, 0, 0)
+    if (PHI && nan.check && z == 0 && y == 0 && j == 0 && isnan(v[0].x * sc))
+      atomicCAS(reinterpret_cast<unsigned long long*>(nan.nan_step), (unsigned long long)-1LL,
+                (unsigned long long)(*nan.d_step));
+  }
+}
+
 template <typename T, int NOUT>
 PHAFD_D void xc2r_tile256(int bx, int z, const cpx<T>* __restrict__ in, T* __restrict__ out0,
                           T* __restrict__ out1, T s0, T s1, T dq, const cpx<T>* __restrict__ tw, int Ny, int Nz,
                           const NanArgs& nan, const uint32_t* mask0, const uint32_t* mask1, unsigned char* smraw) {
   constexpr int LP = W / NOUT;
-  constexpr int G = 32 / (int)sizeof(T);  // nodes per 32-byte sector
   cpx<T>* zs = reinterpret_cast<cpx<T>*>(smraw);
   const int y0 = bx * 2 * LP;
   TILE_LOOP(idx, (N / 2 + 1) * LP, 256) {  // unrolled: every load of a thread in flight at once
@@ -265,35 +305,9 @@ PHAFD_D void xc2r_tile256(int bx, int z, const cpx<T>* __restrict__ in, T* __res
   for (int r = 0; r < 16; ++r) v[r] = rb[j + 17 * r];  // element j + 16 r
   __syncwarp();
   row256<T, +1>(v, rb, j, tw);
-  T* out = q == 0 ? out0 : out1;
-  const T sc = q == 0 ? s0 : s1;
-  const uint32_t* msk = q == 0 ? mask0 : mask1;
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int y = y0 + 2 * l + h;
-    if (y >= Ny) continue;
-    const size_t row = ((size_t)z * Ny + y) * N;
-    // the row's sectors are N / G consecutive bits starting at a word boundary
-    uint32_t m0 = ~0u, m1 = ~0u;
-    if (msk) {
-      m0 = msk[(row / G) >> 5];
-      if constexpr (N / G > 32) m1 = msk[((row / G) >> 5) + 1];
-    }
-#pragma unroll
-    for (int r = 0; r < 16; ++r) {
-      const int x = j + 16 * r;
-      const T val = (h == 0 ? v[r].x : v[r].y) * sc + (q == 0 ? (T)nan.offset : (T)0);
-      const int sec = x / G;
-      uint32_t bit;
-      if constexpr (N / G <= 32) bit = (m0 >> sec) & 1u;
-      else bit = sec < 32 ? (m0 >> sec) & 1u : (m1 >> (sec & 31)) & 1u;
-      if (bit) out[row + x] = val;
-    }
-    // integrate.cpp:190: the step's NaN check reads phi at node (0, 0, 0)
-    if (q == 0 && nan.check && z == 0 && y == 0 && j == 0 && isnan(v[0].x * sc))
-      atomicCAS(reinterpret_cast<unsigned long long*>(nan.nan_step), (unsigned long long)-1LL,
-                (unsigned long long)(*nan.d_step));
-  }
+  if (NOUT == 2 && q == 0) xc2r_store256<T, true>(v, j, y0 + 2 * l, z, out0, s0, Ny, nan, nullptr);
+  else xc2r_store256<T, false>(v, j, y0 + 2 * l, z, q == 0 ? out0 : out1, q == 0 ? s0 : s1, Ny, nan,
+                               q == 0 ? mask0 : mask1);
 }
 
 // x r2c of 256-point rows, optionally fused with mu = deposit + FH(phi)
@@ -435,10 +449,177 @@ k_xc2r3_256(const cpx<T>* __restrict__ C, T* __restrict__ phi, T* __restrict__ g
     xc2r_tile256<T, 1>(bx - nb0 - nb1, z, E, gz, nullptr, sg, sg, dq, tw, Ny, Nz, nonan, gm, nullptr, smraw);
 }
 
+// The same three x c2r fed by the tensor memory accelerator (FP32, Ny a
+// multiple of 32): a persistent grid whose CTAs walk the tiles of
+// k_xc2r3_256, numbered plane by plane (per plane z: nb0 tiles of C, nb1
+// of D, nb1 of E), with the grid's stride.  A tile's half-spectrum block
+// (kx = 0..128 by the tile's row pairs) arrives as one or two tensor-map
+// boxes of 129 rows x 128 bytes in a 1024-byte-aligned buffer, 128-byte
+// swizzled (16-byte chunk c of row k at chunk c ^ (k & 7)), so the 16 lanes
+// of a line, which read one pair column at 16 different kx, hit different
+// banks.  Each thread reads its line's 16 elements straight from the block
+// and Hermitian-completes them on the fly.  After the first DFT-16 the
+// block is dead and the same buffer serves as the lines' exchange buffer;
+// once every line has read its exchange back, thread 0 queues the loads of
+// the CTA's next tile into the buffer, which land while the CTA finishes the
+// transform and the stores of the current tile.  A load that does not land
+// within the wait limit sets ST_TIMEOUT and ends the CTA.
+constexpr int XT_BOX = (N / 2 + 1) * 128;  // bytes of one 129 x 128-byte box
+constexpr int XT_HALF = 17 * 1024;         // second box of a one-output tile, 1024-byte aligned
+constexpr int XT_BUF = W * RX * 8;         // the FP32 exchange buffer of 16 lines
+static_assert(XT_HALF + XT_BOX <= XT_BUF, "both boxes of a tile fit in the exchange buffer");
+constexpr size_t XT_SMEM = XT_BUF + 1024 + 16;  // + alignment slack + the mbarrier
+
+struct XTile {
+  int kind, z, y0;  // kind 0: C (phi and dphi/dx, 8 row pairs), 1: D (dphi/dy), 2: E (dphi/dz) (16 pairs)
+};
+PHAFD_D XTile xt_tile(int t, int nb0, int nb1) {
+  const int tp = nb0 + 2 * nb1;
+  XTile x;
+  x.z = t / tp;
+  int b = t - x.z * tp;
+  if (b < nb0) {
+    x.kind = 0;
+    x.y0 = b * W;
+  } else if ((b -= nb0) < nb1) {
+    x.kind = 1;
+    x.y0 = b * 2 * W;
+  } else {
+    x.kind = 2;
+    x.y0 = (b - nb1) * 2 * W;
+  }
+  return x;
+}
+
+// thread 0: the loads of tile x's block into buf, completing on bar
+PHAFD_D void xt_issue(const XTile& x, const CUtensorMap* mC, const CUtensorMap* mD, const CUtensorMap* mE,
+                      unsigned char* buf, uint64_t* bar) {
+  const CUtensorMap* m = x.kind == 0 ? mC : x.kind == 1 ? mD : mE;
+  tc::fence_async_smem();  // the buffer's earlier generic-proxy accesses come before the loads' writes
+  tma::arrive_expect(bar, (x.kind == 0 ? 1u : 2u) * (uint32_t)XT_BOX);
+  tma::load3d(buf, m, 2 * x.y0, x.z, 0, bar);
+  if (x.kind != 0) tma::load3d(buf + XT_HALF, m, 2 * x.y0 + 32, x.z, 0, bar);
+}
+
+// (MINB: CTAs per SM the register allocation is fitted to)
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB)
+k_xc2r3t_256(const __grid_constant__ CUtensorMap mC, const __grid_constant__ CUtensorMap mD,
+             const __grid_constant__ CUtensorMap mE, float* __restrict__ phi, float* __restrict__ gx,
+             float* __restrict__ gy, float* __restrict__ gz, float sp, float sg, float dq,
+             const cpx<float>* __restrict__ tw, int Ny, int Nz, NanArgs nan, const uint32_t* __restrict__ mask,
+             const int* __restrict__ mask_off, int* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char* buf = smraw + ((1024u - (tc::smem_u32(smraw) & 1023u)) & 1023u);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(buf + XT_BUF);
+  const int nb0 = Ny / W, nb1 = Ny / (2 * W);
+  const int ntiles = (nb0 + 2 * nb1) * Nz;
+  const uint32_t* gm = mask && !*mask_off ? mask : nullptr;
+  const int j = threadIdx.x & 15, c = threadIdx.x >> 4;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(bar, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  int t = blockIdx.x;
+  if (threadIdx.x == 0 && t < ntiles) xt_issue(xt_tile(t, nb0, nb1), &mC, &mD, &mE, buf, bar);
+  uint32_t phase = 0;
+  bool failed = false;
+  for (; t < ntiles; t += gridDim.x, phase ^= 1u) {
+    const XTile x = xt_tile(t, nb0, nb1);
+    const bool got = tc::mbar_wait(bar, phase);
+    // line c: output q of row pair l (kind 0: q = c / 8, l = c % 8; else q = 0, l = c)
+    const int q = x.kind == 0 ? c >> 3 : 0;
+    const int l = x.kind == 0 ? c & 7 : c;
+    const unsigned char* box = buf + (l >= 8 ? XT_HALF : 0);
+    const int ch = l & 7;
+    cpx<float> v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {  // element e = j + 16 r of the line: mode k = e (e < 128) or N - e
+      const int e = j + 16 * r;
+      const int k = r < 8 ? e : N - e;
+      const float4 p = *reinterpret_cast<const float4*>(box + k * 128 + ((ch ^ (k & 7)) << 4));
+      cpx<float> a = mk<float>(p.x, p.y), b = mk<float>(p.z, p.w);
+      if (q == 1) {
+        a = deriv(a, dq, k);
+        b = deriv(b, dq, k);
+      }
+      if ((r == 0 || r == 8) && j == 0) {  // k = 0 (r = 0) or N / 2 (r = 8): only at lane 0
+        a.y = 0.f;
+        b.y = 0.f;
+      }
+      v[r] = r < 8 ? mk<float>(a.x - b.y, a.y + b.x) : mk<float>(a.x + b.y, b.x - a.y);
+    }
+    fft::dft16<+1>(v);
+    if (__syncthreads_or(!got)) {  // every line has read the block
+      failed = true;
+      break;
+    }
+    cpx<float>* rb = reinterpret_cast<cpx<float>*>(buf) + c * RX;
+    rput16(rb, v, j);
+    __syncwarp();
+    rget16(rb, v, j);
+    __syncthreads();  // the buffer is free for the next block
+    if (threadIdx.x == 0 && t + (int)gridDim.x < ntiles)
+      xt_issue(xt_tile(t + (int)gridDim.x, nb0, nb1), &mC, &mD, &mE, buf, bar);
+    twiddle16<float, +1>(v, j, tw);
+    fft::dft16<+1>(v);
+    if (x.kind == 0 && q == 0) xc2r_store256<float, true>(v, j, x.y0 + 2 * l, x.z, phi, sp, Ny, nan, nullptr);
+    else xc2r_store256<float, false>(v, j, x.y0 + 2 * l, x.z, x.kind == 0 ? gx : x.kind == 1 ? gy : gz, sg, Ny, nan, gm);
+  }
+  if (failed && threadIdx.x == 0) {
+    atomicOr(status, ST_TIMEOUT);
+    tc::mbar_wait(bar, phase);  // give the late loads time to land before the CTA's shared memory is released
+  }
+}
+
+// launch of k_xc2r3t_256: -3 when it does not apply (tensor maps unavailable)
+inline int xc2r3_tma(const Geom& g, const cpx<float>* C, float* phi, float* gx, const cpx<float>* D, float* gy,
+                     const cpx<float>* E, float* gz, float sp, float sg, const cpx<float>* tw, const NanArgs& nan,
+                     const uint32_t* gmask, const int* gmask_off, int* status, cudaStream_t st) {
+  CUtensorMap m[3];
+  const cpx<float>* src[3] = {C, D, E};
+  for (int i = 0; i < 3; ++i)
+    if (!tma::map3d_f32(&m[i], src[i], 2 * (uint64_t)g.ny, (uint64_t)g.nz, (uint64_t)g.nxh, 32, 1, N / 2 + 1,
+                        CU_TENSOR_MAP_SWIZZLE_128B))
+      return -3;
+  auto k = k_xc2r3t_256<5>;
+  if (set_smem(k, XT_SMEM)) return -1;
+  // resident CTAs of the device, found once per device (outside graph capture: the first launch is eager)
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+  static std::mutex mu;
+  static std::map<int, int> resident;
+  int slots = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = resident.find(dev);
+    if (it == resident.end()) {
+      int sms = 0, per_sm = 0;
+      if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, XT_SMEM) != cudaSuccess || per_sm < 1)
+        return -1;
+      it = resident.emplace(dev, sms * per_sm).first;
+    }
+    slots = it->second;
+  }
+  const long long ntiles = (long long)(g.ny / W + 2 * (g.ny / (2 * W))) * g.nz;
+  const int grid = (int)(ntiles < (long long)slots ? ntiles : (long long)slots);
+  k<<<grid, 256, XT_SMEM, st>>>(m[0], m[1], m[2], phi, gx, gy, gz, sp, sg, (float)g.kq[0], tw, g.ny, g.nz, nan, gmask,
+                                gmask_off, status);
+  return 0;
+}
+
 template <typename T>
 int xc2r3(const Geom& g, const cpx<T>* C, T* phi, T* gx, const cpx<T>* D, T* gy, const cpx<T>* E, T* gz, T sp,
           T sg, const cpx<T>* tw, const NanArgs& nan, const NanArgs& nonan, const uint32_t* gmask,
-          const int* gmask_off, cudaStream_t st) {
+          const int* gmask_off, int* status, cudaStream_t st) {
+  if constexpr (sizeof(T) == 4) {
+    if (g.xc2r_tma && g.ny % (2 * W) == 0 && status) {
+      const int rc = xc2r3_tma(g, C, phi, gx, D, gy, E, gz, sp, sg, tw, nan, gmask, gmask_off, status, st);
+      if (rc != -3) return rc;
+    }
+  }
   const size_t sm = (size_t)W * RX * sizeof(cpx<T>);
   const int nb0 = (g.ny + W - 1) / W, nb1 = (g.ny + 2 * W - 1) / (2 * W);
   auto k = k_xc2r3_256<T>;

@@ -276,6 +276,56 @@ def test_generic_256_point_plan_matches_oracle(gpu_lib, precision, tol):
         assert rel_err(g.grid_get(f), o.grid_get(f)) < (tol if precision == 64 else 1e-4), f
 
 
+def _field_run(nx, ny, nz, tma, steps=3):
+    g = gpu(32, "resident")
+    g.domain([-nx / 2, -ny / 2, -nz / 2], [float(nx), float(ny), float(nz)])
+    g.grid_style(nx, ny, nz)
+    g.grid_populate_constant(0.4, 0.02, 5)
+    g.fix_gradphi(once=False)
+    g.fix_conjugate_volfrac(15, mobility=1.0, temp=0.01, volFH=1.0, gamma=100.0, noise="philox")
+    g.fix_floryhuggins(temp=1.0, volFH=1.0, chi=3.0)
+    g.set_dt(1e-3)
+    g.set_timestep(0)
+    g.set_variants(xc2r_tma=tma)
+    g.setup()
+    g.run(steps)
+    out = {f: g.grid_get(f) for f in ("phi", "gradx", "grady", "gradz")}
+    g.close()
+    return out
+
+
+@pytest.mark.parametrize("shape", [(256, 256, 256), (256, 64, 32)])
+def test_tma_fed_x_c2r_equals_register_resident(gpu_lib, shape):
+    """The tensor-map fed persistent x c2r (PHAFD_TUNE_XC2R_TMA) forms the
+    same lines and runs the same transform as the register-resident merged
+    x c2r: without beads (no floating-point atomics anywhere in the step)
+    phi and the three gradients after three steps are bit-identical."""
+    a = _field_run(*shape, tma=False)
+    b = _field_run(*shape, tma=True)
+    for f in a:
+        assert np.abs(a[f]).max() > 0, f
+        assert np.array_equal(a[f], b[f]), f
+
+
+def test_tma_fed_x_c2r_with_beads_matches_oracle(gpu_lib):
+    """The tensor-map fed x c2r in a 256^3 FP32 step with chains (masked
+    gradient stores, neighbor rebuilds) against the FP64 oracle."""
+    cfg = dict(W.CONFIGS["32cube_64beads"])
+    cfg.update(n=256, L=256.0, origin=-128.0, nchains=4, chain_len=50, field_noise="philox", bead_temp=1.0,
+               dt=1e-4)
+    o = Oracle(); g = gpu(32, "resident")
+    g.set_variants(xc2r_tma=True)
+    chains = None
+    for d in (o, g):
+        chains = W.apply(d, cfg, chains=chains)
+        d.setup()
+        d.run(3)
+    assert rel_err(g.grid_get("phi"), o.grid_get("phi")) < 2e-5
+    xo, xg = o.atoms_get()[0], g.atoms_get()[0]
+    assert np.abs(xg - xo).max() < 1e-5 * np.abs(xo).max()
+    assert g.counters()["timestep"] == 3
+
+
 def test_autotune_steps_are_steps_of_the_run(gpu_lib):
     """The autotuner times each variant on the run's own steps: afterwards
     the state equals the oracle's after the same number of steps, and the
@@ -291,6 +341,7 @@ def test_autotune_steps_are_steps_of_the_run(gpu_lib):
     best, ms = g.autotune(steps=2)
     assert ms[0] > 0 and ms[1] > 0      # separate and plane-fused passes (64 x 64 planes)
     assert ms[2] < 0 and ms[3] < 0      # no 256-point axis
+    assert (ms[4:] < 0).all()           # the tensor-map x c2r: FP32 with Nx = 256 only
     assert best == int(np.argmin(np.where(ms > 0, ms, np.inf)))
     done = g.counters()["timestep"]
     assert done == 2 * (4 + 2)
