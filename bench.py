@@ -292,9 +292,11 @@ def run_gpu(args):
     sampler.start()
     g.run(max(args.warmup, 3))
     # the project's autotuner picks the kernel variants on the run's own steps
-    best, tune_ms = g.autotune(10) if not args.no_autotune else (4, np.zeros(8))
-    names = {0: "register-resident 256, x c2r loading its own tiles", 1: "plane-fused x/y", 2: "generic 256 tiles",
-             3: "plane-fused x/y + generic 256 tiles", 4: "register-resident 256, tensor-map fed x c2r (default)"}
+    best, tune_ms = g.autotune(10) if not args.no_autotune else (12, np.zeros(16))
+    names = {0: "register-resident 256, x passes loading their own tiles", 1: "plane-fused x/y", 2: "generic 256 tiles",
+             3: "plane-fused x/y + generic 256 tiles", 4: "register-resident 256, tensor-map fed x c2r",
+             8: "register-resident 256, tensor-map fed x r2c",
+             12: "register-resident 256, tensor-map fed x r2c and x c2r (default)"}
     autotune = {"best": names[best], "ms_per_step": {names[f]: (float(tune_ms[f]) if tune_ms[f] > 0 else None)
                                                       for f in names}}
 

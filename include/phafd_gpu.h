@@ -173,17 +173,21 @@ int phafd_set_gradient_mask(phafd_ctx* ctx, int on);
  *                          by tensor-map loads, each CTA's next tile landing
  *                          while it transforms the current one (in place of
  *                          the non-persistent grid that loads its own tiles)
+ *   PHAFD_TUNE_XR2C_TMA    the same for the x r2c (with the Flory-Huggins
+ *                          prologue) of phi's rows
  * phafd_set_variants selects a combination; a new context starts with
- * PHAFD_TUNE_XC2R_TMA (it has no effect where it does not apply).
+ * PHAFD_TUNE_XC2R_TMA | PHAFD_TUNE_XR2C_TMA (no effect where they do not
+ * apply).
  * phafd_autotune times every applicable combination over `steps` steps (rounded
  * up to even) of the run itself, after four warm-up steps that capture its
  * graphs, keeps the
  * fastest (*best) and writes the milliseconds per step of each combination
- * to ms[8], indexed by the flags (-1 where a combination does not apply).
+ * to ms[16], indexed by the flags (-1 where a combination does not apply).
  * The tuning steps advance the run like phafd_run. */
 #define PHAFD_TUNE_PLANE 1
 #define PHAFD_TUNE_GENERIC256 2
 #define PHAFD_TUNE_XC2R_TMA 4
+#define PHAFD_TUNE_XR2C_TMA 8
 int phafd_set_variants(phafd_ctx* ctx, int flags);
 int phafd_autotune(phafd_ctx* ctx, int steps, int* best, double* ms);
 #define PHAFD_CENTER_FH 1

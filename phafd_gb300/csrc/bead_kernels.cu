@@ -509,6 +509,7 @@ __global__ void k_step_begin(long long* d_step) { *d_step += 1; }
 // grid units split once per step into an integer part and a fraction, so the
 // per-entry arithmetic is (small integer - fraction) * dx in FP32.
 constexpr int PAIR_TPB = 4;
+constexpr int PB = 4;  // list entries a lane gathers at once
 
 // grid coordinates of a node index (shifts and masks for power-of-two grids)
 PHAFD_D void node_coords(const BeadArgs& a, uint32_t node, int g3[3]) {
@@ -528,6 +529,7 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gtid / PAIR_TPB, sub = gtid % PAIR_TPB;
   const bool live = i < a.n;
+  if (p.step_inc && gtid == 0) *p.step_inc += 1;
   const int ii = live ? i : 0;
   const double xi0 = a.x[3 * ii], xi1 = a.x[3 * ii + 1], xi2 = a.x[3 * ii + 2];
   // Kahan-compensated sums (exact no-ops in double beyond round-off)
@@ -538,24 +540,43 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
     c[d] = (t - f[d]) - y;
     f[d] = t;
   };
+  // Both loops take their entries in batches of PB per lane: the list words
+  // of a batch are loaded together, then every load the batch's entries need,
+  // then the arithmetic, in the entries' order k = sub, sub + PAIR_TPB, ...
+  // (the compensated sums see the same sequence as one entry at a time).
   if (live && p.lj && a.nbr) {
     const int cnt = a.nnbr[i];
-    for (int k = sub; k < cnt; k += PAIR_TPB) {
-      const int e = a.nbr[(size_t)i * a.maxnb + k];
-      const int j = e >> 5, code = e & 31;
-      const double d0 = xi0 - (a.x[3 * j] + img_shift(code, 0, a));
-      const double d1 = xi1 - (a.x[3 * j + 1] + img_shift(code, 1, a));
-      const double d2 = xi2 - (a.x[3 * j + 2] + img_shift(code, 2, a));
-      const T dx = (T)d0, dy = (T)d1, dz = (T)d2;
-      const T rsq = dx * dx + dy * dy + dz * dz;
-      if (rsq < (T)p.lj_cutsq) {
-        const T r2inv = (T)1 / rsq;
-        const T r6inv = r2inv * r2inv * r2inv;
-        const T forcelj = r6inv * ((T)p.lj1 * r6inv - (T)p.lj2);
-        const T fpair = forcelj * r2inv;
-        add(0, dx * fpair);
-        add(1, dy * fpair);
-        add(2, dz * fpair);
+    const int* __restrict__ nl = a.nbr + (size_t)i * a.maxnb;
+    for (int k0 = sub; k0 < cnt; k0 += PAIR_TPB * PB) {
+      int e[PB];
+#pragma unroll
+      for (int b = 0; b < PB; ++b) e[b] = k0 + b * PAIR_TPB < cnt ? nl[k0 + b * PAIR_TPB] : -1;
+      double xj[PB][3];
+#pragma unroll
+      for (int b = 0; b < PB; ++b) {
+        const int j = e[b] >= 0 ? e[b] >> 5 : ii;
+        xj[b][0] = a.x[3 * j];
+        xj[b][1] = a.x[3 * j + 1];
+        xj[b][2] = a.x[3 * j + 2];
+      }
+#pragma unroll
+      for (int b = 0; b < PB; ++b) {
+        if (e[b] < 0) continue;
+        const int code = e[b] & 31;
+        const double d0 = xi0 - (xj[b][0] + img_shift(code, 0, a));
+        const double d1 = xi1 - (xj[b][1] + img_shift(code, 1, a));
+        const double d2 = xi2 - (xj[b][2] + img_shift(code, 2, a));
+        const T dx = (T)d0, dy = (T)d1, dz = (T)d2;
+        const T rsq = dx * dx + dy * dy + dz * dz;
+        if (rsq < (T)p.lj_cutsq) {
+          const T r2inv = (T)1 / rsq;
+          const T r6inv = r2inv * r2inv * r2inv;
+          const T forcelj = r6inv * ((T)p.lj1 * r6inv - (T)p.lj2);
+          const T fpair = forcelj * r2inv;
+          add(0, dx * fpair);
+          add(1, dy * fpair);
+          add(2, dz * fpair);
+        }
       }
     }
   }
@@ -563,6 +584,7 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
     const int cnt = a.ngl[i];
     const int t = a.type[i];
     const T cutsq = (T)p.ga_cutsq[t], eps = (T)p.ga_eps[t], phit = (T)p.ga_phi[t];
+    const bool linear = p.ga_style != PHAFD_GRIDATOM_GAUSSIAN && p.ga_style != PHAFD_GRIDATOM_LJISH;
     // bead position in grid units: integer part + fraction (FP32 path; GB300's
     // FP64 rate makes a divide per axis and thread cost more than the rest)
     int gi[3];
@@ -575,49 +597,75 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
       gf[d] = (T)(ud - fl);
       dxf[d] = (T)a.dx[d];
     }
-    for (int k = sub; k < cnt; k += PAIR_TPB) {
-      const uint32_t e = a.gl[(size_t)i * a.maxg + k];
-      const uint32_t node = e >> 5;
-      const int code = (int)(e & 31u);
-      int g3[3];
-      node_coords(a, node, g3);
-      T dd[3];
-      if constexpr (sizeof(T) == 8) {
-        // node coordinate k*dx + boxlo without contraction (npair_grid_bin.cpp:76-88)
-        for (int d = 0; d < 3; ++d)
-          dd[d] = __dadd_rn(__dmul_rn((double)g3[d], a.dx[d]), a.boxlo[d]) - (xi[d] + img_shift(code, d, a));
-      } else {
-        const int sc[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
-        for (int d = 0; d < 3; ++d) dd[d] = ((T)(g3[d] - gi[d] - sc[d] * a.N[d]) - gf[d]) * dxf[d];
+    const uint32_t* __restrict__ gl = a.gl + (size_t)i * a.maxg;
+    for (int k0 = sub; k0 < cnt; k0 += PAIR_TPB * PB) {
+      uint32_t e[PB];
+#pragma unroll
+      for (int b = 0; b < PB; ++b) e[b] = k0 + b * PAIR_TPB < cnt ? gl[k0 + b * PAIR_TPB] : 0xffffffffu;
+      // separations and the cutoff test (no loads)
+      T rs[PB];
+      bool in[PB];
+#pragma unroll
+      for (int b = 0; b < PB; ++b) {
+        in[b] = false;
+        rs[b] = (T)0;
+        if (e[b] == 0xffffffffu) continue;
+        const uint32_t node = e[b] >> 5;
+        const int code = (int)(e[b] & 31u);
+        int g3[3];
+        node_coords(a, node, g3);
+        T dd[3];
+        if constexpr (sizeof(T) == 8) {
+          // node coordinate k*dx + boxlo without contraction (npair_grid_bin.cpp:76-88)
+          for (int d = 0; d < 3; ++d)
+            dd[d] = __dadd_rn(__dmul_rn((double)g3[d], a.dx[d]), a.boxlo[d]) - (xi[d] + img_shift(code, d, a));
+        } else {
+          const int sc[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+          for (int d = 0; d < 3; ++d) dd[d] = ((T)(g3[d] - gi[d] - sc[d] * a.N[d]) - gf[d]) * dxf[d];
+        }
+        const T rsq = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
+        in[b] = (p.ga_style == PHAFD_GRIDATOM_GAUSSIAN) ? (rsq <= cutsq) : (rsq < cutsq);
+        rs[b] = rsq / cutsq;
       }
-      const T dx = dd[0], dy = dd[1], dz = dd[2];
-      T rsq = dx * dx + dy * dy + dz * dz;
-      const bool inside = (p.ga_style == PHAFD_GRIDATOM_GAUSSIAN) ? (rsq <= cutsq) : (rsq < cutsq);
-      if (!inside) continue;
-      rsq = rsq / cutsq;
-      T expfac, mu_add;
-      if (p.ga_style == PHAFD_GRIDATOM_GAUSSIAN) {
-        // pair_gridatom_gaussian.cpp:97-107
-        expfac = (exp(-rsq / (T)2.0) - exp((T)-0.5)) * exp((T)0.5) * eps;
-        const T delphi = p.phi[node] - phit;
-        mu_add = (T)2 * delphi * expfac;
-        expfac = expfac * ((T)2 * delphi * (T)p.dv);
-      } else if (p.ga_style == PHAFD_GRIDATOM_LJISH) {
-        // pair_gridatom_lj_ish.cpp:104-176
-        expfac = exp((T)-1. / ((T)1 - rsq) + (T)1) * eps;
-        const T delphi = p.phi[node] - phit;
-        mu_add = (T)2 * delphi * expfac;
-        expfac = expfac * ((T)2 * delphi * (T)p.dv);
-      } else {
-        // pair_gridatom_lj_ish_linear.cpp:104-168
-        expfac = (T)-1 * exp((T)-1. / ((T)1 - rsq) + (T)1) * eps;
-        mu_add = expfac;
-        expfac = expfac * (T)p.dv;
+      // the node values of the entries inside the cutoff
+      T ph[PB], q0[PB], q1[PB], q2[PB];
+#pragma unroll
+      for (int b = 0; b < PB; ++b) {
+        const uint32_t node = in[b] ? e[b] >> 5 : 0u;
+        ph[b] = in[b] && !linear ? p.phi[node] : (T)0;
+        q0[b] = in[b] ? p.gx[node] : (T)0;
+        q1[b] = in[b] ? p.gy[node] : (T)0;
+        q2[b] = in[b] ? p.gz[node] : (T)0;
       }
-      if (p.dep) atomicAdd(p.dep + node, mu_add);  // null: forces only (substeps of a macro step)
-      add(0, -p.gx[node] * expfac);
-      add(1, -p.gy[node] * expfac);
-      add(2, -p.gz[node] * expfac);
+#pragma unroll
+      for (int b = 0; b < PB; ++b) {
+        if (!in[b]) continue;
+        const uint32_t node = e[b] >> 5;
+        const T rsq = rs[b];
+        T expfac, mu_add;
+        if (p.ga_style == PHAFD_GRIDATOM_GAUSSIAN) {
+          // pair_gridatom_gaussian.cpp:97-107
+          expfac = (exp(-rsq / (T)2.0) - exp((T)-0.5)) * exp((T)0.5) * eps;
+          const T delphi = ph[b] - phit;
+          mu_add = (T)2 * delphi * expfac;
+          expfac = expfac * ((T)2 * delphi * (T)p.dv);
+        } else if (p.ga_style == PHAFD_GRIDATOM_LJISH) {
+          // pair_gridatom_lj_ish.cpp:104-176
+          expfac = exp((T)-1. / ((T)1 - rsq) + (T)1) * eps;
+          const T delphi = ph[b] - phit;
+          mu_add = (T)2 * delphi * expfac;
+          expfac = expfac * ((T)2 * delphi * (T)p.dv);
+        } else {
+          // pair_gridatom_lj_ish_linear.cpp:104-168
+          expfac = (T)-1 * exp((T)-1. / ((T)1 - rsq) + (T)1) * eps;
+          mu_add = expfac;
+          expfac = expfac * (T)p.dv;
+        }
+        if (p.dep) atomicAdd(p.dep + node, mu_add);  // null: forces only (substeps of a macro step)
+        add(0, -q0[b] * expfac);
+        add(1, -q1[b] * expfac);
+        add(2, -q2[b] * expfac);
+      }
     }
   }
   // combine the PAIR_TPB partial sums of a bead (adjacent lanes)

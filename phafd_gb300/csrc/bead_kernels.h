@@ -68,6 +68,10 @@ struct PairArgs {
   const T *phi, *gx, *gy, *gz;
   T* dep;
   double dv;
+  // the step counter, incremented by the kernel when the step's neighbor
+  // check (which otherwise increments it) ran early, on the previous step's
+  // bead branch (null: no increment)
+  long long* step_inc;
 };
 
 void launch_step_begin(long long* d_step, cudaStream_t st);

@@ -203,11 +203,13 @@ struct phafd_ctx {
   FHArgs plain_fh() const {  // r2c of phi without the Flory-Huggins prologue
     FHArgs f{0, 0, fh_counters(), 0, nullptr};
     center(f, PHAFD_CENTER_FFT);
+    f.status = d_status();
     return f;
   }
   FHArgs step_fh() const {  // mu = deposit + FH(phi), fused into the x r2c of a step
     FHArgs f{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
     center(f, PHAFD_CENTER_FH);
+    f.status = d_status();
     return f;
   }
   // N f(c) tv: what the k = 0 mode of a centered mu spectrum lacks
@@ -272,7 +274,15 @@ struct phafd_ctx {
   int* d_gmask_off() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 6) + 1; }
   // graph
   cudaGraphExec_t gexec = nullptr;
+  cudaGraphExec_t gexecK = nullptr;                 // GRAPH_STEPS steps (resident)
+  int graph_curK = 0;
   cudaGraphExec_t gexec1[2] = {nullptr, nullptr};  // one step, per spectrum parity (resident)
+  // Inside a multi-step graph the neighbor check (and conditional rebuild) of
+  // every step but the first runs at the end of the previous step's bead
+  // branch, where it overlaps that step's inverse chain: check_next_early is
+  // set while such a step is captured, check_done_early while the step
+  // whose check ran early is captured.
+  bool check_next_early = false, check_done_early = false;
   bool eager_done = false;
   long long kernels_per_step = 0;
   long long rebuild_kernels = 0;  // kernels of the conditional rebuild body
@@ -289,6 +299,7 @@ struct phafd_ctx {
 
   ~phafd_ctx() {
     if (gexec) cudaGraphExecDestroy(gexec);
+    if (gexecK) cudaGraphExecDestroy(gexecK);
     for (auto ge : gexec1)
       if (ge) cudaGraphExecDestroy(ge);
     if (uref_h) cudaFreeHost(uref_h);
@@ -304,6 +315,8 @@ struct phafd_ctx {
   void invalidate_graph() {
     if (gexec) cudaGraphExecDestroy(gexec);
     gexec = nullptr;
+    if (gexecK) cudaGraphExecDestroy(gexecK);
+    gexecK = nullptr;
     for (auto& ge : gexec1) {
       if (ge) cudaGraphExecDestroy(ge);
       ge = nullptr;
@@ -711,15 +724,23 @@ struct phafd_ctx {
     // the neighbor check increments the step counter when it runs first
     const bool fold_step = resident && n > 0;
     if (!fold_step) launch_step_begin(d_step(), st);
+    // the check may run on the previous step's bead branch when nothing
+    // between the two reads the beads: no gradient mask (whose guard and
+    // rebuild the inverse chain reads), no touch test at the step's end, no
+    // bead substeps; the pair kernel then increments the step counter
+    const bool pairs_run = n > 0 && (have_lj || ga_style != PHAFD_GRIDATOM_NONE);
+    const bool early_ok = resident && !profiling && pairs_run && nsub <= 1 && !touch_on && !gmask_steps();
+    const bool checked = early_ok && check_done_early;
     // fixgrid_gradphi.cpp:45: "once" tests timestep == firststep after the
     // increment, which never holds inside a run: only "every" recomputes
     if (!resident && (have_conj || (have_gradphi && !gradphi_once))) gradient_from_phi<T>();
     mark(0);
     // neighbor
-    if (n > 0) neighbor_stage(nullptr, fold_step ? d_step() : nullptr);
+    if (n > 0 && !checked) neighbor_stage(nullptr, fold_step ? d_step() : nullptr);
     mark(1);
     // pairs (computed once: the reference's second pass reproduces the first, integrate.cpp:140-146)
     PairArgs<T> pa = pair_args<T>();
+    if (checked) pa.step_inc = d_step();
     if (n > 0 && pair_snapshot && bx_pair.p)
       CK(cudaMemcpyAsync(bx_pair.p, bx.p, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     if (n > 0 && (have_lj || ga_style != PHAFD_GRIDATOM_NONE)) launch_pair<T>(ba, pa, st);
@@ -757,12 +778,14 @@ struct phafd_ctx {
           mark(4);
           dep_reset<T>(fork);
           macro_bead_substeps<T>(bs);
+          if (early_ok && check_next_early && fork) neighbor_stage(st2, nullptr);
           chk(GridOps<T>::ypass(geom, -1, W1, W1, nullptr, twf[1], st), "y fft");
         } else {
           chk(prc, "xy fwd");
           mark(4);
           dep_reset<T>(fork);
           macro_bead_substeps<T>(bs);
+          if (early_ok && check_next_early && fork) neighbor_stage(st2, nullptr);
         }
         mark(5);
         mark(6);
@@ -1567,12 +1590,13 @@ static void apply_variants(phafd_ctx* c, int flags) {
   c->use_plane = (flags & PHAFD_TUNE_PLANE) != 0;
   c->geom.generic256 = (flags & PHAFD_TUNE_GENERIC256) ? 1 : 0;
   c->geom.xc2r_tma = (flags & PHAFD_TUNE_XC2R_TMA) ? 1 : 0;
+  c->geom.xr2c_tma = (flags & PHAFD_TUNE_XR2C_TMA) ? 1 : 0;
   c->invalidate_graph();
 }
 
 int phafd_set_variants(phafd_ctx* c, int flags) {
   API_BEGIN(c)
-  if (flags & ~(PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256 | PHAFD_TUNE_XC2R_TMA))
+  if (flags & ~(PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256 | PHAFD_TUNE_XC2R_TMA | PHAFD_TUNE_XR2C_TMA))
     throw std::invalid_argument("unknown kernel variant");
   apply_variants(c, flags);
   API_END(c)
@@ -1593,13 +1617,14 @@ int phafd_autotune(phafd_ctx* c, int steps, int* best, double* ms) {
   double best_ms = 1e300;
   int best_flags = 0;
   int rc = PHAFD_OK;
-  // the tensor-map x c2r replaces the register-resident merged x c2r only
+  // the tensor-map x passes replace the register-resident x passes only
   const bool tma_ok = c->precision == PHAFD_FP32 && c->N[0] == 256 && c->N[1] % 32 == 0;
-  for (int f = 0; f < 8 && rc == PHAFD_OK; ++f) {
+  const int tma_bits = PHAFD_TUNE_XC2R_TMA | PHAFD_TUNE_XR2C_TMA;
+  for (int f = 0; f < 16 && rc == PHAFD_OK; ++f) {
     ms[f] = -1.0;
     if ((f & PHAFD_TUNE_GENERIC256) && !has256) continue;
     if ((f & PHAFD_TUNE_PLANE) && (c->N[0] != c->N[1] || !c->have_conj)) continue;
-    if ((f & PHAFD_TUNE_XC2R_TMA) && (!tma_ok || (f & (PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256)))) continue;
+    if ((f & tma_bits) && (!tma_ok || (f & (PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256)))) continue;
     apply_variants(c, f);
     enqueue_run(c, 4);  // an eager step, then the graphs' captures
     CK(cudaStreamSynchronize(c->st));
@@ -1706,8 +1731,13 @@ int phafd_run_async(phafd_ctx* c, int nsteps) {
   API_END(c)
 }
 
+// steps captured in one graph for runs of at least that many (even: both
+// spectrum parities of the resident schedule)
+constexpr int GRAPH_STEPS = 8;
+
 static void enqueue_run(phafd_ctx* c, int nsteps) {
   {
+  c->check_done_early = c->check_next_early = false;  // set only while a multi-step graph is captured
   const bool use_graph = c->c_noise != PHAFD_NOISE_REFERENCE || !c->have_conj;
   const bool resident = c->schedule == PHAFD_SCHEDULE_RESIDENT && c->have_conj;
   for (int s = 0; s < nsteps; ++s) {
@@ -1721,28 +1751,37 @@ static void enqueue_run(phafd_ctx* c, int nsteps) {
       CK(cudaGetLastError());
       if (use_graph) c->eager_done = true;
     } else {
-      // Graphs: two steps (both spectrum parities of the resident schedule)
-      // for runs of two or more, one step per parity for the rest.
-      if (resident && nsteps - s >= 2 && (!c->gexec || c->cur == c->graph_cur)) {
-        if (!c->gexec) {
-          c->graph_cur = c->cur;
+      // Graphs: GRAPH_STEPS steps, then two (both spectrum parities of the
+      // resident schedule), one step per parity for the rest.
+      bool launched = false;
+      for (const int k : {GRAPH_STEPS, 2}) {
+        cudaGraphExec_t& ge = k == 2 ? c->gexec : c->gexecK;
+        int& gcur = k == 2 ? c->graph_cur : c->graph_curK;
+        if (!(resident && nsteps - s >= k && (!ge || c->cur == gcur))) continue;
+        if (!ge) {
+          gcur = c->cur;
           cudaGraph_t g;
           CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
-          c->step_once();
-          resident_spectrum_flip(c);
-          c->step_once();
-          resident_spectrum_flip(c);
+          for (int j = 0; j < k; ++j) {
+            c->check_done_early = j > 0;
+            c->check_next_early = j + 1 < k;
+            c->step_once();
+            resident_spectrum_flip(c);
+          }
+          c->check_done_early = c->check_next_early = false;
           CK(cudaStreamEndCapture(c->st, &g));
-          c->kernels_per_step = count_kernels(g) / 2;
-          CK(cudaGraphInstantiate(&c->gexec, g, 0));
+          c->kernels_per_step = count_kernels(g) / k;
+          CK(cudaGraphInstantiate(&ge, g, 0));
           cudaGraphDestroy(g);
         }
-        CK(cudaGraphLaunch(c->gexec, c->st));
-        ++s;
-        c->timestep += 2;
+        CK(cudaGraphLaunch(ge, c->st));
+        s += k - 1;
+        c->timestep += k;
         c->note_step();
-        continue;  // the pair of steps leaves cur unchanged
+        launched = true;
+        break;
       }
+      if (launched) continue;  // an even number of steps leaves cur unchanged
       const int par = resident ? c->cur : 0;
       if (!c->gexec1[par]) {
         cudaGraph_t g;

@@ -12,6 +12,7 @@ struct Geom {
   double kq[3];  // 2*3.141592/L per physical axis (domain.cpp:206-208)
   int generic256;  // 256-point axes take the shared-memory tile transforms, not the register-resident ones
   int xc2r_tma = 1;  // FP32 merged x c2r on 256-point rows fed by tensor-map loads (persistent grid)
+  int xr2c_tma = 1;  // FP32 x r2c on 256-point rows fed by tensor-map loads (persistent grid)
 };
 
 struct FHArgs {
@@ -26,6 +27,7 @@ struct FHArgs {
   // fconst = tv f(c) is added back only where mu is materialised.
   double c, inv_c, fconst;
   int centered;
+  int* status = nullptr;  // device status word a pass with bounded waits flags with ST_TIMEOUT (null: no such pass)
 };
 
 struct NanArgs {

@@ -407,9 +407,175 @@ k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restri
   }
 }
 
+// The same x r2c fed by the tensor memory accelerator (FP32, Ny a multiple
+// of 32): a persistent grid whose CTAs walk the tiles of k_xr2c256 (rows
+// y0 .. y0 + 32 of plane z, numbered plane by plane) with the grid's stride.
+// A tile's rows of phi (and of the deposit) arrive as one 32-row box each.
+// Line c (rows 2c, 2c + 1) is formed by its 16 lanes straight from the
+// boxes; after the first DFT-16 the boxes are dead and their memory serves as
+// the lines' exchange buffer; once every line has read its exchange back,
+// thread 0 queues the boxes of the CTA's next tile, which land while the CTA
+// finishes the transform and writes the current tile.  The Hermitian split
+// needs mode N - k next to mode k: it lives in lane (16 - j) % 16 of the same
+// line, at register 15 - r (lane 0: its own register (16 - r) % 16), so one
+// shuffle per mode brings it and each lane writes its modes k = j + 16 r
+// (r < 8, and k = N/2 at lane 0) directly, 16 bytes (rows 2c, 2c + 1) per mode.
+constexpr int XR_ROWS = 2 * W;                // rows per tile
+constexpr int XR_BOX = XR_ROWS * N * 4;       // bytes of one 32-row box
+static_assert(W * RX * 8 <= 2 * XR_BOX, "the exchange buffer fits in the two boxes' memory");
+constexpr size_t XR_SMEM = 2 * (size_t)XR_BOX + 1024 + 16;  // phi + deposit boxes, alignment slack, mbarrier
+
+template <int PRO>
+__global__ void __launch_bounds__(256, 3)
+k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const __grid_constant__ CUtensorMap mdep,
+           cpx<float>* __restrict__ out, const cpx<float>* __restrict__ tw, int Ny, int Nz, FHArgs fh,
+           int* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smraw[];  // aligned to 1024 below
+  unsigned char* buf = smraw + ((1024u - (tc::smem_u32(smraw) & 1023u)) & 1023u);
+  const float* sphi = reinterpret_cast<const float*>(buf);
+  const float* sdep = reinterpret_cast<const float*>(buf + XR_BOX);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(buf + 2 * XR_BOX);
+  const int tpp = Ny / XR_ROWS;  // tiles per plane
+  const int ntiles = tpp * Nz;
+  const uint32_t bytes = (PRO >= 1 ? 2u : 1u) * (uint32_t)XR_BOX;
+  const int j = threadIdx.x & 15, c = threadIdx.x >> 4;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(bar, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int t) {  // thread 0: the boxes of tile t
+    const int row = (t / tpp) * Ny + (t % tpp) * XR_ROWS;
+    tc::fence_async_smem();
+    tma::arrive_expect(bar, bytes);
+    tma::load2d(buf, &mphi, 0, row, bar);
+    if (PRO >= 1) tma::load2d(buf + XR_BOX, &mdep, 0, row, bar);
+  };
+  int t = blockIdx.x;
+  if (threadIdx.x == 0 && t < ntiles) issue(t);
+  uint32_t phase = 0;
+  bool failed = false;
+  unsigned long long nless = 0, ngreat = 0;
+  const int src = (threadIdx.x & 16) | ((16 - j) & 15);  // the lane holding mode N - k
+  for (; t < ntiles; t += gridDim.x, phase ^= 1u) {
+    const int z = t / tpp, y0 = (t % tpp) * XR_ROWS;
+    const bool got = tc::mbar_wait(bar, phase);
+    cpx<float> v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int x = j + 16 * r;
+      float pr[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int row = 2 * c + h;
+        float p = sphi[row * N + x];
+        if constexpr (PRO >= 1) {  // PRO 2: the Flory-Huggins part relative to f(c)
+          float keep;
+          p = fh_node_t<float, PRO == 2>(p, sdep[row * N + x], fh, nless, ngreat, &keep);
+          if (fh.mu_out) reinterpret_cast<float*>(fh.mu_out)[((size_t)z * Ny + y0 + row) * N + x] = keep;
+        } else {
+          if (fh.centered) p -= (float)fh.c;  // transform phi - c
+        }
+        pr[h] = p;
+      }
+      v[r] = mk<float>(pr[0], pr[1]);
+    }
+    fft::dft16<-1>(v);
+    if (__syncthreads_or(!got)) {  // every line has read the boxes
+      failed = true;
+      break;
+    }
+    cpx<float>* rb = reinterpret_cast<cpx<float>*>(buf) + c * RX;
+    rput16(rb, v, j);
+    __syncwarp();
+    rget16(rb, v, j);
+    __syncthreads();  // the boxes' memory is free for the next tile
+    if (threadIdx.x == 0 && t + (int)gridDim.x < ntiles) issue(t + (int)gridDim.x);
+    twiddle16<float, -1>(v, j, tw);
+    fft::dft16<-1>(v);  // v[r] = mode j + 16 r of line c
+    const int y = y0 + 2 * c;
+#pragma unroll
+    for (int r = 0; r <= 8; ++r) {
+      // mode N - k of k = j + 16 r: lane src's register 15 - r, or (lane 0) own register (16 - r) % 16
+      cpx<float> zm;
+      if (r < 8) {
+        zm.x = __shfl_sync(0xffffffffu, v[15 - r].x, src);
+        zm.y = __shfl_sync(0xffffffffu, v[15 - r].y, src);
+        if (j == 0) zm = v[(16 - r) & 15];
+      } else {
+        if (j != 0) continue;
+        zm = v[8];
+      }
+      zm = conjg(zm);
+      const cpx<float> zk = v[r];
+      const cpx<float> a = scale(zk + zm, 0.5f);
+      const cpx<float> d = zk - zm;
+      const cpx<float> b = mk<float>(0.5f * d.y, -0.5f * d.x);
+      const int k = j + 16 * r;
+      *reinterpret_cast<float4*>(&out[((size_t)k * Nz + z) * Ny + y]) = make_float4(a.x, a.y, b.x, b.y);
+    }
+  }
+  if constexpr (PRO >= 1) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      nless += __shfl_down_sync(0xffffffffu, nless, off);
+      ngreat += __shfl_down_sync(0xffffffffu, ngreat, off);
+    }
+    if ((threadIdx.x & 31) == 0 && (nless | ngreat)) {
+      if (nless) atomicAdd(fh.counters + 0, nless);
+      if (ngreat) atomicAdd(fh.counters + 1, ngreat);
+    }
+  }
+  if (failed && threadIdx.x == 0) {
+    atomicOr(status, ST_TIMEOUT);
+    tc::mbar_wait(bar, phase);  // give the late loads time to land before the CTA's shared memory is released
+  }
+}
+
+// launch of k_xr2c256t: -3 when it does not apply (tensor maps unavailable)
+inline int xr2c_tma(const Geom& g, const float* in, const float* dep, cpx<float>* out, const cpx<float>* tw,
+                    const FHArgs& fh, int* status, cudaStream_t st) {
+  CUtensorMap mphi, mdep;
+  const uint64_t rows = (uint64_t)g.ny * g.nz;
+  if (!tma::map2d_f32(&mphi, in, N, rows, N, XR_ROWS)) return -3;
+  if (dep && !tma::map2d_f32(&mdep, dep, N, rows, N, XR_ROWS)) return -3;
+  if (!dep) mdep = mphi;
+  const int pro = !dep ? 0 : (fh.centered && fh.enabled) ? 2 : 1;
+  void (*k)(const CUtensorMap, const CUtensorMap, cpx<float>*, const cpx<float>*, int, int, FHArgs, int*) =
+      pro == 0 ? k_xr2c256t<0> : pro == 1 ? k_xr2c256t<1> : k_xr2c256t<2>;
+  if (set_smem(k, XR_SMEM)) return -1;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, int> resident;  // (device, pro) -> CTAs the device holds at once
+  int slots = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = resident.find({dev, pro});
+    if (it == resident.end()) {
+      int sms = 0, per_sm = 0;
+      if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, XR_SMEM) != cudaSuccess || per_sm < 1)
+        return -1;
+      it = resident.emplace(std::make_pair(dev, pro), sms * per_sm).first;
+    }
+    slots = it->second;
+  }
+  const long long ntiles = (long long)(g.ny / XR_ROWS) * g.nz;
+  const int grid = (int)(ntiles < (long long)slots ? ntiles : (long long)slots);
+  k<<<grid, 256, XR_SMEM, st>>>(mphi, mdep, out, tw, g.ny, g.nz, fh, status);
+  return 0;
+}
+
 template <typename T>
 int xr2c(const Geom& g, const T* in, const T* dep, cpx<T>* out, const cpx<T>* tw, const FHArgs& fh,
          cudaStream_t st) {
+  if constexpr (sizeof(T) == 4) {
+    if (g.xr2c_tma && g.ny % XR_ROWS == 0 && fh.status) {
+      const int rc = xr2c_tma(g, in, dep, out, tw, fh, fh.status, st);
+      if (rc != -3) return rc;
+    }
+  }
   const size_t tiles = (size_t)2 * W * N * sizeof(T) * (dep ? 2 : 1);
   const size_t lines = (size_t)W * RX * sizeof(cpx<T>);
   const size_t sm = tiles > lines ? tiles : lines;
@@ -509,7 +675,7 @@ k_xc2r3t_256(const __grid_constant__ CUtensorMap mC, const __grid_constant__ CUt
              float* __restrict__ gy, float* __restrict__ gz, float sp, float sg, float dq,
              const cpx<float>* __restrict__ tw, int Ny, int Nz, NanArgs nan, const uint32_t* __restrict__ mask,
              const int* __restrict__ mask_off, int* __restrict__ status) {
-  extern __shared__ __align__(1024) unsigned char smraw[];
+  extern __shared__ __align__(16) unsigned char smraw[];  // aligned to 1024 below
   unsigned char* buf = smraw + ((1024u - (tc::smem_u32(smraw) & 1023u)) & 1023u);
   uint64_t* bar = reinterpret_cast<uint64_t*>(buf + XT_BUF);
   const int nb0 = Ny / W, nb1 = Ny / (2 * W);

@@ -21,6 +21,16 @@ PHAFD_D void arrive_expect(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
+// box at element coordinates (x, y) of a rank-2 map into shared memory at
+// dst; completes `bar`'s transaction bytes
+PHAFD_D void load2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];\n" ::"r"(tc::smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(tc::smem_u32(bar))
+      : "memory");
+}
+
 // box at element coordinates (x, y, z) of a rank-3 map into shared memory at
 // dst; completes `bar`'s transaction bytes.  x times the element size must
 // be a multiple of 16 bytes.
@@ -43,6 +53,20 @@ inline PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
   }();
   return fn;
+}
+
+// rank-2 FP32 map of a dense [d1][d0] array, box b0 x b1 elements, no
+// swizzle; false when encoding fails
+inline bool map2d_f32(CUtensorMap* m, const void* base, uint64_t d0, uint64_t d1, uint32_t b0, uint32_t b1) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {d0, d1};
+  const cuuint64_t strides[1] = {d0 * 4};
+  const cuuint32_t box[2] = {b0, b1};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // rank-3 FP32 map of a dense [d2][d1][d0] array, box b0 x b1 x b2 elements,

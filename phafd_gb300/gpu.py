@@ -205,16 +205,17 @@ class PhafdGPU:
         """Store grad phi only near the beads during steps (off by default)."""
         self._call("phafd_set_gradient_mask", int(on))
 
-    def set_variants(self, plane=False, generic256=False, xc2r_tma=True):
+    def set_variants(self, plane=False, generic256=False, xc2r_tma=True, xr2c_tma=True):
         """Kernel variants of the step (PHAFD_TUNE_*; a new context has
-        xc2r_tma on)."""
-        self._call("phafd_set_variants", (1 if plane else 0) | (2 if generic256 else 0) | (4 if xc2r_tma else 0))
+        xc2r_tma and xr2c_tma on)."""
+        self._call("phafd_set_variants", (1 if plane else 0) | (2 if generic256 else 0) | (4 if xc2r_tma else 0)
+                   | (8 if xr2c_tma else 0))
 
     def autotune(self, steps=10):
         """Time every variant over `steps` steps of the run, keep the fastest:
         returns (best flags, ms per step by flags, -1 where not applicable)."""
         best = C.c_int(0)
-        ms = np.zeros(8)
+        ms = np.zeros(16)
         self._call("phafd_autotune", steps, C.byref(best), ms)
         return best.value, ms
 

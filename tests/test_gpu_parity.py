@@ -276,8 +276,8 @@ def test_generic_256_point_plan_matches_oracle(gpu_lib, precision, tol):
         assert rel_err(g.grid_get(f), o.grid_get(f)) < (tol if precision == 64 else 1e-4), f
 
 
-def _field_run(nx, ny, nz, tma, steps=3):
-    g = gpu(32, "resident")
+def _field_run(nx, ny, nz, tma, schedule="resident", steps=3):
+    g = gpu(32, schedule)
     g.domain([-nx / 2, -ny / 2, -nz / 2], [float(nx), float(ny), float(nz)])
     g.grid_style(nx, ny, nz)
     g.grid_populate_constant(0.4, 0.02, 5)
@@ -286,35 +286,41 @@ def _field_run(nx, ny, nz, tma, steps=3):
     g.fix_floryhuggins(temp=1.0, volFH=1.0, chi=3.0)
     g.set_dt(1e-3)
     g.set_timestep(0)
-    g.set_variants(xc2r_tma=tma)
+    g.set_variants(xc2r_tma=tma, xr2c_tma=tma)
     g.setup()
     g.run(steps)
     out = {f: g.grid_get(f) for f in ("phi", "gradx", "grady", "gradz")}
+    out["counters"] = np.array([g.counters()[k] for k in ("num_less_zero", "num_great_zero")])
     g.close()
     return out
 
 
-@pytest.mark.parametrize("shape", [(256, 256, 256), (256, 64, 32)])
-def test_tma_fed_x_c2r_equals_register_resident(gpu_lib, shape):
-    """The tensor-map fed persistent x c2r (PHAFD_TUNE_XC2R_TMA) forms the
-    same lines and runs the same transform as the register-resident merged
-    x c2r: without beads (no floating-point atomics anywhere in the step)
-    phi and the three gradients after three steps are bit-identical."""
-    a = _field_run(*shape, tma=False)
-    b = _field_run(*shape, tma=True)
+@pytest.mark.parametrize("shape,schedule", [((256, 256, 256), "resident"), ((256, 64, 32), "resident"),
+                                            ((256, 64, 32), "reference")])
+def test_tma_fed_x_passes_equal_register_resident(gpu_lib, shape, schedule):
+    """The tensor-map fed persistent x r2c and x c2r (PHAFD_TUNE_XR2C_TMA,
+    PHAFD_TUNE_XC2R_TMA) form the same lines and run the same transforms as
+    the register-resident x passes that load their own tiles: without beads
+    (no floating-point atomics anywhere in the step) phi, the three
+    gradients and the Flory-Huggins reflection counters after three steps
+    are bit-identical.  The reference schedule adds the plain r2c of phi
+    (no Flory-Huggins prologue) to every step."""
+    a = _field_run(*shape, tma=False, schedule=schedule)
+    b = _field_run(*shape, tma=True, schedule=schedule)
     for f in a:
-        assert np.abs(a[f]).max() > 0, f
+        if f != "counters":
+            assert np.abs(a[f]).max() > 0, f
         assert np.array_equal(a[f], b[f]), f
 
 
-def test_tma_fed_x_c2r_with_beads_matches_oracle(gpu_lib):
-    """The tensor-map fed x c2r in a 256^3 FP32 step with chains (masked
+def test_tma_fed_x_passes_with_beads_match_oracle(gpu_lib):
+    """The tensor-map fed x passes in a 256^3 FP32 step with chains (masked
     gradient stores, neighbor rebuilds) against the FP64 oracle."""
     cfg = dict(W.CONFIGS["32cube_64beads"])
     cfg.update(n=256, L=256.0, origin=-128.0, nchains=4, chain_len=50, field_noise="philox", bead_temp=1.0,
                dt=1e-4)
     o = Oracle(); g = gpu(32, "resident")
-    g.set_variants(xc2r_tma=True)
+    g.set_variants(xc2r_tma=True, xr2c_tma=True)
     chains = None
     for d in (o, g):
         chains = W.apply(d, cfg, chains=chains)
