@@ -333,7 +333,9 @@ k_ypass_inv2(const cpx<T>* A, cpx<T>* C, cpx<T>* D, const cpx<T>* B, cpx<T>* E, 
 // this project's indices: the reference's (i, j, k) = (ky, kz, kx).
 // Model-B update of one mode from its old spectrum value ph (unnormalised)
 // and mu_hat value mu; (cy, cz) is the canonical mode that owns the noise.
-template <typename T>
+// (QPOS: the caller guarantees q^2 > 0, so the FP32 path may take |q| as
+// q^2 rsqrt(q^2): a few ulps, on the noise amplitude only)
+template <typename T, bool QPOS = false>
 PHAFD_D cpx<T> update_value(const UpdateArgs<T>& u, int kx, int cy, int cz, cpx<T> ph, cpx<T> mu, bool real,
                             const uint32_t* words = nullptr) {
   const int Ny = u.Ny, Nz = u.Nz;
@@ -372,7 +374,9 @@ PHAFD_D cpx<T> update_value(const UpdateArgs<T>& u, int kx, int cy, int cz, cpx<
     else field_noise_words(kx, cy, cz, Ny, Nz, (uint32_t)(*u.d_step), u.seed, c);
     field_noise_pair(c, cz, u0, u1);
   }
-  const T sq = sqrt(q2);
+  T sq;
+  if constexpr (QPOS && sizeof(T) == 4) sq = q2 * rsqrtf(q2);
+  else sq = sqrt(q2);
   if (real) {
     r.x += u.rpref * sq * u.sqrtdt * u0 * namp;
   } else {

@@ -46,13 +46,17 @@ PHAFD_D void get16(const cpx<T>* buf, cpx<T>* v, int j, int c) {
 // NOISE and MACRO fix the noise mode and whether the update is a macro step
 // (nsub > 1) at compile time, so the update inlined for the 16 modes of a
 // thread carries no branches or code for the other cases.
-template <typename T, int NOISE, bool MACRO>
+// NYC: Ny known at compile time (256: every strided address is a constant
+// offset from the column's base), 0: run time.
+template <typename T, int NOISE, bool MACRO, int NYC>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
 k_zfused256(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>* __restrict__ out0,
-            cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny,
+            cpx<T>* __restrict__ out1, T dq, const cpx<T>* __restrict__ twf, const cpx<T>* __restrict__ twi, int Ny_rt,
             UpdateArgs<T> u, int store_mu, int kx0) {
   u.noise = NOISE;
   if (!MACRO) u.nsub = 1;
+  const int Ny = NYC > 0 ? NYC : Ny_rt;
+  if (NYC > 0) u.Ny = NYC;
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* bufA = reinterpret_cast<cpx<T>*>(smraw);  // N x W
   cpx<T>* bufB = bufA + N * W;                        // N x W (phi_hat staging, then second ifft)
@@ -98,7 +102,7 @@ k_zfused256(const cpx<T>* __restrict__ muin, cpx<T>* __restrict__ muhat, cpx<T>*
     cpx<T> nv = mk<T>(0, 0);
     if (live) {
       const cpx<T> ph = scale(bufB[kz * W + c], u.phi_scale);
-      nv = update_value(u, kx, ky, kz, ph, v[r], false, words);
+      nv = update_value<T, true>(u, kx, ky, kz, ph, v[r], false, words);  // bulk kx >= 1: q^2 > 0
       u.phi_new[col + (size_t)kz * Ny] = scale(nv, u.store_scale);
     }
     v[r] = nv;
@@ -834,7 +838,7 @@ template <typename T, int NOISE, bool MACRO>
 int zfused_launch(const Geom& g, const cpx<T>* muin, cpx<T>* muhat, cpx<T>* out0, cpx<T>* out1, const cpx<T>* twf,
                   const cpx<T>* twi, const UpdateArgs<T>& u, int store_mu, int kx0, cudaStream_t st) {
   const size_t sm = (size_t)2 * N * W * sizeof(cpx<T>);
-  auto k = k_zfused256<T, NOISE, MACRO>;
+  auto k = g.ny == N ? k_zfused256<T, NOISE, MACRO, N> : k_zfused256<T, NOISE, MACRO, 0>;
   if (set_smem(k, sm)) return -1;
   dim3 grid((g.ny + W - 1) / W, g.nxh - 2 * kx0);
   launch_grid(k, grid, dim3(256), sm, st, muin, muhat, out0, out1, (T)g.kq[2], twf, twi, g.ny, u, store_mu, kx0);
