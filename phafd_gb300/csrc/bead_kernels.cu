@@ -898,6 +898,25 @@ __global__ void k_gmask_build(BeadArgs a) {
   }
 }
 
+// deposit support: the sectors of every grid-list node (the pair stage
+// deposits only on listed nodes)
+__global__ void k_dmask_clear(BeadArgs a) {
+  if (!*a.flag) return;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < a.gmask_words;
+       k += (long long)gridDim.x * blockDim.x)
+    a.dmask[k] = 0u;
+}
+__global__ void k_dmask_build(BeadArgs a) {
+  if (!*a.flag) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int cnt = a.ngl[i];
+  for (int k = 0; k < cnt; ++k) {
+    const long long sec = (long long)(a.gl[(size_t)i * a.maxg + k] >> 5) / a.gmask_g;
+    atomicOr(a.dmask + (sec >> 5), 1u << (sec & 31));
+  }
+}
+
 __global__ void k_gmask_guard(BeadArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -972,6 +991,10 @@ void launch_rebuild(const BeadArgs& a, cudaStream_t st) {
   if (a.gmask) {
     k_gmask_clear<<<1024, 256, 0, st>>>(a);
     k_gmask_build<<<nblk(a.n, 128), 128, 0, st>>>(a);
+  }
+  if (a.dmask && a.gl) {
+    k_dmask_clear<<<256, 256, 0, st>>>(a);
+    k_dmask_build<<<nblk(a.n, 128), 128, 0, st>>>(a);
   }
   k_build_done<<<1, 1, 0, st>>>(a);
 }

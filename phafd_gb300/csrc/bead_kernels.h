@@ -30,6 +30,8 @@ struct BeadArgs {
   double gmask_r;       // radius of the mask: coupling cutoff + skin (+ a round-off margin)
   double gmask_guardsq; // squared displacement since the last rebuild up to which the mask covers every read
   int* gmask_off;       // set: the mask does not cover the current positions (cleared by a rebuild)
+  uint32_t* dmask;      // bit per 32-byte sector (gmask_g nodes) holding a node of the grid lists, rebuilt with
+                        // them: the deposit's support (null: none)
   int* check_done;      // blocks of k_check finished (last one sets the graph condition)
   int* status;          // sticky ST_* bits
   long long* ncalls;    // Neighbor::ncalls

@@ -210,6 +210,7 @@ struct phafd_ctx {
     FHArgs f{fh_temp / fh_volFH, fh_chi, fh_counters(), have_fh ? 1 : 0, keep_chempot ? mu.p : nullptr};
     center(f, PHAFD_CENTER_FH);
     f.status = d_status();
+    if (dmask.p && n > 0) f.dep_mask = dmask.as<uint32_t>();
     return f;
   }
   // N f(c) tv: what the k = 0 mode of a centered mu spectrum lacks
@@ -231,6 +232,7 @@ struct phafd_ctx {
   DevBuf nbr, nnbr, gl, ngl;
   DevBuf dragc, sf_fix, sf_start, sf_len, sf_par;
   DevBuf gmask;  // one bit per 32-byte sector of a real field (beads with a grid coupling)
+  DevBuf dmask;  // the same sectors: the deposit's support, rebuilt with the grid lists
   DevBuf bx_pair, bf_tmp;  // positions of the last pair stage (phafd_set_pair_snapshot); compute pair's forces
   // run_until_touching: a check after every step while set
   DevBuf touch;
@@ -519,6 +521,7 @@ struct phafd_ctx {
     a.gmask_r = ga_maxcut + skin + 1e-3 * std::min(a.dx[0], std::min(a.dx[1], a.dx[2]));
     a.gmask_guardsq = skin * skin;
     a.gmask_off = d_gmask_off();
+    a.dmask = dmask.p ? dmask.as<uint32_t>() : nullptr;
   }
 
   // steps store grad phi at masked nodes only (single-substep resident steps
@@ -615,6 +618,10 @@ struct phafd_ctx {
     ba.maxg = maxg;
     if (ga_style != PHAFD_GRIDATOM_NONE) gl.alloc((size_t)std::max(n, 1) * maxg * 4);
     ngl.alloc(std::max(n, 1) * 4);
+    if (ga_style != PHAFD_GRIDATOM_NONE && gridset) {  // zero until the first build: so is the deposit
+      dmask.alloc(((nreal / (32 / rsz()) + 32) / 32) * 4);
+      dmask.zero(st);
+    }
     if (use_gmask) alloc_gmask();
     nnbr.zero(st);
     ngl.zero(st);
@@ -2161,7 +2168,8 @@ int phafd_ctx_copy_state(phafd_ctx* dst, phafd_ctx* src) {
                   std::make_pair(&dst->bin_start, &src->bin_start), std::make_pair(&dst->sorted, &src->sorted),
                   std::make_pair(&dst->bin_off, &src->bin_off), std::make_pair(&dst->nbr, &src->nbr),
                   std::make_pair(&dst->nnbr, &src->nnbr), std::make_pair(&dst->gl, &src->gl),
-                  std::make_pair(&dst->ngl, &src->ngl), std::make_pair(&dst->d_counters, &src->d_counters)})
+                  std::make_pair(&dst->ngl, &src->ngl), std::make_pair(&dst->d_counters, &src->d_counters),
+                  std::make_pair(&dst->dmask, &src->dmask)})
     cp(*pr.first, *pr.second);
   // the gradient node mask travels with the counters (its stale flag) only
   // when both contexts keep one; otherwise dst's mask is stale until its

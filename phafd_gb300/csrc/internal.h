@@ -28,6 +28,10 @@ struct FHArgs {
   double c, inv_c, fconst;
   int centered;
   int* status = nullptr;  // device status word a pass with bounded waits flags with ST_TIMEOUT (null: no such pass)
+  // bit per 32-byte sector of the deposit holding a node of the current grid
+  // lists (the only nodes the pair stage deposits on); a pass may read the
+  // deposit only where the bit is set (null: everywhere)
+  const uint32_t* dep_mask = nullptr;
 };
 
 struct NanArgs {

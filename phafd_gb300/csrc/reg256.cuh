@@ -414,46 +414,46 @@ k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restri
 // The same x r2c fed by the tensor memory accelerator (FP32, Ny a multiple
 // of 32): a persistent grid whose CTAs walk the tiles of k_xr2c256 (rows
 // y0 .. y0 + 32 of plane z, numbered plane by plane) with the grid's stride.
-// A tile's rows of phi (and of the deposit) arrive as one 32-row box each.
-// Line c (rows 2c, 2c + 1) is formed by its 16 lanes straight from the
-// boxes; after the first DFT-16 the boxes are dead and their memory serves as
-// the lines' exchange buffer; once every line has read its exchange back,
-// thread 0 queues the boxes of the CTA's next tile, which land while the CTA
-// finishes the transform and writes the current tile.  The Hermitian split
-// needs mode N - k next to mode k: it lives in lane (16 - j) % 16 of the same
-// line, at register 15 - r (lane 0: its own register (16 - r) % 16), so one
-// shuffle per mode brings it and each lane writes its modes k = j + 16 r
-// (r < 8, and k = N/2 at lane 0) directly, 16 bytes (rows 2c, 2c + 1) per mode.
+// A tile's rows of phi arrive as one 32-row box; the deposit, zero except on
+// the nodes of the grid lists, is read straight from global memory in the
+// 32-byte sectors its support mask sets (fh.dep_mask; every sector when the
+// mask is null), so the mostly-zero array costs no full read and no shared
+// memory.  Line c (rows 2c, 2c + 1) is formed by its 16 lanes; after the
+// first DFT-16 the box is dead and its memory serves as the lines' exchange
+// buffer; once every line has read its exchange back, thread 0 queues the
+// box of the CTA's next tile, which lands while the CTA finishes the
+// transform and writes the current tile.  The Hermitian split needs mode
+// N - k next to mode k: it lives in lane (16 - j) % 16 of the same line, at
+// register 15 - r (lane 0: its own register (16 - r) % 16), so one shuffle
+// per mode brings it and each lane writes its modes k = j + 16 r (r < 8, and
+// k = N/2 at lane 0) directly, 16 bytes (rows 2c, 2c + 1) per mode.
 constexpr int XR_ROWS = 2 * W;                // rows per tile
 constexpr int XR_BOX = XR_ROWS * N * 4;       // bytes of one 32-row box
-static_assert(W * RX * 8 <= 2 * XR_BOX, "the exchange buffer fits in the two boxes' memory");
-constexpr size_t XR_SMEM = 2 * (size_t)XR_BOX + 1024 + 16;  // phi + deposit boxes, alignment slack, mbarrier
+constexpr int XR_BUF = W * RX * 8;            // the lines' exchange buffer (covers the box)
+static_assert(XR_BOX <= XR_BUF, "the box fits in the exchange buffer");
+constexpr size_t XR_SMEM = (size_t)XR_BUF + 1024 + 16;  // + alignment slack + the mbarrier
 
-template <int PRO>
-__global__ void __launch_bounds__(256, 3)
-k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const __grid_constant__ CUtensorMap mdep,
-           cpx<float>* __restrict__ out, const cpx<float>* __restrict__ tw, int Ny, int Nz, FHArgs fh,
-           int* __restrict__ status) {
+template <int PRO, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const float* __restrict__ dep, cpx<float>* __restrict__ out,
+           const cpx<float>* __restrict__ tw, int Ny, int Nz, FHArgs fh, int* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char smraw[];  // aligned to 1024 below
   unsigned char* buf = smraw + ((1024u - (tc::smem_u32(smraw) & 1023u)) & 1023u);
   const float* sphi = reinterpret_cast<const float*>(buf);
-  const float* sdep = reinterpret_cast<const float*>(buf + XR_BOX);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(buf + 2 * XR_BOX);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(buf + XR_BUF);
   const int tpp = Ny / XR_ROWS;  // tiles per plane
   const int ntiles = tpp * Nz;
-  const uint32_t bytes = (PRO >= 1 ? 2u : 1u) * (uint32_t)XR_BOX;
   const int j = threadIdx.x & 15, c = threadIdx.x >> 4;
+  const uint32_t* __restrict__ dmask = fh.dep_mask;
   if (threadIdx.x == 0) {
     tc::mbar_init(bar, 1);
     tc::fence_mbar_init();
   }
   __syncthreads();
-  auto issue = [&](int t) {  // thread 0: the boxes of tile t
-    const int row = (t / tpp) * Ny + (t % tpp) * XR_ROWS;
+  auto issue = [&](int t) {  // thread 0: the box of tile t
     tc::fence_async_smem();
-    tma::arrive_expect(bar, bytes);
-    tma::load2d(buf, &mphi, 0, row, bar);
-    if (PRO >= 1) tma::load2d(buf + XR_BOX, &mdep, 0, row, bar);
+    tma::arrive_expect(bar, (uint32_t)XR_BOX);
+    tma::load2d(buf, &mphi, 0, (t / tpp) * Ny + (t % tpp) * XR_ROWS, bar);
   };
   int t = blockIdx.x;
   if (threadIdx.x == 0 && t < ntiles) issue(t);
@@ -463,6 +463,19 @@ k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const __grid_constant__ CUt
   const int src = (threadIdx.x & 16) | ((16 - j) & 15);  // the lane holding mode N - k
   for (; t < ntiles; t += gridDim.x, phase ^= 1u) {
     const int z = t / tpp, y0 = (t % tpp) * XR_ROWS;
+    const size_t row0 = (size_t)z * Ny + y0 + 2 * c;  // the line's first row
+    // the deposit of the line's two rows where its support mask is set (one
+    // mask word per 256-node row), loaded while the box is in flight
+    float dd[2][16];
+    if constexpr (PRO >= 1) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const uint32_t m = dmask ? dmask[row0 + h] >> (j >> 3) : 0xffffffffu;
+        const float* drow = dep + (row0 + h) * N + j;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) dd[h][r] = (m >> (2 * r)) & 1u ? drow[16 * r] : 0.f;
+      }
+    }
     const bool got = tc::mbar_wait(bar, phase);
     cpx<float> v[16];
 #pragma unroll
@@ -471,12 +484,11 @@ k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const __grid_constant__ CUt
       float pr[2];
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int row = 2 * c + h;
-        float p = sphi[row * N + x];
+        float p = sphi[(2 * c + h) * N + x];
         if constexpr (PRO >= 1) {  // PRO 2: the Flory-Huggins part relative to f(c)
           float keep;
-          p = fh_node_t<float, PRO == 2>(p, sdep[row * N + x], fh, nless, ngreat, &keep);
-          if (fh.mu_out) reinterpret_cast<float*>(fh.mu_out)[((size_t)z * Ny + y0 + row) * N + x] = keep;
+          p = fh_node_t<float, PRO == 2>(p, dd[h][r], fh, nless, ngreat, &keep);
+          if (fh.mu_out) reinterpret_cast<float*>(fh.mu_out)[(row0 + h) * N + x] = keep;
         } else {
           if (fh.centered) p -= (float)fh.c;  // transform phi - c
         }
@@ -485,7 +497,7 @@ k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const __grid_constant__ CUt
       v[r] = mk<float>(pr[0], pr[1]);
     }
     fft::dft16<-1>(v);
-    if (__syncthreads_or(!got)) {  // every line has read the boxes
+    if (__syncthreads_or(!got)) {  // every line has read the box
       failed = true;
       break;
     }
@@ -493,7 +505,7 @@ k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const __grid_constant__ CUt
     rput16(rb, v, j);
     __syncwarp();
     rget16(rb, v, j);
-    __syncthreads();  // the boxes' memory is free for the next tile
+    __syncthreads();  // the box's memory is free for the next tile
     if (threadIdx.x == 0 && t + (int)gridDim.x < ntiles) issue(t + (int)gridDim.x);
     twiddle16<float, -1>(v, j, tw);
     fft::dft16<-1>(v);  // v[r] = mode j + 16 r of line c
@@ -532,21 +544,19 @@ k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const __grid_constant__ CUt
   }
   if (failed && threadIdx.x == 0) {
     atomicOr(status, ST_TIMEOUT);
-    tc::mbar_wait(bar, phase);  // give the late loads time to land before the CTA's shared memory is released
+    tc::mbar_wait(bar, phase);  // give the late load time to land before the CTA's shared memory is released
   }
 }
 
 // launch of k_xr2c256t: -3 when it does not apply (tensor maps unavailable)
 inline int xr2c_tma(const Geom& g, const float* in, const float* dep, cpx<float>* out, const cpx<float>* tw,
                     const FHArgs& fh, int* status, cudaStream_t st) {
-  CUtensorMap mphi, mdep;
-  const uint64_t rows = (uint64_t)g.ny * g.nz;
-  if (!tma::map2d_f32(&mphi, in, N, rows, N, XR_ROWS)) return -3;
-  if (dep && !tma::map2d_f32(&mdep, dep, N, rows, N, XR_ROWS)) return -3;
-  if (!dep) mdep = mphi;
+  constexpr int MINB = 4;
+  CUtensorMap mphi;
+  if (!tma::map2d_f32(&mphi, in, N, (uint64_t)g.ny * g.nz, N, XR_ROWS)) return -3;
   const int pro = !dep ? 0 : (fh.centered && fh.enabled) ? 2 : 1;
-  void (*k)(const CUtensorMap, const CUtensorMap, cpx<float>*, const cpx<float>*, int, int, FHArgs, int*) =
-      pro == 0 ? k_xr2c256t<0> : pro == 1 ? k_xr2c256t<1> : k_xr2c256t<2>;
+  void (*k)(const CUtensorMap, const float*, cpx<float>*, const cpx<float>*, int, int, FHArgs, int*) =
+      pro == 0 ? k_xr2c256t<0, MINB> : pro == 1 ? k_xr2c256t<1, MINB> : k_xr2c256t<2, MINB>;
   if (set_smem(k, XR_SMEM)) return -1;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1;
@@ -567,7 +577,7 @@ inline int xr2c_tma(const Geom& g, const float* in, const float* dep, cpx<float>
   }
   const long long ntiles = (long long)(g.ny / XR_ROWS) * g.nz;
   const int grid = (int)(ntiles < (long long)slots ? ntiles : (long long)slots);
-  k<<<grid, 256, XR_SMEM, st>>>(mphi, mdep, out, tw, g.ny, g.nz, fh, status);
+  k<<<grid, 256, XR_SMEM, st>>>(mphi, dep, out, tw, g.ny, g.nz, fh, status);
   return 0;
 }
 

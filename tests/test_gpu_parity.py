@@ -332,6 +332,31 @@ def test_tma_fed_x_passes_with_beads_match_oracle(gpu_lib):
     assert g.counters()["timestep"] == 3
 
 
+def test_tma_x_r2c_reads_the_whole_deposit(gpu_lib):
+    """The tensor-map fed x r2c reads the bead deposit only in the sectors of
+    its support mask (rebuilt with the grid lists): the chempot it
+    materialises (deposit + Flory-Huggins part) equals the one of the x r2c
+    that reads the deposit everywhere, over steps that include neighbor
+    rebuilds (the deposits' floating-point atomics differ in order only)."""
+    cfg = dict(W.CONFIGS["32cube_64beads"])
+    cfg.update(n=256, L=256.0, origin=-128.0, nchains=16, chain_len=200, field_noise="philox", bead_temp=1.0,
+               dt=1e-3)
+    out = []
+    chains = None
+    for tma in (False, True):
+        g = gpu(32, "resident")
+        chains = W.apply(g, cfg, chains=chains)
+        g.set_keep_chempot(True)
+        g.set_variants(xc2r_tma=True, xr2c_tma=tma)
+        g.setup()
+        g.run(6)
+        out.append((g.grid_get("chempot"), g.counters()["neighbor_calls"]))
+        g.close()
+    (a, na), (b, nb) = out
+    assert na == nb and na >= 2
+    assert np.abs(b - a).max() < 1e-5 * np.abs(a).max()
+
+
 def test_autotune_steps_are_steps_of_the_run(gpu_lib):
     """The autotuner times each variant on the run's own steps: afterwards
     the state equals the oracle's after the same number of steps, and the
