@@ -66,6 +66,37 @@ PHAFD_D T fh_node_t(T p, T dd, const FHArgs& fh, unsigned long long& nless, unsi
   *keep = CENTER ? m + (T)fh.fconst : m;
   return m;
 }
+// The FP32 constants of the Flory-Huggins node, converted once per thread
+// (the same roundings as fh_node_t's casts, so the same results): for the
+// persistent x pass, whose loop over tiles would otherwise convert them per
+// node.
+struct FHf {
+  float tv, chi, c, inv_c, fconst;
+  bool enabled;
+};
+PHAFD_D FHf fh_floats(const FHArgs& fh) {
+  return FHf{(float)fh.tv, (float)fh.chi, (float)fh.c, (float)fh.inv_c, (float)fh.fconst, fh.enabled != 0};
+}
+template <bool CENTER>
+PHAFD_D float fh_node_f(float p, float dd, const FHf& f, unsigned& nless, unsigned& ngreat, float* keep) {
+  if (!f.enabled) {
+    *keep = dd;
+    return dd;
+  }
+  if (p <= 0.0f) { p = -p; nless++; }
+  else if (p >= 1.0f) { p = 1.0f - (p - 1.0f); ngreat++; }
+  float part;
+  if constexpr (CENTER) {
+    const float d = p - f.c;
+    part = f.tv * (log1pf(__fdividef(d * f.inv_c, 1.0f - p)) - 2.0f * f.chi * d);
+  } else {
+    part = f.tv * ((__logf(p) - __logf(1.0f - p)) + f.chi * (1.0f - 2.0f * p));
+  }
+  const float m = dd + part;
+  *keep = CENTER ? m + f.fconst : m;
+  return m;
+}
+
 // the same with the form chosen at run time (the generic and plane kernels)
 template <typename T>
 PHAFD_D T fh_node(T p, T dd, const FHArgs& fh, unsigned long long& nless, unsigned long long& ngreat, T* keep) {

@@ -459,7 +459,11 @@ k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const float* __restrict__ d
   if (threadIdx.x == 0 && t < ntiles) issue(t);
   uint32_t phase = 0;
   bool failed = false;
-  unsigned long long nless = 0, ngreat = 0;
+  unsigned nless = 0, ngreat = 0;
+  const FHf fhf = fh_floats(fh);
+  float* __restrict__ mu_out = reinterpret_cast<float*>(fh.mu_out);
+  const float cshift = (float)fh.c;
+  const bool center_fft = fh.centered != 0;
   const int src = (threadIdx.x & 16) | ((16 - j) & 15);  // the lane holding mode N - k
   for (; t < ntiles; t += gridDim.x, phase ^= 1u) {
     const int z = t / tpp, y0 = (t % tpp) * XR_ROWS;
@@ -487,10 +491,10 @@ k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const float* __restrict__ d
         float p = sphi[(2 * c + h) * N + x];
         if constexpr (PRO >= 1) {  // PRO 2: the Flory-Huggins part relative to f(c)
           float keep;
-          p = fh_node_t<float, PRO == 2>(p, dd[h][r], fh, nless, ngreat, &keep);
-          if (fh.mu_out) reinterpret_cast<float*>(fh.mu_out)[(row0 + h) * N + x] = keep;
+          p = fh_node_f<PRO == 2>(p, dd[h][r], fhf, nless, ngreat, &keep);
+          if (mu_out) mu_out[(row0 + h) * N + x] = keep;
         } else {
-          if (fh.centered) p -= (float)fh.c;  // transform phi - c
+          if (center_fft) p -= cshift;  // transform phi - c
         }
         pr[h] = p;
       }
@@ -538,8 +542,8 @@ k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const float* __restrict__ d
       ngreat += __shfl_down_sync(0xffffffffu, ngreat, off);
     }
     if ((threadIdx.x & 31) == 0 && (nless | ngreat)) {
-      if (nless) atomicAdd(fh.counters + 0, nless);
-      if (ngreat) atomicAdd(fh.counters + 1, ngreat);
+      if (nless) atomicAdd(fh.counters + 0, (unsigned long long)nless);
+      if (ngreat) atomicAdd(fh.counters + 1, (unsigned long long)ngreat);
     }
   }
   if (failed && threadIdx.x == 0) {
