@@ -71,10 +71,7 @@ __global__ void k_check(BeadArgs a, cudaGraphConditionalHandle h, int use_cond, 
 }
 
 // domain.cpp:102-163 then Domain::unmap
-__global__ void k_pbc(BeadArgs a) {
-  if (!*a.flag) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+PHAFD_D void pbc_at(const BeadArgs& a, int i) {
   int im = a.image[i];
   double x[3] = {a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2]};
   for (int d = 0; d < 3; ++d) {
@@ -106,18 +103,13 @@ __global__ void k_pbc(BeadArgs a) {
   a.ux[3 * i + 2] = __dadd_rn(x[2], __dmul_rn((double)zbox, a.period[2]));
 }
 
-__global__ void k_bin_clear(BeadArgs a) {
-  if (!*a.flag) return;
-  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < a.nbins; b += (long long)gridDim.x * blockDim.x) {
-    a.bin_count[b] = 0;
-    a.bin_cursor[b] = 0;
-  }
-}
-
-__global__ void k_bin_count(BeadArgs a) {
+// pbc, then the bead's bin and its count (the counts are zero here: the
+// build that used the previous ones reset the bins it had filled)
+__global__ void k_pbc_bin(BeadArgs a) {
   if (!*a.flag) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
+  pbc_at(a, i);
   const int bx = bin_coord(a.x[3 * i], a.boxlo[0], a.bininv[0], a.nb[0]);
   const int by = bin_coord(a.x[3 * i + 1], a.boxlo[1], a.bininv[1], a.nb[1]);
   const int bz = bin_coord(a.x[3 * i + 2], a.boxlo[2], a.bininv[2], a.nb[2]);
@@ -215,9 +207,14 @@ __global__ void k_bin_fill(BeadArgs a) {
   a.sorted[pos] = i;
 }
 
-// order beads inside each bin by index so that the lists are deterministic
+// order beads inside each bin by index so that the lists are deterministic;
+// also clears the deposit support mask that the build then sets
 __global__ void k_bin_sort(BeadArgs a) {
   if (!*a.flag) return;
+  if (a.dmask)
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < a.gmask_words;
+         k += (long long)gridDim.x * blockDim.x)
+      a.dmask[k] = 0u;
   for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < a.nbins; b += (long long)gridDim.x * blockDim.x) {
     const int s = a.bin_start[b], e = a.bin_start[b + 1];
     for (int p = s + 1; p < e; ++p) {
@@ -227,6 +224,19 @@ __global__ void k_bin_sort(BeadArgs a) {
       a.sorted[q + 1] = v;
     }
   }
+}
+
+// the deposit support mask: the sector of a grid-list node
+PHAFD_D void dmask_set(const BeadArgs& a, uint32_t node) {
+  const long long sec = (long long)node / a.gmask_g;
+  atomicOr(a.dmask + (sec >> 5), 1u << (sec & 31));
+}
+// the bin counts the next rebuild starts from: zero again in the bead's bin
+// (every filled bin holds a bead, so this clears them all)
+PHAFD_D void bin_reset(const BeadArgs& a, int i) {
+  const int b = a.bin_of[i];
+  a.bin_count[b] = 0;
+  a.bin_cursor[b] = 0;
 }
 
 // stencil scans: full bead list and per-bead grid list
@@ -319,7 +329,10 @@ __global__ void k_build(BeadArgs a) {
           if (rsq <= cutsq) {
             const uint32_t node = (uint32_t)(((long long)wz * a.N[1] + wy) * a.N[0] + wx);
             const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
-            if (cnt < a.maxg) a.gl[(size_t)i * a.maxg + cnt] = (node << 5) | (uint32_t)code;
+            if (cnt < a.maxg) {
+              a.gl[(size_t)i * a.maxg + cnt] = (node << 5) | (uint32_t)code;
+              if (a.dmask) dmask_set(a, node);
+            }
             ++cnt;
           }
         }
@@ -328,6 +341,7 @@ __global__ void k_build(BeadArgs a) {
     if (cnt > a.maxg) { atomicOr(a.status, ST_OVERFLOW); cnt = a.maxg; }
     a.ngl[i] = cnt;
   }
+  bin_reset(a, i);
   // neighbor.cpp:106-109
   a.xhold[3 * i] = xi[0];
   a.xhold[3 * i + 1] = xi[1];
@@ -462,6 +476,7 @@ __global__ void k_build_fp32(BeadArgs a) {
               const uint32_t node = (uint32_t)(((long long)wz * a.N[1] + wy) * a.N[0] + wx);
               const int code = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
               a.gl[(size_t)i * a.maxg + base + cnt] = (node << 5) | (uint32_t)code;
+              if (a.dmask) dmask_set(a, node);
             }
             ++cnt;
           }
@@ -483,6 +498,7 @@ __global__ void k_build_fp32(BeadArgs a) {
     }
   }
   if (live && lane == 0) {
+    bin_reset(a, i);
     a.xhold[3 * i] = xi[0];
     a.xhold[3 * i + 1] = xi[1];
     a.xhold[3 * i + 2] = xi[2];
@@ -742,9 +758,7 @@ __global__ void k_drag(BeadArgs a, double dt) {
 // Bond vectors are differences of FP64 positions taken in FP64, then the
 // force arithmetic runs in T; positions stay FP64.
 template <typename T>
-__global__ void k_chain_force(BeadArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+PHAFD_D void chain_force_at(const BeadArgs& a, int i) {
   const int fi = a.sf_fix[i];
   if (fi < 0) return;
   const SemiDev& P = a.sf[fi];
@@ -793,12 +807,16 @@ __global__ void k_chain_force(BeadArgs a) {
   }
 }
 
+template <typename T>
+__global__ void k_chain_force(BeadArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) chain_force_at<T>(a, i);
+}
+
 // (nsub > 1: substep `sub` of a macro step; its noise is keyed by
 // step * nsub + sub so that every substep draws fresh numbers)
 template <typename T>
-__global__ void k_chain_move(BeadArgs a, int half, double dt, int nsub, int sub) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+PHAFD_D void chain_move_at(const BeadArgs& a, int i, int half, double dt, int nsub, int sub) {
   const int fi = a.sf_fix[i];
   if (fi < 0) return;
   const SemiDev& P = a.sf[fi];
@@ -829,6 +847,28 @@ __global__ void k_chain_move(BeadArgs a, int half, double dt, int nsub, int sub)
     bad |= !isfinite(nu);
   }
   if (bad) atomicOr(a.status, ST_CONSTRAINT);
+}
+
+template <typename T>
+__global__ void k_chain_move(BeadArgs a, int half, double dt, int nsub, int sub) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) chain_move_at<T>(a, i, half, dt, nsub, sub);
+}
+
+// Both half-steps of the chain model in one launch: one CTA per chain (the
+// chains are contiguous ranges of beads), its threads striding over the
+// chain's beads; a CTA barrier separates the force and the move of each half,
+// as the launch boundaries of k_chain_force / k_chain_move do.
+template <typename T>
+__global__ void k_chain_step(BeadArgs a, double dt, int nsub, int sub) {
+  const int s = a.chain_start[blockIdx.x];
+  const int len = a.sf_len[s];
+  for (int half = 0; half < 2; ++half) {
+    for (int b = threadIdx.x; b < len; b += blockDim.x) chain_force_at<T>(a, s + b);
+    __syncthreads();
+    for (int b = threadIdx.x; b < len; b += blockDim.x) chain_move_at<T>(a, s + b, half, dt, nsub, sub);
+    __syncthreads();
+  }
 }
 
 // ---------------------------------------------------------------- launchers
@@ -898,25 +938,6 @@ __global__ void k_gmask_build(BeadArgs a) {
   }
 }
 
-// deposit support: the sectors of every grid-list node (the pair stage
-// deposits only on listed nodes)
-__global__ void k_dmask_clear(BeadArgs a) {
-  if (!*a.flag) return;
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < a.gmask_words;
-       k += (long long)gridDim.x * blockDim.x)
-    a.dmask[k] = 0u;
-}
-__global__ void k_dmask_build(BeadArgs a) {
-  if (!*a.flag) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  const int cnt = a.ngl[i];
-  for (int k = 0; k < cnt; ++k) {
-    const long long sec = (long long)(a.gl[(size_t)i * a.maxg + k] >> 5) / a.gmask_g;
-    atomicOr(a.dmask + (sec >> 5), 1u << (sec & 31));
-  }
-}
-
 __global__ void k_gmask_guard(BeadArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -970,9 +991,7 @@ void launch_touch(const double* x, int n, double touch_point, int delay_step, co
 void launch_rebuild(const BeadArgs& a, cudaStream_t st) {
   if (a.n == 0) return;
   const int T = 256;
-  k_pbc<<<nblk(a.n, T), T, 0, st>>>(a);
-  k_bin_clear<<<nblk(a.nbins, T) > 4096 ? 4096 : nblk(a.nbins, T), T, 0, st>>>(a);
-  k_bin_count<<<nblk(a.n, T), T, 0, st>>>(a);
+  k_pbc_bin<<<nblk(a.n, T), T, 0, st>>>(a);
   const int nblocks = (int)((a.nbins + 1023) / 1024);
   k_scan_block<<<nblocks, 1024, 0, st>>>(a);
   k_scan_sums<<<1, 1024, 0, st>>>(a, nblocks);
@@ -991,10 +1010,6 @@ void launch_rebuild(const BeadArgs& a, cudaStream_t st) {
   if (a.gmask) {
     k_gmask_clear<<<1024, 256, 0, st>>>(a);
     k_gmask_build<<<nblk(a.n, 128), 128, 0, st>>>(a);
-  }
-  if (a.dmask && a.gl) {
-    k_dmask_clear<<<256, 256, 0, st>>>(a);
-    k_dmask_build<<<nblk(a.n, 128), 128, 0, st>>>(a);
   }
   k_build_done<<<1, 1, 0, st>>>(a);
 }
@@ -1028,5 +1043,13 @@ void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st, 
 }
 template void launch_chain_half<float>(const BeadArgs&, int, double, cudaStream_t, int, int);
 template void launch_chain_half<double>(const BeadArgs&, int, double, cudaStream_t, int, int);
+
+template <typename T>
+void launch_chain_step(const BeadArgs& a, double dt, cudaStream_t st, int nsub, int sub) {
+  if (a.n == 0 || !a.any_semi) return;
+  k_chain_step<T><<<a.nchains, 256, 0, st>>>(a, dt, nsub, sub);
+}
+template void launch_chain_step<float>(const BeadArgs&, double, cudaStream_t, int, int);
+template void launch_chain_step<double>(const BeadArgs&, double, cudaStream_t, int, int);
 
 }  // namespace phafd

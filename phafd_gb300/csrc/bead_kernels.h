@@ -59,6 +59,8 @@ struct BeadArgs {
   int *sf_fix, *sf_start, *sf_len;
   const SemiDev* sf;
   int any_semi;
+  const int* chain_start;  // first bead of every chain of the semiflexible fixes
+  int nchains;
 };
 
 template <typename T>
@@ -103,5 +105,8 @@ template <typename T> void launch_density(const BeadArgs& a, const PairArgs<T>& 
 void launch_drag(const BeadArgs& a, double dt, cudaStream_t st);
 template <typename T>
 void launch_chain_half(const BeadArgs& a, int half, double dt, cudaStream_t st, int nsub = 1, int sub = 0);
+// both halves (force, move, force, move) in one launch, one CTA per chain
+template <typename T>
+void launch_chain_step(const BeadArgs& a, double dt, cudaStream_t st, int nsub = 1, int sub = 0);
 
 }  // namespace phafd

@@ -230,7 +230,7 @@ struct phafd_ctx {
   DevBuf bx, bux, bf, bxhold, bfchain, btang, bimage, btype;
   DevBuf bin_of, bin_count, bin_cursor, bin_start, sorted, scan_tmp, bin_off;
   DevBuf nbr, nnbr, gl, ngl;
-  DevBuf dragc, sf_fix, sf_start, sf_len, sf_par;
+  DevBuf dragc, sf_fix, sf_start, sf_len, sf_par, chain0;
   DevBuf gmask;  // one bit per 32-byte sector of a real field (beads with a grid coupling)
   DevBuf dmask;  // the same sectors: the deposit's support, rebuilt with the grid lists
   DevBuf bx_pair, bf_tmp;  // positions of the last pair stage (phafd_set_pair_snapshot); compute pair's forces
@@ -258,6 +258,7 @@ struct phafd_ctx {
   double fh_temp = 1, fh_volFH = 1, fh_chi = 1;
   std::vector<std::pair<std::vector<Range>, double>> drags;
   std::vector<std::pair<std::vector<Range>, phafd_semiflexible_params>> semis;
+  int nchains = 0;
   // integrate
   double dt = 0;
   long long timestep = 0, firststep = 0;
@@ -515,6 +516,8 @@ struct phafd_ctx {
     a.sf_fix = sf_fix.as<int>(); a.sf_start = sf_start.as<int>(); a.sf_len = sf_len.as<int>();
     a.sf = sf_par.as<SemiDev>();
     a.any_semi = !semis.empty();
+    a.chain_start = chain0.as<int>();
+    a.nchains = nchains;
     a.gmask = use_gmask && gmask.p ? gmask.as<uint32_t>() : nullptr;
     a.gmask_g = 32 / (int)rsz();
     a.gmask_words = ((long long)nreal / a.gmask_g + 32) / 32;
@@ -603,6 +606,8 @@ struct phafd_ctx {
     bin_of.alloc(std::max(n, 1) * 4);
     bin_count.alloc(nbins * 4);
     bin_cursor.alloc(nbins * 4);
+    bin_count.zero(st);  // then zero after every build (the build resets the bins it filled)
+    bin_cursor.zero(st);
     bin_start.alloc((nbins + 1) * 4);
     sorted.alloc(std::max(n, 1) * 4);
     bin_off.alloc((size_t)std::max(n, 1) * sizeof(float4));
@@ -639,6 +644,7 @@ struct phafd_ctx {
     CK(cudaMemcpy(dragc.p, dc.data(), dc.size() * 8, cudaMemcpyHostToDevice));
     std::vector<int> fix(std::max(n, 1), -1), s0(std::max(n, 1), 0), ln(std::max(n, 1), 0);
     std::vector<SemiDev> par;
+    std::vector<int> starts;
     for (size_t k = 0; k < semis.size(); ++k) {
       const auto& p = semis[k].second;
       SemiDev d{p.bondlength, p.zeta_para, p.zeta_perp, p.bending, p.temp, p.kbond, (uint32_t)p.seed, p.noise,
@@ -648,16 +654,21 @@ struct phafd_ctx {
       d.sinv_perp = 1.0 / std::sqrt(p.zeta_perp);
       d.dsinv = 1.0 / std::sqrt(p.zeta_para) - 1.0 / std::sqrt(p.zeta_perp);
       par.push_back(d);
-      for (auto& r : semis[k].first)
+      for (auto& r : semis[k].first) {
+        if (r.end > r.start) starts.push_back(r.start);
         for (int j = r.start; j < r.end; ++j) {
           if (fix[j] >= 0) throw std::runtime_error("a bead may belong to one semiflexible fix only");
           fix[j] = (int)k; s0[j] = r.start; ln[j] = r.end - r.start;
         }
+      }
     }
     sf_fix.alloc(fix.size() * 4); sf_start.alloc(s0.size() * 4); sf_len.alloc(ln.size() * 4);
     CK(cudaMemcpy(sf_fix.p, fix.data(), fix.size() * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(sf_start.p, s0.data(), s0.size() * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(sf_len.p, ln.data(), ln.size() * 4, cudaMemcpyHostToDevice));
+    nchains = (int)starts.size();
+    chain0.alloc(std::max<size_t>(starts.size(), 1) * 4);
+    if (!starts.empty()) CK(cudaMemcpy(chain0.p, starts.data(), starts.size() * 4, cudaMemcpyHostToDevice));
     sf_par.alloc(std::max<size_t>(par.size(), 1) * sizeof(SemiDev));
     if (!par.empty()) CK(cudaMemcpy(sf_par.p, par.data(), par.size() * sizeof(SemiDev), cudaMemcpyHostToDevice));
     if (ntypes > 0) {
@@ -760,13 +771,22 @@ struct phafd_ctx {
       CK(cudaEventRecord(ev_fork, st));
       CK(cudaStreamWaitEvent(st2, ev_fork, 0));
     }
-    // initial_integrate
-    launch_drag(ba, dt, bs);
-    launch_chain_half<T>(ba, 0, dt, bs, nsub, 0);
-    // final_integrate of the beads (independent of the field update)
-    launch_drag(ba, dt, bs);
-    launch_chain_half<T>(ba, 1, dt, bs, nsub, 0);
-    const bool masked = resident && gmask_steps();
+    // initial_integrate, then final_integrate of the beads (independent of
+    // the field update).  Without drag fixes both chain halves are one launch;
+    // on the resident bead branch it follows the deposit reset, so it runs
+    // beside the y and z passes rather than beside the persistent x r2c
+    // (whose CTAs fill the SMs and would otherwise wait for its blocks)
+    const bool one_launch = !(ba.any_drag || ba.nchains == 0);
+    const bool masked = resident && gmask_steps();  // its guard reads the integrated positions
+    const bool late_chain = one_launch && fork && resident && have_conj && !masked;
+    if (!one_launch) {
+      launch_drag(ba, dt, bs);
+      launch_chain_half<T>(ba, 0, dt, bs, nsub, 0);
+      launch_drag(ba, dt, bs);
+      launch_chain_half<T>(ba, 1, dt, bs, nsub, 0);
+    } else if (!late_chain) {
+      launch_chain_step<T>(ba, dt, bs, nsub, 0);
+    }
     if (masked) {
       launch_gmask_guard(ba, bs);
       grad_partial = true;
@@ -784,6 +804,7 @@ struct phafd_ctx {
           chk(GridOps<T>::xr2c(geom, phi.as<T>(), dep.as<T>(), W1, twf[0], fh, st), "x r2c");
           mark(4);
           dep_reset<T>(fork);
+          if (late_chain) launch_chain_step<T>(ba, dt, bs, nsub, 0);
           macro_bead_substeps<T>(bs);
           if (early_ok && check_next_early && fork) neighbor_stage(st2, nullptr);
           chk(GridOps<T>::ypass(geom, -1, W1, W1, nullptr, twf[1], st), "y fft");
@@ -791,6 +812,7 @@ struct phafd_ctx {
           chk(prc, "xy fwd");
           mark(4);
           dep_reset<T>(fork);
+          if (late_chain) launch_chain_step<T>(ba, dt, bs, nsub, 0);
           macro_bead_substeps<T>(bs);
           if (early_ok && check_next_early && fork) neighbor_stage(st2, nullptr);
         }
@@ -886,10 +908,14 @@ struct phafd_ctx {
     for (int sub = 1; sub < nsub; ++sub) {
       neighbor_stage(bs);
       if (have_lj || ga_style != PHAFD_GRIDATOM_NONE) launch_pair<T>(ba, pa, bs);
-      launch_drag(ba, dt, bs);
-      launch_chain_half<T>(ba, 0, dt, bs, nsub, sub);
-      launch_drag(ba, dt, bs);
-      launch_chain_half<T>(ba, 1, dt, bs, nsub, sub);
+      if (ba.any_drag || ba.nchains == 0) {
+        launch_drag(ba, dt, bs);
+        launch_chain_half<T>(ba, 0, dt, bs, nsub, sub);
+        launch_drag(ba, dt, bs);
+        launch_chain_half<T>(ba, 1, dt, bs, nsub, sub);
+      } else {
+        launch_chain_step<T>(ba, dt, bs, nsub, sub);
+      }
     }
   }
 
