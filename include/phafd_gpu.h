@@ -189,6 +189,12 @@ int phafd_set_gradient_mask(phafd_ctx* ctx, int on);
 #define PHAFD_TUNE_XC2R_TMA 4
 #define PHAFD_TUNE_XR2C_TMA 8
 int phafd_set_variants(phafd_ctx* ctx, int flags);
+/* Steps per CUDA graph of a run (even, >= 2; default 8): runs launch graphs
+ * of this many steps, then two-step and one-step graphs for the rest.  Long
+ * graphs keep a single system's neighbor checks off its critical path (every
+ * step but a graph's first checks on the previous step's bead branch); many
+ * contexts sharing one GPU interleave better with two-step graphs. */
+int phafd_set_graph_steps(phafd_ctx* ctx, int steps);
 int phafd_autotune(phafd_ctx* ctx, int steps, int* best, double* ms);
 #define PHAFD_CENTER_FH 1
 #define PHAFD_CENTER_FFT 2

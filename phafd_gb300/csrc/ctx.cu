@@ -277,7 +277,8 @@ struct phafd_ctx {
   int* d_gmask_off() const { return reinterpret_cast<int*>(d_counters.as<long long>() + 6) + 1; }
   // graph
   cudaGraphExec_t gexec = nullptr;
-  cudaGraphExec_t gexecK = nullptr;                 // GRAPH_STEPS steps (resident)
+  cudaGraphExec_t gexecK = nullptr;                 // graph_steps steps (resident)
+  int graph_steps = 8;
   int graph_curK = 0;
   cudaGraphExec_t gexec1[2] = {nullptr, nullptr};  // one step, per spectrum parity (resident)
   // Inside a multi-step graph the neighbor check (and conditional rebuild) of
@@ -1627,6 +1628,14 @@ static void apply_variants(phafd_ctx* c, int flags) {
   c->invalidate_graph();
 }
 
+int phafd_set_graph_steps(phafd_ctx* c, int steps) {
+  API_BEGIN(c)
+  if (steps < 2 || (steps & 1)) throw std::invalid_argument("graph steps: an even number >= 2");
+  c->graph_steps = steps;
+  c->invalidate_graph();
+  API_END(c)
+}
+
 int phafd_set_variants(phafd_ctx* c, int flags) {
   API_BEGIN(c)
   if (flags & ~(PHAFD_TUNE_PLANE | PHAFD_TUNE_GENERIC256 | PHAFD_TUNE_XC2R_TMA | PHAFD_TUNE_XR2C_TMA))
@@ -1764,10 +1773,6 @@ int phafd_run_async(phafd_ctx* c, int nsteps) {
   API_END(c)
 }
 
-// steps captured in one graph for runs of at least that many (even: both
-// spectrum parities of the resident schedule)
-constexpr int GRAPH_STEPS = 8;
-
 static void enqueue_run(phafd_ctx* c, int nsteps) {
   {
   c->check_done_early = c->check_next_early = false;  // set only while a multi-step graph is captured
@@ -1784,10 +1789,11 @@ static void enqueue_run(phafd_ctx* c, int nsteps) {
       CK(cudaGetLastError());
       if (use_graph) c->eager_done = true;
     } else {
-      // Graphs: GRAPH_STEPS steps, then two (both spectrum parities of the
+      // Graphs: graph_steps steps, then two (both spectrum parities of the
       // resident schedule), one step per parity for the rest.
       bool launched = false;
-      for (const int k : {GRAPH_STEPS, 2}) {
+      for (const int k : {c->graph_steps, 2}) {
+        if (k == c->graph_steps && k == 2) continue;  // the two-step graph comes next
         cudaGraphExec_t& ge = k == 2 ? c->gexec : c->gexecK;
         int& gcur = k == 2 ? c->graph_cur : c->graph_curK;
         if (!(resident && nsteps - s >= k && (!ge || c->cur == gcur))) continue;

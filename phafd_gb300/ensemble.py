@@ -35,6 +35,7 @@ class Ensemble:
         self.replicas = []
         for k, cfg in enumerate(configs):
             g = PhafdGPU(precision=precision, device=device)
+            g.set_graph_steps(2)  # many contexts on one GPU interleave better with short graphs
             W.apply(g, cfg, chains=None if chains is None else chains[k])
             g.setup()
             self.replicas.append(g)

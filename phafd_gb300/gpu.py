@@ -29,7 +29,7 @@ EXPORTS = [
     "phafd_grid_populate_sphere", "phafd_grid_set", "phafd_grid_get",
     "phafd_set_zghost", "phafd_set_schedule", "phafd_set_keep_chempot", "phafd_set_plane_fusion",
     "phafd_set_gradient_mask", "phafd_set_fp32_centering", "phafd_set_pair_snapshot", "phafd_compute_pair",
-    "phafd_set_variants", "phafd_autotune",
+    "phafd_set_variants", "phafd_autotune", "phafd_set_graph_steps",
     "phafd_atoms_create", "phafd_atoms_get", "phafd_atoms_set_images",
     "phafd_pair_gridatom", "phafd_pair_gridatom_coeff", "phafd_pair_lj_cut",
     "phafd_neighbor",
@@ -92,6 +92,7 @@ def load(path=None):
         "phafd_set_fp32_centering": [vp, C.c_int],
         "phafd_set_pair_snapshot": [vp, C.c_int],
         "phafd_set_variants": [vp, C.c_int],
+        "phafd_set_graph_steps": [vp, C.c_int],
         "phafd_autotune": [vp, C.c_int, C.POINTER(C.c_int), dp],
         "phafd_compute_pair": [vp, C.c_int, C.c_int, dp],
         "phafd_domain": [vp, dp, dp],
@@ -210,6 +211,10 @@ class PhafdGPU:
         xc2r_tma and xr2c_tma on)."""
         self._call("phafd_set_variants", (1 if plane else 0) | (2 if generic256 else 0) | (4 if xc2r_tma else 0)
                    | (8 if xr2c_tma else 0))
+
+    def set_graph_steps(self, steps):
+        """Steps per CUDA graph of a run (even, >= 2; default 8)."""
+        self._call("phafd_set_graph_steps", steps)
 
     def autotune(self, steps=10):
         """Time every variant over `steps` steps of the run, keep the fastest:

@@ -357,6 +357,30 @@ def test_tma_x_r2c_reads_the_whole_deposit(gpu_lib):
     assert np.abs(b - a).max() < 1e-5 * np.abs(a).max()
 
 
+@pytest.mark.parametrize("graph_steps", [2, 8, 16])
+def test_graph_length_does_not_change_the_run(gpu_lib, graph_steps):
+    """Runs of 19 steps (8- or 16-step graphs, whose later steps check their
+    neighbor lists on the previous step's bead branch, then 2- and 1-step
+    graphs) match the oracle within 1e-10, lists included."""
+    cfg = dict(W.CONFIGS["32cube_64beads"])
+    cfg.update(field_noise="philox", bead_temp=1.0, dt=1e-3)
+    o = Oracle(); g = gpu(64, "resident")
+    g.set_graph_steps(graph_steps)
+    chains = None
+    for d in (o, g):
+        chains = W.apply(d, cfg, chains=chains)
+        d.setup()
+        d.run(19)
+    assert rel_err(g.grid_get("phi"), o.grid_get("phi")) < 1e-10
+    xo, xg = o.atoms_get()[0], g.atoms_get()[0]
+    assert np.abs(xg - xo).max() < 1e-10 * np.abs(xo).max()
+    assert g.counters()["neighbor_calls"] == o.counters()["neighbor_calls"] >= 2
+    assert canon_half(g.half_list()) == canon_half(o.half_list())
+    assert canon_grid(g.grid_list()) == canon_grid(o.grid_list())
+    with pytest.raises(Exception):
+        g.set_graph_steps(3)
+
+
 def test_autotune_steps_are_steps_of_the_run(gpu_lib):
     """The autotuner times each variant on the run's own steps: afterwards
     the state equals the oracle's after the same number of steps, and the
