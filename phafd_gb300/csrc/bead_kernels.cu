@@ -41,9 +41,27 @@ __device__ __forceinline__ int bin_coord(double x, double lo, double inv, int nb
 // neighbor.cpp:79-97
 // With use_cond the last block to finish (threadfence pattern) copies the
 // flag into the graph conditional that gates the rebuild body.
+// It also zeroes the deposit on the bead's grid-list nodes (the last pair
+// stage deposited there; the pass that reads the deposit ran before this
+// check), list words gathered four at a time.
 __global__ void k_check(BeadArgs a, cudaGraphConditionalHandle h, int use_cond, long long* step_inc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (step_inc && i == 0) *step_inc += 1;
+  if (i < a.n && a.dep && a.gl) {
+    const int cnt = a.ngl[i];
+    const uint32_t* __restrict__ gl = a.gl + (size_t)i * a.maxg;
+    for (int k0 = 0; k0 < cnt; k0 += 4) {
+      uint32_t e[4];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) e[b] = k0 + b < cnt ? gl[k0 + b] : 0xffffffffu;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        if (e[b] == 0xffffffffu) continue;
+        if (a.dep_bytes == 8) reinterpret_cast<double*>(a.dep)[e[b] >> 5] = 0.0;
+        else reinterpret_cast<float*>(a.dep)[e[b] >> 5] = 0.f;
+      }
+    }
+  }
   if (i < a.n) {
     const double d0 = a.x[3 * i] - a.xhold[3 * i];
     const double d1 = a.x[3 * i + 1] - a.xhold[3 * i + 1];
@@ -735,15 +753,6 @@ void launch_density(const BeadArgs& a, const PairArgs<T>& p, T* rho, cudaStream_
 template void launch_density<float>(const BeadArgs&, const PairArgs<float>&, float*, cudaStream_t);
 template void launch_density<double>(const BeadArgs&, const PairArgs<double>&, double*, cudaStream_t);
 
-// zero the nodes a bead may have deposited on (sparse reset of dep)
-template <typename T>
-__global__ void k_dep_zero(BeadArgs a, T* dep) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n || !a.gl) return;
-  const int cnt = a.ngl[i];
-  for (int k = 0; k < cnt; ++k) dep[a.gl[(size_t)i * a.maxg + k] >> 5] = (T)0;
-}
-
 // fixatom_drag.cpp:47-52 / 58-62
 __global__ void k_drag(BeadArgs a, double dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1022,13 +1031,6 @@ void launch_pair(const BeadArgs& a, const PairArgs<T>& p, cudaStream_t st) {
 template void launch_pair<float>(const BeadArgs&, const PairArgs<float>&, cudaStream_t);
 template void launch_pair<double>(const BeadArgs&, const PairArgs<double>&, cudaStream_t);
 
-template <typename T>
-void launch_dep_zero(const BeadArgs& a, T* dep, cudaStream_t st) {
-  if (a.n == 0) return;
-  k_dep_zero<T><<<nblk(a.n, 256), 256, 0, st>>>(a, dep);
-}
-template void launch_dep_zero<float>(const BeadArgs&, float*, cudaStream_t);
-template void launch_dep_zero<double>(const BeadArgs&, double*, cudaStream_t);
 
 void launch_drag(const BeadArgs& a, double dt, cudaStream_t st) {
   if (a.n == 0 || !a.any_drag) return;

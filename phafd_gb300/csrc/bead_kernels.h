@@ -32,6 +32,8 @@ struct BeadArgs {
   int* gmask_off;       // set: the mask does not cover the current positions (cleared by a rebuild)
   uint32_t* dmask;      // bit per 32-byte sector (gmask_g nodes) holding a node of the grid lists, rebuilt with
                         // them: the deposit's support (null: none)
+  void* dep;            // the mu deposit (dep_bytes per node): the check zeroes the nodes of the current grid
+  int dep_bytes;        // lists, which hold the last pair stage's deposits (null: nothing to zero)
   int* check_done;      // blocks of k_check finished (last one sets the graph condition)
   int* status;          // sticky ST_* bits
   long long* ncalls;    // Neighbor::ncalls
@@ -100,7 +102,6 @@ void launch_touch(const double* x, int n, double touch_point, int delay_step, co
 // sets *gmask_off when a bead moved more than sqrt(gmask_guardsq) since the last rebuild
 void launch_gmask_guard(const BeadArgs& a, cudaStream_t st);
 template <typename T> void launch_pair(const BeadArgs& a, const PairArgs<T>& p, cudaStream_t st);
-template <typename T> void launch_dep_zero(const BeadArgs& a, T* dep, cudaStream_t st);
 template <typename T> void launch_density(const BeadArgs& a, const PairArgs<T>& p, T* rho, cudaStream_t st);
 void launch_drag(const BeadArgs& a, double dt, cudaStream_t st);
 template <typename T>

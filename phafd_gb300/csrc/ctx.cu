@@ -526,6 +526,8 @@ struct phafd_ctx {
     a.gmask_guardsq = skin * skin;
     a.gmask_off = d_gmask_off();
     a.dmask = dmask.p ? dmask.as<uint32_t>() : nullptr;
+    a.dep = ga_style != PHAFD_GRIDATOM_NONE ? dep.p : nullptr;
+    a.dep_bytes = (int)rsz();
   }
 
   // steps store grad phi at masked nodes only (single-substep resident steps
@@ -920,18 +922,14 @@ struct phafd_ctx {
     }
   }
 
-  // zero the deposit nodes once the x pass has consumed them: on the bead
-  // branch when forked, so it overlaps the field passes
+  // The deposit is zeroed by the next neighbor check (on its grid lists);
+  // forked, the bead branch waits here for the x pass that reads the
+  // deposit, since its check comes later on that branch.
   template <typename T>
   void dep_reset(bool fork) {
-    if (n == 0 || ga_style == PHAFD_GRIDATOM_NONE) return;
-    if (fork) {
-      CK(cudaEventRecord(ev_dep, st));
-      CK(cudaStreamWaitEvent(st2, ev_dep, 0));
-      launch_dep_zero<T>(ba, dep.as<T>(), st2);
-    } else {
-      launch_dep_zero<T>(ba, dep.as<T>(), st);
-    }
+    if (n == 0 || ga_style == PHAFD_GRIDATOM_NONE || !fork) return;
+    CK(cudaEventRecord(ev_dep, st));
+    CK(cudaStreamWaitEvent(st2, ev_dep, 0));
   }
 
   void step_once() {
@@ -1564,6 +1562,7 @@ int phafd_setup(phafd_ctx* c) {
     c->setup_neighbor_structs();
     c->upload_fix_tables();
     c->fill_bead_args();
+    c->dep.zero(c->st);  // the lists about to be built replace those the next check would zero on
     launch_neighbor(c->ba, true, c->st);  // Integrate::setup: pbc, borders, build
     c->bf.zero(c->st);
   }
@@ -2008,6 +2007,7 @@ int phafd_stage_borders_and_build(phafd_ctx* c) {
     c->upload_fix_tables();
   }
   c->fill_bead_args();
+  c->dep.zero(c->st);  // the lists about to be built replace those the next check would zero on
   launch_neighbor(c->ba, true, c->st);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
