@@ -203,6 +203,20 @@ int phafd_set_fp32_centering(phafd_ctx* ctx, int stages);
 /* ---- beads (atom_style / atom_populate, atom.cpp:26-110,219-252) ---- */
 int phafd_atoms_create(phafd_ctx* ctx, int n, const int* tags, const int* mol, const int* types, const double* x);
 int phafd_atoms_get(phafd_ctx* ctx, double* x, double* ux, double* f, int* images);
+/* Read-back pipelined with the steps: phafd_atoms_get_async enqueues the
+ * copies of x, ux, F and the image flags (NULL skips one) into host memory
+ * at the current end of the context's stream, after the steps enqueued so
+ * far, and returns; slot (0..3) names the copy.  phafd_wait_slot waits for
+ * that copy only (later steps may still run) and reports the device status
+ * as of the copy (NaN step, overflow, constraint failure).  With page-locked
+ * host buffers (phafd_host_register) the copies run on the copy engine
+ * while the next steps compute, so a caller that reads every step's beads
+ * can enqueue step k + 1 before it waits for step k's copy. */
+int phafd_atoms_get_async(phafd_ctx* ctx, double* x, double* ux, double* f, int* images, int slot);
+int phafd_wait_slot(phafd_ctx* ctx, int slot);
+/* page-lock (and release) a caller's host buffer for asynchronous copies */
+int phafd_host_register(void* ptr, size_t bytes);
+int phafd_host_unregister(void* ptr);
 /* image flags of every bead, packed as Domain::set_image (x in bits 0-9, y in
  * 10-19, z from 20, each offset by 512): the "ix" attribute that
  * atom_populate read_dump restores (read_dump.cpp:239-240); called after

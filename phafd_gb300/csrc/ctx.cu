@@ -150,6 +150,10 @@ struct phafd_ctx {
   cudaStream_t st3 = nullptr;           // Hermitian-plane branch, forked from st inside a step
   cudaStream_t stc = nullptr;           // capture of the conditional rebuild body only
   cudaEvent_t ev_fork = nullptr, ev_dep = nullptr, ev_join = nullptr;
+  // pipelined read-back: per slot an event after its copies and the status
+  // words copied with them into page-locked memory
+  cudaEvent_t ev_slot[4] = {nullptr, nullptr, nullptr, nullptr};
+  long long* slot_status = nullptr;  // [slot][2]: nan step, flag|status
   cudaEvent_t ev_pl_fork = nullptr, ev_pl_join = nullptr;
   // domain / grid
   bool boxset = false, gridset = false, populated = false;
@@ -308,6 +312,8 @@ struct phafd_ctx {
       if (ge) cudaGraphExecDestroy(ge);
     if (uref_h) cudaFreeHost(uref_h);
     for (cudaEvent_t e : {ev_fork, ev_dep, ev_join, ev_pl_fork, ev_pl_join}) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : ev_slot) if (e) cudaEventDestroy(e);
+    if (slot_status) cudaFreeHost(slot_status);
     if (stc) cudaStreamDestroy(stc);
     if (st3) cudaStreamDestroy(st3);
     if (st2) cudaStreamDestroy(st2);
@@ -1392,6 +1398,62 @@ int phafd_atoms_get(phafd_ctx* c, double* x, double* ux, double* f, int* images)
   if (f) CK(cudaMemcpy(f, c->bf.p, 3 * n * 8, cudaMemcpyDeviceToHost));
   if (images) CK(cudaMemcpy(images, c->bimage.p, n * 4, cudaMemcpyDeviceToHost));
   API_END(c)
+}
+
+int phafd_atoms_get_async(phafd_ctx* c, double* x, double* ux, double* f, int* images, int slot) {
+  API_BEGIN(c)
+  if (slot < 0 || slot > 3) throw std::invalid_argument("slot: 0..3");
+  CK(cudaSetDevice(c->device));
+  if (!c->ev_slot[slot]) CK(cudaEventCreateWithFlags(&c->ev_slot[slot], cudaEventDisableTiming));
+  if (!c->slot_status) CK(cudaHostAlloc(reinterpret_cast<void**>(&c->slot_status), 8 * sizeof(long long), 0));
+  const size_t n = c->n;
+  if (n > 0) {
+    if (x) CK(cudaMemcpyAsync(x, c->bx.p, 3 * n * 8, cudaMemcpyDeviceToHost, c->st));
+    if (ux) CK(cudaMemcpyAsync(ux, c->bux.p, 3 * n * 8, cudaMemcpyDeviceToHost, c->st));
+    if (f) CK(cudaMemcpyAsync(f, c->bf.p, 3 * n * 8, cudaMemcpyDeviceToHost, c->st));
+    if (images) CK(cudaMemcpyAsync(images, c->bimage.p, n * 4, cudaMemcpyDeviceToHost, c->st));
+  }
+  CK(cudaMemcpyAsync(c->slot_status + 2 * slot, c->d_counters.as<long long>() + 3, sizeof(long long),
+                     cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(c->slot_status + 2 * slot + 1, c->d_counters.as<long long>() + 5, sizeof(long long),
+                     cudaMemcpyDeviceToHost, c->st));
+  CK(cudaEventRecord(c->ev_slot[slot], c->st));
+  API_END(c)
+}
+
+int phafd_wait_slot(phafd_ctx* c, int slot) {
+  API_BEGIN(c)
+  if (slot < 0 || slot > 3 || !c->ev_slot[slot]) throw std::invalid_argument("no read-back enqueued on this slot");
+  CK(cudaEventSynchronize(c->ev_slot[slot]));
+  const long long nan_step = c->slot_status[2 * slot];
+  const int status = reinterpret_cast<const int*>(c->slot_status + 2 * slot + 1)[1];
+  if (nan_step >= 0) {
+    c->err = "NAN encountered in phi. (step " + std::to_string(nan_step) + ")";
+    return PHAFD_ERR_NAN;
+  }
+  if (status & ST_OVERFLOW) {
+    c->err = "Neighbor list overflow";
+    return PHAFD_ERR_OVERFLOW;
+  }
+  if (status & ST_CONSTRAINT) {
+    c->err = "Failed to maintain polymer bond-length constraints.";
+    return PHAFD_ERR_CONSTRAINT;
+  }
+  if (status & ST_TIMEOUT) {
+    c->err = "a grid pass gave up waiting for its tensor-map loads";
+    return PHAFD_ERR_TIMEOUT;
+  }
+  API_END(c)
+}
+
+int phafd_host_register(void* ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return PHAFD_ERR_INVALID;
+  return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? PHAFD_OK : PHAFD_ERR_CUDA;
+}
+
+int phafd_host_unregister(void* ptr) {
+  if (!ptr) return PHAFD_ERR_INVALID;
+  return cudaHostUnregister(ptr) == cudaSuccess ? PHAFD_OK : PHAFD_ERR_CUDA;
 }
 
 int phafd_atoms_set_images(phafd_ctx* c, const int* images) {

@@ -30,7 +30,8 @@ EXPORTS = [
     "phafd_set_zghost", "phafd_set_schedule", "phafd_set_keep_chempot", "phafd_set_plane_fusion",
     "phafd_set_gradient_mask", "phafd_set_fp32_centering", "phafd_set_pair_snapshot", "phafd_compute_pair",
     "phafd_set_variants", "phafd_autotune", "phafd_set_graph_steps",
-    "phafd_atoms_create", "phafd_atoms_get", "phafd_atoms_set_images",
+    "phafd_atoms_create", "phafd_atoms_get", "phafd_atoms_set_images", "phafd_atoms_get_async", "phafd_wait_slot",
+    "phafd_host_register", "phafd_host_unregister",
     "phafd_pair_gridatom", "phafd_pair_gridatom_coeff", "phafd_pair_lj_cut",
     "phafd_neighbor",
     "phafd_fix_conjugate_volfrac", "phafd_fix_floryhuggins", "phafd_fix_gradphi", "phafd_fix_drag",
@@ -104,6 +105,10 @@ def load(path=None):
         "phafd_grid_get": [vp, C.c_int, dp],
         "phafd_atoms_create": [vp, C.c_int, ip, ip, ip, dp],
         "phafd_atoms_get": [vp, dp, dp, dp, ip],
+        "phafd_atoms_get_async": [vp, dp, dp, dp, ip, C.c_int],
+        "phafd_wait_slot": [vp, C.c_int],
+        "phafd_host_register": [C.c_void_p, C.c_size_t],
+        "phafd_host_unregister": [C.c_void_p],
         "phafd_atoms_set_images": [vp, ip],
         "phafd_pair_gridatom": [vp, C.c_int, C.c_double],
         "phafd_pair_gridatom_coeff": [vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double],
@@ -341,6 +346,18 @@ class PhafdGPU:
         self._call("phafd_atoms_get", x.reshape(-1), ux.reshape(-1), f.reshape(-1), im)
         return x[:self.n], ux[:self.n], f[:self.n], im[:self.n]
 
+    def atoms_get_async(self, bufs, slot):
+        """Enqueue the beads' read-back (x, ux, F, image flags) into the
+        caller's arrays bufs = (x, ux, f, images), which must stay alive until
+        wait_slot(slot); page-locked (host_register) they fill while later
+        steps compute."""
+        x, ux, f, im = bufs
+        self._call("phafd_atoms_get_async", x.reshape(-1), ux.reshape(-1), f.reshape(-1), im, slot)
+
+    def wait_slot(self, slot):
+        """Wait for the read-back enqueued on `slot`; raise on a device error."""
+        self._call("phafd_wait_slot", slot)
+
     def noise_state(self):
         """the reference-noise generator's state (text), for a restart"""
         n = C.c_int(0)
@@ -456,6 +473,17 @@ class PhafdGPU:
         out = np.zeros(3 * max(n.value, 1), np.int32)
         self._call("phafd_grid_list", out)
         return out[:3 * n.value].reshape(n.value, 3)
+
+
+def host_register(arr):
+    """Page-lock a numpy array's memory for asynchronous copies."""
+    rc = load().phafd_host_register(arr.ctypes.data, arr.nbytes)
+    if rc:
+        raise PhafdError(rc, "cudaHostRegister failed")
+
+
+def host_unregister(arr):
+    load().phafd_host_unregister(arr.ctypes.data)
 
 
 def build_info():

@@ -381,6 +381,46 @@ def test_graph_length_does_not_change_the_run(gpu_lib, graph_steps):
         g.set_graph_steps(3)
 
 
+def test_pipelined_bead_readback(gpu_lib):
+    """phafd_atoms_get_async / phafd_wait_slot: every step's beads read back
+    while the next step is already enqueued equal a step-by-step run with
+    blocking reads (page-locked buffers, two slots alternating)."""
+    from phafd_gb300 import gpu as G
+    cfg = dict(W.CONFIGS["32cube_64beads"])
+    cfg.update(field_noise="philox", bead_temp=1.0, dt=1e-3)
+    a = gpu(64, "resident"); b = gpu(64, "resident")
+    chains = None
+    for d in (a, b):
+        chains = W.apply(d, cfg, chains=chains)
+        d.setup()
+    n = a.n
+    bufs = [(np.empty((n, 3)), np.empty((n, 3)), np.empty((n, 3)), np.empty(n, np.int32)) for _ in range(2)]
+    for bb in bufs:
+        for arr in bb:
+            G.host_register(arr)
+    got = []
+    steps = 7
+    for s in range(steps):
+        a.run_async(1)
+        a.atoms_get_async(bufs[s & 1], s & 1)
+        if s:
+            a.wait_slot((s - 1) & 1)
+            got.append([arr.copy() for arr in bufs[(s - 1) & 1]])
+    a.wait_slot((steps - 1) & 1)
+    got.append([arr.copy() for arr in bufs[(steps - 1) & 1]])
+    for bb in bufs:
+        for arr in bb:
+            G.host_unregister(arr)
+    for s in range(steps):
+        b.run(1)
+        want = b.atoms_get()
+        for g_, w_ in zip(got[s], want):
+            assert np.allclose(g_, w_, rtol=1e-12, atol=1e-12), s
+    assert not np.array_equal(got[0][0], got[-1][0])  # the beads moved
+    with pytest.raises(Exception):
+        a.wait_slot(3)  # nothing enqueued there
+
+
 def test_autotune_steps_are_steps_of_the_run(gpu_lib):
     """The autotuner times each variant on the run's own steps: afterwards
     the state equals the oracle's after the same number of steps, and the
