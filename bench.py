@@ -386,75 +386,37 @@ def run_gpu(args):
         e.setup()
         e.run(1)
         e.atoms_get()
-        # the per-step read-back ring: 16 page-locked slots, the copies inside
-        # the 8-step graphs; the host waits for one launch's 8 slots while the
-        # next launch runs
-        K = 8
-        ring = [(np.empty((nb, 3)), np.empty((nb, 3)), np.empty((nb, 3)), np.empty(nb, np.int32))
-                for _ in range(2 * K)]
-        for b in ring:
-            for a in b:
-                G.host_register(a)
-        e.set_step_readback(ring)
-        e.run(K)  # captures the ring's graphs (both slot sets) and the single-step graphs
-        e.run(K)
-        e.synchronize()
-        kk = (k // K) * K
-        checksum = 0.0
-        t1 = time.perf_counter()
-        for L in range(kk // K):
-            e.run_async(K)
-            if L:
-                for j in range(K):
-                    sl = ((L - 1) * K + j) % (2 * K)
-                    e.wait_step_readback(sl)
-                    checksum += float(ring[sl][0][0, 0])  # the host reads each step's beads
-        for j in range(K):
-            sl = ((kk // K - 1) * K + j) % (2 * K)
-            e.wait_step_readback(sl)
-            checksum += float(ring[sl][0][0, 0])
-        out = e.grid_get("phi")
-        t2 = time.perf_counter()
-        e.set_step_readback([])
-        for b in ring:
-            for a in b:
-                G.host_unregister(a)
-        # the same, one step per run call: pipelined async reads, then blocking reads
         bufs = [(np.empty((nb, 3)), np.empty((nb, 3)), np.empty((nb, 3)), np.empty(nb, np.int32)) for _ in range(2)]
         for b in bufs:
             for a in b:
                 G.host_register(a)
-        e.synchronize()
-        t3 = time.perf_counter()
+        t1 = time.perf_counter()
         for s in range(k):
             e.run_async(1)
             e.atoms_get_async(bufs[s & 1], s & 1)
             if s:
-                e.wait_slot((s - 1) & 1)
+                e.wait_slot((s - 1) & 1)  # step s - 1's beads are in host memory
         e.wait_slot((k - 1) & 1)
-        t4 = time.perf_counter()
+        out = e.grid_get("phi")
+        t2 = time.perf_counter()
         for _ in range(k):
             e.run(1)
             e.atoms_get()
-        t5 = time.perf_counter()
+        t3 = time.perf_counter()
         for b in bufs:
             for a in b:
                 G.host_unregister(a)
-        steady = world * kk / ranks_max(t2 - t1)
+        steady = world * k / ranks_max(t2 - t1)
         line["e2e"] = {"value": steady, "unit": "steps/s", "h2d_bytes_per_step": 0,
-                       "d2h_bytes_per_step": int(nb * (3 * 8 * 3 + 4) + out.size * 4 / kk),
+                       "d2h_bytes_per_step": int(nb * (3 * 8 * 3 + 4) + out.size * 4 / k),
                        "setup_s": t1 - t0, "setup_h2d_bytes": int(phi_host.size * 4 + xs.size * 8 + nb * 12),
-                       "steps": kk, "single_step_runs_value": world * k / ranks_max(t4 - t3),
-                       "blocking_read_value": world * k / ranks_max(t5 - t4),
-                       "note": "steady state: %d steps run as phafd_run_async(ctx, 8) with the per-step read-back "
-                               "ring (phafd_set_step_readback): every step's beads' x, ux, F and image flags land "
-                               "in page-locked host memory, the copies inside the steps' graphs, and the host "
-                               "waits for and reads each step's slot while the next 8 steps run; phi read after "
-                               "the last.  single_step_runs_value: phafd_run_async(ctx, 1) per step with "
-                               "phafd_atoms_get_async, the host waiting for step s while step s + 1 runs; "
-                               "blocking_read_value: phafd_run(ctx, 1) then phafd_atoms_get per step; set-up "
-                               "(context, state uploaded from host arrays, first step with list build and graph "
-                               "capture) timed apart as setup_s, the ring's graph captures excluded" % kk}
+                       "steps": k, "blocking_read_value": world * k / ranks_max(t3 - t2),
+                       "note": "steady state: %d steps, each enqueued (phafd_run_async(ctx, 1)) with a read of its "
+                               "beads' x, ux, F and image flags into page-locked host memory "
+                               "(phafd_atoms_get_async), the host waiting for step s's read while step s + 1 runs; "
+                               "phi read after the last; blocking_read_value: each step phafd_run(ctx, 1) then "
+                               "phafd_atoms_get; set-up (context, state uploaded from host arrays, first step with "
+                               "list build and graph capture) timed apart as setup_s" % k}
         e.close()
 
     # FP32 production path against the FP64 path and the FP64 oracle from the

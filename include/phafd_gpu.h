@@ -214,18 +214,6 @@ int phafd_atoms_get(phafd_ctx* ctx, double* x, double* ux, double* f, int* image
  * can enqueue step k + 1 before it waits for step k's copy. */
 int phafd_atoms_get_async(phafd_ctx* ctx, double* x, double* ux, double* f, int* images, int slot);
 int phafd_wait_slot(phafd_ctx* ctx, int slot);
-/* Per-step read-back ring: from now on the beads' x, ux, F and image flags
- * after every step land in slot (i mod nslots) of the caller's page-locked
- * arrays (x[slot] etc., 3 n doubles or n ints each; a NULL array or entry
- * skips that field), i counting the steps run since this call; nslots = 2 x
- * the steps per graph (16 by default), 0 stops the ring.  The copies are
- * part of the steps' CUDA graphs, so runs keep their multi-step graphs
- * (each step's copy taken before the next step's neighbor check, which may
- * wrap positions).  phafd_wait_step_readback(ctx, slot) waits for the last
- * copy enqueued on `slot` and reports the device status as of that copy. */
-int phafd_set_step_readback(phafd_ctx* ctx, int nslots, double* const* x, double* const* ux, double* const* f,
-                            int* const* images);
-int phafd_wait_step_readback(phafd_ctx* ctx, int slot);
 /* page-lock (and release) a caller's host buffer for asynchronous copies */
 int phafd_host_register(void* ptr, size_t bytes);
 int phafd_host_unregister(void* ptr);

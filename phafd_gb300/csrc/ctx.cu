@@ -154,18 +154,6 @@ struct phafd_ctx {
   // words copied with them into page-locked memory
   cudaEvent_t ev_slot[4] = {nullptr, nullptr, nullptr, nullptr};
   long long* slot_status = nullptr;  // [slot][2]: nan step, flag|status
-  // per-step read-back ring (phafd_set_step_readback): step i of the run
-  // sequence since the ring was set lands in slot i mod rb_slots
-  int rb_slots = 0;
-  std::vector<double*> rb_x, rb_ux, rb_f;
-  std::vector<int*> rb_im;
-  std::vector<cudaEvent_t> rb_ev;
-  long long* rb_status = nullptr;  // page-locked [slot][2]: nan step, flag|status
-  long long rb_step = 0;
-  int rb_pending_slot = -1;  // the slot of the step being enqueued or captured (-1: none)
-  bool rb_early_done = false;
-  cudaGraphExec_t gexecRB[2] = {nullptr, nullptr};  // graph_steps-step graphs writing slots [0, K) and [K, 2K)
-  int graph_curRB[2] = {0, 0};
   cudaEvent_t ev_pl_fork = nullptr, ev_pl_join = nullptr;
   // domain / grid
   bool boxset = false, gridset = false, populated = false;
@@ -326,9 +314,6 @@ struct phafd_ctx {
     for (cudaEvent_t e : {ev_fork, ev_dep, ev_join, ev_pl_fork, ev_pl_join}) if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : ev_slot) if (e) cudaEventDestroy(e);
     if (slot_status) cudaFreeHost(slot_status);
-    for (cudaEvent_t e : rb_ev) if (e) cudaEventDestroy(e);
-    if (rb_status) cudaFreeHost(rb_status);
-    for (auto ge : gexecRB) if (ge) cudaGraphExecDestroy(ge);
     if (stc) cudaStreamDestroy(stc);
     if (st3) cudaStreamDestroy(st3);
     if (st2) cudaStreamDestroy(st2);
@@ -342,10 +327,6 @@ struct phafd_ctx {
     gexec = nullptr;
     if (gexecK) cudaGraphExecDestroy(gexecK);
     gexecK = nullptr;
-    for (auto& ge : gexecRB) {
-      if (ge) cudaGraphExecDestroy(ge);
-      ge = nullptr;
-    }
     for (auto& ge : gexec1) {
       if (ge) cudaGraphExecDestroy(ge);
       ge = nullptr;
@@ -834,12 +815,7 @@ struct phafd_ctx {
           dep_reset<T>(fork);
           if (late_chain) launch_chain_step<T>(ba, dt, bs, nsub, 0);
           macro_bead_substeps<T>(bs);
-          if (early_ok && check_next_early && fork) {
-            // the step's read-back precedes the next step's check (its rebuild wraps positions)
-            if (rb_pending_slot >= 0) readback_copies(rb_pending_slot, st2);
-            rb_early_done = rb_pending_slot >= 0;
-            neighbor_stage(st2, nullptr);
-          }
+          if (early_ok && check_next_early && fork) neighbor_stage(st2, nullptr);
           chk(GridOps<T>::ypass(geom, -1, W1, W1, nullptr, twf[1], st), "y fft");
         } else {
           chk(prc, "xy fwd");
@@ -847,12 +823,7 @@ struct phafd_ctx {
           dep_reset<T>(fork);
           if (late_chain) launch_chain_step<T>(ba, dt, bs, nsub, 0);
           macro_bead_substeps<T>(bs);
-          if (early_ok && check_next_early && fork) {
-            // the step's read-back precedes the next step's check (its rebuild wraps positions)
-            if (rb_pending_slot >= 0) readback_copies(rb_pending_slot, st2);
-            rb_early_done = rb_pending_slot >= 0;
-            neighbor_stage(st2, nullptr);
-          }
+          if (early_ok && check_next_early && fork) neighbor_stage(st2, nullptr);
         }
         mark(5);
         mark(6);
@@ -897,8 +868,6 @@ struct phafd_ctx {
     }
     if (touch_on && n > 0)
       launch_touch(bx.as<double>(), n, touch_point, touch_delay, d_step(), touch.as<TouchState>(), st);
-    if (rb_pending_slot >= 0 && !rb_early_done) readback_copies(rb_pending_slot, st);
-    rb_early_done = false;
   }
 
   // Neighbor::decide + build.  Inside a graph capture the rebuild kernels
@@ -972,25 +941,6 @@ struct phafd_ctx {
   void step_once() {
     if (precision == PHAFD_FP64) enqueue_step<double>();
     else enqueue_step<float>();
-  }
-
-  // the beads' x, ux, F, image flags and the status words into read-back
-  // slot `slot` on stream `s`, then the slot's event (a node of the graph
-  // when the stream is being captured)
-  void readback_copies(int slot, cudaStream_t s) {
-    const size_t nn = n;
-    if (nn) {
-      if (rb_x[slot]) CK(cudaMemcpyAsync(rb_x[slot], bx.p, 3 * nn * 8, cudaMemcpyDeviceToHost, s));
-      if (rb_ux[slot]) CK(cudaMemcpyAsync(rb_ux[slot], bux.p, 3 * nn * 8, cudaMemcpyDeviceToHost, s));
-      if (rb_f[slot]) CK(cudaMemcpyAsync(rb_f[slot], bf.p, 3 * nn * 8, cudaMemcpyDeviceToHost, s));
-      if (rb_im[slot]) CK(cudaMemcpyAsync(rb_im[slot], bimage.p, nn * 4, cudaMemcpyDeviceToHost, s));
-    }
-    CK(cudaMemcpyAsync(rb_status + 2 * slot, d_counters.as<long long>() + 3, 8, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(rb_status + 2 * slot + 1, d_counters.as<long long>() + 5, 8, cudaMemcpyDeviceToHost, s));
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    CK(cudaStreamIsCapturing(s, &cs));
-    if (cs == cudaStreamCaptureStatusActive) CK(cudaEventRecordWithFlags(rb_ev[slot], s, cudaEventRecordExternal));
-    else CK(cudaEventRecord(rb_ev[slot], s));
   }
 };
 
@@ -1496,60 +1446,6 @@ int phafd_wait_slot(phafd_ctx* c, int slot) {
   API_END(c)
 }
 
-int phafd_set_step_readback(phafd_ctx* c, int nslots, double* const* x, double* const* ux, double* const* f,
-                            int* const* images) {
-  API_BEGIN(c)
-  CK(cudaSetDevice(c->device));
-  if (nslots != 0 && nslots != 2 * c->graph_steps)
-    throw std::invalid_argument("read-back ring: 2 x the steps per graph slots (or 0 to stop)");
-  CK(cudaStreamSynchronize(c->st));
-  for (cudaEvent_t e : c->rb_ev) if (e) cudaEventDestroy(e);
-  c->rb_ev.clear();
-  c->invalidate_graph();  // the ring's graphs hold the old pointers
-  c->rb_slots = nslots;
-  c->rb_step = 0;
-  c->rb_x.assign(x ? x : (double* const*)nullptr, x ? x + nslots : (double* const*)nullptr);
-  c->rb_ux.assign(ux ? ux : (double* const*)nullptr, ux ? ux + nslots : (double* const*)nullptr);
-  c->rb_f.assign(f ? f : (double* const*)nullptr, f ? f + nslots : (double* const*)nullptr);
-  c->rb_im.assign(images ? images : (int* const*)nullptr, images ? images + nslots : (int* const*)nullptr);
-  c->rb_x.resize(nslots, nullptr);
-  c->rb_ux.resize(nslots, nullptr);
-  c->rb_f.resize(nslots, nullptr);
-  c->rb_im.resize(nslots, nullptr);
-  if (nslots > 0) {
-    if (!c->rb_status) CK(cudaHostAlloc(reinterpret_cast<void**>(&c->rb_status), 2 * 64 * sizeof(long long), 0));
-    if (nslots > 64) throw std::invalid_argument("read-back ring: at most 64 slots");
-    c->rb_ev.resize(nslots, nullptr);
-    for (auto& e : c->rb_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  }
-  API_END(c)
-}
-
-int phafd_wait_step_readback(phafd_ctx* c, int slot) {
-  API_BEGIN(c)
-  if (slot < 0 || slot >= c->rb_slots) throw std::invalid_argument("no such read-back slot");
-  CK(cudaEventSynchronize(c->rb_ev[slot]));
-  const long long nan_step = c->rb_status[2 * slot];
-  const int status = reinterpret_cast<const int*>(c->rb_status + 2 * slot + 1)[1];
-  if (nan_step >= 0) {
-    c->err = "NAN encountered in phi. (step " + std::to_string(nan_step) + ")";
-    return PHAFD_ERR_NAN;
-  }
-  if (status & ST_OVERFLOW) {
-    c->err = "Neighbor list overflow";
-    return PHAFD_ERR_OVERFLOW;
-  }
-  if (status & ST_CONSTRAINT) {
-    c->err = "Failed to maintain polymer bond-length constraints.";
-    return PHAFD_ERR_CONSTRAINT;
-  }
-  if (status & ST_TIMEOUT) {
-    c->err = "a grid pass gave up waiting for its tensor-map loads";
-    return PHAFD_ERR_TIMEOUT;
-  }
-  API_END(c)
-}
-
 int phafd_host_register(void* ptr, size_t bytes) {
   if (!ptr || bytes == 0) return PHAFD_ERR_INVALID;
   return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? PHAFD_OK : PHAFD_ERR_CUDA;
@@ -1949,67 +1845,11 @@ static void enqueue_run(phafd_ctx* c, int nsteps) {
       c->fill_reference_uniforms();
       CK(cudaMemcpyAsync(c->uref.p, c->uref_h, c->ncplx * sizeof(double2), cudaMemcpyHostToDevice, c->st));
     }
-    const bool rb = c->rb_slots > 0;
     if (!use_graph || !c->eager_done) {
-      c->rb_pending_slot = rb ? (int)(c->rb_step % c->rb_slots) : -1;
       c->step_once();
-      c->rb_pending_slot = -1;
-      if (rb) ++c->rb_step;
       CK(cudaGetLastError());
       if (use_graph) c->eager_done = true;
     } else {
-      // With the read-back ring: graphs of graph_steps steps that write ring
-      // slots [0, K) or [K, 2K) (the copies are nodes of the graph), taken
-      // when the run's step sequence is at a multiple of K, else one step at
-      // a time with the copies after its graph.
-      if (rb) {
-        const int K = c->graph_steps;
-        const int set = (int)((c->rb_step / K) & 1);
-        cudaGraphExec_t& ge = c->gexecRB[set];
-        if (resident && nsteps - s >= K && c->rb_slots == 2 * K && c->rb_step % K == 0 &&
-            (!ge || c->cur == c->graph_curRB[set])) {
-          if (!ge) {
-            c->graph_curRB[set] = c->cur;
-            cudaGraph_t g;
-            CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
-            for (int j = 0; j < K; ++j) {
-              c->check_done_early = j > 0;
-              c->check_next_early = j + 1 < K;
-              c->rb_pending_slot = set * K + j;
-              c->step_once();
-              resident_spectrum_flip(c);
-            }
-            c->check_done_early = c->check_next_early = false;
-            c->rb_pending_slot = -1;
-            CK(cudaStreamEndCapture(c->st, &g));
-            CK(cudaGraphInstantiate(&ge, g, 0));
-            cudaGraphDestroy(g);
-          }
-          CK(cudaGraphLaunch(ge, c->st));
-          s += K - 1;
-          c->timestep += K;
-          c->rb_step += K;
-          c->note_step();
-          continue;  // an even number of steps leaves cur unchanged
-        }
-        const int par = resident ? c->cur : 0;
-        if (!c->gexec1[par]) {
-          cudaGraph_t g;
-          CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
-          c->step_once();
-          CK(cudaStreamEndCapture(c->st, &g));
-          if (!c->kernels_per_step) c->kernels_per_step = count_kernels(g);
-          CK(cudaGraphInstantiate(&c->gexec1[par], g, 0));
-          cudaGraphDestroy(g);
-        }
-        CK(cudaGraphLaunch(c->gexec1[par], c->st));
-        c->readback_copies((int)(c->rb_step % c->rb_slots), c->st);
-        ++c->rb_step;
-        c->timestep += 1;
-        c->note_step();
-        if (resident) resident_spectrum_flip(c);
-        continue;
-      }
       // Graphs: graph_steps steps, then two (both spectrum parities of the
       // resident schedule), one step per parity for the rest.
       bool launched = false;

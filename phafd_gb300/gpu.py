@@ -31,7 +31,7 @@ EXPORTS = [
     "phafd_set_gradient_mask", "phafd_set_fp32_centering", "phafd_set_pair_snapshot", "phafd_compute_pair",
     "phafd_set_variants", "phafd_autotune", "phafd_set_graph_steps",
     "phafd_atoms_create", "phafd_atoms_get", "phafd_atoms_set_images", "phafd_atoms_get_async", "phafd_wait_slot",
-    "phafd_host_register", "phafd_host_unregister", "phafd_set_step_readback", "phafd_wait_step_readback",
+    "phafd_host_register", "phafd_host_unregister",
     "phafd_pair_gridatom", "phafd_pair_gridatom_coeff", "phafd_pair_lj_cut",
     "phafd_neighbor",
     "phafd_fix_conjugate_volfrac", "phafd_fix_floryhuggins", "phafd_fix_gradphi", "phafd_fix_drag",
@@ -109,8 +109,6 @@ def load(path=None):
         "phafd_wait_slot": [vp, C.c_int],
         "phafd_host_register": [C.c_void_p, C.c_size_t],
         "phafd_host_unregister": [C.c_void_p],
-        "phafd_set_step_readback": [vp, C.c_int, vp, vp, vp, vp],
-        "phafd_wait_step_readback": [vp, C.c_int],
         "phafd_atoms_set_images": [vp, ip],
         "phafd_pair_gridatom": [vp, C.c_int, C.c_double],
         "phafd_pair_gridatom_coeff": [vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double],
@@ -355,27 +353,6 @@ class PhafdGPU:
         steps compute."""
         x, ux, f, im = bufs
         self._call("phafd_atoms_get_async", x.reshape(-1), ux.reshape(-1), f.reshape(-1), im, slot)
-
-    def set_step_readback(self, slots):
-        """Per-step read-back ring: slots = [(x, ux, f, images), ...] of
-        page-locked arrays (2 x the steps per graph of them; None entries skip
-        a field); [] stops it.  Step i of the runs that follow lands in slot
-        i mod len(slots)."""
-        n = len(slots)
-        self._rb_keep = slots  # the arrays must outlive the ring
-        if n == 0:
-            self._call("phafd_set_step_readback", 0, None, None, None, None)
-            return
-        ptrs = []
-        for k in range(4):
-            t = C.c_void_p * n
-            ptrs.append(t(*[(s[k].ctypes.data if s[k] is not None else None) for s in slots]))
-        self._rb_ptrs = ptrs
-        self._call("phafd_set_step_readback", n, *[C.cast(p, C.c_void_p) for p in ptrs])
-
-    def wait_step_readback(self, slot):
-        """Wait for the last read-back enqueued on ring slot `slot`."""
-        self._call("phafd_wait_step_readback", slot)
 
     def wait_slot(self, slot):
         """Wait for the read-back enqueued on `slot`; raise on a device error."""

@@ -421,51 +421,6 @@ def test_pipelined_bead_readback(gpu_lib):
         a.wait_slot(3)  # nothing enqueued there
 
 
-@pytest.mark.parametrize("steps", [19, 40])
-def test_step_readback_ring(gpu_lib, steps):
-    """phafd_set_step_readback: every step's beads, copied by the steps'
-    graphs into a 16-slot ring (8-step graphs writing alternate halves, single
-    steps with their copies after the graph), equal a step-by-step run with
-    blocking reads; the copy of a step precedes the next step's neighbor
-    check, so positions are those before its periodic wrap, as the blocking
-    read sees them."""
-    from phafd_gb300 import gpu as G
-    cfg = dict(W.CONFIGS["32cube_64beads"])
-    cfg.update(field_noise="philox", bead_temp=1.0, dt=1e-3)
-    a = gpu(64, "resident"); b = gpu(64, "resident")
-    chains = None
-    for d in (a, b):
-        chains = W.apply(d, cfg, chains=chains)
-        d.setup()
-    n = a.n
-    ring = [(np.empty((n, 3)), np.empty((n, 3)), np.empty((n, 3)), np.empty(n, np.int32)) for _ in range(16)]
-    for r in ring:
-        for arr in r:
-            G.host_register(arr)
-    a.set_step_readback(ring)
-    got = []
-    done = 0
-    # an eager first step and single steps, then ring graphs of both halves
-    # (at step counts 8, 24, 32) between misaligned single steps
-    chunks = (8, 8, 3) if steps == 19 else (8, 8, 3, 5, 8, 8)
-    for chunk in chunks:
-        a.run_async(chunk)
-        for i in range(done, done + chunk):
-            a.wait_step_readback(i % 16)
-            got.append([arr.copy() for arr in ring[i % 16]])
-        done += chunk
-    a.set_step_readback([])
-    for r in ring:
-        for arr in r:
-            G.host_unregister(arr)
-    for s in range(done):
-        b.run(1)
-        want = b.atoms_get()
-        for g_, w_ in zip(got[s], want):
-            assert np.allclose(g_, w_, rtol=1e-12, atol=1e-12), s
-    assert a.counters()["neighbor_calls"] == b.counters()["neighbor_calls"] >= 2
-
-
 def test_autotune_steps_are_steps_of_the_run(gpu_lib):
     """The autotuner times each variant on the run's own steps: afterwards
     the state equals the oracle's after the same number of steps, and the
