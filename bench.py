@@ -390,6 +390,10 @@ def run_gpu(args):
         for b in bufs:
             for a in b:
                 G.host_register(a)
+        for s in range(4):  # capture the single-step graphs (both spectrum parities) before the timed steps
+            e.run_async(1)
+            e.atoms_get_async(bufs[s & 1], s & 1)
+        e.wait_slot(1)
         t1 = time.perf_counter()
         for s in range(k):
             e.run_async(1)
@@ -416,7 +420,8 @@ def run_gpu(args):
                                "(phafd_atoms_get_async), the host waiting for step s's read while step s + 1 runs; "
                                "phi read after the last; blocking_read_value: each step phafd_run(ctx, 1) then "
                                "phafd_atoms_get; set-up (context, state uploaded from host arrays, first step with "
-                               "list build and graph capture) timed apart as setup_s" % k}
+                               "list build and graph capture) timed apart as setup_s, and four pipelined steps that "
+                               "capture the single-step graphs before the timed ones" % k}
         e.close()
 
     # FP32 production path against the FP64 path and the FP64 oracle from the
