@@ -19,7 +19,7 @@ namespace BeadRodPmer {
 class ChainStandIn {
  public:
   explicit ChainStandIn(const std::vector<std::string>&) {
-    throw std::runtime_error("beadrodpmer (the external chain integrator) is not available in this build");
+    throw std::runtime_error("beadrodpmer (the external chain integrator) is not part of the reference checkout");
   }
   void setup(const Eigen::ColsView&) {}
   void first_step(const Eigen::ColsView&, const Eigen::ColsView&, double) {}
