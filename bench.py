@@ -283,9 +283,23 @@ def run_gpu(args):
 
     cfg = replica_cfg(W.CONFIGS[args.workload], rank)
     chains = make_chains(cfg, rank)
+
+    def device_free():
+        try:
+            import torch
+            return torch.cuda.mem_get_info(local)
+        except Exception:  # no torch: the footprint is not reported
+            return None, None
+
+    free0, total = device_free()
     g = PhafdGPU(precision=32, device=local, schedule="resident")
     W.apply(g, cfg, chains=chains)
     g.setup()
+    g.run(1)
+    free1, _ = device_free()
+    memory = None if free0 is None else {"context_bytes": int(free0 - free1), "device_total_bytes": int(total),
+                                         "note": "device memory taken by the context (state, lists, spectra, "
+                                                 "graphs) after set-up and one step: free before minus free after"}
     # clocks are sampled from the warm-up through the timed region and a
     # continuation of the same steps of at least one second
     sampler = ClockSampler(local)
@@ -348,6 +362,7 @@ def run_gpu(args):
         "step_roofline": step_roofline,
         "stage_ms": prof,
         "autotune": autotune,
+        "memory": memory,
         "clocks": clocks,
         "gpu_launches": int(counters.get("kernels_per_step", 0)) * args.steps if counters.get("kernels_per_step") else None,
         "neighbor_calls": counters["neighbor_calls"],
