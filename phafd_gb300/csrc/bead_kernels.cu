@@ -574,6 +574,27 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
     c[d] = (t - f[d]) - y;
     f[d] = t;
   };
+  // the grid coupling's per-bead values, loaded ahead of the bead-bead loop
+  // so that their latency overlaps it
+  const bool ga = live && p.ga_style != PHAFD_GRIDATOM_NONE && a.gl;
+  const int gcnt = ga ? a.ngl[i] : 0;
+  const int gt = ga ? a.type[i] : 0;
+  const T cutsq = ga ? (T)p.ga_cutsq[gt] : (T)0, eps = ga ? (T)p.ga_eps[gt] : (T)0,
+          phit = ga ? (T)p.ga_phi[gt] : (T)0;
+  // bead position in grid units: integer part + fraction (FP32 path; GB300's
+  // FP64 rate makes a divide per axis and thread cost more than the rest)
+  int gi[3];
+  T gf[3], dxf[3];
+  const double xi[3] = {xi0, xi1, xi2};
+  if (ga) {
+    for (int d = 0; d < 3; ++d) {
+      const double ud = (xi[d] - a.boxlo[d]) * a.invdx[d];
+      const double fl = floor(ud);
+      gi[d] = (int)fl;
+      gf[d] = (T)(ud - fl);
+      dxf[d] = (T)a.dx[d];
+    }
+  }
   // Both loops take their entries in batches of PB per lane: the list words
   // of a batch are loaded together, then every load the batch's entries need,
   // then the arithmetic, in the entries' order k = sub, sub + PAIR_TPB, ...
@@ -614,23 +635,9 @@ __global__ void k_pair(BeadArgs a, PairArgs<T> p) {
       }
     }
   }
-  if (live && p.ga_style != PHAFD_GRIDATOM_NONE && a.gl) {
-    const int cnt = a.ngl[i];
-    const int t = a.type[i];
-    const T cutsq = (T)p.ga_cutsq[t], eps = (T)p.ga_eps[t], phit = (T)p.ga_phi[t];
+  if (ga) {
+    const int cnt = gcnt;
     const bool linear = p.ga_style != PHAFD_GRIDATOM_GAUSSIAN && p.ga_style != PHAFD_GRIDATOM_LJISH;
-    // bead position in grid units: integer part + fraction (FP32 path; GB300's
-    // FP64 rate makes a divide per axis and thread cost more than the rest)
-    int gi[3];
-    T gf[3], dxf[3];
-    const double xi[3] = {xi0, xi1, xi2};
-    for (int d = 0; d < 3; ++d) {
-      const double ud = (xi[d] - a.boxlo[d]) * a.invdx[d];
-      const double fl = floor(ud);
-      gi[d] = (int)fl;
-      gf[d] = (T)(ud - fl);
-      dxf[d] = (T)a.dx[d];
-    }
     const uint32_t* __restrict__ gl = a.gl + (size_t)i * a.maxg;
     for (int k0 = sub; k0 < cnt; k0 += PAIR_TPB * PB) {
       uint32_t e[PB];
