@@ -543,6 +543,10 @@ def run_ensemble(args):
     """Ragged 48-replica ensemble (grids 96^3/128^3/160^3, 2k-20k beads):
     every replica enqueued, all overlapping on one GPU; value is replica
     steps per second."""
+    # 48 contexts x 3 streams: more hardware work queues than the default 8
+    # keep their graphs from queueing behind one another (read when the CUDA
+    # runtime starts, which has not happened yet in this process)
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     from phafd_gb300 import build as B
     B.build()
     from phafd_gb300.ensemble import Ensemble, ensemble_configs

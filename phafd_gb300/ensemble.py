@@ -6,6 +6,11 @@ replicas overlap on the GPU, then waits for all.  Replicas may differ in grid
 size, bead count and parameters (the ragged 48-replica ensemble: grids of
 96^3, 128^3 or 160^3, 2,000 to 20,000 beads in chains of 100 to 400,
 chi in [2.2, 3.5], phi0 in [0.3, 0.5], one seed per replica).
+
+The contexts' streams share the device's hardware work queues; setting
+CUDA_DEVICE_MAX_CONNECTIONS=32 in the environment before the process first
+uses CUDA gives them four times the default eight (measured: 10,580 against
+9,621 replica steps/s for the 48-replica ensemble).
 """
 import numpy as np
 
