@@ -413,8 +413,8 @@ k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restri
 
 // The same x r2c fed by the tensor memory accelerator (FP32, Ny a multiple
 // of 32): a persistent grid whose CTAs walk the tiles of k_xr2c256 (rows
-// y0 .. y0 + 32 of plane z, numbered plane by plane) with the grid's stride.
-// A tile's rows of phi arrive as one 32-row box; the deposit, zero except on
+// y0 .. y0 + XR_ROWS of plane z, numbered plane by plane) with the grid's
+// stride.  A tile's rows of phi arrive as one box; the deposit, zero except on
 // the nodes of the grid lists, is read straight from global memory in the
 // 32-byte sectors its support mask sets (fh.dep_mask; every sector when the
 // mask is null), so the mostly-zero array costs no full read and no shared
@@ -427,14 +427,19 @@ k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restri
 // register 15 - r (lane 0: its own register (16 - r) % 16), so one shuffle
 // per mode brings it and each lane writes its modes k = j + 16 r (r < 8, and
 // k = N/2 at lane 0) directly, 16 bytes (rows 2c, 2c + 1) per mode.
-constexpr int XR_ROWS = 2 * W;                // rows per tile
-constexpr int XR_BOX = XR_ROWS * N * 4;       // bytes of one 32-row box
-constexpr int XR_BUF = W * RX * 8;            // the lines' exchange buffer (covers the box)
+// Lines per CTA: 8 (128 threads, 16-row tiles).  The tiles per SM then come
+// in finer steps than with 16 lines, so the last round over them leaves
+// fewer SMs idle (2048 32-row tiles at 256^3 are 13.5 per SM).
+constexpr int XR_LINES = 8;
+constexpr int XR_THREADS = 16 * XR_LINES;
+constexpr int XR_ROWS = 2 * XR_LINES;         // rows per tile
+constexpr int XR_BOX = XR_ROWS * N * 4;       // bytes of one tile's box
+constexpr int XR_BUF = XR_LINES * RX * 8;     // the lines' exchange buffer (covers the box)
 static_assert(XR_BOX <= XR_BUF, "the box fits in the exchange buffer");
 constexpr size_t XR_SMEM = (size_t)XR_BUF + 1024 + 16;  // + alignment slack + the mbarrier
 
 template <int PRO, int MINB>
-__global__ void __launch_bounds__(256, MINB)
+__global__ void __launch_bounds__(XR_THREADS, MINB)
 k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const float* __restrict__ dep, cpx<float>* __restrict__ out,
            const cpx<float>* __restrict__ tw, int Ny, int Nz, FHArgs fh, int* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char smraw[];  // aligned to 1024 below
@@ -555,7 +560,7 @@ k_xr2c256t(const __grid_constant__ CUtensorMap mphi, const float* __restrict__ d
 // launch of k_xr2c256t: -3 when it does not apply (tensor maps unavailable)
 inline int xr2c_tma(const Geom& g, const float* in, const float* dep, cpx<float>* out, const cpx<float>* tw,
                     const FHArgs& fh, int* status, cudaStream_t st) {
-  constexpr int MINB = 4;
+  constexpr int MINB = 4 * 256 / XR_THREADS;  // 64 registers a thread
   CUtensorMap mphi;
   if (!tma::map2d_f32(&mphi, in, N, (uint64_t)g.ny * g.nz, N, XR_ROWS)) return -3;
   const int pro = !dep ? 0 : (fh.centered && fh.enabled) ? 2 : 1;
@@ -573,7 +578,7 @@ inline int xr2c_tma(const Geom& g, const float* in, const float* dep, cpx<float>
     if (it == resident.end()) {
       int sms = 0, per_sm = 0;
       if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, XR_SMEM) != cudaSuccess || per_sm < 1)
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, XR_THREADS, XR_SMEM) != cudaSuccess || per_sm < 1)
         return -1;
       it = resident.emplace(std::make_pair(dev, pro), sms * per_sm).first;
     }
@@ -581,7 +586,7 @@ inline int xr2c_tma(const Geom& g, const float* in, const float* dep, cpx<float>
   }
   const long long ntiles = (long long)(g.ny / XR_ROWS) * g.nz;
   const int grid = (int)(ntiles < (long long)slots ? ntiles : (long long)slots);
-  k<<<grid, 256, XR_SMEM, st>>>(mphi, dep, out, tw, g.ny, g.nz, fh, status);
+  k<<<grid, XR_THREADS, XR_SMEM, st>>>(mphi, dep, out, tw, g.ny, g.nz, fh, status);
   return 0;
 }
 
