@@ -189,7 +189,8 @@ int phafd_set_gradient_mask(phafd_ctx* ctx, int on);
 #define PHAFD_TUNE_XC2R_TMA 4
 #define PHAFD_TUNE_XR2C_TMA 8
 int phafd_set_variants(phafd_ctx* ctx, int flags);
-/* Steps per CUDA graph of a run (even, >= 2; default 8): runs launch graphs
+/* Steps per CUDA graph of a run (no counterpart in the reference; even, >= 2;
+ * default 8): runs launch graphs
  * of this many steps, then two-step and one-step graphs for the rest.  Long
  * graphs keep a single system's neighbor checks off its critical path (every
  * step but a graph's first checks on the previous step's bead branch); many
@@ -203,7 +204,9 @@ int phafd_set_fp32_centering(phafd_ctx* ctx, int stages);
 /* ---- beads (atom_style / atom_populate, atom.cpp:26-110,219-252) ---- */
 int phafd_atoms_create(phafd_ctx* ctx, int n, const int* tags, const int* mol, const int* types, const double* x);
 int phafd_atoms_get(phafd_ctx* ctx, double* x, double* ux, double* f, int* images);
-/* Read-back pipelined with the steps: phafd_atoms_get_async enqueues the
+/* Read-back pipelined with the steps (no counterpart in the reference, whose
+ * dumps are written inside its step loop, integrate.cpp:180-186):
+ * phafd_atoms_get_async enqueues the
  * copies of x, ux, F and the image flags (NULL skips one) into host memory
  * at the current end of the context's stream, after the steps enqueued so
  * far, and returns; slot (0..3) names the copy.  phafd_wait_slot waits for
