@@ -205,7 +205,7 @@ int phafd_set_fp32_centering(phafd_ctx* ctx, int stages);
 int phafd_atoms_create(phafd_ctx* ctx, int n, const int* tags, const int* mol, const int* types, const double* x);
 int phafd_atoms_get(phafd_ctx* ctx, double* x, double* ux, double* f, int* images);
 /* Read-back pipelined with the steps (no counterpart in the reference, whose
- * dumps are written inside its step loop, integrate.cpp:180-186):
+ * dumps are written inside its step loop, integrate.cpp:178-186):
  * phafd_atoms_get_async enqueues the
  * copies of x, ux, F and the image flags (NULL skips one) into host memory
  * at the current end of the context's stream, after the steps enqueued so
