@@ -435,9 +435,9 @@ class PhafdGPU:
         self._call("phafd_run_timed", nsteps, C.byref(ms))
         return ms.value
 
-    # stage 6 is the z fft of mu in the reference schedule and the sparse
-    # deposit reset in the resident one (its z fft is fused into stage 7)
-    STAGES = ["gradient", "neighbor", "pairs", "bead_integrate", "x_r2c_fh", "y_fft", "z_fft_or_dep_zero",
+    # stage 6 is the z fft of mu in the reference schedule; the resident one
+    # fuses its z fft into stage 7 (its stage 6 is empty)
+    STAGES = ["gradient", "neighbor", "pairs", "bead_integrate", "x_r2c_fh", "y_fft", "z_fft",
               "z_update_ifft", "y_ifft", "x_c2r"]
 
     def profile_stages(self, nsteps):
