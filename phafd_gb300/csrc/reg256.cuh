@@ -412,7 +412,7 @@ k_xr2c256(const T* __restrict__ in0, const T* __restrict__ dep, cpx<T>* __restri
 }
 
 // The same x r2c fed by the tensor memory accelerator (FP32, Ny a multiple
-// of 32): a persistent grid whose CTAs walk the tiles of k_xr2c256 (rows
+// of XR_ROWS): a persistent grid whose CTAs walk tiles of XR_ROWS rows (rows
 // y0 .. y0 + XR_ROWS of plane z, numbered plane by plane) with the grid's
 // stride.  A tile's rows of phi arrive as one box; the deposit, zero except on
 // the nodes of the grid lists, is read straight from global memory in the
